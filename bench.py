@@ -1,0 +1,310 @@
+"""Benchmark: spin-flip attempts/ns of one PT cycle on one GB300.
+
+Workload (default, the batched configuration): L=32 cubic periodic lattices, NCONF=64 disorder
+configurations (PHI=2, XI=3, seeds IRINIT+k), each with a 32-replica ladder linear over
+T=8.0-11.5, HOT starts; J1=1, J2=-1, Jperp=1, no dilution.  2048 lattices resident on the GPU.
+One step = one PT cycle: PTSWAPEVER=5 fused FP32 sweeps of all lattices, the observable
+reduction, the replica exchange and the FP64 running sums.  Synthetic inputs of the reference's
+shapes (no dataset is involved).  The FP64 plain form is timed beside it on the L=24, 16-replica
+PT configuration.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "j1j2-public_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "spin-flip attempts/ns, FP32 batched vs FP64 plain on 1 GB300; % HBM roofline"
+UNIT = "attempts/ns"
+B_PER_ATTEMPT_FP32 = 11.8  # full PT cycle model: 10 B per sweep attempt + 9 B/site measure / 5
+B_PER_ATTEMPT_FP64 = 21.4
+L2_FLUSH_BYTES = 256 << 20
+
+WORKLOADS = {
+    "batched_fp32_L32_64x32": dict(L=32, nconf=64, nrep=32, precision=1),
+    "plain_fp64_L24_1x16": dict(L=24, nconf=1, nrep=16, precision=0),
+    "batched_fp64_L32_64x32": dict(L=32, nconf=64, nrep=32, precision=0),
+}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        return {}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        mhz, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            try:
+                mhz.append(float(f[1]))
+                mx.append(float(f[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not mhz:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def make_engine(jc, w, device, conf_base=0, flags=0, irinit=1):
+    L, nconf, nrep = w["L"], w["nconf"], w["nrep"]
+    eng = jc.Engine(L, L, nconf=nconf, nreplica=nrep, ptswapever=5, precision=w["precision"],
+                    seed=irinit, conf_base=conf_base, device=device, flags=flags)
+    betas = 1.0 / jc.ladder(nrep, 8.0, 11.5)
+    for k in range(nconf):
+        eng.set_disorder(k, jc.disorder(L, L, irinit + conf_base + k, 2.0, 3.0))
+    eng.set_ladder(-1, np.tile(betas, nconf))
+    for k in range(nconf):
+        eng.init_spins(k, jc.START_HOT)
+    eng.reset_measurements()
+    return eng, betas
+
+
+def time_steps(torch, eng, steps, warmup, flush):
+    """Device time of `steps` PT cycles (CUDA events on the engine's stream), L2 flushed
+    before every step outside the timed interval."""
+    stream = torch.cuda.current_stream()
+    eng.set_stream(stream.cuda_stream)
+    eng.run(warmup, measure=True, restart_swap_phase=True)
+    torch.cuda.synchronize()
+    total_ms = 0.0
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for k in range(steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        eng.run(1, measure=True, restart_swap_phase=False)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    for a, b in ev:
+        total_ms += a.elapsed_time(b)
+    return total_ms
+
+
+def run_ours(args):
+    import torch
+
+    import j1j2cuda as jc
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    wname = args.workload
+    w = WORKLOADS[wname]
+    eng, betas = make_engine(jc, w, local, conf_base=rank * w["nconf"],
+                             flags=jc.FLAG_PROFILE)
+    cfg = eng.config()
+    occ = int(eng.nocc.sum()) * w["nrep"]
+    attempts_per_step = occ * 5
+
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        ms0 = eng.profile()[0]
+        total_ms = time_steps(torch, eng, args.steps, args.warmup, flush)
+        prof_ms, prof_n, _ = eng.profile()
+    torch.cuda.synchronize()
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    sweep_ms_avg = (prof_ms - ms0) / max(args.steps, 1)  # sweep kernel, per launch (timed steps)
+    value = attempts_per_step * args.steps * ws / (total_ms * 1e6)
+
+    # end to end through the public API with host buffers: ladder H2D, one cycle, all running
+    # sums and observables D2H, every step
+    host_betas = np.tile(betas, w["nconf"])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.set_ladder(-1, host_betas)
+        eng.run(1, measure=True, restart_swap_phase=False)
+        sums, nm = eng.slot_sums(-1)
+        obs = eng.observables(-1)
+    e2e_s = time.perf_counter() - t0
+    e2e = attempts_per_step * args.steps * ws / (e2e_s * 1e9)
+    h2d = host_betas.nbytes
+    d2h = sums.nbytes + nm.nbytes + obs.nbytes
+    assert np.isfinite(sums).all()
+
+    pk = peaks()
+    hbm = pk.get("hbm_gbs")
+    peak_src = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    bpa = B_PER_ATTEMPT_FP32 if w["precision"] == 1 else B_PER_ATTEMPT_FP64
+    achieved = attempts_per_step * bpa / (sweep_ms_avg * 1e-3) / 1e9 if sweep_ms_avg > 0 else 0.0
+
+    # FP64 plain form on the L=24, 16-replica PT configuration (the 10x target's denominator)
+    w64 = WORKLOADS["plain_fp64_L24_1x16"]
+    eng64, _ = make_engine(jc, w64, local)
+    s64 = max(4, args.steps // 4)
+    ms64 = time_steps(torch, eng64, s64, 2, flush)
+    fp64_val = int(eng64.nocc.sum()) * w64["nrep"] * 5 * s64 / (ms64 * 1e6)
+    eng64.close()
+
+    cpu = cpu_baseline() if (rank == 0 and not args.no_cpu) else None
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (corr_rand_3d disorder from seeds IRINIT+k, HOT starts)",
+        "config": {"workload": wname, "L": w["L"], "H": w["L"], "nconf_per_gpu": w["nconf"],
+                   "nreplica": w["nrep"], "ptswapever": 5, "T": [8.0, 11.5], "phi": 2.0,
+                   "xi": 3.0, "lattices_per_gpu": w["nconf"] * w["nrep"],
+                   "attempts_per_step": attempts_per_step * ws, "l2": "flushed before each step",
+                   "block_threads": cfg["block_threads"], "sites_per_thread": cfg["sites_per_thread"],
+                   "smem_bytes": cfg["smem_bytes"], "parallelism": f"confs x{ws}"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
+                     "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": None,
+                     "peak_source": peak_src, "bytes_per_attempt": bpa,
+                     "sweep_kernel_ms": round(sweep_ms_avg, 4)},
+        "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "fp64_plain": {"value": round(fp64_val, 4), "unit": UNIT, "workload": "plain_fp64_L24_1x16",
+                       "ratio_fp32_over_fp64": round(value / fp64_val / ws, 2)},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clocks,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    eng.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(nthreads=None, ncycles=1):
+    """The oracle's restatement of the reference PT cycle (sequential site order, KISS, FP64,
+    neighbour tables), one ladder per host thread, on a bounded sample of the workload."""
+    from oracle import oracle as O
+    import j1j2cuda as jc
+
+    nthreads = nthreads or os.cpu_count() or 1
+    L, nrep = 32, 32
+    M = O.Model(L, L, jc.disorder(L, L, 1))
+    betas = 1.0 / O.ladder(nrep, 8.0, 11.5)
+    secs = M.bench_pt(nthreads, betas, 5, ncycles)
+    attempts = nthreads * nrep * 5 * ncycles * L ** 3
+    return {"value": round(attempts / secs / 1e9, 5), "unit": UNIT, "cores": nthreads,
+            "kind": "port",
+            "sample": f"{nthreads} independent L=32 ladders x 32 replicas x {ncycles} PT cycle(s) "
+                      f"of 5 sweeps, one ladder per thread ({attempts} attempts, {secs:.2f} s)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O  # the reference's CPU path (restated; Fortran not buildable)
+    import j1j2cuda as jc
+
+    nthreads = os.cpu_count() or 1
+    L, nrep = 32, 32
+    M = O.Model(L, L, jc.disorder(L, L, 1))
+    betas = 1.0 / O.ladder(nrep, 8.0, 11.5)
+    for _ in range(args.warmup):
+        M.bench_pt(nthreads, betas, 5, 1)
+    secs = 0.0
+    for _ in range(args.steps):
+        secs += M.bench_pt(nthreads, betas, 5, 1)
+    attempts = nthreads * nrep * 5 * L ** 3 * args.steps
+    value = attempts / secs / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": UNIT,
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(secs * 1e3 / args.steps, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (corr_rand_3d disorder seed 1, HOT starts)",
+            "config": {"workload": args.workload, "L": L, "nreplica": nrep, "ptswapever": 5,
+                       "ladders_per_step": nthreads, "threads": nthreads},
+            "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": nthreads,
+                             "kind": "port",
+                             "sample": f"{nthreads} L=32 ladders x 32 replicas, 1 PT cycle per "
+                                       "step, one ladder per thread (Fortran toolchain absent)"},
+            "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batched_fp32_L32_64x32", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,212 @@
+/*
+ * libj1j2cuda — GB300 (sm_103a) Monte Carlo engine for the hot path of sim/J1J2_6tv.f90
+ * (ShadowQFT/J1J2-public): single-spin Metropolis sweeps of the L x L x H J1-J2-Jperp model with
+ * the random field on the nematic variable, the parallel-tempering (PT) swap, the observable
+ * reductions and the per-slot running sums.  All disorder configurations ("confs") and all
+ * replicas of their temperature ladders stay resident on one GPU.
+ *
+ * C ABI: plain pointers and sizes, int status (0 = OK, negative = error, text in
+ * j1j2c_last_error).  Host arrays are caller-owned and are copied during the call; no pointer is
+ * kept after a call returns.  Site order of every per-site array is the reference's
+ * site = ix + L*iy + L*L*iz (J:539).  Replica, slot and pair indices are 0-based (the Fortran
+ * binding adds 1).  Calls are synchronous at return unless stated otherwise.
+ *
+ * Each entry point names the reference code it replaces ("J:" = sim/J1J2_6tv.f90,
+ * "CR:" = sim/corr_rand_3d.f90).
+ */
+#ifndef J1J2C_H
+#define J1J2C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (argument checks mirror Validate_run_options, J:841-925) */
+#define J1J2C_OK 0
+#define J1J2C_EINVAL -1   /* bad argument: odd L or H, NREPLICA != ladder size, bad enum ...    */
+#define J1J2C_ECUDA -2    /* CUDA runtime error (text in j1j2c_last_error)                      */
+#define J1J2C_ETIMEOUT -3 /* a bounded device wait expired                                      */
+#define J1J2C_ENOMEM -4   /* device or host allocation failed                                   */
+#define J1J2C_ESTATE -5   /* call order: e.g. run before every conf has disorder and a ladder  */
+
+/* precision of the sweep (the swap, energies and running sums are FP64 in both forms) */
+#define J1J2C_FP64_PLAIN 0   /* FP64 field and acceptance, bit-identical to the host replay      */
+#define J1J2C_FP32_BATCHED 1 /* FP32 field and acceptance (ln u < -beta dE form)                 */
+
+/* START / STRAXIS (J:62-63, Initialize_spin_array J:1179-1209) */
+#define J1J2C_START_HOT 0 /* device Philox stream: s = +1 when u < 1/2                           */
+#define J1J2C_START_FER 1
+#define J1J2C_START_STR 2
+#define J1J2C_AXIS_X 0 /* stripes run along x: s = (-1)^iy */
+#define J1J2C_AXIS_Y 1 /* stripes run along y: s = (-1)^ix */
+
+/* j1j2c_params.flags */
+#define J1J2C_FLAG_NO_GRAPH 1u   /* launch kernels directly instead of replaying a CUDA graph     */
+#define J1J2C_FLAG_PROFILE 2u    /* time every sweep launch with CUDA events (j1j2c_get_profile)  */
+#define J1J2C_FLAG_GENERIC 4u    /* force the per-site kernel path (testing)                      */
+
+/* Run parameters: the compile-time constants of J:43-96 that the hot path consumes. */
+typedef struct {
+    int32_t L, H;          /* lattice (both even: the 8-colour update needs it)                  */
+    double J1h, J1v;       /* nearest-neighbour couplings along x and y (J1 +/- deltaJ1)        */
+    double J2, J3;         /* diagonal and inter-layer couplings                                 */
+    int32_t nconf;         /* disorder configurations resident in this context                  */
+    int32_t nreplica;      /* PT ladder length per conf (NREPLICA = NTEMP); 1 = LOCAL sampler   */
+    int32_t ptswapever;    /* sweeps per PT cycle (PTSWAPEVER)                                   */
+    int32_t precision;     /* J1J2C_FP64_PLAIN or J1J2C_FP32_BATCHED                             */
+    uint32_t seed;         /* Philox key word 0 (IRINIT)                                         */
+    uint32_t conf_base;    /* Philox key word 1 of conf 0 (conf c uses conf_base + c)           */
+    int32_t device;        /* CUDA device ordinal                                                */
+    uint32_t flags;        /* J1J2C_FLAG_*                                                       */
+    int32_t block_threads; /* 0 = autotuned; otherwise threads per CTA (multiple of 32, <=1024) */
+} j1j2c_params;
+
+/* Per (conf, slot) running sums of Pt_measurement_loop (J:1440-1513), in this order. */
+typedef struct {
+    double mag, absmag, mag2, mag4;
+    double en, en2;
+    double strx_abs, stry_abs, strx2, strx4, stry2, stry4;
+    double str2, str4, absstr, nem;
+    double nbar, nbarabs, nbar2, nbar4;
+    double best_en, final_en;
+    int64_t nmeasure;
+} j1j2c_slot_sums;
+
+/* ---------------------------------------------------------------------------------------------
+ * Context life cycle
+ * ------------------------------------------------------------------------------------------- */
+
+/* Allocates every device buffer for nconf x nreplica lattices.  Replaces the MPI set-up and the
+ * per-rank arrays (J:115-207, Setup_mpi J:415-420, Setup_neighbor_table J:532-586). */
+int j1j2c_create(void **ctx, const j1j2c_params *params);
+
+/* Frees everything (J:401 MPI_FINALIZE's role for this context). */
+void j1j2c_destroy(void *ctx);
+
+/* Text of the last error on this context (or of the last failed create when ctx is NULL). */
+const char *j1j2c_last_error(void *ctx);
+
+/* Use a caller-provided cudaStream_t for all later work (NULL = the context's own stream). */
+int j1j2c_set_stream(void *ctx, void *cuda_stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Inputs (replace the per-config set-up that feeds the hot path)
+ * ------------------------------------------------------------------------------------------- */
+
+/* Disorder of one conf: random field p (N doubles), occupancy (N int8, NULL = all occupied),
+ * bond masks jh / jv (N int8, NULL = all bonds present).  Replaces the arrays filled by
+ * Setup_vacancies (J:1111-1165) and Setup_phi_table (J:590-633) as the sweep reads them. */
+int j1j2c_set_disorder(void *ctx, int32_t conf, const double *p, const int8_t *occu,
+                       const int8_t *jh, const int8_t *jv);
+
+/* Inverse temperatures of the ladder slots of one conf (NREPLICA doubles, slot 0 = TMIN);
+ * conf < 0 sets every conf from nconf x NREPLICA doubles.  Replaces beta_ladder
+ * (Setup_temperature_ladder J:928-962). */
+int j1j2c_set_ladder(void *ctx, int32_t conf, const double *beta);
+
+/* Initial spins of every replica of a conf, identity slot maps and zeroed swap counters.
+ * spins == NULL generates START/STRAXIS (HOT from the device Philox stream); otherwise spins
+ * holds NREPLICA x N int8 (+1/-1, replica-major).  Vacancies are stored as 0.  Must follow
+ * j1j2c_set_disorder of the conf.  Replaces Initialize_pt_state (J:1218-1247) /
+ * Initialize_spin_array (J:1179-1209). */
+int j1j2c_init_spins(void *ctx, int32_t conf, int32_t start, int32_t axis, const int8_t *spins);
+
+/* Zero the running sums, measurement counts and visit flags of one conf (conf < 0: all) and
+ * reset best_en to +inf, as at the start of Pt_measurement_loop (J:1361-1389, J:1394-1395).
+ * Swap counters run on across both loops, as cfg_ptswap_* do (reset by j1j2c_init_spins). */
+int j1j2c_reset_measurements(void *ctx, int32_t conf);
+
+/* ---------------------------------------------------------------------------------------------
+ * Hot path
+ * ------------------------------------------------------------------------------------------- */
+
+/* ncycles PT cycles over every conf: PTSWAPEVER sweeps of every replica at its slot's beta, the
+ * observable reduction of every replica, the alternating odd/even adjacent swap and (measure != 0)
+ * the visit flags and per-slot running sums.  restart_swap_phase != 0 starts with pairs
+ * (0,1),(2,3),... as both PT loops do (J:1266, J:1429).  Replaces Pt_equilibration_loop
+ * (J:1250-1279) and the cycle loop of Pt_measurement_loop (J:1428-1532); with NREPLICA = 1 and
+ * PTSWAPEVER = 1 it is the LOCAL Equilibration_loop / Measurement_loop (J:2122-2216). */
+int j1j2c_run(void *ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_phase);
+
+/* Drop-in for one call of Metro_sweep (J:2544-2608) on one lattice: nsweeps FP64 sweeps of
+ * replica rep of conf at inverse temperature beta, Philox sweep counter starting at sweep_index.
+ * On return mag/en/strx/stry (each may be NULL) hold the Measurement values (J:2807-2842) of the
+ * new configuration; Fortran callers pass their curmag/curen/curstrx/curstry. */
+int j1j2c_metro_sweep_fp64(void *ctx, int32_t conf, int32_t rep, double beta,
+                           uint32_t sweep_index, int32_t nsweeps, double *mag, double *en,
+                           double *strx, double *stry);
+
+/* Deterministic replay audit of the FP32 form: nsweeps FP64 sweeps of every lattice at its slot's
+ * beta, evaluating at every attempt the FP32 decision on the same configuration and uniform.
+ * Adds to *attempts and *mismatches (FP32 decision != FP64 decision).  No reference
+ * counterpart: it quantifies the FP32 form's deviation from the FP64 acceptance of J:2572-2604. */
+int j1j2c_audit_fp32(void *ctx, int32_t nsweeps, int64_t *attempts, int64_t *mismatches);
+
+/* ---------------------------------------------------------------------------------------------
+ * Outputs
+ * ------------------------------------------------------------------------------------------- */
+
+/* Running sums of every slot of a conf (NREPLICA records; conf < 0: nconf x NREPLICA). */
+int j1j2c_get_slot_sums(void *ctx, int32_t conf, j1j2c_slot_sums *out);
+
+/* Swap attempts / accepts per adjacent pair (NREPLICA-1 each, may be NULL) and the number of
+ * replicas that visited both ladder ends while measuring (cfg_ptswap_* and cfg_ptvisitboth,
+ * J:1303-1338, J:1537). */
+int j1j2c_get_pt_stats(void *ctx, int32_t conf, int64_t *attempts, int64_t *accepts,
+                       int32_t *visited_both);
+
+/* Slot maps rep_at_temp / temp_of_rep (NREPLICA each, 0-based; either may be NULL). */
+int j1j2c_get_maps(void *ctx, int32_t conf, int32_t *rep_at_temp, int32_t *temp_of_rep);
+
+/* Spins of one replica (N int8 in site order; vacancies read 0). */
+int j1j2c_get_spins(void *ctx, int32_t conf, int32_t rep, int8_t *out);
+
+/* Observables of every replica after the last cycle: NREPLICA x {mag, en, strx, stry, nbar}
+ * (per occupied site; en includes the phi term, J:2835-2840; nbar as J:1028-1048);
+ * conf < 0: every conf, nconf x NREPLICA x 5. */
+int j1j2c_get_observables(void *ctx, int32_t conf, double *out);
+
+/* Sweep-kernel timing accumulated under J1J2C_FLAG_PROFILE: milliseconds, launches, and the
+ * attempts those launches made (occupied sites x sweeps). */
+int j1j2c_get_profile(void *ctx, double *sweep_ms, int64_t *sweep_launches, int64_t *attempts);
+
+/* Kernel configuration the context chose: threads per CTA, sites per thread per colour phase
+ * (4 = quad path, 1 = per-site path), dynamic shared memory bytes per CTA. */
+int j1j2c_get_config(void *ctx, int32_t *block_threads, int32_t *sites_per_thread,
+                     int32_t *smem_bytes);
+
+/* ---------------------------------------------------------------------------------------------
+ * Host-side model helpers (no GPU needed)
+ * ------------------------------------------------------------------------------------------- */
+
+/* make_corr_rand_3d (CR:191-386): exponential correlation of length xi on the power-of-two
+ * padded periodic cube, KISS polar Gaussian noise after gkissinit(seed), Fourier filter, crop,
+ * and (do_uniform) the erfcc map to [-max_value, max_value].  out[(k*n2 + j)*n1 + i] = x(i,j,k).
+ * FP64 throughout. */
+int j1j2c_corr_rand_3d(int32_t n1, int32_t n2, int32_t n3, double xi, int32_t seed,
+                       int32_t do_uniform, double max_value, double *out);
+
+/* Setup_vacancies (J:1111-1165) after kissinit(seed): mode 0 = RAN (Bernoulli pp per site),
+ * 1 = COR (anticorrelated); then bond masks with pph / ppv.  Returns the vacancy count (>= 0). */
+int j1j2c_setup_vacancies(int32_t seed, int32_t L, int32_t H, double pp, double pph, double ppv,
+                          int32_t mode, int8_t *occu, int8_t *jh, int8_t *jv);
+
+/* Initialize_spin_array (J:1179-1209) after kissinit(seed), for callers that want the
+ * reference's KISS-generated HOT start (then pass the result to j1j2c_init_spins). */
+int j1j2c_kiss_spins(int32_t seed, int32_t L, int32_t H, int32_t start, int32_t axis, int8_t *s);
+
+/* Temperatures of Setup_temperature_ladder (J:928-962, PT branch): split = 0 LINEAR,
+ * 1 SPLIT around tmid with fraction tfrac of the intervals below it. */
+int j1j2c_ladder(int32_t n, double tmin, double tmax, int32_t split, double tmid, double tfrac,
+                 double *temps);
+
+/* Library version string. */
+const char *j1j2c_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* J1J2C_H */

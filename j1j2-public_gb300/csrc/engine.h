@@ -1,0 +1,89 @@
+// Kernel argument blocks and launchers shared by the kernels (kernels.cu) and the C-ABI host
+// code (api.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device_common.cuh"
+
+namespace j1j2 {
+
+// Per-lattice reduction written by the sweep kernel after its last sweep: exact integer sums and
+// the fixed-point energy (sum over occupied sites of llrint(-s_i*field_i * 2^32)).
+struct LatObs {
+    long long eacc;
+    int M, SX, SY, NB;
+    int pad[2];
+};
+
+enum : int { kModeSweep = 0, kModeAudit = 1 };
+
+struct SweepArgs {
+    Geo g;
+    uint8_t* spins;          // lattice l at spins + l*lat_stride (biased bytes, compact layout)
+    long long lat_stride;    // bytes, multiple of 16
+    const float* pf;         // conf c at pf + c*p_stride (compact), FP32 random field
+    const double* pd;        // conf c at pd + c*p_stride (compact), FP64 random field
+    const uint8_t* bm;       // conf c at bm + c*lat_stride: bit0 = jh, bit1 = jv (or nullptr)
+    long long p_stride;      // elements, multiple of 4
+    const double* beta;      // [nconf*nrep], by slot
+    const int* temp_of_rep;  // [nconf*nrep]
+    const uint32_t* ctl;     // ctl[0] = PT cycle counter
+    LatObs* obs;             // [nlat]
+    unsigned long long* audit;  // [2]: attempts, mismatches (audit mode)
+    double J1h, J1v, J2, J3;
+    float J1hf, J1vf, J2f, J3f;
+    int nrep;
+    int nsweeps;             // sweeps per launch
+    int ptswapever;          // sweep counter = cycle*ptswapever (+ sweep within the cycle)
+    uint32_t seed, conf_base;
+    int lat0;                // lattice handled by blockIdx.x == 0
+    int use_override;        // 1: beta_override / sweep_override instead of ladder / cycle
+    double beta_override;
+    uint32_t sweep_override;
+};
+
+struct SwapArgs {
+    const LatObs* obs;   // [nconf*nrep]
+    const double* beta;  // [nconf*nrep]
+    const int* nocc;     // [nconf]
+    int* rat;            // rep_at_temp [nconf*nrep]
+    int* tor;            // temp_of_rep [nconf*nrep]
+    double* sums;        // [nconf*nrep*22]
+    long long* nmeas;    // [nconf*nrep]
+    long long* att;      // [nconf*nrep] (pair index)
+    long long* acc;      // [nconf*nrep]
+    uint8_t* visited;    // [nconf*nrep] bit0 cold end, bit1 hot end
+    double* last_obs;    // [nconf*nrep*5]
+    uint32_t* ctl;       // ctl[0] cycle, ctl[1] swap phase (1 or 2)
+    int nconf, nrep, measure;
+    uint32_t seed, conf_base;
+};
+
+struct InitArgs {
+    Geo g;
+    uint8_t* spins;          // first lattice of the conf
+    long long lat_stride;
+    const uint8_t* occ;      // compact occupancy of the conf
+    int nrep, start, axis;
+    uint32_t seed, key1;
+};
+
+// Kernel variant of one sweep launch
+struct SweepVariant {
+    bool fp64;     // FP64 form (else FP32)
+    bool quad;     // four sites per thread per colour phase (L % 8 == 0)
+    bool stage_p;  // random field staged in shared memory
+    bool masks;    // bond dilution present
+    int mode;      // kModeSweep / kModeAudit
+};
+
+size_t sweep_smem_bytes(const Geo& g, const SweepVariant& v);
+cudaError_t prepare_sweep_variant(const SweepVariant& v, size_t smem);
+cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks, int nthreads,
+                         size_t smem, cudaStream_t st);
+cudaError_t launch_swap(const SwapArgs& a, cudaStream_t st);
+cudaError_t launch_init(const InitArgs& a, cudaStream_t st);
+
+}  // namespace j1j2

@@ -1,0 +1,690 @@
+// sm_103a kernels of the engine:
+//   sweep_kernel  one CTA per lattice: stage the lattice in shared memory, run the fused sweeps
+//                 of one PT cycle colour by colour (8 colour phases per sweep, one barrier each),
+//                 reduce the observables of the new configuration, write the lattice back.
+//                 Replaces Metro_sweep / Compute_local_field (J:2498-2608) and Measurement /
+//                 Spatial_mean_local_nematic (J:2807-2842, J:1028-1048).
+//   swap_kernel   one CTA for all confs: observables, the odd/even adjacent replica exchange of
+//                 Pt_attempt_swaps (J:1303-1338), visit flags and the per-slot running sums of
+//                 Pt_measurement_loop (J:1440-1513).
+//   init_kernel   HOT/FER/STR starts (Initialize_spin_array J:1179-1209) on the device.
+#include "engine.h"
+
+namespace j1j2 {
+namespace {
+
+struct Acc {
+    long long e;
+    int M, SX, SY, NB;
+};
+
+__device__ __forceinline__ int wrap_p(int v, int n) { return v + 1 == n ? 0 : v + 1; }
+__device__ __forceinline__ int wrap_m(int v, int n) { return v == 0 ? n - 1 : v - 1; }
+
+// fixed-point energy contribution of one site: llrint(e * 2^32)
+__device__ __forceinline__ long long efix(double e)
+{
+    return __double2ll_rn(__dmul_rn(e, 4294967296.0));
+}
+
+template <class Real>
+__device__ __forceinline__ const Real* field_base(const SweepArgs& a, int conf)
+{
+    if constexpr (sizeof(Real) == 8)
+        return a.pd + (long long)conf * a.p_stride;
+    else
+        return a.pf + (long long)conf * a.p_stride;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Per-site path (any even L, H): one site per thread per colour phase.
+// ------------------------------------------------------------------------------------------------
+template <class Real, bool MASKS, int MODE, bool MEASURE>
+__device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint8_t* S,
+                                          const Real* P, const uint8_t* BM, const float* Pf32,
+                                          int c, int X, int Y, int Z, uint32_t sweep, uint32_t rep,
+                                          uint32_t k0, uint32_t k1, double beta, float kb,
+                                          Acc& acc)
+{
+    const int px = c & 1, py = (c >> 1) & 1, pz = c >> 2;
+    const int Xp = px ? wrap_p(X, g.Lh) : X, Xm = px ? X : wrap_m(X, g.Lh);
+    const int Yp = py ? wrap_p(Y, g.Lh) : Y, Ym = py ? Y : wrap_m(Y, g.Lh);
+    const int Zp = pz ? wrap_p(Z, g.Hh) : Z, Zm = pz ? Z : wrap_m(Z, g.Hh);
+    const int i = cidx(g, c, Z, Y, X);
+    const int b = S[i];
+    if (b == 1) return;  // vacancy: no attempt and no measured term (J:2563, J:2825)
+    const int i1 = cidx(g, c ^ 2, Z, Yp, X), i2 = cidx(g, c ^ 2, Z, Ym, X);
+    const int i3 = cidx(g, c ^ 1, Z, Y, Xp), i4 = cidx(g, c ^ 1, Z, Y, Xm);
+    const int i5 = cidx(g, c ^ 3, Z, Yp, Xp), i6 = cidx(g, c ^ 3, Z, Yp, Xm);
+    const int i7 = cidx(g, c ^ 3, Z, Ym, Xp), i8 = cidx(g, c ^ 3, Z, Ym, Xm);
+    const int i9 = cidx(g, c ^ 4, Zp, Y, X), i10 = cidx(g, c ^ 4, Zm, Y, X);
+    const int s = b - 1;
+    int jh_own = 1, jh_m4 = 1, jv_own = 1, jv_m2 = 1;
+    if constexpr (MASKS) {
+        jh_own = BM[i] & 1;
+        jv_own = (BM[i] >> 1) & 1;
+        jh_m4 = BM[i4] & 1;
+        jv_m2 = (BM[i2] >> 1) & 1;
+    }
+
+    if constexpr (MEASURE) {
+        acc.M += s;
+        acc.SX += px ? -s : s;
+        acc.SY += py ? -s : s;
+        acc.NB += s * ((int)S[i3] + (int)S[i4] - (int)S[i1] - (int)S[i2]);
+    }
+
+    bool flip64 = false;
+    double f64 = 0.0;
+    if constexpr (sizeof(Real) == 8) {
+        Nbr64 n;
+        n.s[0] = (int)S[i1] - 1;
+        n.s[1] = (int)S[i2] - 1;
+        n.s[2] = (int)S[i3] - 1;
+        n.s[3] = (int)S[i4] - 1;
+        n.s[4] = (int)S[i5] - 1;
+        n.s[5] = (int)S[i6] - 1;
+        n.s[6] = (int)S[i7] - 1;
+        n.s[7] = (int)S[i8] - 1;
+        n.s[8] = (int)S[i9] - 1;
+        n.s[9] = (int)S[i10] - 1;
+        n.p1 = P[i1];
+        n.p2 = P[i2];
+        n.p3 = P[i3];
+        n.p4 = P[i4];
+        n.jv_own = jv_own;
+        n.jv_m2 = jv_m2;
+        n.jh_own = jh_own;
+        n.jh_m4 = jh_m4;
+        f64 = field_fp64(n, P[i], a.J1h, a.J1v, a.J2, a.J3, nullptr);
+        if constexpr (MEASURE) {
+            acc.e += efix(-((double)s * f64));
+            return;
+        }
+    }
+
+    // FP32 field (the FP32 form, or the FP32 side of the audit)
+    float f32 = 0.0f;
+    if constexpr (sizeof(Real) == 4 || MODE == kModeAudit) {
+        const float* Q;
+        if constexpr (sizeof(Real) == 4)
+            Q = reinterpret_cast<const float*>(P);
+        else
+            Q = Pf32;
+        Nbr32 n;
+        n.syp = (float)((int)S[i1] - 1);
+        n.sym = (float)((int)S[i2] - 1);
+        n.sxp = (float)((int)S[i3] - 1);
+        n.sxm = (float)((int)S[i4] - 1);
+        n.D = (float)((int)S[i5] + (int)S[i6] + (int)S[i7] + (int)S[i8] - 4);
+        n.Zs = (float)((int)S[i9] + (int)S[i10] - 2);
+        n.pyp = Q[i1];
+        n.pym = Q[i2];
+        n.pxp = Q[i3];
+        n.pxm = Q[i4];
+        if constexpr (MASKS)
+            f32 = field_fp32_masked(n, Q[i], a.J1hf, a.J1vf, a.J2f, a.J3f, (float)jh_own,
+                                    (float)jh_m4, (float)jv_own, (float)jv_m2);
+        else
+            f32 = field_fp32(n, Q[i], a.J1hf, a.J1vf, a.J2f, a.J3f);
+        if constexpr (MEASURE && sizeof(Real) == 4) {
+            acc.e += efix((double)(-((float)s * f32)));
+            return;
+        }
+    }
+
+    const uint32_t grp = (uint32_t)(((c * g.Hh + Z) * g.Lh + Y) * g.Qr + (X >> 2));
+    const int w = X & 3;
+    uint32_t r = 0;
+    if constexpr (sizeof(Real) == 8) {
+        // FP64 acceptance, J:2572-2604: no uniform is needed when dE <= 0
+        if (s == 1 ? f64 <= 0.0 : f64 >= 0.0) {
+            flip64 = true;
+        } else {
+            r = u4_word(philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1), w);
+            const double u = (double)r * 0x1p-32;
+            const double t2 = __dmul_rn(__dmul_rn(2.0, f64), beta);
+            flip64 = u < own_exp(s == 1 ? -t2 : t2);
+        }
+        if constexpr (MODE == kModeAudit) {
+            r = u4_word(philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1), w);
+            const float sf = __fmul_rn((float)s, f32);
+            const bool flip32 = u01_f32(r) < ex2_approx(__fmul_rn(kb, sf));
+            acc.M += 1;
+            acc.SX += (flip32 != flip64);
+        }
+        if (flip64) S[i] = (uint8_t)(2 - b);
+    } else {
+        r = u4_word(philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1), w);
+        const float sf = __fmul_rn((float)s, f32);
+        if (u01_f32(r) < ex2_approx(__fmul_rn(kb, sf))) S[i] = (uint8_t)(2 - b);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Quad path (Lh % 4 == 0): a thread owns four consecutive compact X of one colour in one row,
+// i.e. one 32-bit word of spins and one Philox call (four uniforms).  Its neighbours are whole
+// words of the neighbouring colours, or words shifted by one byte (__byte_perm with the next /
+// previous word); diagonal and inter-layer neighbours are summed bytewise in 32-bit adds.
+// ------------------------------------------------------------------------------------------------
+struct QuadNbr {
+    uint32_t own, xp, xm, yp, ym, dpp, dpm, dmp, dmm, zp, zm;
+};
+
+__device__ __forceinline__ void x_pair(int px, uint32_t A, uint32_t B, uint32_t& plus,
+                                       uint32_t& minus)
+{
+    if (px) {  // site X: +x neighbour at compact X+1, -x at X
+        minus = A;
+        plus = __byte_perm(A, B, 0x4321);
+    } else {  // +x at X, -x at X-1
+        plus = A;
+        minus = __byte_perm(B, A, 0x6543);
+    }
+}
+
+template <class Real, bool MASKS, bool MEASURE>
+__device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, uint32_t* S32,
+                                          const Real* P, const uint8_t* BM, int c, int q,
+                                          uint32_t sweep, uint32_t rep, uint32_t k0, uint32_t k1,
+                                          double beta, float kb, Acc& acc)
+{
+    const int Qr = g.Qr;
+    const int row = q / Qr;
+    const int qx = q - row * Qr;
+    const int Z = row / g.Lh;
+    const int Y = row - Z * g.Lh;
+    const int px = c & 1, py = (c >> 1) & 1, pz = c >> 2;
+    const int Yp = py ? wrap_p(Y, g.Lh) : Y, Ym = py ? Y : wrap_m(Y, g.Lh);
+    const int Zp = pz ? wrap_p(Z, g.Hh) : Z, Zm = pz ? Z : wrap_m(Z, g.Hh);
+    const int qn = px ? wrap_p(qx, Qr) : wrap_m(qx, Qr);
+    const int rowstride = g.Lh * Qr;       // words per compact z-plane
+    const int colstride = g.Hh * rowstride;  // words per colour
+    auto W = [&](int cc, int ZZ, int YY, int qq) {
+        return cc * colstride + ZZ * rowstride + YY * Qr + qq;
+    };
+    QuadNbr n;
+    const int wown = W(c, Z, Y, qx);
+    n.own = S32[wown];
+    x_pair(px, S32[W(c ^ 1, Z, Y, qx)], S32[W(c ^ 1, Z, Y, qn)], n.xp, n.xm);
+    n.yp = S32[W(c ^ 2, Z, Yp, qx)];
+    n.ym = S32[W(c ^ 2, Z, Ym, qx)];
+    x_pair(px, S32[W(c ^ 3, Z, Yp, qx)], S32[W(c ^ 3, Z, Yp, qn)], n.dpp, n.dpm);
+    x_pair(px, S32[W(c ^ 3, Z, Ym, qx)], S32[W(c ^ 3, Z, Ym, qn)], n.dmp, n.dmm);
+    n.zp = S32[W(c ^ 4, Zp, Y, qx)];
+    n.zm = S32[W(c ^ 4, Zm, Y, qx)];
+
+    uint32_t mown = 0xFFFFFFFFu, mxm = 0xFFFFFFFFu, mym = 0xFFFFFFFFu;
+    if constexpr (MASKS) {
+        const uint32_t* BM32 = reinterpret_cast<const uint32_t*>(BM);
+        mown = BM32[wown];
+        uint32_t dummy;
+        x_pair(px, BM32[W(c ^ 1, Z, Y, qx)], BM32[W(c ^ 1, Z, Y, qn)], dummy, mxm);
+        mym = BM32[W(c ^ 2, Z, Ym, qx)];
+    }
+
+    // random field: own, x neighbours (same word and one shifted element), y rows
+    Real pown[4], pxa[4], pyp[4], pym[4];
+    const int X0 = 4 * qx;
+    const int bo = cidx(g, c, Z, Y, X0), bx = cidx(g, c ^ 1, Z, Y, X0);
+    const int byp = cidx(g, c ^ 2, Z, Yp, X0), bym = cidx(g, c ^ 2, Z, Ym, X0);
+    const Real pextra = P[cidx(g, c ^ 1, Z, Y, px ? 4 * qn : 4 * qn + 3)];
+    if constexpr (sizeof(Real) == 4) {
+        const float4 v0 = *reinterpret_cast<const float4*>(P + bo);
+        const float4 v1 = *reinterpret_cast<const float4*>(P + bx);
+        const float4 v2 = *reinterpret_cast<const float4*>(P + byp);
+        const float4 v3 = *reinterpret_cast<const float4*>(P + bym);
+        pown[0] = v0.x, pown[1] = v0.y, pown[2] = v0.z, pown[3] = v0.w;
+        pxa[0] = v1.x, pxa[1] = v1.y, pxa[2] = v1.z, pxa[3] = v1.w;
+        pyp[0] = v2.x, pyp[1] = v2.y, pyp[2] = v2.z, pyp[3] = v2.w;
+        pym[0] = v3.x, pym[1] = v3.y, pym[2] = v3.z, pym[3] = v3.w;
+    } else {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const double2 v0 = *reinterpret_cast<const double2*>(P + bo + 2 * h);
+            const double2 v1 = *reinterpret_cast<const double2*>(P + bx + 2 * h);
+            const double2 v2 = *reinterpret_cast<const double2*>(P + byp + 2 * h);
+            const double2 v3 = *reinterpret_cast<const double2*>(P + bym + 2 * h);
+            pown[2 * h] = v0.x, pown[2 * h + 1] = v0.y;
+            pxa[2 * h] = v1.x, pxa[2 * h + 1] = v1.y;
+            pyp[2 * h] = v2.x, pyp[2 * h + 1] = v2.y;
+            pym[2 * h] = v3.x, pym[2 * h + 1] = v3.y;
+        }
+    }
+
+    U4 rnd{0, 0, 0, 0};
+    if constexpr (!MEASURE) {
+        const uint32_t grp = (uint32_t)(c * colstride + q);
+        rnd = philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1);
+    }
+    uint32_t flipmask = 0;
+    const uint32_t dsum = n.dpp + n.dpm + n.dmp + n.dmm;  // bytewise, <= 8 each
+    const uint32_t zsum = n.zp + n.zm;                    // bytewise, <= 4 each
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int sh = 8 * k;
+        const int b = (n.own >> sh) & 0xFF;
+        const Real pxp = px ? (k < 3 ? pxa[k + 1] : pextra) : pxa[k];
+        const Real pxm = px ? pxa[k] : (k > 0 ? pxa[k - 1] : pextra);
+        const int jh_own = (mown >> sh) & 1, jv_own = (mown >> (sh + 1)) & 1;
+        const int jh_m4 = (mxm >> sh) & 1, jv_m2 = (mym >> (sh + 1)) & 1;
+        if constexpr (sizeof(Real) == 4) {
+            Nbr32 nb;
+            nb.sxp = byte_f(n.xp, k) - 1.0f;
+            nb.sxm = byte_f(n.xm, k) - 1.0f;
+            nb.syp = byte_f(n.yp, k) - 1.0f;
+            nb.sym = byte_f(n.ym, k) - 1.0f;
+            nb.D = byte_f(dsum, k) - 4.0f;
+            nb.Zs = byte_f(zsum, k) - 2.0f;
+            nb.pxp = pxp;
+            nb.pxm = pxm;
+            nb.pyp = pyp[k];
+            nb.pym = pym[k];
+            float f;
+            if constexpr (MASKS)
+                f = field_fp32_masked(nb, pown[k], a.J1hf, a.J1vf, a.J2f, a.J3f, (float)jh_own,
+                                      (float)jh_m4, (float)jv_own, (float)jv_m2);
+            else
+                f = field_fp32(nb, pown[k], a.J1hf, a.J1vf, a.J2f, a.J3f);
+            const float sf = __fmul_rn((float)(b - 1), f);
+            if constexpr (MEASURE) {
+                const int s = b - 1;
+                acc.e += efix((double)(-sf));
+                acc.M += s;
+                acc.SX += px ? -s : s;
+                acc.SY += py ? -s : s;
+                acc.NB += s * ((int)((n.xp >> sh) & 0xFF) + (int)((n.xm >> sh) & 0xFF) -
+                               (int)((n.yp >> sh) & 0xFF) - (int)((n.ym >> sh) & 0xFF));
+            } else {
+                const bool flip = (b != 1) &&
+                                  (u01_f32(u4_word(rnd, k)) < ex2_approx(__fmul_rn(kb, sf)));
+                flipmask |= flip ? (2u << sh) : 0u;
+            }
+        } else {
+            if (b == 1) continue;
+            Nbr64 nb;
+            nb.s[0] = (int)((n.yp >> sh) & 0xFF) - 1;
+            nb.s[1] = (int)((n.ym >> sh) & 0xFF) - 1;
+            nb.s[2] = (int)((n.xp >> sh) & 0xFF) - 1;
+            nb.s[3] = (int)((n.xm >> sh) & 0xFF) - 1;
+            nb.s[4] = (int)((n.dpp >> sh) & 0xFF) - 1;
+            nb.s[5] = (int)((n.dpm >> sh) & 0xFF) - 1;
+            nb.s[6] = (int)((n.dmp >> sh) & 0xFF) - 1;
+            nb.s[7] = (int)((n.dmm >> sh) & 0xFF) - 1;
+            nb.s[8] = (int)((n.zp >> sh) & 0xFF) - 1;
+            nb.s[9] = (int)((n.zm >> sh) & 0xFF) - 1;
+            nb.p1 = pyp[k];
+            nb.p2 = pym[k];
+            nb.p3 = pxp;
+            nb.p4 = pxm;
+            nb.jv_own = jv_own;
+            nb.jv_m2 = jv_m2;
+            nb.jh_own = jh_own;
+            nb.jh_m4 = jh_m4;
+            const double f = field_fp64(nb, pown[k], a.J1h, a.J1v, a.J2, a.J3, nullptr);
+            const int s = b - 1;
+            if constexpr (MEASURE) {
+                acc.e += efix(-((double)s * f));
+                acc.M += s;
+                acc.SX += px ? -s : s;
+                acc.SY += py ? -s : s;
+                acc.NB += s * (nb.s[2] + nb.s[3] - nb.s[0] - nb.s[1]);
+            } else {
+                bool flip;
+                if (s == 1 ? f <= 0.0 : f >= 0.0) {
+                    flip = true;
+                } else {
+                    const double u = (double)u4_word(rnd, k) * 0x1p-32;
+                    const double t2 = __dmul_rn(__dmul_rn(2.0, f), beta);
+                    flip = u < own_exp(s == 1 ? -t2 : t2);
+                }
+                flipmask |= flip ? (2u << sh) : 0u;
+            }
+        }
+    }
+    if constexpr (!MEASURE) {
+        if (flipmask) S32[wown] = n.own ^ flipmask;
+    }
+}
+
+__device__ __forceinline__ void warp_reduce(Acc& v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.e += __shfl_down_sync(0xFFFFFFFFu, v.e, o);
+        v.M += __shfl_down_sync(0xFFFFFFFFu, v.M, o);
+        v.SX += __shfl_down_sync(0xFFFFFFFFu, v.SX, o);
+        v.SY += __shfl_down_sync(0xFFFFFFFFu, v.SY, o);
+        v.NB += __shfl_down_sync(0xFFFFFFFFu, v.NB, o);
+    }
+}
+
+__device__ __forceinline__ Acc block_reduce(Acc v)
+{
+    __shared__ Acc red[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    warp_reduce(v);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        v = lane < nw ? red[lane] : Acc{0, 0, 0, 0, 0};
+        warp_reduce(v);
+    }
+    return v;  // valid in thread 0
+}
+
+template <class Real, bool QUAD, bool STAGE_P, bool MASKS, int MODE>
+__global__ void __launch_bounds__(1024) sweep_kernel(SweepArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Geo g = a.g;
+    const int lat = a.lat0 + (int)blockIdx.x;
+    const int conf = lat / a.nrep;
+    const int rep = lat - conf * a.nrep;
+    const int tid = (int)threadIdx.x, NT = (int)blockDim.x;
+    const int Nb = (g.N + 15) & ~15;
+    uint8_t* S = smem;
+    Real* Ps = reinterpret_cast<Real*>(smem + Nb);
+    uint8_t* Sg = a.spins + (long long)lat * a.lat_stride;
+    const Real* Pg = field_base<Real>(a, conf);
+    const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
+    const float* Pf32 = (MODE == kModeAudit) ? a.pf + (long long)conf * a.p_stride : nullptr;
+
+    {  // stage the lattice (and the random field) in shared memory with 16-byte vectors
+        const uint4* src = reinterpret_cast<const uint4*>(Sg);
+        uint4* dst = reinterpret_cast<uint4*>(S);
+        for (int k = tid; k < Nb / 16; k += NT) dst[k] = src[k];
+        if constexpr (STAGE_P) {
+            const int nv = (int)((g.N * sizeof(Real) + 15) / 16);
+            const uint4* ps = reinterpret_cast<const uint4*>(Pg);
+            uint4* pdst = reinterpret_cast<uint4*>(Ps);
+            for (int k = tid; k < nv; k += NT) pdst[k] = __ldg(ps + k);
+        }
+    }
+    __syncthreads();
+    const Real* P = STAGE_P ? Ps : Pg;
+
+    double beta;
+    uint32_t sweep0;
+    if (a.use_override) {
+        beta = a.beta_override;
+        sweep0 = a.sweep_override;
+    } else {
+        beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+        sweep0 = a.ctl[0] * (uint32_t)a.ptswapever;
+    }
+    const float kb = (float)(-2.0 * beta * 1.4426950408889634);
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    Acc acc{0, 0, 0, 0, 0};
+
+    for (int t = 0; t < a.nsweeps; ++t) {
+        const uint32_t sweep = sweep0 + (uint32_t)t;
+#pragma unroll 1
+        for (int c = 0; c < 8; ++c) {
+            if constexpr (QUAD) {
+                const int nq = g.Nc >> 2;
+                for (int q = tid; q < nq; q += NT)
+                    quad_step<Real, MASKS, false>(a, g, reinterpret_cast<uint32_t*>(S), P, BM, c,
+                                                  q, sweep, (uint32_t)rep, k0, k1, beta, kb, acc);
+            } else {
+                for (int k = tid; k < g.Nc; k += NT) {
+                    const int X = k % g.Lh, r = k / g.Lh;
+                    const int Y = r % g.Lh, Z = r / g.Lh;
+                    site_step<Real, MASKS, MODE, false>(a, g, S, P, BM, Pf32, c, X, Y, Z, sweep,
+                                                        (uint32_t)rep, k0, k1, beta, kb, acc);
+                }
+            }
+            __syncthreads();
+        }
+    }
+
+    if constexpr (MODE == kModeAudit) {
+        Acc t = block_reduce(acc);
+        if (tid == 0) {
+            atomicAdd(&a.audit[0], (unsigned long long)t.M);
+            atomicAdd(&a.audit[1], (unsigned long long)t.SX);
+        }
+        __syncthreads();
+        acc = Acc{0, 0, 0, 0, 0};
+    }
+
+    // observables of the new configuration (no writes: no barrier between colours)
+#pragma unroll 1
+    for (int c = 0; c < 8; ++c) {
+        if constexpr (QUAD) {
+            const int nq = g.Nc >> 2;
+            for (int q = tid; q < nq; q += NT)
+                quad_step<Real, MASKS, true>(a, g, reinterpret_cast<uint32_t*>(S), P, BM, c, q, 0u,
+                                             0u, 0u, 0u, beta, kb, acc);
+        } else {
+            for (int k = tid; k < g.Nc; k += NT) {
+                const int X = k % g.Lh, r = k / g.Lh;
+                const int Y = r % g.Lh, Z = r / g.Lh;
+                site_step<Real, MASKS, MODE, true>(a, g, S, P, BM, Pf32, c, X, Y, Z, 0u, 0u, 0u,
+                                                   0u, beta, kb, acc);
+            }
+        }
+    }
+    const Acc tot = block_reduce(acc);
+    if (tid == 0) {
+        LatObs o;
+        o.eacc = tot.e;
+        o.M = tot.M;
+        o.SX = tot.SX;
+        o.SY = tot.SY;
+        o.NB = tot.NB;
+        o.pad[0] = o.pad[1] = 0;
+        a.obs[lat] = o;
+    }
+    {  // write the lattice back
+        const uint4* src = reinterpret_cast<const uint4*>(S);
+        uint4* dst = reinterpret_cast<uint4*>(Sg);
+        for (int k = tid; k < Nb / 16; k += NT) dst[k] = src[k];
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// PT swap + per-slot accumulation: one CTA, one warp per conf.
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) swap_kernel(SwapArgs a)
+{
+    const uint32_t cycle = a.ctl[0];
+    const int phase = (int)a.ctl[1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int conf = warp; conf < a.nconf; conf += nw) {
+        const int base = conf * a.nrep;
+        const double dn = (double)a.nocc[conf];
+        const double dn1 = (double)(a.nocc[conf] < 1 ? 1 : a.nocc[conf]);
+        for (int rep = lane; rep < a.nrep; rep += 32) {
+            const LatObs o = a.obs[base + rep];
+            double* lo = a.last_obs + 5 * (base + rep);
+            lo[0] = (double)o.M / dn;
+            lo[1] = __dmul_rn((double)o.eacc, 0x1p-33) / dn;
+            lo[2] = (double)o.SX / dn;
+            lo[3] = (double)o.SY / dn;
+            lo[4] = (double)o.NB / dn1;
+        }
+        __syncwarp();
+        // Pt_attempt_swaps: disjoint pairs (s, s+1), s = phase-1, phase+1, ...
+        for (int s = (phase == 1 ? 0 : 1) + 2 * lane; s < a.nrep - 1; s += 64) {
+            const int rlo = a.rat[base + s], rhi = a.rat[base + s + 1];
+            a.att[base + s] += 1;
+            const double elo = __dmul_rn((double)a.obs[base + rlo].eacc, 0x1p-33);
+            const double ehi = __dmul_rn((double)a.obs[base + rhi].eacc, 0x1p-33);
+            const double delta =
+                __dmul_rn(__dsub_rn(a.beta[base + s], a.beta[base + s + 1]), __dsub_rn(elo, ehi));
+            bool accept = delta >= 0.0;
+            if (!accept) {
+                const U4 r = philox4x32_10(cycle, (uint32_t)s, 0u, kTagSwap, a.seed,
+                                           a.conf_base + (uint32_t)conf);
+                accept = (double)r.x * 0x1p-32 < own_exp(delta);
+            }
+            if (accept) {
+                a.acc[base + s] += 1;
+                a.rat[base + s] = rhi;
+                a.rat[base + s + 1] = rlo;
+                a.tor[base + rlo] = s + 1;
+                a.tor[base + rhi] = s;
+            }
+        }
+        __syncwarp();
+        if (a.measure) {
+            for (int rep = lane; rep < a.nrep; rep += 32) {
+                const int t = a.tor[base + rep];
+                if (t == 0) a.visited[base + rep] |= 1;
+                if (t == a.nrep - 1) a.visited[base + rep] |= 2;
+            }
+            for (int sl = lane; sl < a.nrep; sl += 32) {
+                const double* o = a.last_obs + 5 * (base + a.rat[base + sl]);
+                double* S = a.sums + 22 * (base + sl);
+                const double amag = o[0], aen = o[1], ax = o[2], ay = o[3], anb = o[4];
+                const double x2 = __dmul_rn(ax, ax), y2 = __dmul_rn(ay, ay);
+                const double str2 = __dadd_rn(x2, y2);
+                const double absstr = __dsqrt_rn(str2);
+                const double nem = fabs(__dsub_rn(y2, x2));
+                const double m2 = __dmul_rn(amag, amag), nb2 = __dmul_rn(anb, anb);
+                S[0] = __dadd_rn(S[0], amag);
+                S[1] = __dadd_rn(S[1], fabs(amag));
+                S[2] = __dadd_rn(S[2], m2);
+                S[3] = __dadd_rn(S[3], __dmul_rn(m2, m2));
+                S[4] = __dadd_rn(S[4], aen);
+                S[5] = __dadd_rn(S[5], __dmul_rn(aen, aen));
+                S[6] = __dadd_rn(S[6], fabs(ax));
+                S[7] = __dadd_rn(S[7], fabs(ay));
+                S[8] = __dadd_rn(S[8], x2);
+                S[9] = __dadd_rn(S[9], __dmul_rn(x2, x2));
+                S[10] = __dadd_rn(S[10], y2);
+                S[11] = __dadd_rn(S[11], __dmul_rn(y2, y2));
+                S[12] = __dadd_rn(S[12], str2);
+                S[13] = __dadd_rn(S[13], __dmul_rn(str2, str2));
+                S[14] = __dadd_rn(S[14], absstr);
+                S[15] = __dadd_rn(S[15], nem);
+                S[16] = __dadd_rn(S[16], anb);
+                S[17] = __dadd_rn(S[17], fabs(anb));
+                S[18] = __dadd_rn(S[18], nb2);
+                S[19] = __dadd_rn(S[19], __dmul_rn(nb2, nb2));
+                if (aen < S[20]) S[20] = aen;
+                S[21] = aen;
+                a.nmeas[base + sl] += 1;
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        a.ctl[0] = cycle + 1u;
+        a.ctl[1] = (uint32_t)(3 - phase);
+    }
+}
+
+// HOT (device Philox), FER, STR starts for every replica of one conf; vacancies stored as 0
+__global__ void init_kernel(InitArgs a)
+{
+    const Geo g = a.g;
+    const int rep = (int)blockIdx.y;
+    uint8_t* S = a.spins + (long long)rep * a.lat_stride;
+    for (int i = (int)(blockIdx.x * blockDim.x + threadIdx.x); i < g.N;
+         i += (int)(gridDim.x * blockDim.x)) {
+        const int c = i / g.Nc, k = i - c * g.Nc;
+        const int X = k % g.Lh, r = k / g.Lh;
+        const int Y = r % g.Lh, Z = r / g.Lh;
+        const int x = 2 * X + (c & 1), y = 2 * Y + ((c >> 1) & 1);
+        int s;
+        if (a.start == 0) {
+            const uint32_t grp = (uint32_t)(((c * g.Hh + Z) * g.Lh + Y) * g.Qr + (X >> 2));
+            const uint32_t w =
+                u4_word(philox4x32_10((uint32_t)rep, 0u, grp, kTagInit, a.seed, a.key1), X & 3);
+            s = w < 0x80000000u ? 1 : -1;
+        } else if (a.start == 1) {
+            s = 1;
+        } else {
+            s = (((a.axis == 0) ? y : x) & 1) ? -1 : 1;
+        }
+        S[i] = a.occ[i] ? (uint8_t)(s + 1) : (uint8_t)1;
+    }
+}
+
+template <class Real, bool QUAD, bool STAGE_P, bool MASKS, int MODE>
+cudaError_t do_launch(const SweepArgs& a, int nblocks, int nthreads, size_t smem,
+                      cudaStream_t st, bool prepare)
+{
+    auto k = sweep_kernel<Real, QUAD, STAGE_P, MASKS, MODE>;
+    if (prepare)
+        return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<nblocks, nthreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <class Real, bool QUAD, bool STAGE_P>
+cudaError_t dispatch_masks(const SweepArgs& a, const SweepVariant& v, int nb, int nt, size_t sm,
+                           cudaStream_t st, bool prep)
+{
+    if (v.mode == kModeAudit) {
+        if constexpr (sizeof(Real) == 8 && !QUAD && !STAGE_P) {
+            return v.masks ? do_launch<Real, false, false, true, kModeAudit>(a, nb, nt, sm, st, prep)
+                           : do_launch<Real, false, false, false, kModeAudit>(a, nb, nt, sm, st,
+                                                                              prep);
+        }
+        return cudaErrorInvalidValue;
+    }
+    return v.masks ? do_launch<Real, QUAD, STAGE_P, true, kModeSweep>(a, nb, nt, sm, st, prep)
+                   : do_launch<Real, QUAD, STAGE_P, false, kModeSweep>(a, nb, nt, sm, st, prep);
+}
+
+template <class Real>
+cudaError_t dispatch_shape(const SweepArgs& a, const SweepVariant& v, int nb, int nt, size_t sm,
+                           cudaStream_t st, bool prep)
+{
+    if (v.quad)
+        return v.stage_p ? dispatch_masks<Real, true, true>(a, v, nb, nt, sm, st, prep)
+                         : dispatch_masks<Real, true, false>(a, v, nb, nt, sm, st, prep);
+    return v.stage_p ? dispatch_masks<Real, false, true>(a, v, nb, nt, sm, st, prep)
+                     : dispatch_masks<Real, false, false>(a, v, nb, nt, sm, st, prep);
+}
+
+cudaError_t dispatch(const SweepArgs& a, const SweepVariant& v, int nb, int nt, size_t sm,
+                     cudaStream_t st, bool prep)
+{
+    return v.fp64 ? dispatch_shape<double>(a, v, nb, nt, sm, st, prep)
+                  : dispatch_shape<float>(a, v, nb, nt, sm, st, prep);
+}
+
+}  // namespace
+
+size_t sweep_smem_bytes(const Geo& g, const SweepVariant& v)
+{
+    size_t b = (size_t)((g.N + 15) & ~15);
+    if (v.stage_p) b += (size_t)g.N * (v.fp64 ? 8 : 4);
+    return (b + 15) & ~(size_t)15;
+}
+
+cudaError_t prepare_sweep_variant(const SweepVariant& v, size_t smem)
+{
+    SweepArgs dummy{};
+    return dispatch(dummy, v, 0, 0, smem, nullptr, true);
+}
+
+cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks, int nthreads,
+                         size_t smem, cudaStream_t st)
+{
+    return dispatch(a, v, nblocks, nthreads, smem, st, false);
+}
+
+cudaError_t launch_swap(const SwapArgs& a, cudaStream_t st)
+{
+    int nt = 32 * a.nconf;
+    if (nt > 1024) nt = 1024;
+    swap_kernel<<<1, nt, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init(const InitArgs& a, cudaStream_t st)
+{
+    int bx = (a.g.N + 255) / 256;
+    if (bx > 1024) bx = 1024;
+    dim3 grid((unsigned)bx, (unsigned)a.nrep);
+    init_kernel<<<grid, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace j1j2

@@ -1,0 +1,362 @@
+"""Python host side of libj1j2cuda (ctypes over the C ABI in include/j1j2c.h).
+
+Mirrors the parts of sim/J1J2_6tv.f90 that sit around the GPU hot path: the run parameters
+(J:43-96), the PT SERIAL driver (Initialize_pt_state J:1218-1247, Pt_equilibration_loop
+J:1250-1279, Pt_measurement_loop J:1341-1684) and the LOCAL sampler (J:2122-2474), with the
+sweeps, swaps and running sums executed by the CUDA engine.  There is no CPU fallback: every
+call goes through libj1j2cuda.so and fails loudly when it cannot be loaded.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libj1j2cuda.so")
+
+OK, EINVAL, ECUDA, ETIMEOUT, ENOMEM, ESTATE = 0, -1, -2, -3, -4, -5
+FP64_PLAIN, FP32_BATCHED = 0, 1
+START_HOT, START_FER, START_STR = 0, 1, 2
+AXIS_X, AXIS_Y = 0, 1
+FLAG_NO_GRAPH, FLAG_PROFILE, FLAG_GENERIC = 1, 2, 4
+
+SUM_FIELDS = ("mag", "absmag", "mag2", "mag4", "en", "en2", "strx_abs", "stry_abs", "strx2",
+              "strx4", "stry2", "stry4", "str2", "str4", "absstr", "nem", "nbar", "nbarabs",
+              "nbar2", "nbar4", "best_en", "final_en")
+
+EXPORTS = ("j1j2c_create", "j1j2c_destroy", "j1j2c_last_error", "j1j2c_set_stream",
+           "j1j2c_set_disorder", "j1j2c_set_ladder", "j1j2c_init_spins",
+           "j1j2c_reset_measurements", "j1j2c_run", "j1j2c_metro_sweep_fp64", "j1j2c_audit_fp32",
+           "j1j2c_get_slot_sums", "j1j2c_get_pt_stats", "j1j2c_get_maps", "j1j2c_get_spins",
+           "j1j2c_get_observables", "j1j2c_get_profile", "j1j2c_get_config",
+           "j1j2c_corr_rand_3d", "j1j2c_setup_vacancies", "j1j2c_kiss_spins", "j1j2c_ladder",
+           "j1j2c_version")
+
+
+class J1J2CError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"libj1j2cuda error {code}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [("L", C.c_int32), ("H", C.c_int32), ("J1h", C.c_double), ("J1v", C.c_double),
+                ("J2", C.c_double), ("J3", C.c_double), ("nconf", C.c_int32),
+                ("nreplica", C.c_int32), ("ptswapever", C.c_int32), ("precision", C.c_int32),
+                ("seed", C.c_uint32), ("conf_base", C.c_uint32), ("device", C.c_int32),
+                ("flags", C.c_uint32), ("block_threads", C.c_int32)]
+
+
+class SlotSums(C.Structure):
+    _fields_ = [(f, C.c_double) for f in SUM_FIELDS] + [("nmeasure", C.c_int64)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libj1j2cuda.so (built by build.py); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} not built: run j1j2-public_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        for name in EXPORTS:
+            getattr(L, name)
+        L.j1j2c_last_error.restype = C.c_char_p
+        L.j1j2c_last_error.argtypes = [C.c_void_p]
+        L.j1j2c_version.restype = C.c_char_p
+        L.j1j2c_destroy.restype = None
+        L.j1j2c_destroy.argtypes = [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def _check(ctx, rc):
+    if rc < 0:
+        msg = lib().j1j2c_last_error(ctx)
+        raise J1J2CError(rc, msg.decode() if msg else "")
+    return rc
+
+
+# ------------------------------------------------------------------------------------------------
+# host helpers (no GPU)
+# ------------------------------------------------------------------------------------------------
+def corr_rand_3d(n1, n2, n3, xi, seed, do_uniform=True, max_value=2.0) -> np.ndarray:
+    """make_corr_rand_3d (CR:191-386); returns x[k, j, i] = x(i, j, k), i.e. site order."""
+    out = np.empty(n1 * n2 * n3, np.float64)
+    _check(None, lib().j1j2c_corr_rand_3d(C.c_int32(n1), C.c_int32(n2), C.c_int32(n3),
+                                          C.c_double(xi), C.c_int32(seed),
+                                          C.c_int32(int(do_uniform)), C.c_double(max_value),
+                                          _p(out, C.c_double)))
+    return out.reshape(n3, n2, n1)
+
+
+def setup_vacancies(seed, L, H, pp=0.0, pph=0.0, ppv=0.0, mode=0):
+    """Setup_vacancies (J:1111-1165) after kissinit(seed): (occu, jh, jv, nimp)."""
+    N = L * L * H
+    occu, jh, jv = (np.empty(N, np.int8) for _ in range(3))
+    nimp = _check(None, lib().j1j2c_setup_vacancies(
+        C.c_int32(seed), C.c_int32(L), C.c_int32(H), C.c_double(pp), C.c_double(pph),
+        C.c_double(ppv), C.c_int32(mode), _p(occu, C.c_int8), _p(jh, C.c_int8),
+        _p(jv, C.c_int8)))
+    return occu, jh, jv, nimp
+
+
+def kiss_spins(seed, L, H, start, axis=AXIS_X) -> np.ndarray:
+    """Initialize_spin_array (J:1179-1209) after kissinit(seed)."""
+    s = np.empty(L * L * H, np.int8)
+    _check(None, lib().j1j2c_kiss_spins(C.c_int32(seed), C.c_int32(L), C.c_int32(H),
+                                        C.c_int32(start), C.c_int32(axis), _p(s, C.c_int8)))
+    return s
+
+
+def ladder(n, tmin, tmax, split=False, tmid=9.5, tfrac=0.7) -> np.ndarray:
+    """Setup_temperature_ladder (J:928-962, PT branch)."""
+    t = np.empty(n)
+    _check(None, lib().j1j2c_ladder(C.c_int32(n), C.c_double(tmin), C.c_double(tmax),
+                                    C.c_int32(int(split)), C.c_double(tmid), C.c_double(tfrac),
+                                    _p(t, C.c_double)))
+    return t
+
+
+def disorder(L, H, seed, phi=2.0, xi=3.0, map_uniform=True) -> np.ndarray:
+    """Setup_phi_table (J:590-633): p(site) for disorder seed IRINIT + iconf - 1."""
+    return corr_rand_3d(L, L, H, xi, seed, map_uniform, phi).reshape(-1)
+
+
+# ------------------------------------------------------------------------------------------------
+# engine context
+# ------------------------------------------------------------------------------------------------
+class Engine:
+    """One libj1j2cuda context: nconf disorder configurations x nreplica ladder replicas."""
+
+    def __init__(self, L, H=None, nconf=1, nreplica=1, ptswapever=5, precision=FP32_BATCHED,
+                 seed=1, conf_base=0, J1h=1.0, J1v=1.0, J2=-1.0, J3=1.0, device=0, flags=0,
+                 block_threads=0):
+        H = L if H is None else H
+        self.L, self.H, self.N = int(L), int(H), int(L) * int(L) * int(H)
+        self.nconf, self.nrep, self.ptswapever = int(nconf), int(nreplica), int(ptswapever)
+        self.precision = precision
+        self.params = Params(self.L, self.H, J1h, J1v, J2, J3, self.nconf, self.nrep,
+                             self.ptswapever, precision, seed, conf_base, device, flags,
+                             block_threads)
+        self._ctx = C.c_void_p()
+        _check(None, lib().j1j2c_create(C.byref(self._ctx), C.byref(self.params)))
+        self.nocc = np.full(self.nconf, self.N, np.int64)
+
+    # life cycle --------------------------------------------------------------------------------
+    def close(self):
+        if self._ctx:
+            lib().j1j2c_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def ctx(self):
+        return self._ctx
+
+    def _ck(self, rc):
+        return _check(self._ctx, rc)
+
+    def set_stream(self, stream_ptr):
+        self._ck(lib().j1j2c_set_stream(self._ctx, C.c_void_p(stream_ptr)))
+
+    # inputs ------------------------------------------------------------------------------------
+    def set_disorder(self, conf, p, occu=None, jh=None, jv=None):
+        p = np.ascontiguousarray(p, np.float64).reshape(-1)
+        assert p.size == self.N
+        arrs = [None if a is None else np.ascontiguousarray(a, np.int8).reshape(-1)
+                for a in (occu, jh, jv)]
+        ptrs = [None if a is None else _p(a, C.c_int8) for a in arrs]
+        self._ck(lib().j1j2c_set_disorder(self._ctx, C.c_int32(conf), _p(p, C.c_double), *ptrs))
+        self.nocc[conf] = self.N if arrs[0] is None else int((arrs[0] != 0).sum())
+
+    def set_ladder(self, conf, beta):
+        """beta of one conf (nrep), or of every conf when conf < 0 (nconf x nrep)."""
+        b = np.ascontiguousarray(beta, np.float64)
+        assert b.size == (self.nconf * self.nrep if conf < 0 else self.nrep)
+        self._ck(lib().j1j2c_set_ladder(self._ctx, C.c_int32(conf), _p(b, C.c_double)))
+
+    def init_spins(self, conf, start=START_HOT, axis=AXIS_X, spins=None):
+        if spins is None:
+            self._ck(lib().j1j2c_init_spins(self._ctx, C.c_int32(conf), C.c_int32(start),
+                                            C.c_int32(axis), None))
+        else:
+            s = np.ascontiguousarray(spins, np.int8).reshape(self.nrep, self.N)
+            self._ck(lib().j1j2c_init_spins(self._ctx, C.c_int32(conf), C.c_int32(start),
+                                            C.c_int32(axis), _p(s, C.c_int8)))
+
+    def reset_measurements(self, conf=-1):
+        self._ck(lib().j1j2c_reset_measurements(self._ctx, C.c_int32(conf)))
+
+    # hot path ----------------------------------------------------------------------------------
+    def run(self, ncycles, measure=True, restart_swap_phase=True):
+        self._ck(lib().j1j2c_run(self._ctx, C.c_int32(ncycles), C.c_int32(int(measure)),
+                                 C.c_int32(int(restart_swap_phase))))
+
+    def metro_sweep_fp64(self, conf, rep, beta, sweep_index, nsweeps=1):
+        out = [C.c_double() for _ in range(4)]
+        self._ck(lib().j1j2c_metro_sweep_fp64(self._ctx, C.c_int32(conf), C.c_int32(rep),
+                                              C.c_double(beta), C.c_uint32(sweep_index),
+                                              C.c_int32(nsweeps), *[C.byref(o) for o in out]))
+        return tuple(o.value for o in out)
+
+    def audit_fp32(self, nsweeps):
+        att, mis = C.c_int64(0), C.c_int64(0)
+        self._ck(lib().j1j2c_audit_fp32(self._ctx, C.c_int32(nsweeps), C.byref(att),
+                                        C.byref(mis)))
+        return att.value, mis.value
+
+    # outputs -----------------------------------------------------------------------------------
+    def slot_sums(self, conf):
+        """(nrep, 22) running sums in SUM_FIELDS order and the (nrep,) measurement counts;
+        conf < 0 returns every conf, (nconf*nrep, 22) and (nconf*nrep,)."""
+        n = self.nrep * (self.nconf if conf < 0 else 1)
+        raw = np.zeros(n, dtype=np.dtype([("s", np.float64, 22), ("n", np.int64)]))
+        self._ck(lib().j1j2c_get_slot_sums(self._ctx, C.c_int32(conf),
+                                           raw.ctypes.data_as(C.c_void_p)))
+        return raw["s"].copy(), raw["n"].copy()
+
+    def pt_stats(self, conf):
+        n = max(self.nrep - 1, 1)
+        att, acc = np.zeros(n, np.int64), np.zeros(n, np.int64)
+        vb = C.c_int32()
+        self._ck(lib().j1j2c_get_pt_stats(self._ctx, C.c_int32(conf), _p(att, C.c_int64),
+                                          _p(acc, C.c_int64), C.byref(vb)))
+        return att[:self.nrep - 1], acc[:self.nrep - 1], vb.value
+
+    def maps(self, conf):
+        rat, tor = np.empty(self.nrep, np.int32), np.empty(self.nrep, np.int32)
+        self._ck(lib().j1j2c_get_maps(self._ctx, C.c_int32(conf), _p(rat, C.c_int32),
+                                      _p(tor, C.c_int32)))
+        return rat, tor
+
+    def spins(self, conf, rep):
+        s = np.empty(self.N, np.int8)
+        self._ck(lib().j1j2c_get_spins(self._ctx, C.c_int32(conf), C.c_int32(rep),
+                                       _p(s, C.c_int8)))
+        return s
+
+    def observables(self, conf):
+        out = np.empty((self.nrep * (self.nconf if conf < 0 else 1), 5))
+        self._ck(lib().j1j2c_get_observables(self._ctx, C.c_int32(conf), _p(out, C.c_double)))
+        return out
+
+    def profile(self):
+        ms, n, att = C.c_double(), C.c_int64(), C.c_int64()
+        self._ck(lib().j1j2c_get_profile(self._ctx, C.byref(ms), C.byref(n), C.byref(att)))
+        return ms.value, n.value, att.value
+
+    def config(self):
+        bt, spt, sm = C.c_int32(), C.c_int32(), C.c_int32()
+        self._ck(lib().j1j2c_get_config(self._ctx, C.byref(bt), C.byref(spt), C.byref(sm)))
+        return dict(block_threads=bt.value, sites_per_thread=spt.value, smem_bytes=sm.value)
+
+
+# ------------------------------------------------------------------------------------------------
+# PT driver around the engine (Pt_measurement_loop finalisation, J:1542-1684)
+# ------------------------------------------------------------------------------------------------
+@dataclass
+class SlotResult:
+    T: np.ndarray
+    mag: np.ndarray
+    absmag: np.ndarray
+    mag2: np.ndarray
+    mag4: np.ndarray
+    en: np.ndarray
+    en2: np.ndarray
+    strx: np.ndarray
+    stry: np.ndarray
+    absstr: np.ndarray
+    nem: np.ndarray
+    nbar: np.ndarray
+    nbarabs: np.ndarray
+    nbar2: np.ndarray
+    nbar4: np.ndarray
+    susc: np.ndarray
+    suscstr: np.ndarray
+    UL: np.ndarray
+    US: np.ndarray
+    USX: np.ndarray
+    USY: np.ndarray
+    UBN: np.ndarray
+    sph: np.ndarray
+    stripediff: np.ndarray
+    best_en: np.ndarray
+    final_en: np.ndarray
+
+
+def finalize_slots(sums, nmeas, beta, nocc) -> SlotResult:
+    """Per-slot thermal averages and derived quantities of one conf (J:1542-1600)."""
+    s = np.asarray(sums, np.float64)
+    n = np.maximum(np.asarray(nmeas, np.float64), 1.0)
+    avg = s[:, :20] / n[:, None]
+    mag = np.abs(s[:, 0]) / n
+    absmag, mag2, mag4, en, en2 = avg[:, 1], avg[:, 2], avg[:, 3], avg[:, 4], avg[:, 5]
+    strx, stry, strx2, strx4, stry2, stry4 = (avg[:, k] for k in range(6, 12))
+    str2, str4, absstr, nem = avg[:, 12], avg[:, 13], avg[:, 14], avg[:, 15]
+    nbar, nbarabs, nbar2, nbar4 = avg[:, 16], avg[:, 17], avg[:, 18], avg[:, 19]
+    beta = np.asarray(beta, np.float64)
+
+    def binder(m4, m2, a=1.0, b=3.0):
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return np.where(m2 > 0, a - m4 / (b * m2 ** 2), 0.0)
+
+    return SlotResult(
+        T=1.0 / beta, mag=mag, absmag=absmag, mag2=mag2, mag4=mag4, en=en, en2=en2, strx=strx,
+        stry=stry, absstr=absstr, nem=nem, nbar=nbar, nbarabs=nbarabs, nbar2=nbar2, nbar4=nbar4,
+        susc=(mag2 - absmag ** 2) * nocc * beta, suscstr=(str2 - absstr ** 2) * nocc * beta,
+        UL=binder(mag4, mag2), US=np.where(str2 > 0, 2.0 - str4 / np.where(str2 > 0, str2, 1) ** 2,
+                                            0.0),
+        USX=binder(strx4, strx2), USY=binder(stry4, stry2), UBN=binder(nbar4, nbar2),
+        sph=(en2 - en ** 2) * nocc * beta ** 2, stripediff=strx ** 2 - stry ** 2,
+        best_en=s[:, 20], final_en=s[:, 21])
+
+
+def pt_run(L, betas, nconf=1, neq=100, nmess=100, ptswapever=5, irinit=1, start=START_HOT,
+           axis=AXIS_X, phi=2.0, xi=3.0, pp=0.0, precision=FP32_BATCHED, H=None, engine=None):
+    """PT SERIAL over nconf disorder configurations resident together on the GPU.
+
+    Disorder seed of conf k is IRINIT + k (J:317, J:611); vacancies as Setup_vacancies.
+    Returns (engine, [SlotResult per conf], [pt stats per conf])."""
+    H = L if H is None else H
+    nrep = len(betas)
+    eng = engine or Engine(L, H, nconf=nconf, nreplica=nrep, ptswapever=ptswapever,
+                           precision=precision, seed=irinit)
+    for k in range(nconf):
+        seed = irinit + k
+        occu = None
+        if pp > 0.0:
+            occu, _, _, _ = setup_vacancies(seed, L, H, pp)
+        eng.set_disorder(k, disorder(L, H, seed, phi, xi), occu)
+        eng.set_ladder(k, betas)
+        eng.init_spins(k, start, axis)
+    eng.reset_measurements()
+    eng.run(neq, measure=False, restart_swap_phase=True)
+    eng.reset_measurements()
+    eng.run(nmess, measure=True, restart_swap_phase=True)
+    results, stats = [], []
+    for k in range(nconf):
+        sums, nm = eng.slot_sums(k)
+        results.append(finalize_slots(sums, nm, betas, eng.nocc[k]))
+        stats.append(eng.pt_stats(k))
+    return eng, results, stats

@@ -1,0 +1,179 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the oracle.
+
+* FP64 form: spins, observables, slot maps, swap counters and running sums bit-identical to the
+  oracle's replay of the same colour order, Philox stream, exponential and fixed-point energy.
+* FP32 form: per-site path == quad path bit for bit; decision mismatch rate against FP64 in
+  deterministic replay; observables within statistical error of the FP64 form.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SEED = 1
+
+
+def _betas(nrep, tmin=8.0, tmax=11.5):
+    from oracle import oracle as O
+    return 1.0 / O.ladder(nrep, tmin, tmax)
+
+
+def _setup(jc, O, L, H, nconf, nrep, precision, pp=0.0, bonds=0.0, flags=0, start=0, axis=0,
+           seed=SEED, conf_base=0, ptswapever=5, betas=None):
+    eng = jc.Engine(L, H, nconf=nconf, nreplica=nrep, ptswapever=ptswapever, precision=precision,
+                    seed=seed, conf_base=conf_base, flags=flags)
+    betas = _betas(nrep) if betas is None else betas
+    models = []
+    for k in range(nconf):
+        p = jc.disorder(L, H, seed + k)
+        occu, jh, jv, _ = jc.setup_vacancies(seed + k, L, H, pp, bonds, bonds)
+        eng.set_disorder(k, p, occu, jh if bonds > 0 else None, jv if bonds > 0 else None)
+        eng.set_ladder(k, betas)
+        eng.init_spins(k, start, axis)
+        models.append(O.Model(L, H, p, occu, jh, jv))
+    eng.reset_measurements()
+    return eng, models, betas
+
+
+@pytest.mark.parametrize("L,H", [(8, 4), (10, 10), (4, 2), (16, 6)])
+def test_hot_start_is_the_philox_stream(engine_mod, oracle, L, H):
+    eng, models, _ = _setup(engine_mod, oracle, L, H, 2, 3, engine_mod.FP64_PLAIN, pp=0.1,
+                            conf_base=5)
+    for k in range(2):
+        for r in range(3):
+            exp = oracle.hot_spins_philox(L, H, SEED, 5 + k, r) * models[k].occu
+            np.testing.assert_array_equal(eng.spins(k, r), exp)
+    eng.close()
+
+
+@pytest.mark.parametrize("L,H,pp,bonds,flags", [
+    (16, 16, 0.0, 0.0, 0),      # quad path
+    (8, 4, 0.1, 0.2, 0),        # quad path, vacancies and diluted bonds
+    (10, 10, 0.0, 0.0, 0),      # per-site path (L/2 odd)
+    (4, 2, 0.0, 0.0, 0),        # per-site path, doubled J3 and x/y slots (H = 2)
+    (12, 6, 0.05, 0.1, 0),      # per-site path with dilution
+    (16, 8, 0.05, 0.0, 4),      # per-site path forced on a quad-capable shape
+    (24, 24, 0.0, 0.0, 0),      # config-2 lattice
+])
+def test_fp64_sweep_bit_identical_to_replay(engine_mod, oracle, L, H, pp, bonds, flags):
+    jc = engine_mod
+    eng, models, _ = _setup(jc, oracle, L, H, 2, 2, jc.FP64_PLAIN, pp=pp, bonds=bonds,
+                            flags=flags)
+    for conf in range(2):
+        M = models[conf]
+        for rep, beta, sweep0, nsw in [(0, 0.11, 37, 3), (1, 0.09, 0, 1), (0, 0.125, 1000, 4)]:
+            s = eng.spins(conf, rep).copy()
+            got = eng.metro_sweep_fp64(conf, rep, beta, sweep0, nsw)
+            flips = M.replay_sweeps(s, beta, SEED, conf, rep, sweep0, nsw)
+            assert flips > 0
+            np.testing.assert_array_equal(eng.spins(conf, rep), s)
+            ints, acc, obs = M.replay_measure(s)
+            assert got == (obs[0], obs[1], obs[2], obs[3])
+            ref = M.measurement(s)  # the reference's own Measurement of the same configuration
+            assert got[0] == ref[0] and got[2] == ref[2] and got[3] == ref[3]
+            assert abs(got[1] - ref[1]) < 1e-12
+    eng.close()
+
+
+@pytest.mark.parametrize("L,H,nconf,nrep,pp,flags", [
+    (8, 4, 2, 4, 0.0, 0),
+    (8, 8, 3, 5, 0.08, 0),
+    (10, 4, 2, 4, 0.0, 0),
+    (8, 4, 2, 4, 0.0, 1),   # direct launches instead of the CUDA graph
+    (16, 4, 1, 1, 0.0, 0),  # LOCAL sampler: one replica, no swaps
+])
+def test_fp64_pt_run_bit_identical_to_replay(engine_mod, oracle, L, H, nconf, nrep, pp, flags):
+    jc = engine_mod
+    eng, models, betas = _setup(jc, oracle, L, H, nconf, nrep, jc.FP64_PLAIN, pp=pp, flags=flags)
+    states = []
+    for k in range(nconf):
+        spins = np.stack([eng.spins(k, r) for r in range(nrep)])
+        states.append(oracle.new_pt_state(spins))
+    neq, nmess = 7, 12
+    eng.run(neq, measure=False, restart_swap_phase=True)
+    eng.reset_measurements()
+    eng.run(nmess, measure=True, restart_swap_phase=True)
+    for k in range(nconf):
+        st, M = states[k], models[k]
+        M.replay_pt(st, betas, 5, neq, 0, SEED, k, False, 1)
+        obs = M.replay_pt(st, betas, 5, nmess, neq, SEED, k, True, 1)
+        rat, tor = eng.maps(k)
+        np.testing.assert_array_equal(rat, st["rep_at_temp"])
+        np.testing.assert_array_equal(tor, st["temp_of_rep"])
+        for r in range(nrep):
+            np.testing.assert_array_equal(eng.spins(k, r), st["spins"][r])
+        sums, nm = eng.slot_sums(k)
+        np.testing.assert_array_equal(nm, st["nmeas"])
+        np.testing.assert_array_equal(sums, st["sums"])
+        att, acc, vb = eng.pt_stats(k)
+        np.testing.assert_array_equal(att, st["attempts"][:nrep - 1])
+        np.testing.assert_array_equal(acc, st["accepts"][:nrep - 1])
+        assert vb == int(np.sum(st["visited"] == 3))
+        np.testing.assert_array_equal(eng.observables(k), obs)
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_quad_and_per_site_paths_agree_bitwise(engine_mod, oracle, precision):
+    jc = engine_mod
+    runs = []
+    for flags in (0, jc.FLAG_GENERIC):
+        eng, _, _ = _setup(jc, oracle, 16, 8, 2, 4, precision, pp=0.05, bonds=0.1, flags=flags)
+        assert eng.config()["sites_per_thread"] == (1 if flags else 4)
+        eng.run(10, measure=True)
+        runs.append(([eng.spins(k, r) for k in range(2) for r in range(4)],
+                     [eng.slot_sums(k)[0] for k in range(2)]))
+        eng.close()
+    for a, b in zip(runs[0][0], runs[1][0]):
+        np.testing.assert_array_equal(a, b)
+    for a, b in zip(runs[0][1], runs[1][1]):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_fp32_decision_mismatch_rate(engine_mod, oracle):
+    jc = engine_mod
+    eng, _, _ = _setup(jc, oracle, 16, 16, 4, 8, jc.FP32_BATCHED)
+    eng.run(20, measure=False)
+    att, mis = eng.audit_fp32(20)
+    assert att == 4 * 8 * 16 ** 3 * 20
+    rate = mis / att
+    print(f"FP32 vs FP64 flip-decision mismatch rate: {rate:.3e} ({mis}/{att})")
+    assert rate < 1e-4
+    eng.close()
+
+
+def test_fp32_observables_match_fp64(engine_mod, oracle):
+    """Same disorder and streams: per-conf thermal averages of FP32 and FP64 differ only by
+    statistical noise (the two trajectories decorrelate after the first flipped decision)."""
+    jc = engine_mod
+    nconf, nrep, L = 24, 6, 8
+    res = {}
+    for prec in (jc.FP64_PLAIN, jc.FP32_BATCHED):
+        eng, _, betas = _setup(jc, oracle, L, L, nconf, nrep, prec)
+        eng.run(300, measure=False)
+        eng.reset_measurements()
+        eng.run(1500, measure=True)
+        res[prec] = np.array([eng.slot_sums(k)[0][:, 4] / 1500 for k in range(nconf)])
+        eng.close()
+    d = res[jc.FP32_BATCHED] - res[jc.FP64_PLAIN]
+    se = d.std(axis=0, ddof=1) / np.sqrt(nconf)
+    assert (np.abs(d.mean(axis=0)) < 5 * se + 1e-12).all(), (d.mean(axis=0), se)
+
+
+def test_invalid_calls_fail_cleanly(engine_mod, oracle):
+    jc = engine_mod
+    eng = jc.Engine(8, 4, nconf=2, nreplica=3, precision=jc.FP32_BATCHED)
+    with pytest.raises(jc.J1J2CError) as e:
+        eng.run(1)
+    assert e.value.code == jc.ESTATE
+    with pytest.raises(jc.J1J2CError):
+        eng.set_disorder(5, np.zeros(8 * 8 * 4))
+    with pytest.raises(jc.J1J2CError) as e:
+        eng.init_spins(0)
+    assert e.value.code == jc.ESTATE
+    eng.set_disorder(0, np.zeros(8 * 8 * 4))
+    with pytest.raises(jc.J1J2CError):
+        eng.init_spins(0, spins=np.zeros((3, 256), np.int8))
+    with pytest.raises(jc.J1J2CError):
+        eng.set_ladder(0, np.array([1.0, np.nan, 2.0]))
+    eng.close()

@@ -1,0 +1,194 @@
+"""CPU tests of the oracle: pinned against the committed golden vectors (Ooura-FFT reference build,
+Random123 known answers) and against identities of the reference arithmetic."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_philox_known_answers(oracle):
+    for kat in json.load(open(os.path.join(GOLDEN, "philox_kat.json"))):
+        out = oracle.philox(kat["ctr"], kat["key"])
+        assert [int(v) for v in out] == kat["out"]
+
+
+def test_own_exp_accuracy(oracle):
+    rng = np.random.default_rng(3)
+    xs = np.concatenate([rng.uniform(-745, 709, 20000), rng.uniform(-30, 5, 20000),
+                         [0.0, -0.0, 1e-300, -1e-300, 1.0, -1.0, 700.0, -700.0, -744.0]])
+    for x in xs:
+        ref = math.exp(x)
+        got = oracle.dexp(float(x))
+        if ref == 0.0 or ref < 2.3e-308:
+            assert abs(got - ref) <= 5e-324 * 4
+        else:
+            assert abs(got - ref) <= 1.5 * math.ulp(ref), (x, got, ref)
+    assert oracle.dexp(-800.0) == 0.0
+    assert math.isinf(oracle.dexp(800.0))
+
+
+def _golden_corr():
+    g = np.load(os.path.join(GOLDEN, "corr3d_golden.npz"))
+    cases = {}
+    for k in g.files:
+        name, part = k.split("__")
+        cases.setdefault(name, {})[part] = g[k]
+    for name, d in cases.items():
+        dims, xi, s, u, m = name.split("_")
+        n1, n2, n3 = (int(v) for v in dims[1:].split("x"))
+        yield (n1, n2, n3, float(xi[2:]), int(s[1:]), bool(int(u[1:])), float(m[1:])), d
+
+
+def test_corr3d_restatement_matches_ooura_golden(oracle):
+    from oracle import corr3d
+    n = 0
+    for (n1, n2, n3, xi, seed, uni, mx), d in _golden_corr():
+        x = corr3d.make_corr_rand_3d(n1, n2, n3, xi, seed, uni, mx).reshape(-1)
+        stride = int(d["stride"][0])
+        np.testing.assert_allclose(x[::stride], d["values"], rtol=0, atol=1e-12)
+        np.testing.assert_allclose([x.sum(), (x * x).sum()], d["sum"], rtol=1e-12, atol=1e-9)
+        n += 1
+    assert n >= 5
+
+
+def test_corr3d_uniform_marginal_and_correlation(oracle):
+    from oracle import corr3d
+    x = corr3d.make_corr_rand_3d(32, 32, 32, 3.0, 11, True, 2.0)
+    assert x.min() >= -2.0 and x.max() <= 2.0
+    assert abs(x.mean()) < 0.3
+    # uniform on [-2, 2] has variance 4/3 (sample variance is lower because of correlations)
+    assert 0.7 < x.var() < 1.45
+    g = corr3d.make_corr_rand_3d(32, 32, 32, 3.0, 11, False)
+    c1 = np.mean(g * np.roll(g, 1, axis=2)) / np.mean(g * g)
+    c4 = np.mean(g * np.roll(g, 4, axis=2)) / np.mean(g * g)
+    assert c1 > c4 > 0.0
+
+
+def test_kiss_uniform_and_seeding(oracle):
+    u = oracle.kiss_draw(1, 200000)
+    assert u.min() >= 0.0 and u.max() < 1.0
+    assert abs(u.mean() - 0.5) < 0.005
+    assert not np.array_equal(oracle.kiss_draw(1, 16), oracle.kiss_draw(2, 16))
+    np.testing.assert_array_equal(oracle.kiss_draw(7, 16), oracle.kiss_draw(7, 16))
+    g = oracle.gkiss_fill(5, 100000)
+    assert abs(g.mean()) < 0.02 and abs(g.std() - 1.0) < 0.02
+
+
+def test_neighbor_table_semantics(oracle):
+    L, H = 6, 4
+    m = oracle.neighbors(L, H).reshape(10, -1)
+    for i in range(L * L * H):
+        x, y, z = i % L, (i // L) % L, i // (L * L)
+
+        def site(dx, dy, dz):
+            return (x + dx) % L + L * ((y + dy) % L) + L * L * ((z + dz) % H)
+
+        exp = [site(0, 1, 0), site(0, -1, 0), site(1, 0, 0), site(-1, 0, 0), site(1, 1, 0),
+               site(-1, 1, 0), site(1, -1, 0), site(-1, -1, 0), site(0, 0, 1), site(0, 0, -1)]
+        assert list(m[:, i]) == exp
+
+
+def _model(oracle, L=6, H=4, seed=3, pp=0.0, bonds=0.0):
+    from oracle import corr3d
+    p = corr3d.make_corr_rand_3d(L, L, H, 3.0, seed).reshape(-1)
+    occu, jh, jv, _ = oracle.setup_vacancies(seed, L, H, pp, bonds, bonds)
+    return oracle.Model(L, H, p, occu, jh, jv)
+
+
+def _bond_energy(M, s):
+    """E_total = -sum over bonds of J_eff s_i s_j, bonds counted once (J:2498-2541)."""
+    L, H, N = M.L, M.H, M.N
+    m = M.m.reshape(10, N)
+    occ = M.occu.astype(np.int64)
+    ss = s.astype(np.float64) * occ
+    J1h, J1v, J2, J3 = M.J
+    E = 0.0
+    for i in range(N):
+        if not occ[i]:
+            continue
+        j = m[2, i]  # +x bond owned by i
+        E -= (J1h * M.jh[i] + M.p[i] + M.p[j]) * ss[i] * ss[j]
+        j = m[0, i]  # +y bond owned by i
+        E -= (J1v * M.jv[i] - M.p[i] - M.p[j]) * ss[i] * ss[j]
+        E -= J2 * ss[i] * (ss[m[4, i]] + ss[m[5, i]])  # (+x,+y) and (-x,+y)
+        E -= J3 * ss[i] * ss[m[8, i]]
+    return E
+
+
+@pytest.mark.parametrize("pp,bonds", [(0.0, 0.0), (0.1, 0.0), (0.1, 0.2)])
+def test_energy_identity(oracle, pp, bonds):
+    M = _model(oracle, pp=pp, bonds=bonds)
+    s = oracle.init_spins(9, M.L, M.H, 0)
+    obs = M.measurement(s)
+    nocc = M.N - M.nimp
+    np.testing.assert_allclose(obs[1] * nocc, _bond_energy(M, s), rtol=1e-12, atol=1e-10)
+    # the engine's fixed-point energy equals the FP64 sum to ~1e-9 absolute
+    ints, acc, o5 = M.replay_measure(s)
+    np.testing.assert_allclose(acc * 2.0 ** -33, obs[1] * nocc, rtol=0, atol=1e-6)
+    assert o5[0] == obs[0] and o5[2] == obs[2] and o5[3] == obs[3]
+    assert o5[4] == M.nbar(s)
+
+
+def test_metro_sweep_incremental_observables(oracle):
+    M = _model(oracle, pp=0.05)
+    s = oracle.init_spins(4, M.L, M.H, 0)
+    obs = M.measurement(s)
+    st = oracle.kiss_state(123)
+    for _ in range(20):
+        M.metro_sweep(s, 0.11, obs, st)
+    np.testing.assert_allclose(obs, M.measurement(s), rtol=0, atol=1e-10)
+    M.metro_sweep(s, 0.11, obs, st, rnd=True)
+    np.testing.assert_allclose(obs, M.measurement(s), rtol=0, atol=1e-10)
+
+
+def test_replay_colour_order_is_race_free(oracle):
+    """Within a colour no site neighbours another: updating a colour in reversed order gives the
+    same configuration as the forward order (checked by replaying with a permuted lattice)."""
+    M = _model(oracle, L=8, H=4)
+    s = oracle.hot_spins_philox(M.L, M.H, 1, 0, 0)
+    m = M.m.reshape(10, M.N)
+    col = np.array([(i % 8 & 1) | ((i // 8 % 8) & 1) << 1 | ((i // 64) & 1) << 2
+                    for i in range(M.N)])
+    assert all((col[m[k]] != col).all() for k in range(10))
+    s1 = s.copy()
+    f1 = M.replay_sweeps(s1, 0.12, 1, 0, 0, 0, 3)
+    s2 = s.copy()
+    f2 = M.replay_sweeps(s2, 0.12, 1, 0, 0, 0, 3)
+    assert f1 == f2 and np.array_equal(s1, s2) and f1 > 0
+
+
+def test_replay_pt_bookkeeping(oracle):
+    M = _model(oracle, L=8, H=4)
+    nrep = 4
+    betas = 1.0 / oracle.ladder(nrep, 8.0, 11.5)
+    spins = np.stack([oracle.hot_spins_philox(8, 4, 1, 0, r) for r in range(nrep)])
+    st = oracle.new_pt_state(spins)
+    M.replay_pt(st, betas, 5, 30, 0, 1, 0, True, 1)
+    assert sorted(st["rep_at_temp"]) == list(range(nrep))
+    assert all(st["temp_of_rep"][st["rep_at_temp"][k]] == k for k in range(nrep))
+    assert (st["nmeas"] == 30).all()
+    assert st["attempts"][0] == 15 and st["attempts"][1] == 15 and st["attempts"][2] == 15
+    assert (st["accepts"][:3] <= st["attempts"][:3]).all()
+
+
+def test_pt_serial_reference_runs(oracle):
+    M = _model(oracle, L=6, H=4)
+    betas = 1.0 / oracle.ladder(4, 8.0, 11.5)
+    r = M.pt_serial(betas, 5, 20, 40, 1, 1, 0, 0)
+    sums = r["sums"]
+    assert sums.shape == (4, 22)
+    en = sums[:, 4] / 40
+    assert (np.diff(en) > -0.5).all()  # energy rises with T (within noise)
+    assert (r["attempts"] == 30).all()  # swaps are counted in both loops (J:1224, J:1312)
+    assert sorted(r["rep_at_temp"]) == list(range(4))
+
+
+def test_ladder(oracle):
+    t = oracle.ladder(16, 8.0, 11.5)
+    np.testing.assert_allclose(t, 8.0 + 3.5 * np.arange(16) / 15, rtol=0, atol=1e-15)
+    ts = oracle.ladder(11, 8.0, 11.5, split=True, tmid=9.5, tfrac=0.7)
+    assert ts[0] == 8.0 and ts[-1] == 11.5 and ts[7] == 9.5
