@@ -124,6 +124,7 @@ def time_steps(torch, eng, steps, warmup, flush):
     eng.set_stream(stream.cuda_stream)
     eng.run(warmup, measure=True, restart_swap_phase=True)
     torch.cuda.synchronize()
+    prof0 = eng.profile()[0]
     total_ms = 0.0
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(steps)]
@@ -135,7 +136,7 @@ def time_steps(torch, eng, steps, warmup, flush):
     torch.cuda.synchronize()
     for a, b in ev:
         total_ms += a.elapsed_time(b)
-    return total_ms
+    return total_ms, eng.profile()[0] - prof0
 
 
 def run_ours(args):
@@ -162,16 +163,14 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     with Clocks(local) as clk:
-        ms0 = eng.profile()[0]
-        total_ms = time_steps(torch, eng, args.steps, args.warmup, flush)
-        prof_ms, prof_n, _ = eng.profile()
+        total_ms, prof_ms = time_steps(torch, eng, args.steps, args.warmup, flush)
     torch.cuda.synchronize()
     if ws > 1:
         t = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
         dist.barrier()
-    sweep_ms_avg = (prof_ms - ms0) / max(args.steps, 1)  # sweep kernel, per launch (timed steps)
+    sweep_ms_avg = prof_ms / max(args.steps, 1)  # sweep kernel, per launch (timed steps)
     value = attempts_per_step * args.steps * ws / (total_ms * 1e6)
 
     # end to end through the public API with host buffers: ladder H2D, one cycle, all running
@@ -200,7 +199,7 @@ def run_ours(args):
     w64 = WORKLOADS["plain_fp64_L24_1x16"]
     eng64, _ = make_engine(jc, w64, local)
     s64 = max(4, args.steps // 4)
-    ms64 = time_steps(torch, eng64, s64, 2, flush)
+    ms64, _ = time_steps(torch, eng64, s64, 3, flush)
     fp64_val = int(eng64.nocc.sum()) * w64["nrep"] * 5 * s64 / (ms64 * 1e6)
     eng64.close()
 

@@ -47,6 +47,7 @@ extern "C" {
 #define J1J2C_FLAG_NO_GRAPH 1u   /* launch kernels directly instead of replaying a CUDA graph     */
 #define J1J2C_FLAG_PROFILE 2u    /* time every sweep launch with CUDA events (j1j2c_get_profile)  */
 #define J1J2C_FLAG_GENERIC 4u    /* force the per-site kernel path (testing)                      */
+#define J1J2C_FLAG_NO_FIXED 8u   /* skip the shape-specialised kernels (testing)                  */
 
 /* Run parameters: the compile-time constants of J:43-96 that the hot path consumes. */
 typedef struct {

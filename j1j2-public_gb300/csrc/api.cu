@@ -6,7 +6,10 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/j1j2c.h"
@@ -56,6 +59,7 @@ struct Ctx {
     size_t smem = 0;
     long long occ_total = 0;
 
+    bool tuned = false;
     bool profile = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double prof_ms = 0.0;
@@ -111,18 +115,50 @@ void release(Ctx* c)
     if (c->own) cudaStreamDestroy(c->own);
 }
 
-// Kernel shape for the context's lattices: quad path when L/2 is a multiple of 4, random field
-// staged in shared memory when it fits next to the spins.
+size_t smem_budget(Ctx* c)
+{
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->P.device) !=
+        cudaSuccess)
+        return 0;
+    return (size_t)optin - 2048;  // static shared memory of the reduction
+}
+
+// Kernel shape for the context's lattices: the shape-specialised kernel when one exists for
+// (precision, L, H) and no bond is diluted (its CTA size autotuned at the first run unless
+// block_threads names one), else the generic quad path when L/2 is a multiple of 4, else the
+// per-site path; the random field is staged in shared memory when it fits next to the spins.
 int choose_variant(Ctx* c, bool fp64, SweepVariant& v, size_t& smem, int& nthreads)
 {
-    int dev = c->P.device, optin = 0;
-    CK(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const size_t budget = (size_t)optin - 2048;  // static shared memory of the reduction
+    const size_t budget = smem_budget(c);
+    if (budget == 0) return fail(c, J1J2C_ECUDA, "cannot query the shared-memory limit");
     v = SweepVariant{};
     v.fp64 = fp64;
-    v.quad = (c->g.Lh % 4 == 0) && !(c->P.flags & J1J2C_FLAG_GENERIC);
     v.masks = c->masks;
     v.mode = kModeSweep;
+    if (!(c->P.flags & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED))) {
+        int nts[8];
+        bool sp[8];
+        const int n = fixed_candidates(fp64, c->g.L, c->g.H, c->masks, nts, sp, 8);
+        int pick = n > 0 ? 0 : -1;
+        for (int k = 0; k < n; ++k)
+            if (nts[k] == c->P.block_threads) pick = k;
+        if (pick >= 0) {
+            v.fixed_nt = nts[pick];
+            v.quad = true;
+            v.stage_p = sp[pick];
+            smem = sweep_smem_bytes(c->g, v);
+            if (smem <= budget) {
+                nthreads = nts[pick];
+                SweepArgs none{};
+                none.g = c->g;
+                CK(c, launch_fixed(none, fp64, nthreads, 0, smem, nullptr, true));
+                return J1J2C_OK;
+            }
+            v.fixed_nt = 0;
+        }
+    }
+    v.quad = (c->g.Lh % 4 == 0) && !(c->P.flags & J1J2C_FLAG_GENERIC);
     v.stage_p = true;
     smem = sweep_smem_bytes(c->g, v);
     if (smem > budget) {
@@ -206,9 +242,13 @@ cudaError_t enqueue_cycle(Ctx* c, int measure, cudaStream_t st)
 {
     SweepArgs a = base_args(c);
     cudaError_t e;
-    if (c->profile && (e = cudaEventRecord(c->ev0, st)) != cudaSuccess) return e;
+    if (c->profile && (e = cudaEventRecordWithFlags(c->ev0, st, cudaEventRecordExternal)) !=
+                           cudaSuccess)
+        return e;
     if ((e = launch_sweep(a, c->var, c->nlat, c->nthreads, c->smem, st)) != cudaSuccess) return e;
-    if (c->profile && (e = cudaEventRecord(c->ev1, st)) != cudaSuccess) return e;
+    if (c->profile && (e = cudaEventRecordWithFlags(c->ev1, st, cudaEventRecordExternal)) !=
+                           cudaSuccess)
+        return e;
     return launch_swap(swap_args(c, measure), st);
 }
 
@@ -230,6 +270,88 @@ int build_graph(Ctx* c, int measure)
 }
 
 bool valid_conf(Ctx* c, int conf) { return conf >= 0 && conf < c->nconf; }
+
+// Autotuner: times every CTA size of the shape-specialised kernel on a scratch copy of the
+// context's lattices (the live state is not touched) and keeps the fastest.  Choices are cached
+// per (precision, L, H, lattice count) for the life of the process.
+std::mutex g_tune_mu;
+std::map<std::tuple<bool, int, int, int>, int> g_tune_cache;
+
+int autotune(Ctx* c)
+{
+    if (c->tuned) return J1J2C_OK;
+    c->tuned = true;
+    if (c->var.fixed_nt == 0 || c->P.block_threads > 0) return J1J2C_OK;
+    int nts[8];
+    bool sp[8];
+    const int n = fixed_candidates(c->var.fp64, c->g.L, c->g.H, c->masks, nts, sp, 8);
+    if (n <= 1) return J1J2C_OK;
+    const auto key = std::make_tuple(c->var.fp64, c->g.L, c->g.H, c->nlat);
+    int best_nt = 0;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) best_nt = it->second;
+    }
+    const size_t budget = smem_budget(c);
+    if (best_nt == 0) {
+        uint8_t* tmp = nullptr;
+        LatObs* tobs = nullptr;
+        const size_t bytes = (size_t)c->nlat * c->lat_stride;
+        CK(c, cudaMalloc(&tmp, bytes));
+        if (cudaMalloc(&tobs, sizeof(LatObs) * c->nlat) != cudaSuccess) {
+            cudaFree(tmp);
+            return fail(c, J1J2C_ENOMEM, "autotuner scratch");
+        }
+        cudaError_t e = cudaMemcpyAsync(tmp, c->d_spins, bytes, cudaMemcpyDeviceToDevice, c->own);
+        SweepArgs a = base_args(c);
+        a.spins = tmp;
+        a.obs = tobs;
+        a.use_override = 1;
+        a.beta_override = 1.0 / 9.5;
+        a.sweep_override = 0x5EED0000u;
+        float best_ms = 1e30f;
+        for (int k = 0; k < n && e == cudaSuccess; ++k) {
+            SweepVariant v = c->var;
+            v.fixed_nt = nts[k];
+            v.stage_p = sp[k];
+            const size_t sm = sweep_smem_bytes(c->g, v);
+            if (sm > budget) continue;
+            if ((e = launch_fixed(a, v.fp64, nts[k], 0, sm, nullptr, true)) != cudaSuccess) break;
+            if ((e = launch_fixed(a, v.fp64, nts[k], c->nlat, sm, c->own, false)) != cudaSuccess)
+                break;
+            cudaEventRecord(c->ev0, c->own);
+            for (int r = 0; r < 3 && e == cudaSuccess; ++r)
+                e = launch_fixed(a, v.fp64, nts[k], c->nlat, sm, c->own, false);
+            cudaEventRecord(c->ev1, c->own);
+            if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+            if (e == cudaSuccess && ms < best_ms) {
+                best_ms = ms;
+                best_nt = nts[k];
+            }
+        }
+        cudaStreamSynchronize(c->own);
+        cudaFree(tmp);
+        cudaFree(tobs);
+        if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the sweep kernel");
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = best_nt;
+    }
+    for (int k = 0; k < n; ++k)
+        if (nts[k] == best_nt) {
+            c->var.fixed_nt = nts[k];
+            c->var.stage_p = sp[k];
+            c->smem = sweep_smem_bytes(c->g, c->var);
+            c->nthreads = nts[k];
+            SweepArgs none{};
+            none.g = c->g;
+            CK(c, launch_fixed(none, c->var.fp64, c->nthreads, 0, c->smem, nullptr, true));
+        }
+    free_graphs(c);
+    return J1J2C_OK;
+}
 
 }  // namespace
 
@@ -405,6 +527,7 @@ int j1j2c_set_disorder(void* ctx, int32_t conf, const double* p, const int8_t* o
         int rc = choose_variant(c, c->P.precision == J1J2C_FP64_PLAIN, c->var, c->smem,
                                 c->nthreads);
         if (rc != J1J2C_OK) return rc;
+        c->tuned = false;
     }
     c->have_dis[conf] = 1;
     c->have_spins[conf] = 0;  // vacancies changed: spins must be initialised again
@@ -511,6 +634,8 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
         CK(c, cudaMemcpyAsync(c->d_ctl + 1, &c->host_ctl[1], sizeof(uint32_t),
                               cudaMemcpyHostToDevice, c->st));
     }
+    int rct = autotune(c);
+    if (rct != J1J2C_OK) return rct;
     const bool direct = (c->P.flags & J1J2C_FLAG_NO_GRAPH) != 0;
     if (!direct && !c->graph[m]) {
         int rc = build_graph(c, m);

@@ -244,10 +244,19 @@ __device__ __forceinline__ float ex2_approx(float x)
     return y;
 }
 
-// FP32 uniform in [0, 1) from a Philox word: the top 23 bits as a mantissa, (r >> 9) * 2^-23
+// FP64 uniform in [0, 1) from a Philox word: the word rotated left by 9 bits, times 2^-32.  Its
+// top 23 bits are the word's low 23 bits, i.e. exactly the FP32 uniform below, so both forms
+// test the same random number (to 2^-23) in the deterministic FP32-vs-FP64 replay.
+__host__ __device__ __forceinline__ double u01_f64(uint32_t r)
+{
+    return (double)((r << 9) | (r >> 23)) * 0x1p-32;
+}
+
+// FP32 uniform in [0, 1) from a Philox word: its low 23 bits as a mantissa, (r mod 2^23) * 2^-23
+// (one logic operation; every Philox output bit is equally random)
 __device__ __forceinline__ float u01_f32(uint32_t r)
 {
-    return __fsub_rn(__uint_as_float(0x3F800000u | (r >> 9)), 1.0f);
+    return __fsub_rn(__uint_as_float(0x3F800000u | (r & 0x007FFFFFu)), 1.0f);
 }
 
 // byte k of w as an exact float (b in 0..255)

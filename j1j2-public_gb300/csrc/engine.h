@@ -77,7 +77,13 @@ struct SweepVariant {
     bool stage_p;  // random field staged in shared memory
     bool masks;    // bond dilution present
     int mode;      // kModeSweep / kModeAudit
+    int fixed_nt;  // > 0: shape-specialised kernel with this many threads per CTA
 };
+
+// Shape-specialised kernels (sweep_fixed.cu): CTA sizes available for a shape, and the launch.
+int fixed_candidates(bool fp64, int L, int H, bool masks, int* nts, bool* stage_p, int cap);
+cudaError_t launch_fixed(const SweepArgs& a, bool fp64, int nt, int nblocks, size_t smem,
+                         cudaStream_t st, bool prepare);
 
 size_t sweep_smem_bytes(const Geo& g, const SweepVariant& v);
 cudaError_t prepare_sweep_variant(const SweepVariant& v, size_t smem);

@@ -8,24 +8,10 @@
 //                 Pt_attempt_swaps (J:1303-1338), visit flags and the per-slot running sums of
 //                 Pt_measurement_loop (J:1440-1513).
 //   init_kernel   HOT/FER/STR starts (Initialize_spin_array J:1179-1209) on the device.
-#include "engine.h"
+#include "sweep_common.cuh"
 
 namespace j1j2 {
 namespace {
-
-struct Acc {
-    long long e;
-    int M, SX, SY, NB;
-};
-
-__device__ __forceinline__ int wrap_p(int v, int n) { return v + 1 == n ? 0 : v + 1; }
-__device__ __forceinline__ int wrap_m(int v, int n) { return v == 0 ? n - 1 : v - 1; }
-
-// fixed-point energy contribution of one site: llrint(e * 2^32)
-__device__ __forceinline__ long long efix(double e)
-{
-    return __double2ll_rn(__dmul_rn(e, 4294967296.0));
-}
 
 template <class Real>
 __device__ __forceinline__ const Real* field_base(const SweepArgs& a, int conf)
@@ -128,7 +114,7 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint
         else
             f32 = field_fp32(n, Q[i], a.J1hf, a.J1vf, a.J2f, a.J3f);
         if constexpr (MEASURE && sizeof(Real) == 4) {
-            acc.e += efix((double)(-((float)s * f32)));
+            acc.e += efix32(-__fmul_rn((float)s, f32));
             return;
         }
     }
@@ -142,7 +128,7 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint
             flip64 = true;
         } else {
             r = u4_word(philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1), w);
-            const double u = (double)r * 0x1p-32;
+            const double u = u01_f64(r);
             const double t2 = __dmul_rn(__dmul_rn(2.0, f64), beta);
             flip64 = u < own_exp(s == 1 ? -t2 : t2);
         }
@@ -170,18 +156,6 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint
 struct QuadNbr {
     uint32_t own, xp, xm, yp, ym, dpp, dpm, dmp, dmm, zp, zm;
 };
-
-__device__ __forceinline__ void x_pair(int px, uint32_t A, uint32_t B, uint32_t& plus,
-                                       uint32_t& minus)
-{
-    if (px) {  // site X: +x neighbour at compact X+1, -x at X
-        minus = A;
-        plus = __byte_perm(A, B, 0x4321);
-    } else {  // +x at X, -x at X-1
-        plus = A;
-        minus = __byte_perm(B, A, 0x6543);
-    }
-}
 
 template <class Real, bool MASKS, bool MEASURE>
 __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, uint32_t* S32,
@@ -289,15 +263,17 @@ __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, uint
             const float sf = __fmul_rn((float)(b - 1), f);
             if constexpr (MEASURE) {
                 const int s = b - 1;
-                acc.e += efix((double)(-sf));
+                acc.e += efix32(-sf);
                 acc.M += s;
                 acc.SX += px ? -s : s;
                 acc.SY += py ? -s : s;
                 acc.NB += s * ((int)((n.xp >> sh) & 0xFF) + (int)((n.xm >> sh) & 0xFF) -
                                (int)((n.yp >> sh) & 0xFF) - (int)((n.ym >> sh) & 0xFF));
             } else {
-                const bool flip = (b != 1) &&
-                                  (u01_f32(u4_word(rnd, k)) < ex2_approx(__fmul_rn(kb, sf)));
+                // vacancies (s = 0) never flip: the threshold is scaled by s^2
+                const float s2 = byte_f(n.own, k) - 1.0f;
+                const bool flip = u01_f32(u4_word(rnd, k)) <
+                                  __fmul_rn(ex2_approx(__fmul_rn(kb, sf)), __fmul_rn(s2, s2));
                 flipmask |= flip ? (2u << sh) : 0u;
             }
         } else {
@@ -334,7 +310,7 @@ __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, uint
                 if (s == 1 ? f <= 0.0 : f >= 0.0) {
                     flip = true;
                 } else {
-                    const double u = (double)u4_word(rnd, k) * 0x1p-32;
+                    const double u = u01_f64(u4_word(rnd, k));
                     const double t2 = __dmul_rn(__dmul_rn(2.0, f), beta);
                     flip = u < own_exp(s == 1 ? -t2 : t2);
                 }
@@ -345,33 +321,6 @@ __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, uint
     if constexpr (!MEASURE) {
         if (flipmask) S32[wown] = n.own ^ flipmask;
     }
-}
-
-__device__ __forceinline__ void warp_reduce(Acc& v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        v.e += __shfl_down_sync(0xFFFFFFFFu, v.e, o);
-        v.M += __shfl_down_sync(0xFFFFFFFFu, v.M, o);
-        v.SX += __shfl_down_sync(0xFFFFFFFFu, v.SX, o);
-        v.SY += __shfl_down_sync(0xFFFFFFFFu, v.SY, o);
-        v.NB += __shfl_down_sync(0xFFFFFFFFu, v.NB, o);
-    }
-}
-
-__device__ __forceinline__ Acc block_reduce(Acc v)
-{
-    __shared__ Acc red[32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    warp_reduce(v);
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    if (warp == 0) {
-        const int nw = (blockDim.x + 31) >> 5;
-        v = lane < nw ? red[lane] : Acc{0, 0, 0, 0, 0};
-        warp_reduce(v);
-    }
-    return v;  // valid in thread 0
 }
 
 template <class Real, bool QUAD, bool STAGE_P, bool MASKS, int MODE>
@@ -661,12 +610,14 @@ size_t sweep_smem_bytes(const Geo& g, const SweepVariant& v)
 cudaError_t prepare_sweep_variant(const SweepVariant& v, size_t smem)
 {
     SweepArgs dummy{};
+    if (v.fixed_nt > 0) return cudaErrorInvalidValue;  // prepared with the shape: see api.cu
     return dispatch(dummy, v, 0, 0, smem, nullptr, true);
 }
 
 cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks, int nthreads,
                          size_t smem, cudaStream_t st)
 {
+    if (v.fixed_nt > 0) return launch_fixed(a, v.fp64, v.fixed_nt, nblocks, smem, st, false);
     return dispatch(a, v, nblocks, nthreads, smem, st, false);
 }
 

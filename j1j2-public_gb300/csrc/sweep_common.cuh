@@ -1,0 +1,117 @@
+// Helpers shared by the generic sweep kernels (kernels.cu) and the shape-specialised sweep
+// kernels (sweep_fixed.cu): per-thread reduction state, block reduction, word shifts for the
+// +-x neighbours, fixed-point energy terms, and lattice staging between HBM and shared memory.
+#pragma once
+#include "engine.h"
+
+namespace j1j2 {
+
+struct Acc {
+    long long e;  // fixed-point energy, sum of llrint(-s*field * 2^32)
+    int M, SX, SY, NB;
+};
+
+__device__ __forceinline__ int wrap_p(int v, int n) { return v + 1 == n ? 0 : v + 1; }
+__device__ __forceinline__ int wrap_m(int v, int n) { return v == 0 ? n - 1 : v - 1; }
+
+// fixed-point energy contribution of one site: llrint(e * 2^32)
+__device__ __forceinline__ long long efix(double e)
+{
+    return __double2ll_rn(__dmul_rn(e, 4294967296.0));
+}
+// same value for an FP32 energy term: e * 2^32 is exact in FP32, so no FP64 operation is needed
+__device__ __forceinline__ long long efix32(float e)
+{
+    return __float2ll_rn(__fmul_rn(e, 4294967296.0f));
+}
+
+// efix32 without the 64-bit conversion (which runs on the FP64 pipe): with x = e * 2^16,
+// t = trunc(x) and r = x - t (exact), llrint(e * 2^32) = t * 2^16 + rint(r * 2^16) because
+// t * 2^16 is an even integer, so rounding (ties to even included) only acts on r * 2^16.
+// |t| < 2^23 for |e| < 2^7, so both parts fit 32-bit conversions.
+__device__ __forceinline__ long long efix32_split(float e)
+{
+    const float x = __fmul_rn(e, 65536.0f);
+    const float t = truncf(x);
+    const int hi = __float2int_rz(t);
+    const int lo = __float2int_rn(__fmul_rn(__fsub_rn(x, t), 65536.0f));
+    return ((long long)hi << 16) + (long long)lo;
+}
+
+// Neighbour words along x for a run of four compact X of one colour.  A is the word with the
+// same X range in the neighbouring colour, B the next (px = 1) or previous (px = 0) word.
+__device__ __forceinline__ void x_pair(int px, uint32_t A, uint32_t B, uint32_t& plus,
+                                       uint32_t& minus)
+{
+    if (px) {  // site X: +x neighbour at compact X+1, -x at X
+        minus = A;
+        plus = __byte_perm(A, B, 0x4321);
+    } else {  // +x at X, -x at X-1
+        plus = A;
+        minus = __byte_perm(B, A, 0x6543);
+    }
+}
+
+// byte k of w minus off, as an exact float (one PRMT into a 2^23 exponent field, one FADD)
+__device__ __forceinline__ float byte_off(uint32_t w, int k, float off)
+{
+    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)k)),
+                     8388608.0f + off);
+}
+
+__device__ __forceinline__ void warp_reduce(Acc& v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.e += __shfl_down_sync(0xFFFFFFFFu, v.e, o);
+        v.M += __shfl_down_sync(0xFFFFFFFFu, v.M, o);
+        v.SX += __shfl_down_sync(0xFFFFFFFFu, v.SX, o);
+        v.SY += __shfl_down_sync(0xFFFFFFFFu, v.SY, o);
+        v.NB += __shfl_down_sync(0xFFFFFFFFu, v.NB, o);
+    }
+}
+
+// block-wide sum; the result is valid in thread 0
+__device__ __forceinline__ Acc block_reduce(Acc v)
+{
+    __shared__ Acc red[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    warp_reduce(v);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        v = lane < nw ? red[lane] : Acc{0, 0, 0, 0, 0};
+        warp_reduce(v);
+    }
+    return v;
+}
+
+__device__ __forceinline__ void store_obs(LatObs* out, const Acc& t)
+{
+    LatObs o;
+    o.eacc = t.e;
+    o.M = t.M;
+    o.SX = t.SX;
+    o.SY = t.SY;
+    o.NB = t.NB;
+    o.pad[0] = o.pad[1] = 0;
+    *out = o;
+}
+
+// 16-byte vector copy of nbytes (a multiple of 16) by the whole block
+__device__ __forceinline__ void block_copy16(void* dst, const void* src, int nbytes)
+{
+    const uint4* s = reinterpret_cast<const uint4*>(src);
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    for (int k = (int)threadIdx.x; k < nbytes / 16; k += (int)blockDim.x) d[k] = s[k];
+}
+
+__device__ __forceinline__ void block_copy16_ldg(void* dst, const void* src, int nbytes)
+{
+    const uint4* s = reinterpret_cast<const uint4*>(src);
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    for (int k = (int)threadIdx.x; k < nbytes / 16; k += (int)blockDim.x) d[k] = __ldg(s + k);
+}
+
+}  // namespace j1j2

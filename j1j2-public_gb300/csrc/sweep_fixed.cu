@@ -1,0 +1,350 @@
+// Shape-specialised sweep kernel: the lattice extents (L/2, H/2) and the CTA size are template
+// constants and the eight colour phases of a sweep are unrolled, so colour parities are
+// compile-time.  Each thread owns the same quad(s) in every colour class; the word offsets of the
+// quad's neighbours inside a colour block are computed once, and a colour phase addresses shared
+// memory as [offset + colour base], the base being an immediate.  Same arithmetic, Philox stream
+// and outputs as the generic quad kernel (kernels.cu), bit for bit.  One CTA owns one lattice,
+// staged in shared memory for the PTSWAPEVER fused sweeps of a PT cycle.
+#include "sweep_common.cuh"
+
+namespace j1j2 {
+namespace {
+
+template <int LH, int HH>
+struct Shape {
+    static constexpr int QR = LH / 4;    // 32-bit words per compact row
+    static constexpr int RS = LH * QR;   // words per compact z-plane
+    static constexpr int CS = HH * RS;   // words (= quads) per colour
+    static constexpr int N = 8 * LH * LH * HH;
+    static constexpr int NB = (N + 15) & ~15;
+};
+
+// Word offsets (within a colour block) of a quad and of the words its neighbours live in:
+// same row; row Y+1 / Y-1; plane Z+1 / Z-1; and the words one step along x in those rows.
+struct QuadOff {
+    int self, xp, xm;          // row Y:   words qx, qx+1, qx-1
+    int yp, yp_xp, yp_xm;      // row Y+1: words qx, qx+1, qx-1
+    int ym, ym_xp, ym_xm;      // row Y-1
+    int zp, zm;                // planes Z+1 / Z-1, word qx
+};
+
+template <int LH, int HH>
+__device__ __forceinline__ QuadOff quad_offsets(int q)
+{
+    using Sh = Shape<LH, HH>;
+    const int qx = q % Sh::QR, row = q / Sh::QR;
+    const int Y = row % LH, Z = row / LH;
+    const int qxp = qx + 1 == Sh::QR ? 0 : qx + 1, qxm = qx == 0 ? Sh::QR - 1 : qx - 1;
+    const int Yp = Y + 1 == LH ? 0 : Y + 1, Ym = Y == 0 ? LH - 1 : Y - 1;
+    const int Zp = Z + 1 == HH ? 0 : Z + 1, Zm = Z == 0 ? HH - 1 : Z - 1;
+    const int r0 = Z * Sh::RS + Y * Sh::QR, rp = Z * Sh::RS + Yp * Sh::QR,
+              rm = Z * Sh::RS + Ym * Sh::QR;
+    QuadOff o;
+    o.self = r0 + qx;
+    o.xp = r0 + qxp;
+    o.xm = r0 + qxm;
+    o.yp = rp + qx;
+    o.yp_xp = rp + qxp;
+    o.yp_xm = rp + qxm;
+    o.ym = rm + qx;
+    o.ym_xp = rm + qxp;
+    o.ym_xm = rm + qxm;
+    o.zp = Zp * Sh::RS + Y * Sh::QR + qx;
+    o.zm = Zm * Sh::RS + Y * Sh::QR + qx;
+    return o;
+}
+
+template <class Real, int LH, int HH, int C, bool MEASURE>
+__device__ __forceinline__ void quad_fixed(const SweepArgs& a, uint32_t* S32, const Real* P,
+                                           const QuadOff& o, uint32_t sweep, uint32_t rep,
+                                           uint32_t k0, uint32_t k1, double beta, float kb,
+                                           Acc& acc)
+{
+    using Sh = Shape<LH, HH>;
+    constexpr int px = C & 1, py = (C >> 1) & 1, pz = C >> 2;
+    constexpr int B0 = C * Sh::CS, B1 = (C ^ 1) * Sh::CS, B2 = (C ^ 2) * Sh::CS;
+    constexpr int B3 = (C ^ 3) * Sh::CS, B4 = (C ^ 4) * Sh::CS;
+    // neighbour rows for this colour's parities (J:540-584): odd parity steps +1, even -1
+    const int rYp = py ? o.yp : o.self, rYm = py ? o.self : o.ym;  // +y / -y rows, word qx
+    const int xn = px ? o.xp : o.xm;                                 // same row, shifted word
+    const int rYp_n = py ? (px ? o.yp_xp : o.yp_xm) : xn;
+    const int rYm_n = py ? xn : (px ? o.ym_xp : o.ym_xm);
+    const int rZp = pz ? o.zp : o.self, rZm = pz ? o.self : o.zm;
+
+    const uint32_t own = S32[B0 + o.self];
+    uint32_t wxp, wxm, wdpp, wdpm, wdmp, wdmm;
+    x_pair(px, S32[B1 + o.self], S32[B1 + xn], wxp, wxm);
+    const uint32_t wyp = S32[B2 + rYp], wym = S32[B2 + rYm];
+    x_pair(px, S32[B3 + rYp], S32[B3 + rYp_n], wdpp, wdpm);
+    x_pair(px, S32[B3 + rYm], S32[B3 + rYm_n], wdmp, wdmm);
+    const uint32_t wzp = S32[B4 + rZp], wzm = S32[B4 + rZm];
+
+    Real pown[4], pxa[4], pyp[4], pym[4];
+    const Real pextra = P[4 * (B1 + xn) + (px ? 0 : 3)];
+    if constexpr (sizeof(Real) == 4) {
+        const float4* P4 = reinterpret_cast<const float4*>(P);
+        const float4 v0 = P4[B0 + o.self], v1 = P4[B1 + o.self];
+        const float4 v2 = P4[B2 + rYp], v3 = P4[B2 + rYm];
+        pown[0] = v0.x, pown[1] = v0.y, pown[2] = v0.z, pown[3] = v0.w;
+        pxa[0] = v1.x, pxa[1] = v1.y, pxa[2] = v1.z, pxa[3] = v1.w;
+        pyp[0] = v2.x, pyp[1] = v2.y, pyp[2] = v2.z, pyp[3] = v2.w;
+        pym[0] = v3.x, pym[1] = v3.y, pym[2] = v3.z, pym[3] = v3.w;
+    } else {
+        const double2* P2 = reinterpret_cast<const double2*>(P);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const double2 v0 = P2[2 * (B0 + o.self) + h], v1 = P2[2 * (B1 + o.self) + h];
+            const double2 v2 = P2[2 * (B2 + rYp) + h], v3 = P2[2 * (B2 + rYm) + h];
+            pown[2 * h] = v0.x, pown[2 * h + 1] = v0.y;
+            pxa[2 * h] = v1.x, pxa[2 * h + 1] = v1.y;
+            pyp[2 * h] = v2.x, pyp[2 * h + 1] = v2.y;
+            pym[2 * h] = v3.x, pym[2 * h + 1] = v3.y;
+        }
+    }
+
+    U4 rnd{0, 0, 0, 0};
+    if constexpr (!MEASURE)
+        rnd = philox4x32_10(rep, sweep, (uint32_t)(B0 + o.self), kTagSweep, k0, k1);
+    const uint32_t dsum = wdpp + wdpm + wdmp + wdmm;  // bytewise, <= 8
+    const uint32_t zsum = wzp + wzm;                  // bytewise, <= 4
+    uint32_t flipmask = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const Real pxp = px ? (k < 3 ? pxa[k + 1] : pextra) : pxa[k];
+        const Real pxm = px ? pxa[k] : (k > 0 ? pxa[k - 1] : pextra);
+        if constexpr (sizeof(Real) == 4) {
+            Nbr32 nb;
+            nb.sxp = byte_off(wxp, k, 1.0f);
+            nb.sxm = byte_off(wxm, k, 1.0f);
+            nb.syp = byte_off(wyp, k, 1.0f);
+            nb.sym = byte_off(wym, k, 1.0f);
+            nb.D = byte_off(dsum, k, 4.0f);
+            nb.Zs = byte_off(zsum, k, 2.0f);
+            nb.pxp = pxp;
+            nb.pxm = pxm;
+            nb.pyp = pyp[k];
+            nb.pym = pym[k];
+            const float f = field_fp32(nb, pown[k], a.J1hf, a.J1vf, a.J2f, a.J3f);
+            const float si = byte_off(own, k, 1.0f);
+            const float sf = __fmul_rn(si, f);
+            if constexpr (MEASURE) {
+                const int s = (int)si;
+                acc.e += efix32_split(-sf);
+                acc.M += s;
+                acc.SX += px ? -s : s;
+                acc.SY += py ? -s : s;
+                acc.NB += s * (int)(nb.sxp + nb.sxm - nb.syp - nb.sym);
+            } else {
+                // Metropolis test u < exp(-beta dE) as 2^(kb s f); vacancies (s = 0) never flip
+                // because the threshold is scaled by s^2 (FMA-pipe work instead of a compare)
+                const float thr = __fmul_rn(ex2_approx(__fmul_rn(kb, sf)), __fmul_rn(si, si));
+                if (u01_f32(u4_word(rnd, k)) < thr) flipmask |= 2u << (8 * k);
+            }
+        } else {
+            const int sh = 8 * k;
+            const int b = (own >> sh) & 0xFF;
+            if (b == 1) continue;
+            Nbr64 nb;
+            nb.s[0] = (int)((wyp >> sh) & 0xFF) - 1;
+            nb.s[1] = (int)((wym >> sh) & 0xFF) - 1;
+            nb.s[2] = (int)((wxp >> sh) & 0xFF) - 1;
+            nb.s[3] = (int)((wxm >> sh) & 0xFF) - 1;
+            nb.s[4] = (int)((wdpp >> sh) & 0xFF) - 1;
+            nb.s[5] = (int)((wdpm >> sh) & 0xFF) - 1;
+            nb.s[6] = (int)((wdmp >> sh) & 0xFF) - 1;
+            nb.s[7] = (int)((wdmm >> sh) & 0xFF) - 1;
+            nb.s[8] = (int)((wzp >> sh) & 0xFF) - 1;
+            nb.s[9] = (int)((wzm >> sh) & 0xFF) - 1;
+            nb.p1 = pyp[k];
+            nb.p2 = pym[k];
+            nb.p3 = pxp;
+            nb.p4 = pxm;
+            nb.jv_own = nb.jv_m2 = nb.jh_own = nb.jh_m4 = 1;
+            const double f = field_fp64(nb, pown[k], a.J1h, a.J1v, a.J2, a.J3, nullptr);
+            const int s = b - 1;
+            if constexpr (MEASURE) {
+                acc.e += efix(-((double)s * f));
+                acc.M += s;
+                acc.SX += px ? -s : s;
+                acc.SY += py ? -s : s;
+                acc.NB += s * (nb.s[2] + nb.s[3] - nb.s[0] - nb.s[1]);
+            } else {
+                bool flip;
+                if (s == 1 ? f <= 0.0 : f >= 0.0) {
+                    flip = true;
+                } else {
+                    const double u = u01_f64(u4_word(rnd, k));
+                    const double t2 = __dmul_rn(__dmul_rn(2.0, f), beta);
+                    flip = u < own_exp(s == 1 ? -t2 : t2);
+                }
+                flipmask |= flip ? (2u << sh) : 0u;
+            }
+        }
+    }
+    if constexpr (!MEASURE) {
+        if (flipmask) S32[B0 + o.self] = own ^ flipmask;
+    }
+}
+
+// Offsets are held in registers for the whole kernel when a thread owns at most two quads;
+// with more quads they are recomputed in every phase (a few constant-divisor operations) to keep
+// register pressure down.
+template <int QPT>
+struct OffsetCache {
+    static constexpr bool kHold = QPT <= 2;
+    QuadOff off[kHold ? QPT : 1];
+};
+
+template <int LH, int HH, int NT, int QPT>
+__device__ __forceinline__ QuadOff offsets_for(const OffsetCache<QPT>& oc, int j)
+{
+    if constexpr (OffsetCache<QPT>::kHold) {
+        return oc.off[j];
+    } else {
+        int tid;  // opaque read: stops the per-phase arithmetic from being hoisted and kept live
+        asm volatile("mov.u32 %0, %%tid.x;" : "=r"(tid));
+        const int q = tid + j * NT;
+        return quad_offsets<LH, HH>(q < Shape<LH, HH>::CS ? q : 0);
+    }
+}
+
+template <class Real, int LH, int HH, int NT, int QPT, bool MEASURE>
+__device__ __forceinline__ void all_colours(const SweepArgs& a, uint32_t* S32, const Real* P,
+                                            const OffsetCache<QPT>& oc, uint32_t sweep,
+                                            uint32_t rep, uint32_t k0, uint32_t k1, double beta,
+                                            float kb, Acc& acc)
+{
+    constexpr int NQ = Shape<LH, HH>::CS;
+    // One barrier per colour.  The measurement only reads, but without the barrier the
+    // instruction scheduler interleaves all eight read-only phases and runs out of registers.
+#define J1J2_PHASE(C)                                                                       \
+    _Pragma("unroll 2") for (int j = 0; j < QPT; ++j) if (QPT * NT == NQ ||                 \
+                                                          (int)threadIdx.x + j * NT < NQ)   \
+        quad_fixed<Real, LH, HH, C, MEASURE>(a, S32, P, offsets_for<LH, HH, NT, QPT>(oc, j), \
+                                             sweep, rep, k0, k1, beta, kb, acc);            \
+    __syncthreads();
+    J1J2_PHASE(0)
+    J1J2_PHASE(1)
+    J1J2_PHASE(2)
+    J1J2_PHASE(3)
+    J1J2_PHASE(4)
+    J1J2_PHASE(5)
+    J1J2_PHASE(6)
+    J1J2_PHASE(7)
+#undef J1J2_PHASE
+}
+
+template <class Real, int LH, int HH, int NT, int MINB, bool STAGE_P>
+__global__ void __launch_bounds__(NT, MINB) sweep_fixed_kernel(SweepArgs a)
+{
+    using Sh = Shape<LH, HH>;
+    constexpr int QPT = (Sh::CS + NT - 1) / NT;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lat = a.lat0 + (int)blockIdx.x;
+    const int conf = lat / a.nrep;
+    const int rep = lat - conf * a.nrep;
+    uint8_t* S = smem;
+    Real* Ps = reinterpret_cast<Real*>(smem + Sh::NB);
+    uint8_t* Sg = a.spins + (long long)lat * a.lat_stride;
+    const Real* Pg;
+    if constexpr (sizeof(Real) == 8)
+        Pg = a.pd + (long long)conf * a.p_stride;
+    else
+        Pg = a.pf + (long long)conf * a.p_stride;
+
+    block_copy16(S, Sg, Sh::NB);
+    if constexpr (STAGE_P)
+        block_copy16_ldg(Ps, Pg, (int)((Sh::N * sizeof(Real) + 15) & ~(size_t)15));
+    OffsetCache<QPT> off;
+    if constexpr (OffsetCache<QPT>::kHold) {
+#pragma unroll
+        for (int j = 0; j < QPT; ++j) {
+            const int q = (int)threadIdx.x + j * NT;
+            off.off[j] = quad_offsets<LH, HH>(q < Sh::CS ? q : 0);
+        }
+    }
+    __syncthreads();
+    const Real* P = STAGE_P ? Ps : Pg;
+    uint32_t* S32 = reinterpret_cast<uint32_t*>(S);
+
+    double beta;
+    uint32_t sweep0;
+    if (a.use_override) {
+        beta = a.beta_override;
+        sweep0 = a.sweep_override;
+    } else {
+        beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+        sweep0 = a.ctl[0] * (uint32_t)a.ptswapever;
+    }
+    const float kb = (float)(-2.0 * beta * 1.4426950408889634);
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    Acc acc{0, 0, 0, 0, 0};
+#pragma unroll 1
+    for (int t = 0; t < a.nsweeps; ++t)
+        all_colours<Real, LH, HH, NT, QPT, false>(a, S32, P, off, sweep0 + (uint32_t)t,
+                                                  (uint32_t)rep, k0, k1, beta, kb, acc);
+    all_colours<Real, LH, HH, NT, QPT, true>(a, S32, P, off, 0u, 0u, 0u, 0u, beta, kb, acc);
+    const Acc tot = block_reduce(acc);
+    if (threadIdx.x == 0) store_obs(a.obs + lat, tot);
+    block_copy16(Sg, S, Sh::NB);
+}
+
+template <class Real, int LH, int HH, int NT, int MINB, bool STAGE_P>
+cudaError_t run_fixed(const SweepArgs& a, int nblocks, size_t smem, cudaStream_t st, bool prep)
+{
+    auto k = sweep_fixed_kernel<Real, LH, HH, NT, MINB, STAGE_P>;
+    if (prep) return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<nblocks, NT, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+using FixedFn = cudaError_t (*)(const SweepArgs&, int, size_t, cudaStream_t, bool);
+
+struct FixedEntry {
+    bool fp64;
+    int L, H, nt;
+    bool stage_p;
+    FixedFn fn;
+};
+
+// Shapes of the reference's configurations (L = 16, 24, 32, 48 with H = L) and the CTA sizes
+// the autotuner chooses from; the second number is the CTAs per SM that shared memory allows
+// (it bounds the registers per thread).
+const FixedEntry kFixed[] = {
+    {false, 16, 16, 128, true, run_fixed<float, 8, 8, 128, 8, true>},
+    {false, 16, 16, 64, true, run_fixed<float, 8, 8, 64, 10, true>},
+    {false, 24, 24, 448, true, run_fixed<float, 12, 12, 448, 2, true>},
+    {false, 24, 24, 224, true, run_fixed<float, 12, 12, 224, 2, true>},
+    {false, 32, 32, 1024, true, run_fixed<float, 16, 16, 1024, 1, true>},
+    {false, 32, 32, 512, true, run_fixed<float, 16, 16, 512, 1, true>},
+    {false, 48, 48, 864, false, run_fixed<float, 24, 24, 864, 1, false>},
+    {false, 48, 48, 576, false, run_fixed<float, 24, 24, 576, 1, false>},
+    {true, 24, 24, 448, true, run_fixed<double, 12, 12, 448, 1, true>},
+    {true, 32, 32, 512, false, run_fixed<double, 16, 16, 512, 1, false>},
+};
+
+}  // namespace
+
+int fixed_candidates(bool fp64, int L, int H, bool masks, int* nts, bool* stage_p, int cap)
+{
+    if (masks) return 0;
+    int n = 0;
+    for (const auto& e : kFixed)
+        if (e.fp64 == fp64 && e.L == L && e.H == H && n < cap) {
+            nts[n] = e.nt;
+            stage_p[n] = e.stage_p;
+            ++n;
+        }
+    return n;
+}
+
+cudaError_t launch_fixed(const SweepArgs& a, bool fp64, int nt, int nblocks, size_t smem,
+                         cudaStream_t st, bool prepare)
+{
+    for (const auto& e : kFixed)
+        if (e.fp64 == fp64 && e.L == a.g.L && e.H == a.g.H && e.nt == nt)
+            return e.fn(a, nblocks, smem, st, prepare);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace j1j2

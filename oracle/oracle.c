@@ -742,8 +742,9 @@ int64_t or_replay_sweeps(const or_lat *g, int8_t *s, double beta, uint32_t seed,
                             uint32_t gi;
                             int w;
                             site_group(L, H, x, y, z, &gi, &w);
-                            double u = (double)philox_word(seed, conf, rep, sweep, gi, TAG_SWEEP,
-                                                           w) * 0x1p-32;
+                            uint32_t r = philox_word(seed, conf, rep, sweep, gi, TAG_SWEEP, w);
+                            /* FP64 uniform: the word rotated left by 9, times 2^-32 */
+                            double u = (double)((r << 9) | (r >> 23)) * 0x1p-32;
                             double t2 = (2.0 * field) * beta;
                             flip = u < or_dexp(s[i] == 1 ? -t2 : t2);
                         }
