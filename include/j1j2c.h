@@ -48,6 +48,7 @@ extern "C" {
 #define J1J2C_FLAG_PROFILE 2u    /* time every sweep launch with CUDA events (j1j2c_get_profile)  */
 #define J1J2C_FLAG_GENERIC 4u    /* force the per-site kernel path (testing)                      */
 #define J1J2C_FLAG_NO_FIXED 8u   /* skip the shape-specialised kernels (testing)                  */
+#define J1J2C_FLAG_GLOBAL 16u    /* force the global-memory (one launch per colour) path (testing) */
 
 /* Run parameters: the compile-time constants of J:43-96 that the hot path consumes. */
 typedef struct {
@@ -83,6 +84,16 @@ typedef struct {
 /* Allocates every device buffer for nconf x nreplica lattices.  Replaces the MPI set-up and the
  * per-rank arrays (J:115-207, Setup_mpi J:415-420, Setup_neighbor_table J:532-586). */
 int j1j2c_create(void **ctx, const j1j2c_params *params);
+
+/* Mixed lattice shapes in one context (one graph per PT cycle covers every group): group k
+ * contributes groups[k].nconf confs of groups[k].L x L x H with groups[k].nreplica replicas;
+ * confs are numbered across groups in order.  Couplings, ptswapever, precision, seed,
+ * conf_base, device and flags are taken from groups[0]; block_threads is per group.  No
+ * reference counterpart: the reference runs one lattice size per build (J:43-44). */
+int j1j2c_create_multi(void **ctx, const j1j2c_params *groups, int32_t ngroups);
+
+/* Lattice extents and ladder length of one conf (useful with j1j2c_create_multi). */
+int j1j2c_conf_shape(void *ctx, int32_t conf, int32_t *L, int32_t *H, int32_t *nreplica);
 
 /* Frees everything (J:401 MPI_FINALIZE's role for this context). */
 void j1j2c_destroy(void *ctx);

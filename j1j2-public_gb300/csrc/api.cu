@@ -1,5 +1,9 @@
 // C-ABI of libj1j2cuda: context management, layout conversion between the reference's site order
 // and the engine's colour-compact layout, the CUDA-graph replay of one PT cycle, and the outputs.
+//
+// A context holds one or more lattice-shape groups (mixed L in one batch).  Each group has its
+// own kernel variant; one PT cycle is one graph: the groups' sweep launches as parallel branches,
+// then one swap / accumulate launch over every conf.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -21,11 +25,23 @@ namespace {
 
 thread_local std::string g_create_error;
 
+struct Group {
+    Geo g{};
+    int nconf = 0, nrep = 0, conf0 = 0, rep0 = 0, block_threads = 0;
+    long long lat_stride = 0, p_stride = 0;        // bytes per lattice, field elements per conf
+    long long spin_off = 0, p_off = 0, mask_off = 0;  // offsets into the context's arrays
+    SweepVariant var{};
+    int nthreads = 0;
+    size_t smem = 0;
+    bool tuned = false;
+    int nlat() const { return nconf * nrep; }
+};
+
 struct Ctx {
     j1j2c_params P{};
-    Geo g{};
-    int nconf = 0, nrep = 0, nlat = 0;
-    long long lat_stride = 0, p_stride = 0;
+    std::vector<Group> G;
+    int nconf = 0, nentries = 0;  // confs, replica-indexed entries (sum of nconf*nrep)
+    std::vector<int> conf_group, conf_rbase, conf_nrep;
 
     uint8_t* d_spins = nullptr;
     float* d_pf = nullptr;
@@ -44,28 +60,27 @@ struct Ctx {
     double* d_last = nullptr;
     uint32_t* d_ctl = nullptr;
     int* d_nocc = nullptr;
+    int* d_rbase = nullptr;
+    int* d_nreps = nullptr;
     unsigned long long* d_audit = nullptr;
 
     std::vector<uint8_t> have_dis, have_ladder, have_spins;
-    std::vector<int> nocc;
-    std::vector<uint8_t> bm_host;  // per conf, compact; tells whether bond masks are present
-    std::vector<int> conf_masks;
+    std::vector<int> nocc, conf_masks;
     bool masks = false;
 
     cudaStream_t own = nullptr, st = nullptr;
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> join_ev;
+    cudaEvent_t fork_ev = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    SweepVariant var{};
-    int nthreads = 0;
-    size_t smem = 0;
     long long occ_total = 0;
 
-    bool tuned = false;
     bool profile = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double prof_ms = 0.0;
     long long prof_launches = 0, prof_attempts = 0;
 
-    uint32_t host_ctl[2] = {0, 1};
+    uint32_t host_ctl[4] = {0, 1, 0, 0};
     std::string err;
 };
 
@@ -78,7 +93,7 @@ int fail(Ctx* c, int code, const std::string& msg)
 int cuda_fail(Ctx* c, cudaError_t e, const char* what)
 {
     std::string m = std::string(what) + ": " + cudaGetErrorString(e);
-    return fail(c, J1J2C_ECUDA, m);
+    return fail(c, e == cudaErrorMemoryAllocation ? J1J2C_ENOMEM : J1J2C_ECUDA, m);
 }
 
 #define CK(c, call)                                               \
@@ -105,11 +120,15 @@ void free_graphs(Ctx* c)
 void release(Ctx* c)
 {
     free_graphs(c);
-    void* ptrs[] = {c->d_spins, c->d_pf,   c->d_pd,   c->d_bm,  c->d_occ,   c->d_beta,
-                    c->d_rat,   c->d_tor,  c->d_obs,  c->d_sums, c->d_nmeas, c->d_att,
-                    c->d_acc,   c->d_vis,  c->d_last, c->d_ctl, c->d_nocc,  c->d_audit};
+    void* ptrs[] = {c->d_spins, c->d_pf,    c->d_pd,   c->d_bm,    c->d_occ,   c->d_beta,
+                    c->d_rat,   c->d_tor,   c->d_obs,  c->d_sums,  c->d_nmeas, c->d_att,
+                    c->d_acc,   c->d_vis,   c->d_last, c->d_ctl,   c->d_nocc,  c->d_rbase,
+                    c->d_nreps, c->d_audit};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    for (auto s : c->side) cudaStreamDestroy(s);
+    for (auto e : c->join_ev) cudaEventDestroy(e);
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own) cudaStreamDestroy(c->own);
@@ -124,54 +143,60 @@ size_t smem_budget(Ctx* c)
     return (size_t)optin - 2048;  // static shared memory of the reduction
 }
 
-// Kernel shape for the context's lattices: the shape-specialised kernel when one exists for
-// (precision, L, H) and no bond is diluted (its CTA size autotuned at the first run unless
-// block_threads names one), else the generic quad path when L/2 is a multiple of 4, else the
-// per-site path; the random field is staged in shared memory when it fits next to the spins.
-int choose_variant(Ctx* c, bool fp64, SweepVariant& v, size_t& smem, int& nthreads)
+// Kernel shape for a group: the shape-specialised kernel when one exists for (precision, L, H)
+// and no bond is diluted (its CTA size autotuned at the first run unless block_threads names
+// one); else the generic CTA-per-lattice kernel with the lattice in shared memory (quad path when
+// L/2 is a multiple of 4, else per-site; the field staged when it fits); else, for lattices too
+// large for shared memory, the global-memory path with one launch per colour phase.
+int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem, int& nthreads)
 {
     const size_t budget = smem_budget(c);
     if (budget == 0) return fail(c, J1J2C_ECUDA, "cannot query the shared-memory limit");
+    const uint32_t fl = c->P.flags;
     v = SweepVariant{};
     v.fp64 = fp64;
     v.masks = c->masks;
     v.mode = kModeSweep;
-    if (!(c->P.flags & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED))) {
+    const bool quad_ok = (grp.g.Lh % 4 == 0) && !(fl & J1J2C_FLAG_GENERIC);
+    if (!(fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_GLOBAL))) {
         int nts[8];
         bool sp[8];
-        const int n = fixed_candidates(fp64, c->g.L, c->g.H, c->masks, nts, sp, 8);
+        const int n = fixed_candidates(fp64, grp.g.L, grp.g.H, c->masks, nts, sp, 8);
         int pick = n > 0 ? 0 : -1;
         for (int k = 0; k < n; ++k)
-            if (nts[k] == c->P.block_threads) pick = k;
+            if (nts[k] == grp.block_threads) pick = k;
         if (pick >= 0) {
             v.fixed_nt = nts[pick];
             v.quad = true;
             v.stage_p = sp[pick];
-            smem = sweep_smem_bytes(c->g, v);
+            smem = sweep_smem_bytes(grp.g, v);
             if (smem <= budget) {
                 nthreads = nts[pick];
                 SweepArgs none{};
-                none.g = c->g;
+                none.g = grp.g;
                 CK(c, launch_fixed(none, fp64, nthreads, 0, smem, nullptr, true));
                 return J1J2C_OK;
             }
             v.fixed_nt = 0;
         }
     }
-    v.quad = (c->g.Lh % 4 == 0) && !(c->P.flags & J1J2C_FLAG_GENERIC);
+    v.quad = quad_ok;
+    const int work = v.quad ? grp.g.Nc / 4 : grp.g.Nc;
     v.stage_p = true;
-    smem = sweep_smem_bytes(c->g, v);
+    smem = sweep_smem_bytes(grp.g, v);
     if (smem > budget) {
         v.stage_p = false;
-        smem = sweep_smem_bytes(c->g, v);
+        smem = sweep_smem_bytes(grp.g, v);
     }
-    if (smem > budget)
-        return fail(c, J1J2C_EINVAL,
-                    "lattice of " + std::to_string(c->g.N) +
-                        " sites does not fit the shared-memory sweep kernel");
-    const int work = v.quad ? c->g.Nc / 4 : c->g.Nc;
-    if (c->P.block_threads > 0) {
-        nthreads = c->P.block_threads;
+    if (smem > budget || (fl & J1J2C_FLAG_GLOBAL)) {
+        v.global = true;
+        v.stage_p = false;
+        smem = 0;
+        nthreads = 256;
+        return J1J2C_OK;
+    }
+    if (grp.block_threads > 0) {
+        nthreads = grp.block_threads;
     } else {
         nthreads = ((work + 31) / 32) * 32;
         if (nthreads > 1024) nthreads = 1024;
@@ -181,20 +206,20 @@ int choose_variant(Ctx* c, bool fp64, SweepVariant& v, size_t& smem, int& nthrea
     return J1J2C_OK;
 }
 
-SweepArgs base_args(Ctx* c)
+SweepArgs group_args(Ctx* c, const Group& grp)
 {
     SweepArgs a{};
-    a.g = c->g;
-    a.spins = c->d_spins;
-    a.lat_stride = c->lat_stride;
-    a.pf = c->d_pf;
-    a.pd = c->d_pd;
-    a.bm = c->masks ? c->d_bm : nullptr;
-    a.p_stride = c->p_stride;
-    a.beta = c->d_beta;
-    a.temp_of_rep = c->d_tor;
+    a.g = grp.g;
+    a.spins = c->d_spins + grp.spin_off;
+    a.lat_stride = grp.lat_stride;
+    a.pf = c->d_pf + grp.p_off;
+    a.pd = c->d_pd + grp.p_off;
+    a.bm = c->masks ? c->d_bm + grp.mask_off : nullptr;
+    a.p_stride = grp.p_stride;
+    a.beta = c->d_beta + grp.rep0;
+    a.temp_of_rep = c->d_tor + grp.rep0;
     a.ctl = c->d_ctl;
-    a.obs = c->d_obs;
+    a.obs = c->d_obs + grp.rep0;
     a.audit = c->d_audit;
     a.J1h = c->P.J1h;
     a.J1v = c->P.J1v;
@@ -204,11 +229,11 @@ SweepArgs base_args(Ctx* c)
     a.J1vf = (float)c->P.J1v;
     a.J2f = (float)c->P.J2;
     a.J3f = (float)c->P.J3;
-    a.nrep = c->nrep;
+    a.nrep = grp.nrep;
     a.nsweeps = c->P.ptswapever;
     a.ptswapever = c->P.ptswapever;
     a.seed = c->P.seed;
-    a.conf_base = c->P.conf_base;
+    a.conf_base = c->P.conf_base + (uint32_t)grp.conf0;
     a.lat0 = 0;
     a.use_override = 0;
     return a;
@@ -220,6 +245,8 @@ SwapArgs swap_args(Ctx* c, int measure)
     s.obs = c->d_obs;
     s.beta = c->d_beta;
     s.nocc = c->d_nocc;
+    s.rbase = c->d_rbase;
+    s.nreps = c->d_nreps;
     s.rat = c->d_rat;
     s.tor = c->d_tor;
     s.sums = c->d_sums;
@@ -230,24 +257,54 @@ SwapArgs swap_args(Ctx* c, int measure)
     s.last_obs = c->d_last;
     s.ctl = c->d_ctl;
     s.nconf = c->nconf;
-    s.nrep = c->nrep;
     s.measure = measure;
     s.seed = c->P.seed;
     s.conf_base = c->P.conf_base;
     return s;
 }
 
-// one PT cycle: fused sweeps + observables of every lattice, then swap / accumulate
+// PTSWAPEVER sweeps and the observable reduction of lattices [lat0, lat0 + nlat) of a group
+cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int nthreads,
+                          size_t smem, SweepArgs a, int nlat, cudaStream_t st)
+{
+    cudaError_t e;
+    if (!v.global) return launch_sweep(a, v, nlat, nthreads, smem, st);
+    for (int t = 0; t < a.nsweeps; ++t)
+        for (int col = 0; col < 8; ++col)
+            if ((e = launch_sweep_global(a, v, col, t, nlat, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(a.obs + a.lat0, 0, sizeof(LatObs) * nlat, st)) != cudaSuccess)
+        return e;
+    (void)grp;
+    (void)c;
+    return launch_measure_global(a, v, nlat, st);
+}
+
+// one PT cycle: every group's sweeps + observables (parallel branches), then swap / accumulate
 cudaError_t enqueue_cycle(Ctx* c, int measure, cudaStream_t st)
 {
-    SweepArgs a = base_args(c);
     cudaError_t e;
-    if (c->profile && (e = cudaEventRecordWithFlags(c->ev0, st, cudaEventRecordExternal)) !=
-                           cudaSuccess)
+    if (c->profile &&
+        (e = cudaEventRecordWithFlags(c->ev0, st, cudaEventRecordExternal)) != cudaSuccess)
         return e;
-    if ((e = launch_sweep(a, c->var, c->nlat, c->nthreads, c->smem, st)) != cudaSuccess) return e;
-    if (c->profile && (e = cudaEventRecordWithFlags(c->ev1, st, cudaEventRecordExternal)) !=
-                           cudaSuccess)
+    if (c->G.size() == 1) {
+        const Group& grp = c->G[0];
+        e = enqueue_group(c, grp, grp.var, grp.nthreads, grp.smem, group_args(c, grp), grp.nlat(),
+                          st);
+        if (e != cudaSuccess) return e;
+    } else {
+        if ((e = cudaEventRecord(c->fork_ev, st)) != cudaSuccess) return e;
+        for (size_t k = 0; k < c->G.size(); ++k) {
+            const Group& grp = c->G[k];
+            if ((e = cudaStreamWaitEvent(c->side[k], c->fork_ev, 0)) != cudaSuccess) return e;
+            e = enqueue_group(c, grp, grp.var, grp.nthreads, grp.smem, group_args(c, grp),
+                              grp.nlat(), c->side[k]);
+            if (e != cudaSuccess) return e;
+            if ((e = cudaEventRecord(c->join_ev[k], c->side[k])) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(st, c->join_ev[k], 0)) != cudaSuccess) return e;
+        }
+    }
+    if (c->profile &&
+        (e = cudaEventRecordWithFlags(c->ev1, st, cudaEventRecordExternal)) != cudaSuccess)
         return e;
     return launch_swap(swap_args(c, measure), st);
 }
@@ -272,21 +329,22 @@ int build_graph(Ctx* c, int measure)
 bool valid_conf(Ctx* c, int conf) { return conf >= 0 && conf < c->nconf; }
 
 // Autotuner: times every CTA size of the shape-specialised kernel on a scratch copy of the
-// context's lattices (the live state is not touched) and keeps the fastest.  Choices are cached
-// per (precision, L, H, lattice count) for the life of the process.
+// group's lattices (the live state is not touched) and keeps the fastest.  Choices are cached per
+// (precision, L, H, lattice count) for the life of the process.
 std::mutex g_tune_mu;
 std::map<std::tuple<bool, int, int, int>, int> g_tune_cache;
 
-int autotune(Ctx* c)
+int autotune(Ctx* c, Group& grp)
 {
-    if (c->tuned) return J1J2C_OK;
-    c->tuned = true;
-    if (c->var.fixed_nt == 0 || c->P.block_threads > 0) return J1J2C_OK;
+    if (grp.tuned) return J1J2C_OK;
+    grp.tuned = true;
+    if (grp.var.fixed_nt == 0 || grp.block_threads > 0) return J1J2C_OK;
     int nts[8];
     bool sp[8];
-    const int n = fixed_candidates(c->var.fp64, c->g.L, c->g.H, c->masks, nts, sp, 8);
+    const int n = fixed_candidates(grp.var.fp64, grp.g.L, grp.g.H, c->masks, nts, sp, 8);
     if (n <= 1) return J1J2C_OK;
-    const auto key = std::make_tuple(c->var.fp64, c->g.L, c->g.H, c->nlat);
+    const int nlat = grp.nlat();
+    const auto key = std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, nlat);
     int best_nt = 0;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -297,14 +355,15 @@ int autotune(Ctx* c)
     if (best_nt == 0) {
         uint8_t* tmp = nullptr;
         LatObs* tobs = nullptr;
-        const size_t bytes = (size_t)c->nlat * c->lat_stride;
+        const size_t bytes = (size_t)nlat * grp.lat_stride;
         CK(c, cudaMalloc(&tmp, bytes));
-        if (cudaMalloc(&tobs, sizeof(LatObs) * c->nlat) != cudaSuccess) {
+        if (cudaMalloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess) {
             cudaFree(tmp);
             return fail(c, J1J2C_ENOMEM, "autotuner scratch");
         }
-        cudaError_t e = cudaMemcpyAsync(tmp, c->d_spins, bytes, cudaMemcpyDeviceToDevice, c->own);
-        SweepArgs a = base_args(c);
+        cudaError_t e = cudaMemcpyAsync(tmp, c->d_spins + grp.spin_off, bytes,
+                                        cudaMemcpyDeviceToDevice, c->own);
+        SweepArgs a = group_args(c, grp);
         a.spins = tmp;
         a.obs = tobs;
         a.use_override = 1;
@@ -312,17 +371,17 @@ int autotune(Ctx* c)
         a.sweep_override = 0x5EED0000u;
         float best_ms = 1e30f;
         for (int k = 0; k < n && e == cudaSuccess; ++k) {
-            SweepVariant v = c->var;
+            SweepVariant v = grp.var;
             v.fixed_nt = nts[k];
             v.stage_p = sp[k];
-            const size_t sm = sweep_smem_bytes(c->g, v);
+            const size_t sm = sweep_smem_bytes(grp.g, v);
             if (sm > budget) continue;
             if ((e = launch_fixed(a, v.fp64, nts[k], 0, sm, nullptr, true)) != cudaSuccess) break;
-            if ((e = launch_fixed(a, v.fp64, nts[k], c->nlat, sm, c->own, false)) != cudaSuccess)
+            if ((e = launch_fixed(a, v.fp64, nts[k], nlat, sm, c->own, false)) != cudaSuccess)
                 break;
             cudaEventRecord(c->ev0, c->own);
             for (int r = 0; r < 3 && e == cudaSuccess; ++r)
-                e = launch_fixed(a, v.fp64, nts[k], c->nlat, sm, c->own, false);
+                e = launch_fixed(a, v.fp64, nts[k], nlat, sm, c->own, false);
             cudaEventRecord(c->ev1, c->own);
             if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
             float ms = 0.0f;
@@ -341,23 +400,57 @@ int autotune(Ctx* c)
     }
     for (int k = 0; k < n; ++k)
         if (nts[k] == best_nt) {
-            c->var.fixed_nt = nts[k];
-            c->var.stage_p = sp[k];
-            c->smem = sweep_smem_bytes(c->g, c->var);
-            c->nthreads = nts[k];
+            grp.var.fixed_nt = nts[k];
+            grp.var.stage_p = sp[k];
+            grp.smem = sweep_smem_bytes(grp.g, grp.var);
+            grp.nthreads = nts[k];
             SweepArgs none{};
-            none.g = c->g;
-            CK(c, launch_fixed(none, c->var.fp64, c->nthreads, 0, c->smem, nullptr, true));
+            none.g = grp.g;
+            CK(c, launch_fixed(none, grp.var.fp64, grp.nthreads, 0, grp.smem, nullptr, true));
         }
     free_graphs(c);
     return J1J2C_OK;
+}
+
+int check_params(const j1j2c_params* p, std::string& why)
+{
+    if (p->L < 2 || p->H < 2 || (p->L & 1) || (p->H & 1)) {
+        why = "L and H must be even and >= 2 (8-colour update)";
+        return J1J2C_EINVAL;
+    }
+    if ((long long)p->L * p->L * p->H > (1ll << 28)) {
+        why = "lattice too large";
+        return J1J2C_EINVAL;
+    }
+    if (p->nconf < 1 || p->nreplica < 1) {
+        why = "nconf and nreplica must be >= 1";
+        return J1J2C_EINVAL;
+    }
+    if (p->block_threads < 0 || p->block_threads > 1024 || (p->block_threads % 32)) {
+        why = "block_threads must be 0 or a multiple of 32 up to 1024";
+        return J1J2C_EINVAL;
+    }
+    return J1J2C_OK;
+}
+
+Geo make_geo(int L, int H)
+{
+    Geo g{};
+    g.L = L;
+    g.H = H;
+    g.Lh = L / 2;
+    g.Hh = H / 2;
+    g.N = L * L * H;
+    g.Nc = g.Lh * g.Lh * g.Hh;
+    g.Qr = (g.Lh + 3) / 4;
+    return g;
 }
 
 }  // namespace
 
 extern "C" {
 
-const char* j1j2c_version(void) { return "j1j2cuda 0.1 (sm_103a)"; }
+const char* j1j2c_version(void) { return "j1j2cuda 0.2 (sm_103a)"; }
 
 const char* j1j2c_last_error(void* ctx)
 {
@@ -365,45 +458,58 @@ const char* j1j2c_last_error(void* ctx)
     return static_cast<Ctx*>(ctx)->err.c_str();
 }
 
-int j1j2c_create(void** out, const j1j2c_params* p)
+int j1j2c_create_multi(void** out, const j1j2c_params* groups, int32_t ngroups)
 {
     g_create_error.clear();
-    if (!out || !p) {
-        g_create_error = "null argument";
+    if (!out || !groups || ngroups < 1 || ngroups > 64) {
+        g_create_error = "null argument or bad group count";
         return J1J2C_EINVAL;
     }
     *out = nullptr;
+    const j1j2c_params* p = &groups[0];
     auto bad = [](const std::string& m) {
         g_create_error = m;
         return J1J2C_EINVAL;
     };
-    if (p->L < 2 || p->H < 2 || (p->L & 1) || (p->H & 1))
-        return bad("L and H must be even and >= 2 (8-colour update)");
-    if ((long long)p->L * p->L * p->H > (1ll << 28)) return bad("lattice too large");
-    if (p->nconf < 1 || p->nreplica < 1) return bad("nconf and nreplica must be >= 1");
+    for (int k = 0; k < ngroups; ++k) {
+        std::string why;
+        if (check_params(&groups[k], why) != J1J2C_OK) return bad(why);
+    }
     if (p->ptswapever < 1) return bad("ptswapever must be positive (J:909-912)");
     if (p->precision != J1J2C_FP64_PLAIN && p->precision != J1J2C_FP32_BATCHED)
         return bad("precision must be J1J2C_FP64_PLAIN or J1J2C_FP32_BATCHED");
-    if (p->block_threads < 0 || p->block_threads > 1024 || (p->block_threads % 32))
-        return bad("block_threads must be 0 or a multiple of 32 up to 1024");
     if (!std::isfinite(p->J1h) || !std::isfinite(p->J1v) || !std::isfinite(p->J2) ||
         !std::isfinite(p->J3))
         return bad("couplings must be finite");
 
     Ctx* c = new Ctx();
     c->P = *p;
-    c->g.L = p->L;
-    c->g.H = p->H;
-    c->g.Lh = p->L / 2;
-    c->g.Hh = p->H / 2;
-    c->g.N = p->L * p->L * p->H;
-    c->g.Nc = c->g.Lh * c->g.Lh * c->g.Hh;
-    c->g.Qr = (c->g.Lh + 3) / 4;
-    c->nconf = p->nconf;
-    c->nrep = p->nreplica;
-    c->nlat = p->nconf * p->nreplica;
-    c->lat_stride = ((long long)c->g.N + 15) & ~15ll;
-    c->p_stride = ((long long)c->g.N + 3) & ~3ll;
+    long long spin_bytes = 0, p_elems = 0, mask_bytes = 0;
+    for (int k = 0; k < ngroups; ++k) {
+        Group grp;
+        grp.g = make_geo(groups[k].L, groups[k].H);
+        grp.nconf = groups[k].nconf;
+        grp.nrep = groups[k].nreplica;
+        grp.block_threads = groups[k].block_threads;
+        grp.conf0 = c->nconf;
+        grp.rep0 = c->nentries;
+        grp.lat_stride = ((long long)grp.g.N + 15) & ~15ll;
+        grp.p_stride = ((long long)grp.g.N + 3) & ~3ll;
+        grp.spin_off = spin_bytes;
+        grp.p_off = p_elems;
+        grp.mask_off = mask_bytes;
+        spin_bytes += (long long)grp.nlat() * grp.lat_stride;
+        p_elems += (long long)grp.nconf * grp.p_stride;
+        mask_bytes += (long long)grp.nconf * grp.lat_stride;
+        for (int j = 0; j < grp.nconf; ++j) {
+            c->conf_group.push_back(k);
+            c->conf_rbase.push_back(c->nentries + j * grp.nrep);
+            c->conf_nrep.push_back(grp.nrep);
+        }
+        c->nconf += grp.nconf;
+        c->nentries += grp.nlat();
+        c->G.push_back(grp);
+    }
     c->have_dis.assign(c->nconf, 0);
     c->have_ladder.assign(c->nconf, 0);
     c->have_spins.assign(c->nconf, 0);
@@ -419,47 +525,72 @@ int j1j2c_create(void** out, const j1j2c_params* p)
     };
     cudaError_t e = cudaSetDevice(p->device);
     if (e != cudaSuccess) return cfail(e, "cudaSetDevice");
-    const size_t nl = (size_t)c->nlat, nc = (size_t)c->nconf;
-    if ((e = dalloc(&c->d_spins, nl * c->lat_stride)) != cudaSuccess) return cfail(e, "spins");
-    if ((e = dalloc(&c->d_pf, nc * c->p_stride)) != cudaSuccess) return cfail(e, "field");
-    if ((e = dalloc(&c->d_pd, nc * c->p_stride)) != cudaSuccess) return cfail(e, "field");
-    if ((e = dalloc(&c->d_bm, nc * c->lat_stride)) != cudaSuccess) return cfail(e, "masks");
-    if ((e = dalloc(&c->d_occ, nc * c->lat_stride)) != cudaSuccess) return cfail(e, "occ");
-    if ((e = dalloc(&c->d_beta, nl)) != cudaSuccess) return cfail(e, "beta");
-    if ((e = dalloc(&c->d_rat, nl)) != cudaSuccess) return cfail(e, "maps");
-    if ((e = dalloc(&c->d_tor, nl)) != cudaSuccess) return cfail(e, "maps");
-    if ((e = dalloc(&c->d_obs, nl)) != cudaSuccess) return cfail(e, "obs");
-    if ((e = dalloc(&c->d_sums, nl * 22)) != cudaSuccess) return cfail(e, "sums");
-    if ((e = dalloc(&c->d_nmeas, nl)) != cudaSuccess) return cfail(e, "sums");
-    if ((e = dalloc(&c->d_att, nl)) != cudaSuccess) return cfail(e, "pt stats");
-    if ((e = dalloc(&c->d_acc, nl)) != cudaSuccess) return cfail(e, "pt stats");
-    if ((e = dalloc(&c->d_vis, nl)) != cudaSuccess) return cfail(e, "pt stats");
-    if ((e = dalloc(&c->d_last, nl * 5)) != cudaSuccess) return cfail(e, "obs");
+    const size_t ne = (size_t)c->nentries, nc = (size_t)c->nconf;
+    if ((e = dalloc(&c->d_spins, (size_t)spin_bytes)) != cudaSuccess) return cfail(e, "spins");
+    if ((e = dalloc(&c->d_pf, (size_t)p_elems)) != cudaSuccess) return cfail(e, "field");
+    if ((e = dalloc(&c->d_pd, (size_t)p_elems)) != cudaSuccess) return cfail(e, "field");
+    if ((e = dalloc(&c->d_bm, (size_t)mask_bytes)) != cudaSuccess) return cfail(e, "masks");
+    if ((e = dalloc(&c->d_occ, (size_t)mask_bytes)) != cudaSuccess) return cfail(e, "occ");
+    if ((e = dalloc(&c->d_beta, ne)) != cudaSuccess) return cfail(e, "beta");
+    if ((e = dalloc(&c->d_rat, ne)) != cudaSuccess) return cfail(e, "maps");
+    if ((e = dalloc(&c->d_tor, ne)) != cudaSuccess) return cfail(e, "maps");
+    if ((e = dalloc(&c->d_obs, ne)) != cudaSuccess) return cfail(e, "obs");
+    if ((e = dalloc(&c->d_sums, ne * 22)) != cudaSuccess) return cfail(e, "sums");
+    if ((e = dalloc(&c->d_nmeas, ne)) != cudaSuccess) return cfail(e, "sums");
+    if ((e = dalloc(&c->d_att, ne)) != cudaSuccess) return cfail(e, "pt stats");
+    if ((e = dalloc(&c->d_acc, ne)) != cudaSuccess) return cfail(e, "pt stats");
+    if ((e = dalloc(&c->d_vis, ne)) != cudaSuccess) return cfail(e, "pt stats");
+    if ((e = dalloc(&c->d_last, ne * 5)) != cudaSuccess) return cfail(e, "obs");
     if ((e = dalloc(&c->d_ctl, 4)) != cudaSuccess) return cfail(e, "ctl");
     if ((e = dalloc(&c->d_nocc, nc)) != cudaSuccess) return cfail(e, "nocc");
+    if ((e = dalloc(&c->d_rbase, nc)) != cudaSuccess) return cfail(e, "rbase");
+    if ((e = dalloc(&c->d_nreps, nc)) != cudaSuccess) return cfail(e, "nreps");
     if ((e = dalloc(&c->d_audit, 2)) != cudaSuccess) return cfail(e, "audit");
     if ((e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking)) != cudaSuccess)
         return cfail(e, "stream");
     c->st = c->own;
+    if (ngroups > 1) {
+        if ((e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming)) != cudaSuccess)
+            return cfail(e, "event");
+        for (int k = 0; k < ngroups; ++k) {
+            cudaStream_t s;
+            cudaEvent_t ev;
+            if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess)
+                return cfail(e, "stream");
+            c->side.push_back(s);
+            if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
+                return cfail(e, "event");
+            c->join_ev.push_back(ev);
+        }
+    }
     if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess) return cfail(e, "event");
     if ((e = cudaEventCreate(&c->ev1)) != cudaSuccess) return cfail(e, "event");
-    if ((e = cudaMemset(c->d_spins, 1, nl * c->lat_stride)) != cudaSuccess)
+    if ((e = cudaMemset(c->d_spins, 1, (size_t)spin_bytes)) != cudaSuccess)
         return cfail(e, "memset");
-    if ((e = cudaMemset(c->d_bm, 3, nc * c->lat_stride)) != cudaSuccess) return cfail(e, "memset");
-    if ((e = cudaMemset(c->d_obs, 0, nl * sizeof(LatObs))) != cudaSuccess)
+    if ((e = cudaMemset(c->d_bm, 3, (size_t)mask_bytes)) != cudaSuccess) return cfail(e, "memset");
+    if ((e = cudaMemset(c->d_obs, 0, ne * sizeof(LatObs))) != cudaSuccess)
         return cfail(e, "memset");
-    if ((e = cudaMemcpy(c->d_ctl, c->host_ctl, 2 * sizeof(uint32_t), cudaMemcpyHostToDevice)) !=
+    if ((e = cudaMemcpy(c->d_ctl, c->host_ctl, 4 * sizeof(uint32_t), cudaMemcpyHostToDevice)) !=
         cudaSuccess)
         return cfail(e, "ctl");
-    int rc = choose_variant(c, p->precision == J1J2C_FP64_PLAIN, c->var, c->smem, c->nthreads);
-    if (rc != J1J2C_OK) {
-        g_create_error = c->err;
-        release(c);
-        delete c;
-        return rc;
+    if ((e = cudaMemcpy(c->d_rbase, c->conf_rbase.data(), nc * sizeof(int),
+                        cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cfail(e, "rbase");
+    if ((e = cudaMemcpy(c->d_nreps, c->conf_nrep.data(), nc * sizeof(int),
+                        cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cfail(e, "nreps");
+    for (auto& grp : c->G) {
+        int rc = choose_variant(c, grp, p->precision == J1J2C_FP64_PLAIN, grp.var, grp.smem,
+                                grp.nthreads);
+        if (rc != J1J2C_OK) {
+            g_create_error = c->err;
+            release(c);
+            delete c;
+            return rc;
+        }
     }
     *out = c;
-    rc = j1j2c_reset_measurements(c, -1);
+    int rc = j1j2c_reset_measurements(c, -1);
     if (rc != J1J2C_OK) {
         g_create_error = c->err;
         release(c);
@@ -468,6 +599,15 @@ int j1j2c_create(void** out, const j1j2c_params* p)
         return rc;
     }
     return J1J2C_OK;
+}
+
+int j1j2c_create(void** out, const j1j2c_params* p)
+{
+    if (!p) {
+        g_create_error = "null argument";
+        return J1J2C_EINVAL;
+    }
+    return j1j2c_create_multi(out, p, 1);
 }
 
 void j1j2c_destroy(void* ctx)
@@ -487,6 +627,18 @@ int j1j2c_set_stream(void* ctx, void* stream)
     return J1J2C_OK;
 }
 
+int j1j2c_conf_shape(void* ctx, int32_t conf, int32_t* L, int32_t* H, int32_t* nreplica)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!valid_conf(c, conf)) return fail(c, J1J2C_EINVAL, "conf out of range");
+    const Group& grp = c->G[c->conf_group[conf]];
+    if (L) *L = grp.g.L;
+    if (H) *H = grp.g.H;
+    if (nreplica) *nreplica = grp.nrep;
+    return J1J2C_OK;
+}
+
 int j1j2c_set_disorder(void* ctx, int32_t conf, const double* p, const int8_t* occu,
                        const int8_t* jh, const int8_t* jv)
 {
@@ -494,10 +646,11 @@ int j1j2c_set_disorder(void* ctx, int32_t conf, const double* p, const int8_t* o
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!valid_conf(c, conf)) return fail(c, J1J2C_EINVAL, "conf out of range");
     if (!p) return fail(c, J1J2C_EINVAL, "p is null");
-    const Geo& g = c->g;
-    std::vector<double> pd((size_t)c->p_stride, 0.0);
-    std::vector<float> pf((size_t)c->p_stride, 0.0f);
-    std::vector<uint8_t> occ((size_t)c->lat_stride, 0), bm((size_t)c->lat_stride, 3);
+    Group& grp = c->G[c->conf_group[conf]];
+    const Geo& g = grp.g;
+    std::vector<double> pd((size_t)grp.p_stride, 0.0);
+    std::vector<float> pf((size_t)grp.p_stride, 0.0f);
+    std::vector<uint8_t> occ((size_t)grp.lat_stride, 0), bm((size_t)grp.lat_stride, 3);
     int nocc = 0, anymask = 0;
     for (int s = 0; s < g.N; ++s) {
         if (!std::isfinite(p[s])) return fail(c, J1J2C_EINVAL, "p must be finite");
@@ -511,11 +664,15 @@ int j1j2c_set_disorder(void* ctx, int32_t conf, const double* p, const int8_t* o
         bm[ci] = (uint8_t)(h | (v << 1));
         anymask |= (h == 0 || v == 0);
     }
-    const size_t off = (size_t)conf;
-    CK(c, cudaMemcpy(c->d_pd + off * c->p_stride, pd.data(), pd.size() * 8, cudaMemcpyHostToDevice));
-    CK(c, cudaMemcpy(c->d_pf + off * c->p_stride, pf.data(), pf.size() * 4, cudaMemcpyHostToDevice));
-    CK(c, cudaMemcpy(c->d_occ + off * c->lat_stride, occ.data(), occ.size(), cudaMemcpyHostToDevice));
-    CK(c, cudaMemcpy(c->d_bm + off * c->lat_stride, bm.data(), bm.size(), cudaMemcpyHostToDevice));
+    const int lc = conf - grp.conf0;
+    CK(c, cudaMemcpy(c->d_pd + grp.p_off + (size_t)lc * grp.p_stride, pd.data(), pd.size() * 8,
+                     cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(c->d_pf + grp.p_off + (size_t)lc * grp.p_stride, pf.data(), pf.size() * 4,
+                     cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(c->d_occ + grp.mask_off + (size_t)lc * grp.lat_stride, occ.data(),
+                     occ.size(), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(c->d_bm + grp.mask_off + (size_t)lc * grp.lat_stride, bm.data(), bm.size(),
+                     cudaMemcpyHostToDevice));
     CK(c, cudaMemcpy(c->d_nocc + conf, &nocc, sizeof(int), cudaMemcpyHostToDevice));
     c->nocc[conf] = nocc;
     c->conf_masks[conf] = anymask;
@@ -524,15 +681,17 @@ int j1j2c_set_disorder(void* ctx, int32_t conf, const double* p, const int8_t* o
     if (masks != c->masks) {
         c->masks = masks;
         free_graphs(c);
-        int rc = choose_variant(c, c->P.precision == J1J2C_FP64_PLAIN, c->var, c->smem,
-                                c->nthreads);
-        if (rc != J1J2C_OK) return rc;
-        c->tuned = false;
+        for (auto& gr : c->G) {
+            int rc = choose_variant(c, gr, c->P.precision == J1J2C_FP64_PLAIN, gr.var, gr.smem,
+                                    gr.nthreads);
+            if (rc != J1J2C_OK) return rc;
+            gr.tuned = false;
+        }
     }
     c->have_dis[conf] = 1;
     c->have_spins[conf] = 0;  // vacancies changed: spins must be initialised again
     c->occ_total = 0;
-    for (int k = 0; k < c->nconf; ++k) c->occ_total += (long long)c->nocc[k] * c->nrep;
+    for (int k = 0; k < c->nconf; ++k) c->occ_total += (long long)c->nocc[k] * c->conf_nrep[k];
     return J1J2C_OK;
 }
 
@@ -542,14 +701,18 @@ int j1j2c_set_ladder(void* ctx, int32_t conf, const double* beta)
     Ctx* c = static_cast<Ctx*>(ctx);
     if (conf >= c->nconf) return fail(c, J1J2C_EINVAL, "conf out of range");
     if (!beta) return fail(c, J1J2C_EINVAL, "beta is null");
-    const int c0 = conf < 0 ? 0 : conf, nc = conf < 0 ? c->nconf : 1;
-    for (int k = 0; k < nc * c->nrep; ++k)
+    const int off = conf < 0 ? 0 : c->conf_rbase[conf];
+    const int n = conf < 0 ? c->nentries : c->conf_nrep[conf];
+    for (int k = 0; k < n; ++k)
         if (!std::isfinite(beta[k]) || beta[k] < 0.0)
             return fail(c, J1J2C_EINVAL, "beta must be finite and >= 0");
-    CK(c, cudaMemcpyAsync(c->d_beta + (size_t)c0 * c->nrep, beta,
-                          sizeof(double) * c->nrep * nc, cudaMemcpyHostToDevice, c->st));
+    CK(c, cudaMemcpyAsync(c->d_beta + off, beta, sizeof(double) * n, cudaMemcpyHostToDevice,
+                          c->st));
     CK(c, cudaStreamSynchronize(c->st));
-    for (int k = c0; k < c0 + nc; ++k) c->have_ladder[k] = 1;
+    if (conf < 0)
+        for (int k = 0; k < c->nconf; ++k) c->have_ladder[k] = 1;
+    else
+        c->have_ladder[conf] = 1;
     return J1J2C_OK;
 }
 
@@ -562,28 +725,30 @@ int j1j2c_init_spins(void* ctx, int32_t conf, int32_t start, int32_t axis, const
     if (!spins && (start < 0 || start > 2)) return fail(c, J1J2C_EINVAL, "START must be HOT/FER/STR");
     if (!spins && start == J1J2C_START_STR && axis != 0 && axis != 1)
         return fail(c, J1J2C_EINVAL, "STRAXIS must be X or Y");
-    const Geo& g = c->g;
-    uint8_t* dst = c->d_spins + (size_t)conf * c->nrep * c->lat_stride;
+    const Group& grp = c->G[c->conf_group[conf]];
+    const Geo& g = grp.g;
+    const int lc = conf - grp.conf0, nrep = grp.nrep;
+    uint8_t* dst = c->d_spins + grp.spin_off + (size_t)lc * nrep * grp.lat_stride;
+    const uint8_t* occd = c->d_occ + grp.mask_off + (size_t)lc * grp.lat_stride;
     if (spins) {
         std::vector<uint8_t> occ((size_t)g.N);
-        CK(c, cudaMemcpy(occ.data(), c->d_occ + (size_t)conf * c->lat_stride, g.N,
-                         cudaMemcpyDeviceToHost));
-        std::vector<uint8_t> buf((size_t)c->nrep * c->lat_stride, 1);
-        for (int r = 0; r < c->nrep; ++r)
+        CK(c, cudaMemcpy(occ.data(), occd, g.N, cudaMemcpyDeviceToHost));
+        std::vector<uint8_t> buf((size_t)nrep * grp.lat_stride, 1);
+        for (int r = 0; r < nrep; ++r)
             for (int s = 0; s < g.N; ++s) {
                 const int8_t v = spins[(size_t)r * g.N + s];
                 if (v != 1 && v != -1) return fail(c, J1J2C_EINVAL, "spins must be +1 or -1");
                 const int ci = compact_of_site(g, s);
-                buf[(size_t)r * c->lat_stride + ci] = occ[ci] ? (uint8_t)(v + 1) : (uint8_t)1;
+                buf[(size_t)r * grp.lat_stride + ci] = occ[ci] ? (uint8_t)(v + 1) : (uint8_t)1;
             }
         CK(c, cudaMemcpy(dst, buf.data(), buf.size(), cudaMemcpyHostToDevice));
     } else {
         InitArgs a{};
         a.g = g;
         a.spins = dst;
-        a.lat_stride = c->lat_stride;
-        a.occ = c->d_occ + (size_t)conf * c->lat_stride;
-        a.nrep = c->nrep;
+        a.lat_stride = grp.lat_stride;
+        a.occ = occd;
+        a.nrep = nrep;
         a.start = start;
         a.axis = axis;
         a.seed = c->P.seed;
@@ -591,14 +756,15 @@ int j1j2c_init_spins(void* ctx, int32_t conf, int32_t start, int32_t axis, const
         CK(c, launch_init(a, c->st));
     }
     // Initialize_pt_state: identity maps, swap counters zeroed (J:1222-1233)
-    CK(c, cudaMemsetAsync(c->d_att + (size_t)conf * c->nrep, 0, sizeof(long long) * c->nrep, c->st));
-    CK(c, cudaMemsetAsync(c->d_acc + (size_t)conf * c->nrep, 0, sizeof(long long) * c->nrep, c->st));
-    std::vector<int> ident((size_t)c->nrep);
-    for (int r = 0; r < c->nrep; ++r) ident[r] = r;
-    CK(c, cudaMemcpyAsync(c->d_rat + (size_t)conf * c->nrep, ident.data(), sizeof(int) * c->nrep,
-                          cudaMemcpyHostToDevice, c->st));
-    CK(c, cudaMemcpyAsync(c->d_tor + (size_t)conf * c->nrep, ident.data(), sizeof(int) * c->nrep,
-                          cudaMemcpyHostToDevice, c->st));
+    const int rb = c->conf_rbase[conf];
+    CK(c, cudaMemsetAsync(c->d_att + rb, 0, sizeof(long long) * nrep, c->st));
+    CK(c, cudaMemsetAsync(c->d_acc + rb, 0, sizeof(long long) * nrep, c->st));
+    std::vector<int> ident((size_t)nrep);
+    for (int r = 0; r < nrep; ++r) ident[r] = r;
+    CK(c, cudaMemcpyAsync(c->d_rat + rb, ident.data(), sizeof(int) * nrep, cudaMemcpyHostToDevice,
+                          c->st));
+    CK(c, cudaMemcpyAsync(c->d_tor + rb, ident.data(), sizeof(int) * nrep, cudaMemcpyHostToDevice,
+                          c->st));
     CK(c, cudaStreamSynchronize(c->st));
     c->have_spins[conf] = 1;
     return J1J2C_OK;
@@ -609,8 +775,8 @@ int j1j2c_reset_measurements(void* ctx, int32_t conf)
     if (!ctx) return J1J2C_EINVAL;
     Ctx* c = static_cast<Ctx*>(ctx);
     if (conf >= c->nconf) return fail(c, J1J2C_EINVAL, "conf out of range");
-    const int c0 = conf < 0 ? 0 : conf, c1 = conf < 0 ? c->nconf : conf + 1;
-    const size_t n = (size_t)(c1 - c0) * c->nrep, off = (size_t)c0 * c->nrep;
+    const size_t off = conf < 0 ? 0 : (size_t)c->conf_rbase[conf];
+    const size_t n = conf < 0 ? (size_t)c->nentries : (size_t)c->conf_nrep[conf];
     std::vector<double> sums(n * 22, 0.0);
     for (size_t k = 0; k < n; ++k) sums[k * 22 + 20] = std::numeric_limits<double>::infinity();
     CK(c, cudaMemcpy(c->d_sums + off * 22, sums.data(), sums.size() * 8, cudaMemcpyHostToDevice));
@@ -634,8 +800,10 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
         CK(c, cudaMemcpyAsync(c->d_ctl + 1, &c->host_ctl[1], sizeof(uint32_t),
                               cudaMemcpyHostToDevice, c->st));
     }
-    int rct = autotune(c);
-    if (rct != J1J2C_OK) return rct;
+    for (auto& grp : c->G) {
+        int rct = autotune(c, grp);
+        if (rct != J1J2C_OK) return rct;
+    }
     const bool direct = (c->P.flags & J1J2C_FLAG_NO_GRAPH) != 0;
     if (!direct && !c->graph[m]) {
         int rc = build_graph(c, m);
@@ -646,7 +814,7 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
             CK(c, enqueue_cycle(c, m, c->st));
         else
             CK(c, cudaGraphLaunch(c->graph[m], c->st));
-        if (c->profile) {  // the events bracket the sweep kernel (graph event-record nodes)
+        if (c->profile) {  // the events bracket the sweep launches (graph event-record nodes)
             CK(c, cudaEventSynchronize(c->ev1));
             float ms = 0.0f;
             CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
@@ -666,26 +834,28 @@ int j1j2c_metro_sweep_fp64(void* ctx, int32_t conf, int32_t rep, double beta,
 {
     if (!ctx) return J1J2C_EINVAL;
     Ctx* c = static_cast<Ctx*>(ctx);
-    if (!valid_conf(c, conf) || rep < 0 || rep >= c->nrep)
+    if (!valid_conf(c, conf) || rep < 0 || rep >= c->conf_nrep[conf])
         return fail(c, J1J2C_EINVAL, "conf or replica out of range");
     if (!c->have_dis[conf] || !c->have_spins[conf])
         return fail(c, J1J2C_ESTATE, "conf lacks disorder or spins");
     if (nsweeps < 0 || !std::isfinite(beta) || beta < 0.0)
         return fail(c, J1J2C_EINVAL, "bad nsweeps or beta");
+    Group& grp = c->G[c->conf_group[conf]];
     SweepVariant v;
     size_t smem;
     int nt;
-    int rc = choose_variant(c, true, v, smem, nt);
+    int rc = choose_variant(c, grp, true, v, smem, nt);
     if (rc != J1J2C_OK) return rc;
-    SweepArgs a = base_args(c);
-    a.lat0 = conf * c->nrep + rep;
+    SweepArgs a = group_args(c, grp);
+    const int lat = (conf - grp.conf0) * grp.nrep + rep;
+    a.lat0 = lat;
     a.nsweeps = nsweeps;
     a.use_override = 1;
     a.beta_override = beta;
     a.sweep_override = sweep_index;
-    CK(c, launch_sweep(a, v, 1, nt, smem, c->st));
+    CK(c, enqueue_group(c, grp, v, nt, smem, a, 1, c->st));
     LatObs o;
-    CK(c, cudaMemcpyAsync(&o, c->d_obs + a.lat0, sizeof o, cudaMemcpyDeviceToHost, c->st));
+    CK(c, cudaMemcpyAsync(&o, a.obs + lat, sizeof o, cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaStreamSynchronize(c->st));
     const double dn = (double)c->nocc[conf];
     if (mag) *mag = (double)o.M / dn;
@@ -703,21 +873,24 @@ int j1j2c_audit_fp32(void* ctx, int32_t nsweeps, int64_t* attempts, int64_t* mis
     for (int k = 0; k < c->nconf; ++k)
         if (!c->have_dis[k] || !c->have_ladder[k] || !c->have_spins[k])
             return fail(c, J1J2C_ESTATE, "every conf needs disorder, ladder and spins");
-    SweepVariant v{};
-    v.fp64 = true;
-    v.quad = false;
-    v.stage_p = false;
-    v.masks = c->masks;
-    v.mode = kModeAudit;
-    const size_t smem = sweep_smem_bytes(c->g, v);
-    CK(c, prepare_sweep_variant(v, smem));
-    int nt = ((c->g.Nc + 31) / 32) * 32;
-    if (nt > 512) nt = 512;
-    if (nt < 64) nt = 64;
+    const size_t budget = smem_budget(c);
     CK(c, cudaMemsetAsync(c->d_audit, 0, 2 * sizeof(unsigned long long), c->st));
-    SweepArgs a = base_args(c);
-    a.nsweeps = nsweeps;
-    CK(c, launch_sweep(a, v, c->nlat, nt, smem, c->st));
+    for (auto& grp : c->G) {
+        SweepVariant v{};
+        v.fp64 = true;
+        v.masks = c->masks;
+        v.mode = kModeAudit;
+        const size_t smem = sweep_smem_bytes(grp.g, v);
+        if (smem > budget)
+            return fail(c, J1J2C_EINVAL, "the audit needs lattices that fit shared memory");
+        CK(c, prepare_sweep_variant(v, smem));
+        int nt = ((grp.g.Nc + 31) / 32) * 32;
+        if (nt > 512) nt = 512;
+        if (nt < 64) nt = 64;
+        SweepArgs a = group_args(c, grp);
+        a.nsweeps = nsweeps;
+        CK(c, launch_sweep(a, v, grp.nlat(), nt, smem, c->st));
+    }
     unsigned long long h[2];
     CK(c, cudaMemcpyAsync(h, c->d_audit, sizeof h, cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaStreamSynchronize(c->st));
@@ -731,8 +904,8 @@ int j1j2c_get_slot_sums(void* ctx, int32_t conf, j1j2c_slot_sums* out)
     if (!ctx) return J1J2C_EINVAL;
     Ctx* c = static_cast<Ctx*>(ctx);
     if (conf >= c->nconf || !out) return fail(c, J1J2C_EINVAL, "bad conf or null output");
-    const size_t off = conf < 0 ? 0 : (size_t)conf * c->nrep;
-    const int nr = (conf < 0 ? c->nconf : 1) * c->nrep;
+    const size_t off = conf < 0 ? 0 : (size_t)c->conf_rbase[conf];
+    const int nr = conf < 0 ? c->nentries : c->conf_nrep[conf];
     std::vector<double> sums((size_t)nr * 22);
     std::vector<long long> nm((size_t)nr);
     CK(c, cudaMemcpyAsync(sums.data(), c->d_sums + off * 22, sums.size() * 8,
@@ -753,14 +926,15 @@ int j1j2c_get_pt_stats(void* ctx, int32_t conf, int64_t* attempts, int64_t* acce
     if (!ctx) return J1J2C_EINVAL;
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!valid_conf(c, conf)) return fail(c, J1J2C_EINVAL, "conf out of range");
-    const size_t off = (size_t)conf * c->nrep;
-    std::vector<long long> at((size_t)c->nrep), ac((size_t)c->nrep);
-    std::vector<uint8_t> vis((size_t)c->nrep);
+    const size_t off = (size_t)c->conf_rbase[conf];
+    const int nrep = c->conf_nrep[conf];
+    std::vector<long long> at((size_t)nrep), ac((size_t)nrep);
+    std::vector<uint8_t> vis((size_t)nrep);
     CK(c, cudaMemcpyAsync(at.data(), c->d_att + off, at.size() * 8, cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaMemcpyAsync(ac.data(), c->d_acc + off, ac.size() * 8, cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaMemcpyAsync(vis.data(), c->d_vis + off, vis.size(), cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaStreamSynchronize(c->st));
-    for (int k = 0; k + 1 < c->nrep; ++k) {
+    for (int k = 0; k + 1 < nrep; ++k) {
         if (attempts) attempts[k] = at[k];
         if (accepts) accepts[k] = ac[k];
     }
@@ -777,7 +951,7 @@ int j1j2c_get_maps(void* ctx, int32_t conf, int32_t* rep_at_temp, int32_t* temp_
     if (!ctx) return J1J2C_EINVAL;
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!valid_conf(c, conf)) return fail(c, J1J2C_EINVAL, "conf out of range");
-    const size_t off = (size_t)conf * c->nrep, nb = sizeof(int) * c->nrep;
+    const size_t off = (size_t)c->conf_rbase[conf], nb = sizeof(int) * c->conf_nrep[conf];
     if (rep_at_temp)
         CK(c, cudaMemcpyAsync(rep_at_temp, c->d_rat + off, nb, cudaMemcpyDeviceToHost, c->st));
     if (temp_of_rep)
@@ -790,12 +964,14 @@ int j1j2c_get_spins(void* ctx, int32_t conf, int32_t rep, int8_t* out)
 {
     if (!ctx) return J1J2C_EINVAL;
     Ctx* c = static_cast<Ctx*>(ctx);
-    if (!valid_conf(c, conf) || rep < 0 || rep >= c->nrep || !out)
+    if (!valid_conf(c, conf) || rep < 0 || rep >= c->conf_nrep[conf] || !out)
         return fail(c, J1J2C_EINVAL, "bad conf, replica or output");
-    const Geo& g = c->g;
+    const Group& grp = c->G[c->conf_group[conf]];
+    const Geo& g = grp.g;
     std::vector<uint8_t> buf((size_t)g.N);
-    CK(c, cudaMemcpyAsync(buf.data(), c->d_spins + ((size_t)conf * c->nrep + rep) * c->lat_stride,
-                          g.N, cudaMemcpyDeviceToHost, c->st));
+    const size_t lat = (size_t)(conf - grp.conf0) * grp.nrep + rep;
+    CK(c, cudaMemcpyAsync(buf.data(), c->d_spins + grp.spin_off + lat * grp.lat_stride, g.N,
+                          cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaStreamSynchronize(c->st));
     for (int s = 0; s < g.N; ++s) out[s] = (int8_t)((int)buf[compact_of_site(g, s)] - 1);
     return J1J2C_OK;
@@ -806,8 +982,8 @@ int j1j2c_get_observables(void* ctx, int32_t conf, double* out)
     if (!ctx) return J1J2C_EINVAL;
     Ctx* c = static_cast<Ctx*>(ctx);
     if (conf >= c->nconf || !out) return fail(c, J1J2C_EINVAL, "bad conf or null output");
-    const size_t off = conf < 0 ? 0 : (size_t)conf * c->nrep;
-    const size_t nr = (size_t)(conf < 0 ? c->nconf : 1) * c->nrep;
+    const size_t off = conf < 0 ? 0 : (size_t)c->conf_rbase[conf];
+    const size_t nr = conf < 0 ? (size_t)c->nentries : (size_t)c->conf_nrep[conf];
     CK(c, cudaMemcpyAsync(out, c->d_last + off * 5, sizeof(double) * 5 * nr,
                           cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaStreamSynchronize(c->st));
@@ -829,9 +1005,10 @@ int j1j2c_get_config(void* ctx, int32_t* block_threads, int32_t* sites_per_threa
 {
     if (!ctx) return J1J2C_EINVAL;
     Ctx* c = static_cast<Ctx*>(ctx);
-    if (block_threads) *block_threads = c->nthreads;
-    if (sites_per_thread) *sites_per_thread = c->var.quad ? 4 : 1;
-    if (smem_bytes) *smem_bytes = (int32_t)c->smem;
+    const Group& grp = c->G[0];
+    if (block_threads) *block_threads = grp.nthreads;
+    if (sites_per_thread) *sites_per_thread = grp.var.quad ? 4 : 1;
+    if (smem_bytes) *smem_bytes = (int32_t)grp.smem;
     return J1J2C_OK;
 }
 

@@ -44,20 +44,24 @@ struct SweepArgs {
     uint32_t sweep_override;
 };
 
+// Replica-indexed arrays are laid out conf by conf: conf c owns entries rbase[c] ..
+// rbase[c] + nreps[c] - 1 (replica, slot or pair index within the conf).
 struct SwapArgs {
-    const LatObs* obs;   // [nconf*nrep]
-    const double* beta;  // [nconf*nrep]
-    const int* nocc;     // [nconf]
-    int* rat;            // rep_at_temp [nconf*nrep]
-    int* tor;            // temp_of_rep [nconf*nrep]
-    double* sums;        // [nconf*nrep*22]
-    long long* nmeas;    // [nconf*nrep]
-    long long* att;      // [nconf*nrep] (pair index)
-    long long* acc;      // [nconf*nrep]
-    uint8_t* visited;    // [nconf*nrep] bit0 cold end, bit1 hot end
-    double* last_obs;    // [nconf*nrep*5]
-    uint32_t* ctl;       // ctl[0] cycle, ctl[1] swap phase (1 or 2)
-    int nconf, nrep, measure;
+    const LatObs* obs;   // per replica
+    const double* beta;  // per slot
+    const int* nocc;     // per conf
+    const int* rbase;    // per conf: first replica-indexed entry
+    const int* nreps;    // per conf: ladder length
+    int* rat;            // rep_at_temp, per slot
+    int* tor;            // temp_of_rep, per replica
+    double* sums;        // 22 per slot
+    long long* nmeas;    // per slot
+    long long* att;      // per pair
+    long long* acc;      // per pair
+    uint8_t* visited;    // per replica: bit0 cold end, bit1 hot end
+    double* last_obs;    // 5 per replica
+    uint32_t* ctl;       // ctl[0] cycle, ctl[1] swap phase (1 or 2), ctl[2] CTA ticket
+    int nconf, measure;
     uint32_t seed, conf_base;
 };
 
@@ -78,7 +82,15 @@ struct SweepVariant {
     bool masks;    // bond dilution present
     int mode;      // kModeSweep / kModeAudit
     int fixed_nt;  // > 0: shape-specialised kernel with this many threads per CTA
+    bool global;   // lattice in HBM, one launch per colour phase (too large for shared memory)
 };
+
+// Global-memory path: one colour phase of sweep t of the cycle, and the observable reduction
+// (adds into a.obs, which the caller zeroes first).
+cudaError_t launch_sweep_global(const SweepArgs& a, const SweepVariant& v, int colour, int t,
+                                int nlat, cudaStream_t st);
+cudaError_t launch_measure_global(const SweepArgs& a, const SweepVariant& v, int nlat,
+                                  cudaStream_t st);
 
 // Shape-specialised kernels (sweep_fixed.cu): CTA sizes available for a shape, and the launch.
 int fixed_candidates(bool fp64, int L, int H, bool masks, int* nts, bool* stage_p, int cap);

@@ -434,18 +434,22 @@ __global__ void __launch_bounds__(1024) sweep_kernel(SweepArgs a)
 }
 
 // ------------------------------------------------------------------------------------------------
-// PT swap + per-slot accumulation: one CTA, one warp per conf.
+// PT swap + per-slot accumulation: one warp per conf, kSwapWarps confs per CTA.  The last CTA to
+// finish (atomic ticket) advances the cycle counter and the swap phase for the next cycle.
 // ------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) swap_kernel(SwapArgs a)
+constexpr int kSwapWarps = 4;
+
+__global__ void __launch_bounds__(32 * kSwapWarps) swap_kernel(SwapArgs a)
 {
     const uint32_t cycle = a.ctl[0];
     const int phase = (int)a.ctl[1];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int conf = warp; conf < a.nconf; conf += nw) {
-        const int base = conf * a.nrep;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int conf = (int)blockIdx.x * kSwapWarps + warp;
+    if (conf < a.nconf) {
+        const int base = a.rbase[conf], nrep = a.nreps[conf];
         const double dn = (double)a.nocc[conf];
         const double dn1 = (double)(a.nocc[conf] < 1 ? 1 : a.nocc[conf]);
-        for (int rep = lane; rep < a.nrep; rep += 32) {
+        for (int rep = lane; rep < nrep; rep += 32) {
             const LatObs o = a.obs[base + rep];
             double* lo = a.last_obs + 5 * (base + rep);
             lo[0] = (double)o.M / dn;
@@ -456,7 +460,7 @@ __global__ void __launch_bounds__(1024) swap_kernel(SwapArgs a)
         }
         __syncwarp();
         // Pt_attempt_swaps: disjoint pairs (s, s+1), s = phase-1, phase+1, ...
-        for (int s = (phase == 1 ? 0 : 1) + 2 * lane; s < a.nrep - 1; s += 64) {
+        for (int s = (phase == 1 ? 0 : 1) + 2 * lane; s < nrep - 1; s += 64) {
             const int rlo = a.rat[base + s], rhi = a.rat[base + s + 1];
             a.att[base + s] += 1;
             const double elo = __dmul_rn((double)a.obs[base + rlo].eacc, 0x1p-33);
@@ -479,12 +483,12 @@ __global__ void __launch_bounds__(1024) swap_kernel(SwapArgs a)
         }
         __syncwarp();
         if (a.measure) {
-            for (int rep = lane; rep < a.nrep; rep += 32) {
+            for (int rep = lane; rep < nrep; rep += 32) {
                 const int t = a.tor[base + rep];
                 if (t == 0) a.visited[base + rep] |= 1;
-                if (t == a.nrep - 1) a.visited[base + rep] |= 2;
+                if (t == nrep - 1) a.visited[base + rep] |= 2;
             }
-            for (int sl = lane; sl < a.nrep; sl += 32) {
+            for (int sl = lane; sl < nrep; sl += 32) {
                 const double* o = a.last_obs + 5 * (base + a.rat[base + sl]);
                 double* S = a.sums + 22 * (base + sl);
                 const double amag = o[0], aen = o[1], ax = o[2], ay = o[3], anb = o[4];
@@ -521,8 +525,91 @@ __global__ void __launch_bounds__(1024) swap_kernel(SwapArgs a)
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        a.ctl[0] = cycle + 1u;
-        a.ctl[1] = (uint32_t)(3 - phase);
+        __threadfence();
+        const unsigned int t = atomicAdd(&a.ctl[2], 1u);
+        if (t == gridDim.x - 1) {  // every other CTA has read ctl and finished
+            a.ctl[0] = cycle + 1u;
+            a.ctl[1] = (uint32_t)(3 - phase);
+            a.ctl[2] = 0u;
+            __threadfence();
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Lattices too large for shared memory (L = 96: 864 KiB of spins): one launch per colour phase,
+// grid (work items / CTA, lattices); the kernel boundary is the barrier between colours.  Spins
+// and the field stay in HBM / L2; the measurement is a separate launch that reduces per CTA and
+// adds into the (zeroed) per-lattice observables with atomics.
+// ------------------------------------------------------------------------------------------------
+template <class Real, bool QUAD, bool MASKS>
+__global__ void __launch_bounds__(256) sweep_global_kernel(SweepArgs a, int colour, int t)
+{
+    const Geo g = a.g;
+    const int lat = a.lat0 + (int)blockIdx.y;
+    const int conf = lat / a.nrep;
+    const int rep = lat - conf * a.nrep;
+    uint8_t* S = a.spins + (long long)lat * a.lat_stride;
+    const Real* P = field_base<Real>(a, conf);
+    const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
+    double beta;
+    uint32_t sweep;
+    if (a.use_override) {
+        beta = a.beta_override;
+        sweep = a.sweep_override + (uint32_t)t;
+    } else {
+        beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+        sweep = a.ctl[0] * (uint32_t)a.ptswapever + (uint32_t)t;
+    }
+    const float kb = (float)(-2.0 * beta * 1.4426950408889634);
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    const int item = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    Acc acc{0, 0, 0, 0, 0};
+    if constexpr (QUAD) {
+        if (item < (g.Nc >> 2))
+            quad_step<Real, MASKS, false>(a, g, reinterpret_cast<uint32_t*>(S), P, BM, colour,
+                                          item, sweep, (uint32_t)rep, k0, k1, beta, kb, acc);
+    } else {
+        if (item < g.Nc) {
+            const int X = item % g.Lh, r = item / g.Lh;
+            site_step<Real, MASKS, kModeSweep, false>(a, g, S, P, BM, nullptr, colour, X,
+                                                      r % g.Lh, r / g.Lh, sweep, (uint32_t)rep,
+                                                      k0, k1, beta, kb, acc);
+        }
+    }
+}
+
+template <class Real, bool QUAD, bool MASKS>
+__global__ void __launch_bounds__(256) measure_global_kernel(SweepArgs a)
+{
+    const Geo g = a.g;
+    const int lat = a.lat0 + (int)blockIdx.y;
+    const int conf = lat / a.nrep;
+    uint8_t* S = a.spins + (long long)lat * a.lat_stride;
+    const Real* P = field_base<Real>(a, conf);
+    const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
+    const int per = QUAD ? (g.Nc >> 2) : g.Nc;
+    const int item = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    Acc acc{0, 0, 0, 0, 0};
+    if (item < 8 * per) {
+        const int c = item / per, k = item - c * per;
+        if constexpr (QUAD) {
+            quad_step<Real, MASKS, true>(a, g, reinterpret_cast<uint32_t*>(S), P, BM, c, k, 0u, 0u,
+                                         0u, 0u, 0.0, 0.0f, acc);
+        } else {
+            const int X = k % g.Lh, r = k / g.Lh;
+            site_step<Real, MASKS, kModeSweep, true>(a, g, S, P, BM, nullptr, c, X, r % g.Lh,
+                                                     r / g.Lh, 0u, 0u, 0u, 0u, 0.0, 0.0f, acc);
+        }
+    }
+    const Acc tot = block_reduce(acc);
+    if (threadIdx.x == 0) {
+        LatObs* o = a.obs + lat;
+        atomicAdd(reinterpret_cast<unsigned long long*>(&o->eacc), (unsigned long long)tot.e);
+        atomicAdd(&o->M, tot.M);
+        atomicAdd(&o->SX, tot.SX);
+        atomicAdd(&o->SY, tot.SY);
+        atomicAdd(&o->NB, tot.NB);
     }
 }
 
@@ -621,11 +708,52 @@ cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks,
     return dispatch(a, v, nblocks, nthreads, smem, st, false);
 }
 
+namespace {
+template <class Real, bool QUAD, bool MASKS>
+cudaError_t global_pass(const SweepArgs& a, int colour, int t, int nlat, cudaStream_t st,
+                        bool measure)
+{
+    const int per = QUAD ? (a.g.Nc >> 2) : a.g.Nc;
+    if (measure) {
+        dim3 grid((unsigned)((8 * per + 255) / 256), (unsigned)nlat);
+        measure_global_kernel<Real, QUAD, MASKS><<<grid, 256, 0, st>>>(a);
+    } else {
+        dim3 grid((unsigned)((per + 255) / 256), (unsigned)nlat);
+        sweep_global_kernel<Real, QUAD, MASKS><<<grid, 256, 0, st>>>(a, colour, t);
+    }
+    return cudaGetLastError();
+}
+
+template <class Real>
+cudaError_t global_dispatch(const SweepArgs& a, const SweepVariant& v, int colour, int t,
+                            int nlat, cudaStream_t st, bool measure)
+{
+    if (v.quad)
+        return v.masks ? global_pass<Real, true, true>(a, colour, t, nlat, st, measure)
+                       : global_pass<Real, true, false>(a, colour, t, nlat, st, measure);
+    return v.masks ? global_pass<Real, false, true>(a, colour, t, nlat, st, measure)
+                   : global_pass<Real, false, false>(a, colour, t, nlat, st, measure);
+}
+}  // namespace
+
+cudaError_t launch_sweep_global(const SweepArgs& a, const SweepVariant& v, int colour, int t,
+                                int nlat, cudaStream_t st)
+{
+    return v.fp64 ? global_dispatch<double>(a, v, colour, t, nlat, st, false)
+                  : global_dispatch<float>(a, v, colour, t, nlat, st, false);
+}
+
+cudaError_t launch_measure_global(const SweepArgs& a, const SweepVariant& v, int nlat,
+                                  cudaStream_t st)
+{
+    return v.fp64 ? global_dispatch<double>(a, v, 0, 0, nlat, st, true)
+                  : global_dispatch<float>(a, v, 0, 0, nlat, st, true);
+}
+
 cudaError_t launch_swap(const SwapArgs& a, cudaStream_t st)
 {
-    int nt = 32 * a.nconf;
-    if (nt > 1024) nt = 1024;
-    swap_kernel<<<1, nt, 0, st>>>(a);
+    const int nb = (a.nconf + kSwapWarps - 1) / kSwapWarps;
+    swap_kernel<<<nb, 32 * kSwapWarps, 0, st>>>(a);
     return cudaGetLastError();
 }
 

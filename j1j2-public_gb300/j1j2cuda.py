@@ -21,13 +21,13 @@ OK, EINVAL, ECUDA, ETIMEOUT, ENOMEM, ESTATE = 0, -1, -2, -3, -4, -5
 FP64_PLAIN, FP32_BATCHED = 0, 1
 START_HOT, START_FER, START_STR = 0, 1, 2
 AXIS_X, AXIS_Y = 0, 1
-FLAG_NO_GRAPH, FLAG_PROFILE, FLAG_GENERIC, FLAG_NO_FIXED = 1, 2, 4, 8
+FLAG_NO_GRAPH, FLAG_PROFILE, FLAG_GENERIC, FLAG_NO_FIXED, FLAG_GLOBAL = 1, 2, 4, 8, 16
 
 SUM_FIELDS = ("mag", "absmag", "mag2", "mag4", "en", "en2", "strx_abs", "stry_abs", "strx2",
               "strx4", "stry2", "stry4", "str2", "str4", "absstr", "nem", "nbar", "nbarabs",
               "nbar2", "nbar4", "best_en", "final_en")
 
-EXPORTS = ("j1j2c_create", "j1j2c_destroy", "j1j2c_last_error", "j1j2c_set_stream",
+EXPORTS = ("j1j2c_create", "j1j2c_create_multi", "j1j2c_conf_shape", "j1j2c_destroy", "j1j2c_last_error", "j1j2c_set_stream",
            "j1j2c_set_disorder", "j1j2c_set_ladder", "j1j2c_init_spins",
            "j1j2c_reset_measurements", "j1j2c_run", "j1j2c_metro_sweep_fp64", "j1j2c_audit_fp32",
            "j1j2c_get_slot_sums", "j1j2c_get_pt_stats", "j1j2c_get_maps", "j1j2c_get_spins",
@@ -136,21 +136,45 @@ def disorder(L, H, seed, phi=2.0, xi=3.0, map_uniform=True) -> np.ndarray:
 # engine context
 # ------------------------------------------------------------------------------------------------
 class Engine:
-    """One libj1j2cuda context: nconf disorder configurations x nreplica ladder replicas."""
+    """One libj1j2cuda context: nconf disorder configurations x nreplica ladder replicas, or
+    several lattice-shape groups (``groups=[(L, H, nconf, nreplica), ...]``) in one batch."""
 
-    def __init__(self, L, H=None, nconf=1, nreplica=1, ptswapever=5, precision=FP32_BATCHED,
+    def __init__(self, L=None, H=None, nconf=1, nreplica=1, ptswapever=5, precision=FP32_BATCHED,
                  seed=1, conf_base=0, J1h=1.0, J1v=1.0, J2=-1.0, J3=1.0, device=0, flags=0,
-                 block_threads=0):
-        H = L if H is None else H
-        self.L, self.H, self.N = int(L), int(H), int(L) * int(L) * int(H)
-        self.nconf, self.nrep, self.ptswapever = int(nconf), int(nreplica), int(ptswapever)
-        self.precision = precision
-        self.params = Params(self.L, self.H, J1h, J1v, J2, J3, self.nconf, self.nrep,
-                             self.ptswapever, precision, seed, conf_base, device, flags,
-                             block_threads)
+                 block_threads=0, groups=None):
+        if groups is None:
+            groups = [(L, L if H is None else H, nconf, nreplica, block_threads)]
+        groups = [tuple(g) + (block_threads,) * (5 - len(g)) for g in groups]
+        self.ptswapever, self.precision = int(ptswapever), precision
+        arr = (Params * len(groups))()
+        for k, (gL, gH, gn, gr, gbt) in enumerate(groups):
+            arr[k] = Params(gL, gH, J1h, J1v, J2, J3, gn, gr, self.ptswapever, precision, seed,
+                            conf_base, device, flags, gbt)
+        self.params = arr
         self._ctx = C.c_void_p()
-        _check(None, lib().j1j2c_create(C.byref(self._ctx), C.byref(self.params)))
-        self.nocc = np.full(self.nconf, self.N, np.int64)
+        _check(None, lib().j1j2c_create_multi(C.byref(self._ctx), arr, C.c_int32(len(groups))))
+        self.shapes = []  # per conf: (L, H, nreplica)
+        for gL, gH, gn, gr, _ in groups:
+            self.shapes += [(int(gL), int(gH), int(gr))] * int(gn)
+        self.nconf = len(self.shapes)
+        self.L, self.H, _, _, _ = (int(v) for v in groups[0])
+        self.nrep = int(groups[0][3])
+        self.N = self.L * self.L * self.H
+        self.rbase = np.cumsum([0] + [s[2] for s in self.shapes])
+        self.nentries = int(self.rbase[-1])
+        self.nocc = np.array([s[0] * s[0] * s[1] for s in self.shapes], np.int64)
+
+    def _shape(self, conf):
+        if not 0 <= conf < self.nconf:
+            raise J1J2CError(EINVAL, f"conf {conf} out of range")
+        return self.shapes[conf]
+
+    def n_of(self, conf):
+        L, H, _ = self._shape(conf)
+        return L * L * H
+
+    def nrep_of(self, conf):
+        return self._shape(conf)[2]
 
     # life cycle --------------------------------------------------------------------------------
     def close(self):
@@ -183,17 +207,17 @@ class Engine:
     # inputs ------------------------------------------------------------------------------------
     def set_disorder(self, conf, p, occu=None, jh=None, jv=None):
         p = np.ascontiguousarray(p, np.float64).reshape(-1)
-        assert p.size == self.N
+        assert p.size == self.n_of(conf)
         arrs = [None if a is None else np.ascontiguousarray(a, np.int8).reshape(-1)
                 for a in (occu, jh, jv)]
         ptrs = [None if a is None else _p(a, C.c_int8) for a in arrs]
         self._ck(lib().j1j2c_set_disorder(self._ctx, C.c_int32(conf), _p(p, C.c_double), *ptrs))
-        self.nocc[conf] = self.N if arrs[0] is None else int((arrs[0] != 0).sum())
+        self.nocc[conf] = p.size if arrs[0] is None else int((arrs[0] != 0).sum())
 
     def set_ladder(self, conf, beta):
         """beta of one conf (nrep), or of every conf when conf < 0 (nconf x nrep)."""
         b = np.ascontiguousarray(beta, np.float64)
-        assert b.size == (self.nconf * self.nrep if conf < 0 else self.nrep)
+        assert b.size == (self.nentries if conf < 0 else self.nrep_of(conf))
         self._ck(lib().j1j2c_set_ladder(self._ctx, C.c_int32(conf), _p(b, C.c_double)))
 
     def init_spins(self, conf, start=START_HOT, axis=AXIS_X, spins=None):
@@ -201,7 +225,7 @@ class Engine:
             self._ck(lib().j1j2c_init_spins(self._ctx, C.c_int32(conf), C.c_int32(start),
                                             C.c_int32(axis), None))
         else:
-            s = np.ascontiguousarray(spins, np.int8).reshape(self.nrep, self.N)
+            s = np.ascontiguousarray(spins, np.int8).reshape(self.nrep_of(conf), self.n_of(conf))
             self._ck(lib().j1j2c_init_spins(self._ctx, C.c_int32(conf), C.c_int32(start),
                                             C.c_int32(axis), _p(s, C.c_int8)))
 
@@ -230,34 +254,36 @@ class Engine:
     def slot_sums(self, conf):
         """(nrep, 22) running sums in SUM_FIELDS order and the (nrep,) measurement counts;
         conf < 0 returns every conf, (nconf*nrep, 22) and (nconf*nrep,)."""
-        n = self.nrep * (self.nconf if conf < 0 else 1)
+        n = self.nentries if conf < 0 else self.nrep_of(conf)
         raw = np.zeros(n, dtype=np.dtype([("s", np.float64, 22), ("n", np.int64)]))
         self._ck(lib().j1j2c_get_slot_sums(self._ctx, C.c_int32(conf),
                                            raw.ctypes.data_as(C.c_void_p)))
         return raw["s"].copy(), raw["n"].copy()
 
     def pt_stats(self, conf):
-        n = max(self.nrep - 1, 1)
+        nrep = self.nrep_of(conf)
+        n = max(nrep - 1, 1)
         att, acc = np.zeros(n, np.int64), np.zeros(n, np.int64)
         vb = C.c_int32()
         self._ck(lib().j1j2c_get_pt_stats(self._ctx, C.c_int32(conf), _p(att, C.c_int64),
                                           _p(acc, C.c_int64), C.byref(vb)))
-        return att[:self.nrep - 1], acc[:self.nrep - 1], vb.value
+        return att[:nrep - 1], acc[:nrep - 1], vb.value
 
     def maps(self, conf):
-        rat, tor = np.empty(self.nrep, np.int32), np.empty(self.nrep, np.int32)
+        nrep = self.nrep_of(conf)
+        rat, tor = np.empty(nrep, np.int32), np.empty(nrep, np.int32)
         self._ck(lib().j1j2c_get_maps(self._ctx, C.c_int32(conf), _p(rat, C.c_int32),
                                       _p(tor, C.c_int32)))
         return rat, tor
 
     def spins(self, conf, rep):
-        s = np.empty(self.N, np.int8)
+        s = np.empty(self.n_of(conf), np.int8)
         self._ck(lib().j1j2c_get_spins(self._ctx, C.c_int32(conf), C.c_int32(rep),
                                        _p(s, C.c_int8)))
         return s
 
     def observables(self, conf):
-        out = np.empty((self.nrep * (self.nconf if conf < 0 else 1), 5))
+        out = np.empty((self.nentries if conf < 0 else self.nrep_of(conf), 5))
         self._ck(lib().j1j2c_get_observables(self._ctx, C.c_int32(conf), _p(out, C.c_double)))
         return out
 

@@ -49,6 +49,8 @@ def test_hot_start_is_the_philox_stream(engine_mod, oracle, L, H):
 @pytest.mark.parametrize("L,H,pp,bonds,flags", [
     (16, 16, 0.0, 0.0, 0),      # quad path
     (8, 4, 0.1, 0.2, 0),        # quad path, vacancies and diluted bonds
+    (8, 4, 0.1, 0.2, 16),       # global-memory path (one launch per colour), quad
+    (10, 6, 0.1, 0.0, 16),      # global-memory path, per-site
     (10, 10, 0.0, 0.0, 0),      # per-site path (L/2 odd)
     (4, 2, 0.0, 0.0, 0),        # per-site path, doubled J3 and x/y slots (H = 2)
     (12, 6, 0.05, 0.1, 0),      # per-site path with dilution
@@ -82,6 +84,7 @@ def test_fp64_sweep_bit_identical_to_replay(engine_mod, oracle, L, H, pp, bonds,
     (8, 4, 2, 4, 0.0, 1),   # direct launches instead of the CUDA graph
     (16, 4, 1, 1, 0.0, 0),  # LOCAL sampler: one replica, no swaps
     (24, 24, 1, 2, 0.0, 0),  # shape-specialised FP64 kernel (config-2 lattice)
+    (8, 4, 3, 4, 0.1, 16),   # global-memory path
 ])
 def test_fp64_pt_run_bit_identical_to_replay(engine_mod, oracle, L, H, nconf, nrep, pp, flags):
     jc = engine_mod
@@ -139,7 +142,8 @@ def test_specialised_kernels_agree_bitwise(engine_mod, oracle, precision, L):
     nts = {16: [128, 64], 24: [448, 224], 32: [1024, 512]}[L] if precision == 1 else \
         {24: [448], 32: [512]}[L]
     runs = []
-    for flags, bt in [(jc.FLAG_NO_FIXED, 0), (jc.FLAG_GENERIC, 0)] + [(0, nt) for nt in nts]:
+    for flags, bt in [(jc.FLAG_NO_FIXED, 0), (jc.FLAG_GENERIC, 0), (jc.FLAG_GLOBAL, 0)] + \
+            [(0, nt) for nt in nts]:
         eng = jc.Engine(L, L, nconf=2, nreplica=3, precision=precision, seed=SEED, flags=flags,
                         block_threads=bt)
         for k in range(2):
@@ -158,6 +162,78 @@ def test_specialised_kernels_agree_bitwise(engine_mod, oracle, precision, L):
             np.testing.assert_array_equal(a, b)
         np.testing.assert_array_equal(runs[0][1], other[1])
         np.testing.assert_array_equal(runs[0][2], other[2])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_mixed_shape_context(engine_mod, oracle, precision):
+    """Several lattice shapes in one context (one graph per cycle): every conf evolves exactly as
+    in a single-shape context with the same Philox key; FP64 confs also match the replay."""
+    jc = engine_mod
+    groups = [(8, 4, 2, 3), (10, 6, 1, 2), (16, 16, 2, 4)]
+    eng = jc.Engine(groups=groups, precision=precision, seed=SEED)
+    models, conf = [], 0
+    for L, H, n, r in groups:
+        for _ in range(n):
+            p = jc.disorder(L, H, SEED + conf)
+            occu, _, _, _ = jc.setup_vacancies(SEED + conf, L, H, 0.05)
+            eng.set_disorder(conf, p, occu)
+            eng.set_ladder(conf, _betas(r))
+            eng.init_spins(conf, jc.START_HOT)
+            models.append((L, H, r, p, occu))
+            conf += 1
+    eng.reset_measurements()
+    eng.run(4, measure=False)
+    eng.reset_measurements()
+    eng.run(6, measure=True)
+    for k, (L, H, r, p, occu) in enumerate(models):
+        single = jc.Engine(L, H, nconf=1, nreplica=r, precision=precision, seed=SEED,
+                           conf_base=k)
+        single.set_disorder(0, p, occu)
+        single.set_ladder(0, _betas(r))
+        single.init_spins(0, jc.START_HOT)
+        single.reset_measurements()
+        single.run(4, measure=False)
+        single.reset_measurements()
+        single.run(6, measure=True)
+        for rep in range(r):
+            np.testing.assert_array_equal(eng.spins(k, rep), single.spins(0, rep))
+        np.testing.assert_array_equal(eng.slot_sums(k)[0], single.slot_sums(0)[0])
+        np.testing.assert_array_equal(eng.maps(k)[0], single.maps(0)[0])
+        single.close()
+        if precision == 0:
+            M = oracle.Model(L, H, p, occu)
+            st = oracle.new_pt_state(np.stack([oracle.hot_spins_philox(L, H, SEED, k, q) * occu
+                                               for q in range(r)]))
+            M.replay_pt(st, _betas(r), 5, 4, 0, SEED, k, False, 1)
+            M.replay_pt(st, _betas(r), 5, 6, 4, SEED, k, True, 1)
+            np.testing.assert_array_equal(eng.slot_sums(k)[0], st["sums"])
+    eng.close()
+
+
+def test_large_diluted_lattice_global_path(engine_mod, oracle):
+    """L = 96 with 5 % vacancies (config 5 shape) runs on the global-memory path; the kernel's
+    observables equal the reference Measurement of the returned configuration."""
+    jc = engine_mod
+    L = 96
+    eng = jc.Engine(L, L, nconf=1, nreplica=2, precision=jc.FP32_BATCHED, seed=SEED)
+    p = jc.disorder(L, L, SEED)
+    occu, _, _, nimp = jc.setup_vacancies(SEED, L, L, 0.05)
+    assert 0.04 < nimp / L ** 3 < 0.06
+    eng.set_disorder(0, p, occu)
+    eng.set_ladder(0, _betas(2))
+    eng.init_spins(0, jc.START_HOT)
+    eng.reset_measurements()
+    eng.run(2, measure=True)
+    M = oracle.Model(L, L, p, occu)
+    obs = eng.observables(0)
+    for rep in range(2):
+        s = eng.spins(0, rep)
+        assert (s[occu == 0] == 0).all() and set(np.unique(s[occu == 1])) <= {-1, 1}
+        ref = M.measurement(s)
+        assert obs[rep, 0] == ref[0] and obs[rep, 2] == ref[2] and obs[rep, 3] == ref[3]
+        assert abs(obs[rep, 1] - ref[1]) < 1e-5  # FP32 field per site
+        assert obs[rep, 4] == M.nbar(s)
+    eng.close()
 
 
 def test_fp32_decision_mismatch_rate(engine_mod, oracle):
