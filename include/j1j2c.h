@@ -49,6 +49,7 @@ extern "C" {
 #define J1J2C_FLAG_GENERIC 4u    /* force the per-site kernel path (testing)                      */
 #define J1J2C_FLAG_NO_FIXED 8u   /* skip the shape-specialised kernels (testing)                  */
 #define J1J2C_FLAG_GLOBAL 16u    /* force the global-memory (one launch per colour) path (testing) */
+#define J1J2C_FLAG_WOLFF 32u     /* one Wolff cluster update at the start of every PT cycle       */
 
 /* Run parameters: the compile-time constants of J:43-96 that the hot path consumes. */
 typedef struct {
@@ -151,6 +152,18 @@ int j1j2c_metro_sweep_fp64(void *ctx, int32_t conf, int32_t rep, double beta,
                            uint32_t sweep_index, int32_t nsweeps, double *mag, double *en,
                            double *strx, double *stry);
 
+/* One Wolff cluster update of every lattice at its slot's beta: bonds with K s_i s_j > 0 are
+ * activated with probability 1 - exp(-2 beta K s_i s_j) (K the per-bond coupling of
+ * Compute_local_field, J:2498-2541), components are labelled by union-find in a scratch array
+ * the context allocates on first use, and the component of a Philox-chosen seed site is flipped.
+ * The random stream is indexed by the PT cycle counter (a cycle with J1J2C_FLAG_WOLFF runs this
+ * before its sweeps).  cluster_sizes (NULL or nconf x NREPLICA) receives the flipped sizes.
+ * Replaces the Wolff update named in the reference's header (J:7), which it never implements. */
+int j1j2c_wolff(void *ctx, int64_t *cluster_sizes);
+
+/* Flipped-cluster sizes of the last Wolff update of one conf (NREPLICA; conf < 0: all). */
+int j1j2c_get_cluster_sizes(void *ctx, int32_t conf, int64_t *out);
+
 /* Deterministic replay audit of the FP32 form: nsweeps FP64 sweeps of every lattice at its slot's
  * beta, evaluating at every attempt the FP32 decision on the same configuration and uniform.
  * Adds to *attempts and *mismatches (FP32 decision != FP64 decision).  No reference
@@ -214,6 +227,16 @@ int j1j2c_kiss_spins(int32_t seed, int32_t L, int32_t H, int32_t start, int32_t 
  * 1 SPLIT around tmid with fraction tfrac of the intervals below it. */
 int j1j2c_ladder(int32_t n, double tmin, double tmax, int32_t split, double tmid, double tfrac,
                  double *temps);
+
+/* Exact thermal averages of a lattice with L*L*H <= 32 sites (e.g. 4 x 4 x 2) by enumerating all
+ * 2^N states on the current GPU, for nbeta (1..4) inverse temperatures; the Hamiltonian is that
+ * of Compute_local_field (J:2498-2541), doubled slots included.  out[b*12 + q] holds, for beta[b]:
+ * q = 0 ln Z, then <e>, <e^2>, <|m|>, <m^2>, <m^4>, <|sx|>, <sx^2>, <|sy|>, <sy^2>, <nbar>,
+ * <nbar^2> with per-occupied-site observables as in Measurement (J:2807-2842, J:1028-1048).
+ * Allocates a small device scratch buffer.  No reference counterpart (the reference samples). */
+int j1j2c_enumerate_exact(int32_t L, int32_t H, double J1h, double J1v, double J2, double J3,
+                          const double *p, const int8_t *occu, const int8_t *jh,
+                          const int8_t *jv, int32_t nbeta, const double *beta, double *out);
 
 /* Library version string. */
 const char *j1j2c_version(void);

@@ -28,7 +28,8 @@ def _nvcc() -> str:
 
 
 def _sources():
-    cu = [os.path.join(CSRC, f) for f in ("sweep_fixed.cu", "kernels.cu", "api.cu")]
+    cu = [os.path.join(CSRC, f)
+          for f in ("sweep_fixed.cu", "kernels.cu", "wolff.cu", "enumerate.cu", "api.cu")]
     cpp = [os.path.join(CSRC, "host_model.cpp")]
     hdr = [os.path.join(CSRC, f) for f in ("device_common.cuh", "engine.h", "sweep_common.cuh")]
     hdr.append(os.path.join(ROOT, "include", "j1j2c.h"))

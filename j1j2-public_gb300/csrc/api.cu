@@ -30,6 +30,7 @@ struct Group {
     int nconf = 0, nrep = 0, conf0 = 0, rep0 = 0, block_threads = 0;
     long long lat_stride = 0, p_stride = 0;        // bytes per lattice, field elements per conf
     long long spin_off = 0, p_off = 0, mask_off = 0;  // offsets into the context's arrays
+    long long lab_off = 0;                            // offset into the Wolff label scratch
     SweepVariant var{};
     int nthreads = 0;
     size_t smem = 0;
@@ -63,6 +64,11 @@ struct Ctx {
     int* d_rbase = nullptr;
     int* d_nreps = nullptr;
     unsigned long long* d_audit = nullptr;
+    int* d_labels = nullptr;        // Wolff union-find scratch, one int per site
+    long long* d_csize = nullptr;   // Wolff cluster size of the last update, per replica
+    int* d_err = nullptr;           // device error word (union-find retry overflow)
+    long long lab_ints = 0;
+    bool wolff = false;
 
     std::vector<uint8_t> have_dis, have_ladder, have_spins;
     std::vector<int> nocc, conf_masks;
@@ -123,7 +129,7 @@ void release(Ctx* c)
     void* ptrs[] = {c->d_spins, c->d_pf,    c->d_pd,   c->d_bm,    c->d_occ,   c->d_beta,
                     c->d_rat,   c->d_tor,   c->d_obs,  c->d_sums,  c->d_nmeas, c->d_att,
                     c->d_acc,   c->d_vis,   c->d_last, c->d_ctl,   c->d_nocc,  c->d_rbase,
-                    c->d_nreps, c->d_audit};
+                    c->d_nreps, c->d_audit, c->d_labels, c->d_csize, c->d_err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto s : c->side) cudaStreamDestroy(s);
@@ -264,10 +270,20 @@ SwapArgs swap_args(Ctx* c, int measure)
 }
 
 // PTSWAPEVER sweeps and the observable reduction of lattices [lat0, lat0 + nlat) of a group
+cudaError_t enqueue_wolff(Ctx* c, const Group& grp, cudaStream_t st)
+{
+    SweepArgs a = group_args(c, grp);
+    cudaError_t e = cudaMemsetAsync(c->d_csize + grp.rep0, 0, sizeof(long long) * grp.nlat(), st);
+    if (e != cudaSuccess) return e;
+    return launch_wolff(a, grp.var.fp64, c->masks, grp.nlat(), c->d_labels + grp.lab_off,
+                        grp.lat_stride, c->d_csize + grp.rep0, c->d_err, st);
+}
+
 cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int nthreads,
-                          size_t smem, SweepArgs a, int nlat, cudaStream_t st)
+                          size_t smem, SweepArgs a, int nlat, cudaStream_t st, bool cycle)
 {
     cudaError_t e;
+    if (cycle && c->wolff && (e = enqueue_wolff(c, grp, st)) != cudaSuccess) return e;
     if (!v.global) return launch_sweep(a, v, nlat, nthreads, smem, st);
     for (int t = 0; t < a.nsweeps; ++t)
         for (int col = 0; col < 8; ++col)
@@ -289,7 +305,7 @@ cudaError_t enqueue_cycle(Ctx* c, int measure, cudaStream_t st)
     if (c->G.size() == 1) {
         const Group& grp = c->G[0];
         e = enqueue_group(c, grp, grp.var, grp.nthreads, grp.smem, group_args(c, grp), grp.nlat(),
-                          st);
+                          st, true);
         if (e != cudaSuccess) return e;
     } else {
         if ((e = cudaEventRecord(c->fork_ev, st)) != cudaSuccess) return e;
@@ -297,7 +313,7 @@ cudaError_t enqueue_cycle(Ctx* c, int measure, cudaStream_t st)
             const Group& grp = c->G[k];
             if ((e = cudaStreamWaitEvent(c->side[k], c->fork_ev, 0)) != cudaSuccess) return e;
             e = enqueue_group(c, grp, grp.var, grp.nthreads, grp.smem, group_args(c, grp),
-                              grp.nlat(), c->side[k]);
+                              grp.nlat(), c->side[k], true);
             if (e != cudaSuccess) return e;
             if ((e = cudaEventRecord(c->join_ev[k], c->side[k])) != cudaSuccess) return e;
             if ((e = cudaStreamWaitEvent(st, c->join_ev[k], 0)) != cudaSuccess) return e;
@@ -498,6 +514,8 @@ int j1j2c_create_multi(void** out, const j1j2c_params* groups, int32_t ngroups)
         grp.spin_off = spin_bytes;
         grp.p_off = p_elems;
         grp.mask_off = mask_bytes;
+        grp.lab_off = c->lab_ints;
+        c->lab_ints += (long long)grp.nlat() * grp.lat_stride;
         spin_bytes += (long long)grp.nlat() * grp.lat_stride;
         p_elems += (long long)grp.nconf * grp.p_stride;
         mask_bytes += (long long)grp.nconf * grp.lat_stride;
@@ -546,6 +564,14 @@ int j1j2c_create_multi(void** out, const j1j2c_params* groups, int32_t ngroups)
     if ((e = dalloc(&c->d_rbase, nc)) != cudaSuccess) return cfail(e, "rbase");
     if ((e = dalloc(&c->d_nreps, nc)) != cudaSuccess) return cfail(e, "nreps");
     if ((e = dalloc(&c->d_audit, 2)) != cudaSuccess) return cfail(e, "audit");
+    if ((e = dalloc(&c->d_csize, ne)) != cudaSuccess) return cfail(e, "cluster sizes");
+    if ((e = dalloc(&c->d_err, 1)) != cudaSuccess) return cfail(e, "error word");
+    if ((e = cudaMemset(c->d_err, 0, sizeof(int))) != cudaSuccess) return cfail(e, "memset");
+    if ((e = cudaMemset(c->d_csize, 0, ne * sizeof(long long))) != cudaSuccess)
+        return cfail(e, "memset");
+    c->wolff = (p->flags & J1J2C_FLAG_WOLFF) != 0;
+    if (c->wolff && (e = dalloc(&c->d_labels, (size_t)c->lab_ints)) != cudaSuccess)
+        return cfail(e, "Wolff labels");
     if ((e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking)) != cudaSuccess)
         return cfail(e, "stream");
     c->st = c->own;
@@ -825,6 +851,43 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
     }
     CK(c, cudaStreamSynchronize(c->st));
     CK(c, cudaGetLastError());
+    if (c->wolff) {
+        int herr = 0;
+        CK(c, cudaMemcpy(&herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
+        if (herr) return fail(c, J1J2C_ETIMEOUT, "Wolff union-find exceeded its retry budget");
+    }
+    return J1J2C_OK;
+}
+
+int j1j2c_wolff(void* ctx, int64_t* cluster_sizes)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    for (int k = 0; k < c->nconf; ++k)
+        if (!c->have_dis[k] || !c->have_ladder[k] || !c->have_spins[k])
+            return fail(c, J1J2C_ESTATE, "every conf needs disorder, ladder and spins");
+    if (!c->d_labels) CK(c, dalloc(&c->d_labels, (size_t)c->lab_ints));
+    for (auto& grp : c->G) CK(c, enqueue_wolff(c, grp, c->st));
+    if (cluster_sizes)
+        CK(c, cudaMemcpyAsync(cluster_sizes, c->d_csize, sizeof(long long) * c->nentries,
+                              cudaMemcpyDeviceToHost, c->st));
+    CK(c, cudaStreamSynchronize(c->st));
+    int herr = 0;
+    CK(c, cudaMemcpy(&herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
+    if (herr) return fail(c, J1J2C_ETIMEOUT, "Wolff union-find exceeded its retry budget");
+    return J1J2C_OK;
+}
+
+int j1j2c_get_cluster_sizes(void* ctx, int32_t conf, int64_t* out)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (conf >= c->nconf || !out) return fail(c, J1J2C_EINVAL, "bad conf or null output");
+    const size_t off = conf < 0 ? 0 : (size_t)c->conf_rbase[conf];
+    const size_t nr = conf < 0 ? (size_t)c->nentries : (size_t)c->conf_nrep[conf];
+    CK(c, cudaMemcpyAsync(out, c->d_csize + off, sizeof(long long) * nr, cudaMemcpyDeviceToHost,
+                          c->st));
+    CK(c, cudaStreamSynchronize(c->st));
     return J1J2C_OK;
 }
 
@@ -853,7 +916,7 @@ int j1j2c_metro_sweep_fp64(void* ctx, int32_t conf, int32_t rep, double beta,
     a.use_override = 1;
     a.beta_override = beta;
     a.sweep_override = sweep_index;
-    CK(c, enqueue_group(c, grp, v, nt, smem, a, 1, c->st));
+    CK(c, enqueue_group(c, grp, v, nt, smem, a, 1, c->st, false));
     LatObs o;
     CK(c, cudaMemcpyAsync(&o, a.obs + lat, sizeof o, cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaStreamSynchronize(c->st));
@@ -987,6 +1050,93 @@ int j1j2c_get_observables(void* ctx, int32_t conf, double* out)
     CK(c, cudaMemcpyAsync(out, c->d_last + off * 5, sizeof(double) * 5 * nr,
                           cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaStreamSynchronize(c->st));
+    return J1J2C_OK;
+}
+
+int j1j2c_enumerate_exact(int32_t L, int32_t H, double J1h, double J1v, double J2, double J3,
+                          const double* p, const int8_t* occu, const int8_t* jh,
+                          const int8_t* jv, int32_t nbeta, const double* beta, double* out)
+{
+    g_create_error.clear();
+    const int N = L * H * L;
+    if (L < 2 || H < 2 || (L & 1) || (H & 1) || N > 32 || !p || !beta || !out || nbeta < 1 ||
+        nbeta > kEnumBeta) {
+        g_create_error = "enumeration needs even L, H with L*L*H <= 32 and 1..4 betas";
+        return J1J2C_EINVAL;
+    }
+    EnumArgs a{};
+    a.N = N;
+    a.LB = N < 16 ? N : 16;
+    a.J1h = J1h;
+    a.J1v = J1v;
+    a.J2 = J2;
+    a.J3 = J3;
+    a.nbeta = nbeta;
+    double pmax = 0.0;
+    int nocc = 0;
+    for (int i = 0; i < N; ++i) {
+        const int x = i % L, y = (i / L) % L, z = i / (L * L);
+        auto site = [&](int dx, int dy, int dz) {
+            return ((x + dx + L) % L) + L * ((y + dy + L) % L) + L * L * ((z + dz + H) % H);
+        };
+        const int nb[10] = {site(0, 1, 0),  site(0, -1, 0), site(1, 0, 0),  site(-1, 0, 0),
+                            site(1, 1, 0),  site(-1, 1, 0), site(1, -1, 0), site(-1, -1, 0),
+                            site(0, 0, 1),  site(0, 0, -1)};
+        for (int k = 0; k < 10; ++k) a.nbr[i][k] = (int8_t)nb[k];
+        a.p[i] = p[i];
+        a.occ[i] = occu ? (occu[i] != 0) : 1;
+        a.jh[i] = jh ? (jh[i] != 0) : 1;
+        a.jv[i] = jv ? (jv[i] != 0) : 1;
+        a.px[i] = (uint8_t)(x & 1);
+        a.py[i] = (uint8_t)(y & 1);
+        nocc += a.occ[i];
+        pmax = std::fmax(pmax, std::fabs(p[i]));
+        if (!std::isfinite(p[i])) {
+            g_create_error = "p must be finite";
+            return J1J2C_EINVAL;
+        }
+    }
+    if (nocc == 0) {
+        g_create_error = "no occupied site";
+        return J1J2C_EINVAL;
+    }
+    a.nocc = (double)nocc;
+    a.E0 = -0.5 * N *
+           (2 * std::fabs(J1h) + 2 * std::fabs(J1v) + 4 * std::fabs(J2) + 2 * std::fabs(J3) +
+            8 * pmax) - 1.0;
+    for (int b = 0; b < nbeta; ++b) {
+        if (!std::isfinite(beta[b]) || beta[b] < 0.0) {
+            g_create_error = "beta must be finite and >= 0";
+            return J1J2C_EINVAL;
+        }
+        a.beta[b] = beta[b];
+    }
+    const int nb = enum_blocks(a);
+    const size_t np = (size_t)nb * kEnumBeta * kEnumSums;
+    double* d_part = nullptr;  // scratch: one partial-sum record per block
+    cudaError_t e = cudaMalloc(&d_part, np * sizeof(double));
+    if (e != cudaSuccess) {
+        g_create_error = std::string("enumeration scratch: ") + cudaGetErrorString(e);
+        return J1J2C_ENOMEM;
+    }
+    std::vector<double> part(np);
+    e = launch_enumerate(a, d_part, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(part.data(), d_part, np * sizeof(double),
+                                         cudaMemcpyDeviceToHost);
+    cudaFree(d_part);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("enumeration: ") + cudaGetErrorString(e);
+        return J1J2C_ECUDA;
+    }
+    for (int b = 0; b < nbeta; ++b) {
+        double s[kEnumSums] = {0};
+        for (int blk = 0; blk < nb; ++blk)
+            for (int q = 0; q < kEnumSums; ++q)
+                s[q] += part[((size_t)blk * kEnumBeta + b) * kEnumSums + q];
+        double* o = out + (size_t)b * kEnumSums;
+        o[0] = std::log(s[0]) - beta[b] * a.E0;  // ln Z
+        for (int q = 1; q < kEnumSums; ++q) o[q] = s[q] / s[0];
+    }
     return J1J2C_OK;
 }
 

@@ -74,6 +74,22 @@ struct InitArgs {
     uint32_t seed, key1;
 };
 
+// Exact enumeration of a lattice of N <= 32 sites (enumerate.cu)
+constexpr int kEnumBeta = 4;   // inverse temperatures per launch
+constexpr int kEnumSums = 12;  // weighted sums per inverse temperature
+struct EnumArgs {
+    int N, LB;         // sites; low bits walked in Gray-code order by each thread
+    double nocc, E0;   // occupied sites; lower bound of the energy
+    double J1h, J1v, J2, J3;
+    int nbeta;
+    double beta[kEnumBeta];
+    double p[32];
+    int8_t nbr[32][10];  // reference neighbour slots m1..m10
+    uint8_t occ[32], jh[32], jv[32], px[32], py[32];
+};
+int enum_blocks(const EnumArgs& a);
+cudaError_t launch_enumerate(const EnumArgs& a, double* partial, cudaStream_t st);
+
 // Kernel variant of one sweep launch
 struct SweepVariant {
     bool fp64;     // FP64 form (else FP32)
@@ -102,6 +118,8 @@ cudaError_t prepare_sweep_variant(const SweepVariant& v, size_t smem);
 cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks, int nthreads,
                          size_t smem, cudaStream_t st);
 cudaError_t launch_swap(const SwapArgs& a, cudaStream_t st);
+cudaError_t launch_wolff(const SweepArgs& a, bool fp64, bool masks, int nlat, int* labels,
+                         long long lab_stride, long long* csize, int* err, cudaStream_t st);
 cudaError_t launch_init(const InitArgs& a, cudaStream_t st);
 
 }  // namespace j1j2

@@ -22,6 +22,7 @@ FP64_PLAIN, FP32_BATCHED = 0, 1
 START_HOT, START_FER, START_STR = 0, 1, 2
 AXIS_X, AXIS_Y = 0, 1
 FLAG_NO_GRAPH, FLAG_PROFILE, FLAG_GENERIC, FLAG_NO_FIXED, FLAG_GLOBAL = 1, 2, 4, 8, 16
+FLAG_WOLFF = 32
 
 SUM_FIELDS = ("mag", "absmag", "mag2", "mag4", "en", "en2", "strx_abs", "stry_abs", "strx2",
               "strx4", "stry2", "stry4", "str2", "str4", "absstr", "nem", "nbar", "nbarabs",
@@ -33,7 +34,10 @@ EXPORTS = ("j1j2c_create", "j1j2c_create_multi", "j1j2c_conf_shape", "j1j2c_dest
            "j1j2c_get_slot_sums", "j1j2c_get_pt_stats", "j1j2c_get_maps", "j1j2c_get_spins",
            "j1j2c_get_observables", "j1j2c_get_profile", "j1j2c_get_config",
            "j1j2c_corr_rand_3d", "j1j2c_setup_vacancies", "j1j2c_kiss_spins", "j1j2c_ladder",
-           "j1j2c_version")
+           "j1j2c_version", "j1j2c_wolff", "j1j2c_get_cluster_sizes", "j1j2c_enumerate_exact")
+
+ENUM_FIELDS = ("lnZ", "e", "e2", "absm", "m2", "m4", "abssx", "sx2", "abssy", "sy2", "nbar",
+               "nbar2")
 
 
 class J1J2CError(RuntimeError):
@@ -125,6 +129,24 @@ def ladder(n, tmin, tmax, split=False, tmid=9.5, tfrac=0.7) -> np.ndarray:
                                     C.c_int32(int(split)), C.c_double(tmid), C.c_double(tfrac),
                                     _p(t, C.c_double)))
     return t
+
+
+def enumerate_exact(L, H, p, betas, occu=None, jh=None, jv=None, J1h=1.0, J1v=1.0, J2=-1.0,
+                    J3=1.0) -> np.ndarray:
+    """Exact averages over all 2^N states (N <= 32) on the GPU: (len(betas), 12) in ENUM_FIELDS
+    order (ln Z, then per-site <e>, <e^2>, <|m|>, <m^2>, <m^4>, <|sx|>, <sx^2>, <|sy|>, <sy^2>,
+    <nbar>, <nbar^2>)."""
+    p = np.ascontiguousarray(p, np.float64).reshape(-1)
+    b = np.ascontiguousarray(betas, np.float64).reshape(-1)
+    out = np.empty((b.size, 12))
+    arrs = [None if a is None else np.ascontiguousarray(a, np.int8).reshape(-1)
+            for a in (occu, jh, jv)]
+    ptrs = [None if a is None else _p(a, C.c_int8) for a in arrs]
+    _check(None, lib().j1j2c_enumerate_exact(C.c_int32(L), C.c_int32(H), C.c_double(J1h),
+                                             C.c_double(J1v), C.c_double(J2), C.c_double(J3),
+                                             _p(p, C.c_double), *ptrs, C.c_int32(b.size),
+                                             _p(b, C.c_double), _p(out, C.c_double)))
+    return out
 
 
 def disorder(L, H, seed, phi=2.0, xi=3.0, map_uniform=True) -> np.ndarray:
@@ -243,6 +265,17 @@ class Engine:
                                               C.c_double(beta), C.c_uint32(sweep_index),
                                               C.c_int32(nsweeps), *[C.byref(o) for o in out]))
         return tuple(o.value for o in out)
+
+    def wolff(self):
+        """One Wolff update of every lattice; returns the flipped-cluster sizes per replica."""
+        out = np.zeros(self.nentries, np.int64)
+        self._ck(lib().j1j2c_wolff(self._ctx, _p(out, C.c_int64)))
+        return out
+
+    def cluster_sizes(self, conf=-1):
+        out = np.zeros(self.nentries if conf < 0 else self.nrep_of(conf), np.int64)
+        self._ck(lib().j1j2c_get_cluster_sizes(self._ctx, C.c_int32(conf), _p(out, C.c_int64)))
+        return out
 
     def audit_fp32(self, nsweeps):
         att, mis = C.c_int64(0), C.c_int64(0)

@@ -854,6 +854,76 @@ void or_replay_pt(const or_lat *g, int32_t nrep, const double *beta, int32_t pts
     free(etot);
 }
 
+/* Wolff update of the engine, restated (FP64 form): bonds owned by each site (+x, +y,
+ * (+x,+y), (-x,+y), +z = slots m3, m1, m5, m6, m9) with coupling K of Compute_local_field
+ * (J:2498-2541); a bond with K s_i s_j > 0 is active when u < 1 - exp(-2 beta K s_i s_j), u from
+ * ctr = (rep, cycle, group, 3 + 16*bond); the component of the seed site floor(w*N/2^32),
+ * w from ctr = (rep, cycle, 0xFFFFFFFF, 4), is flipped (no flip when the seed is a vacancy).
+ * Returns the flipped cluster size. */
+static int32_t uf_find(int32_t *lab, int32_t x)
+{
+    while (lab[x] != x) {
+        lab[x] = lab[lab[x]];
+        x = lab[x];
+    }
+    return x;
+}
+
+int64_t or_wolff_step(const or_lat *g, int8_t *s, double beta, uint32_t seed, uint32_t conf,
+                      uint32_t rep, uint32_t cycle)
+{
+    const int32_t N = g->N, L = g->L, H = g->H;
+    const int32_t *m = g->m;
+    static const int slot[5] = {2, 0, 4, 5, 8};
+    int32_t *lab = (int32_t *)malloc(sizeof(int32_t) * N);
+    for (int32_t i = 0; i < N; i++) lab[i] = i;
+    for (int32_t i = 0; i < N; i++) {
+        if (g->occu[i] != 1) continue;
+        int32_t x = i % L, y = (i / L) % L, z = i / (L * L);
+        uint32_t gi;
+        int w;
+        site_group(L, H, x, y, z, &gi, &w);
+        for (int b = 0; b < 5; b++) {
+            int32_t j = m[slot[b] * N + i];
+            if (g->occu[j] != 1) continue;
+            double K;
+            if (b == 0)
+                K = ((g->jh[i] ? g->J1h : 0.0) + g->p[i]) + g->p[j];
+            else if (b == 1)
+                K = ((g->jv[i] ? g->J1v : 0.0) - g->p[i]) - g->p[j];
+            else if (b < 4)
+                K = g->J2;
+            else
+                K = g->J3;
+            double wgt = (s[i] * s[j] > 0) ? K : -K;
+            if (!(wgt > 0.0)) continue;
+            uint32_t r = philox_word(seed, conf, rep, cycle, gi, 3u + 16u * (uint32_t)b, w);
+            double u = (double)((r << 9) | (r >> 23)) * 0x1p-32;
+            double pa = 1.0 - or_dexp(-((2.0 * wgt) * beta));
+            if (u < pa) {
+                int32_t a = uf_find(lab, i), c = uf_find(lab, j);
+                if (a != c) {
+                    if (a < c) lab[c] = a;
+                    else lab[a] = c;
+                }
+            }
+        }
+    }
+    uint32_t wseed = philox_word(seed, conf, rep, cycle, 0xFFFFFFFFu, 4u, 0);
+    int32_t site = (int32_t)(((uint64_t)wseed * (uint64_t)N) >> 32);
+    int64_t count = 0;
+    if (g->occu[site] == 1) {
+        int32_t root = uf_find(lab, site);
+        for (int32_t i = 0; i < N; i++)
+            if (uf_find(lab, i) == root) {
+                s[i] = (int8_t)(-s[i]);
+                count++;
+            }
+    }
+    free(lab);
+    return count;
+}
+
 /* HOT start from the Philox stream: s = +1 when the site's word is below 2^31 (u < 1/2) */
 void or_hot_spins_philox(int32_t L, int32_t H, uint32_t seed, uint32_t conf, uint32_t rep,
                          int8_t *s)

@@ -77,6 +77,8 @@ void or_replay_pt(const or_lat *g, int32_t nrep, const double *beta, int32_t pts
                   int32_t phase0, int8_t *spins, int32_t *rep_at_temp, int32_t *temp_of_rep,
                   double *sums, int64_t *nmeas, int64_t *attempts, int64_t *accepts,
                   uint8_t *visited, double *obs_out);
+int64_t or_wolff_step(const or_lat *g, int8_t *s, double beta, uint32_t seed, uint32_t conf,
+                      uint32_t rep, uint32_t cycle);
 void or_hot_spins_philox(int32_t L, int32_t H, uint32_t seed, uint32_t conf, uint32_t rep,
                          int8_t *s);
 

@@ -62,6 +62,7 @@ def lib():
         L.or_replay_sweeps.restype = C.c_int64
         L.or_setup_vacancies.restype = C.c_int32
         L.or_bench_pt_ref.restype = C.c_double
+        L.or_wolff_step.restype = C.c_int64
     return _lib
 
 
@@ -187,6 +188,12 @@ class Model:
         return lib().or_replay_sweeps(self.ref(), _p(s, C.c_int8), C.c_double(beta),
                                       C.c_uint32(seed), C.c_uint32(conf), C.c_uint32(rep),
                                       C.c_uint32(sweep0), C.c_int32(nsweeps))
+
+    def wolff_step(self, s, beta, seed, conf, rep, cycle):
+        """The engine's Wolff update restated (FP64 form); modifies s, returns the cluster size."""
+        return lib().or_wolff_step(self.ref(), _p(s, C.c_int8), C.c_double(beta),
+                                   C.c_uint32(seed), C.c_uint32(conf), C.c_uint32(rep),
+                                   C.c_uint32(cycle))
 
     def replay_measure(self, s):
         ints = np.empty(4, np.int64)

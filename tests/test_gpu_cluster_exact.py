@@ -1,0 +1,138 @@
+"""GPU: Wolff cluster update (bit-identical to the oracle's restatement, inside and outside PT
+cycles) and exact enumeration (against a CPU enumeration with the reference Measurement, and
+as the oracle of the sampled Metropolis / PT / Wolff averages on 4 x 4 x 2)."""
+import itertools
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+SEED = 3
+
+
+def _betas(n, tmin=8.0, tmax=11.5):
+    from oracle import oracle as O
+    return 1.0 / O.ladder(n, tmin, tmax)
+
+
+def _engine(jc, L, H, nconf, nrep, precision, flags=0, pp=0.0, bonds=0.0, betas=None,
+            same_disorder=False):
+    eng = jc.Engine(L, H, nconf=nconf, nreplica=nrep, precision=precision, seed=SEED,
+                    flags=flags)
+    betas = _betas(nrep) if betas is None else betas
+    dis = []
+    for k in range(nconf):
+        sd = SEED if same_disorder else SEED + k
+        p = jc.disorder(L, H, sd)
+        occu, jh, jv, _ = jc.setup_vacancies(sd, L, H, pp, bonds, bonds)
+        eng.set_disorder(k, p, occu, jh if bonds else None, jv if bonds else None)
+        eng.set_ladder(k, betas)
+        eng.init_spins(k, jc.START_HOT)
+        dis.append((p, occu, jh, jv))
+    eng.reset_measurements()
+    return eng, dis, betas
+
+
+@pytest.mark.parametrize("L,H,pp,bonds,flags", [(8, 4, 0.1, 0.2, 0), (10, 6, 0.0, 0.0, 0),
+                                                 (4, 2, 0.0, 0.0, 0), (8, 8, 0.05, 0.0, 16)])
+def test_wolff_step_bit_identical(engine_mod, oracle, L, H, pp, bonds, flags):
+    jc = engine_mod
+    eng, dis, betas = _engine(jc, L, H, 2, 3, jc.FP64_PLAIN, flags, pp, bonds)
+    eng.run(3, measure=False)
+    before = {(k, r): eng.spins(k, r).copy() for k in range(2) for r in range(3)}
+    tors = [eng.maps(k)[1] for k in range(2)]
+    sizes = eng.wolff()
+    total = 0
+    for k in range(2):
+        p, occu, jh, jv = dis[k]
+        M = oracle.Model(L, H, p, occu, jh if bonds else None, jv if bonds else None)
+        for r in range(3):
+            s = before[(k, r)].copy()
+            n = M.wolff_step(s, betas[tors[k][r]], SEED, k, r, 3)
+            np.testing.assert_array_equal(eng.spins(k, r), s)
+            assert sizes[3 * k + r] == n
+            total += n
+    assert total > 0
+    eng.close()
+
+
+def test_wolff_inside_pt_cycles(engine_mod, oracle):
+    jc = engine_mod
+    L, H, nrep = 8, 4, 4
+    eng, dis, betas = _engine(jc, L, H, 2, nrep, jc.FP64_PLAIN, jc.FLAG_WOLFF, 0.05)
+    states = [oracle.new_pt_state(np.stack([eng.spins(k, r) for r in range(nrep)]))
+              for k in range(2)]
+    eng.run(6, measure=True)
+    for k in range(2):
+        p, occu, _, _ = dis[k]
+        M = oracle.Model(L, H, p, occu)
+        st = states[k]
+        for cyc in range(6):
+            for r in range(nrep):
+                s = st["spins"][r].copy()
+                M.wolff_step(s, betas[st["temp_of_rep"][r]], SEED, k, r, cyc)
+                st["spins"][r] = s
+            M.replay_pt(st, betas, 5, 1, cyc, SEED, k, True, 1 if cyc % 2 == 0 else 2)
+        for r in range(nrep):
+            np.testing.assert_array_equal(eng.spins(k, r), st["spins"][r])
+        np.testing.assert_array_equal(eng.slot_sums(k)[0], st["sums"])
+    assert (eng.cluster_sizes() >= 0).all()
+    eng.close()
+
+
+def _cpu_exact(oracle, L, H, p, betas):
+    M = oracle.Model(L, H, p)
+    N = L * L * H
+    rows = []
+    for bits in itertools.product((-1, 1), repeat=N):
+        s = np.array(bits[::-1], np.int8)  # any fixed order covers every state
+        m, e, sx, sy = M.measurement(s)
+        rows.append((e, m, sx, sy, M.nbar(s)))
+    a = np.array(rows)
+    out = []
+    for b in betas:
+        Etot = a[:, 0] * N
+        w = np.exp(-b * (Etot - Etot.min()))
+        Z = w.sum()
+        e, m, sx, sy, nb = a.T
+        out.append([np.log(Z) - b * Etot.min(), (w * e).sum() / Z, (w * e * e).sum() / Z,
+                    (w * abs(m)).sum() / Z, (w * m * m).sum() / Z, (w * m ** 4).sum() / Z,
+                    (w * abs(sx)).sum() / Z, (w * sx * sx).sum() / Z, (w * abs(sy)).sum() / Z,
+                    (w * sy * sy).sum() / Z, (w * nb).sum() / Z, (w * nb * nb).sum() / Z])
+    return np.array(out)
+
+
+@pytest.mark.parametrize("L,H", [(2, 2), (2, 4)])
+def test_enumeration_matches_cpu(engine_mod, oracle, L, H):
+    jc = engine_mod
+    p = jc.disorder(L, H, 11)
+    betas = [0.05, 0.1, 0.125, 0.3]
+    gpu = jc.enumerate_exact(L, H, p, betas)
+    cpu = _cpu_exact(oracle, L, H, p, betas)
+    np.testing.assert_allclose(gpu, cpu, rtol=1e-9, atol=1e-11)
+
+
+@pytest.mark.parametrize("precision,flags", [(0, 0), (1, 0), (1, 32)])
+def test_sampling_matches_exact_4x4x2(engine_mod, oracle, precision, flags):
+    """64 independent chains (same disorder, different Philox keys) of a 4-temperature PT ladder
+    on 4 x 4 x 2 against the exact averages over all 2^32 states."""
+    jc = engine_mod
+    L, H, ncopy = 4, 2, 64
+    betas = 1.0 / np.array([6.0, 8.0, 10.0, 12.0])
+    p = jc.disorder(L, H, SEED)
+    exact = jc.enumerate_exact(L, H, p, betas)
+    eng, _, _ = _engine(jc, L, H, ncopy, 4, precision, flags, betas=betas, same_disorder=True)
+    eng.run(300, measure=False)
+    eng.reset_measurements()
+    nm = 3000
+    eng.run(nm, measure=True)
+    sums, cnt = eng.slot_sums(-1)
+    assert (cnt == nm).all()
+    per = sums.reshape(ncopy, 4, 22) / nm
+    checks = {"e": (4, 1), "m2": (2, 4), "abssx": (6, 6), "sx2": (8, 7), "nbar": (16, 10)}
+    for name, (si, ei) in checks.items():
+        est = per[:, :, si]
+        mean, se = est.mean(axis=0), est.std(axis=0, ddof=1) / np.sqrt(ncopy)
+        z = np.abs(mean - exact[:, ei]) / np.maximum(se, 1e-12)
+        assert (z < 4.5).all(), (name, mean, exact[:, ei], se)
+    eng.close()

@@ -187,6 +187,23 @@ def test_pt_serial_reference_runs(oracle):
     assert sorted(r["rep_at_temp"]) == list(range(4))
 
 
+def test_wolff_restatement_limits(oracle):
+    """beta = 0 activates no bond (the cluster is the seed); with ferromagnetic couplings, no
+    field and an aligned start, beta -> infinity activates every bond (the whole lattice)."""
+    from oracle import corr3d
+    L, H = 6, 4
+    p = corr3d.make_corr_rand_3d(L, L, H, 3.0, 2).reshape(-1)
+    M = oracle.Model(L, H, p)
+    s = oracle.init_spins(3, L, H, 0)
+    s0 = s.copy()
+    assert M.wolff_step(s, 0.0, 1, 0, 0, 7) == 1
+    assert int((s != s0).sum()) == 1
+    F = oracle.Model(L, H, np.zeros(L * L * H), J1h=1.0, J1v=1.0, J2=1.0, J3=1.0)
+    s = np.ones(L * L * H, np.int8)
+    assert F.wolff_step(s, 50.0, 1, 0, 0, 7) == L * L * H
+    assert (s == -1).all()
+
+
 def test_ladder(oracle):
     t = oracle.ladder(16, 8.0, 11.5)
     np.testing.assert_allclose(t, 8.0 + 3.5 * np.arange(16) / 15, rtol=0, atol=1e-15)
