@@ -238,6 +238,20 @@ int j1j2c_enumerate_exact(int32_t L, int32_t H, double J1h, double J1v, double J
                           const double *p, const int8_t *occu, const int8_t *jh,
                           const int8_t *jv, int32_t nbeta, const double *beta, double *out);
 
+/* The same exact enumeration without any allocation, for callers that cannot allocate device
+ * memory when they need it (a host framework whose memory pool already holds the whole GPU, or a
+ * latency-bound loop that must not pay for an allocation).  Its scratch is a fixed device array
+ * of the library: at most 512 CTAs x 4 betas x 12 partial sums plus 48 totals (about 192 KiB,
+ * held by every GPU that loads the library until exit), enough for any lattice of <= 32 sites.
+ * Larger requests (more than 32 sites or 4 betas) return J1J2C_EINVAL.  The first call on a
+ * device looks the array's device address up (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race.  Arguments and output as j1j2c_enumerate_exact.  No counterpart in the reference. */
+int j1j2c_enumerate_exact_noalloc(int32_t L, int32_t H, double J1h, double J1v, double J2,
+                                  double J3, const double *p, const int8_t *occu,
+                                  const int8_t *jh, const int8_t *jv, int32_t nbeta,
+                                  const double *beta, double *out);
+
 /* Library version string. */
 const char *j1j2c_version(void);
 

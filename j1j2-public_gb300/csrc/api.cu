@@ -25,6 +25,12 @@ namespace {
 
 thread_local std::string g_create_error;
 
+}  // namespace
+
+void j1j2::set_global_error(const char* msg) { g_create_error = msg; }
+
+namespace {
+
 struct Group {
     Geo g{};
     int nconf = 0, nrep = 0, conf0 = 0, rep0 = 0, block_threads = 0;

@@ -88,6 +88,8 @@ struct EnumArgs {
     uint8_t occ[32], jh[32], jv[32], px[32], py[32];
 };
 int enum_blocks(const EnumArgs& a);
+// message returned by j1j2c_last_error(NULL) (for entry points without a context)
+void set_global_error(const char* msg);
 cudaError_t launch_enumerate(const EnumArgs& a, double* partial, cudaStream_t st);
 
 // Kernel variant of one sweep launch

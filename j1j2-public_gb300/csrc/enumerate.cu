@@ -9,6 +9,11 @@
 // For every beta the kernel accumulates, with weights w = exp(-beta (E - E0)) (E0 a lower bound
 // of E, so w <= 1), the sums of w, w E, w E^2, w |m|, w m^2, w m^4, w |sx|, w sx^2, w |sy|, w sy^2,
 // w nbar, w nbar^2 (per-site observables as in Measurement, J:2807-2842, and J:1028-1048).
+#include <cmath>
+#include <cstdio>
+#include <mutex>
+
+#include "../../include/j1j2c.h"
 #include "engine.h"
 
 namespace j1j2 {
@@ -138,4 +143,155 @@ cudaError_t launch_enumerate(const EnumArgs& a, double* partial, cudaStream_t st
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------------------------------------
+// Allocation-free variant (j1j2c_enumerate_exact_noalloc).  Some callers cannot create device
+// allocations at the moment they need the exact averages: a host program whose memory manager has
+// already reserved the whole GPU for its own pool (a new cudaMalloc fails or fragments that
+// pool), or a latency-bound loop that must not pay for an allocation and its implicit
+// synchronisation.  This variant keeps the per-block partial sums and their total in one fixed
+// device array instead of a buffer allocated per call.
+//
+// Limit: 512 CTAs (the 2^16 threads of a 32-site lattice, 128 per CTA) x 4 inverse temperatures
+// x 12 sums of partials, plus 48 totals: 24624 doubles (about 192 KiB), held by every GPU that
+// loads the library until the process exits.  All calls share the array and overwrite it (every
+// entry a call reads was written earlier in that call, so nothing needs clearing); calls that
+// overlap on the GPU, from two host threads or two processes' streams, race on it.
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+constexpr int kNoAllocMaxBlocks = 512;
+constexpr int kNoAllocPartials = kNoAllocMaxBlocks * kEnumBeta * kEnumSums;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) double g_enum_scratch[kNoAllocPartials + kEnumBeta * kEnumSums];
+
+// totals[b * 12 + q] = sum over blocks of partial[(blk * 4 + b) * 12 + q], in block order
+__global__ void enum_total_kernel(const double* partial, int nblocks, int nbeta, double* totals)
+{
+    const int t = (int)threadIdx.x;
+    if (t < nbeta * kEnumSums) {
+        const int b = t / kEnumSums, q = t - b * kEnumSums;
+        double s = 0.0;
+        for (int blk = 0; blk < nblocks; ++blk)
+            s += partial[((size_t)blk * kEnumBeta + b) * kEnumSums + q];
+        totals[t] = s;
+    }
+}
+
+std::mutex g_scratch_mu;
+double* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_enum_scratch on the current device, looked up once per device.  In host
+// code the symbol is only a host-side stand-in, so the kernel must receive this address.
+cudaError_t scratch_address(double** out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_enum_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_ptr[dev] = static_cast<double*>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+
 }  // namespace j1j2
+
+extern "C" int j1j2c_enumerate_exact_noalloc(int32_t L, int32_t H, double J1h, double J1v,
+                                             double J2, double J3, const double* p,
+                                             const int8_t* occu, const int8_t* jh,
+                                             const int8_t* jv, int32_t nbeta, const double* beta,
+                                             double* out)
+{
+    using namespace j1j2;
+    const int N = L * L * H;
+    if (L < 2 || H < 2 || (L & 1) || (H & 1) || N > 32 || !p || !beta || !out || nbeta < 1 ||
+        nbeta > kEnumBeta) {
+        set_global_error("allocation-free enumeration: needs even L, H with L*L*H <= 32 sites "
+                         "and 1..4 inverse temperatures");
+        return J1J2C_EINVAL;
+    }
+    EnumArgs a{};
+    a.N = N;
+    a.LB = N < 16 ? N : 16;
+    a.J1h = J1h;
+    a.J1v = J1v;
+    a.J2 = J2;
+    a.J3 = J3;
+    a.nbeta = nbeta;
+    double pmax = 0.0;
+    int nocc = 0;
+    for (int i = 0; i < N; ++i) {
+        if (!std::isfinite(p[i])) {
+            set_global_error("allocation-free enumeration: p must be finite");
+            return J1J2C_EINVAL;
+        }
+        const int x = i % L, y = (i / L) % L, z = i / (L * L);
+        const int dx[10] = {0, 0, 1, -1, 1, -1, 1, -1, 0, 0};
+        const int dy[10] = {1, -1, 0, 0, 1, 1, -1, -1, 0, 0};
+        const int dz[10] = {0, 0, 0, 0, 0, 0, 0, 0, 1, -1};
+        for (int k = 0; k < 10; ++k)
+            a.nbr[i][k] = (int8_t)(((x + dx[k] + L) % L) + L * ((y + dy[k] + L) % L) +
+                                   L * L * ((z + dz[k] + H) % H));
+        a.p[i] = p[i];
+        a.occ[i] = occu ? (occu[i] != 0) : 1;
+        a.jh[i] = jh ? (jh[i] != 0) : 1;
+        a.jv[i] = jv ? (jv[i] != 0) : 1;
+        a.px[i] = (uint8_t)(x & 1);
+        a.py[i] = (uint8_t)(y & 1);
+        nocc += a.occ[i];
+        pmax = std::fmax(pmax, std::fabs(p[i]));
+    }
+    if (nocc == 0) {
+        set_global_error("allocation-free enumeration: no occupied site");
+        return J1J2C_EINVAL;
+    }
+    a.nocc = (double)nocc;
+    a.E0 = -0.5 * N *
+               (2 * std::fabs(J1h) + 2 * std::fabs(J1v) + 4 * std::fabs(J2) +
+                2 * std::fabs(J3) + 8 * pmax) -
+           1.0;
+    for (int b = 0; b < nbeta; ++b) {
+        if (!std::isfinite(beta[b]) || beta[b] < 0.0) {
+            set_global_error("allocation-free enumeration: beta must be finite and >= 0");
+            return J1J2C_EINVAL;
+        }
+        a.beta[b] = beta[b];
+    }
+    const int nb = enum_blocks(a);
+    if (nb > kNoAllocMaxBlocks) {
+        set_global_error("allocation-free enumeration: more than 512 CTAs of partial sums");
+        return J1J2C_EINVAL;
+    }
+    double* scratch = nullptr;
+    cudaError_t e = scratch_address(&scratch);
+    if (e == cudaSuccess) e = launch_enumerate(a, scratch, 0);
+    if (e == cudaSuccess) {
+        enum_total_kernel<<<1, kEnumBeta * kEnumSums>>>(scratch, nb, nbeta,
+                                                        scratch + kNoAllocPartials);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpy(out, scratch + kNoAllocPartials, sizeof(double) * kEnumSums * nbeta,
+                       cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        thread_local char msg[192];
+        std::snprintf(msg, sizeof msg, "allocation-free enumeration: %s", cudaGetErrorString(e));
+        set_global_error(msg);
+        return J1J2C_ECUDA;
+    }
+    for (int b = 0; b < nbeta; ++b) {  // totals -> ln Z and averages, in place
+        double* o = out + (size_t)b * kEnumSums;
+        const double z = o[0];
+        for (int q = 1; q < kEnumSums; ++q) o[q] = o[q] / z;
+        o[0] = std::log(z) - beta[b] * a.E0;
+    }
+    return 0;
+}
