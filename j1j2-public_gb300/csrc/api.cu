@@ -77,8 +77,8 @@ struct Ctx {
     bool wolff = false;
 
     std::vector<uint8_t> have_dis, have_ladder, have_spins;
-    std::vector<int> nocc, conf_masks;
-    bool masks = false;
+    std::vector<int> nocc, conf_masks, conf_vac;
+    bool masks = false, vac = false;
 
     cudaStream_t own = nullptr, st = nullptr;
     std::vector<cudaStream_t> side;
@@ -168,12 +168,13 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
     v = SweepVariant{};
     v.fp64 = fp64;
     v.masks = c->masks;
+    v.vac = c->vac;
     v.mode = kModeSweep;
     const bool quad_ok = (grp.g.Lh % 4 == 0) && !(fl & J1J2C_FLAG_GENERIC);
     if (!(fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_GLOBAL))) {
         int nts[8];
         bool sp[8];
-        const int n = fixed_candidates(fp64, grp.g.L, grp.g.H, c->masks, nts, sp, 8);
+        const int n = fixed_candidates(fp64, grp.g.L, grp.g.H, c->masks, c->vac, nts, sp, 8);
         int pick = n > 0 ? 0 : -1;
         for (int k = 0; k < n; ++k)
             if (nts[k] == grp.block_threads) pick = k;
@@ -186,7 +187,7 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
                 nthreads = nts[pick];
                 SweepArgs none{};
                 none.g = grp.g;
-                CK(c, launch_fixed(none, fp64, nthreads, 0, smem, nullptr, true));
+                CK(c, launch_fixed(none, fp64, c->vac, nthreads, 0, smem, nullptr, true));
                 return J1J2C_OK;
             }
             v.fixed_nt = 0;
@@ -363,7 +364,8 @@ int autotune(Ctx* c, Group& grp)
     if (grp.var.fixed_nt == 0 || grp.block_threads > 0) return J1J2C_OK;
     int nts[8];
     bool sp[8];
-    const int n = fixed_candidates(grp.var.fp64, grp.g.L, grp.g.H, c->masks, nts, sp, 8);
+    const int n =
+        fixed_candidates(grp.var.fp64, grp.g.L, grp.g.H, c->masks, c->vac, nts, sp, 8);
     if (n <= 1) return J1J2C_OK;
     const int nlat = grp.nlat();
     const auto key = std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, nlat);
@@ -398,12 +400,15 @@ int autotune(Ctx* c, Group& grp)
             v.stage_p = sp[k];
             const size_t sm = sweep_smem_bytes(grp.g, v);
             if (sm > budget) continue;
-            if ((e = launch_fixed(a, v.fp64, nts[k], 0, sm, nullptr, true)) != cudaSuccess) break;
-            if ((e = launch_fixed(a, v.fp64, nts[k], nlat, sm, c->own, false)) != cudaSuccess)
+            if ((e = launch_fixed(a, v.fp64, c->vac, nts[k], 0, sm, nullptr, true)) !=
+                cudaSuccess)
+                break;
+            if ((e = launch_fixed(a, v.fp64, c->vac, nts[k], nlat, sm, c->own, false)) !=
+                cudaSuccess)
                 break;
             cudaEventRecord(c->ev0, c->own);
             for (int r = 0; r < 3 && e == cudaSuccess; ++r)
-                e = launch_fixed(a, v.fp64, nts[k], nlat, sm, c->own, false);
+                e = launch_fixed(a, v.fp64, c->vac, nts[k], nlat, sm, c->own, false);
             cudaEventRecord(c->ev1, c->own);
             if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
             float ms = 0.0f;
@@ -428,7 +433,8 @@ int autotune(Ctx* c, Group& grp)
             grp.nthreads = nts[k];
             SweepArgs none{};
             none.g = grp.g;
-            CK(c, launch_fixed(none, grp.var.fp64, grp.nthreads, 0, grp.smem, nullptr, true));
+            CK(c, launch_fixed(none, grp.var.fp64, c->vac, grp.nthreads, 0, grp.smem, nullptr,
+                               true));
         }
     free_graphs(c);
     return J1J2C_OK;
@@ -539,6 +545,7 @@ int j1j2c_create_multi(void** out, const j1j2c_params* groups, int32_t ngroups)
     c->have_spins.assign(c->nconf, 0);
     c->nocc.assign(c->nconf, 0);
     c->conf_masks.assign(c->nconf, 0);
+    c->conf_vac.assign(c->nconf, 0);
     c->profile = (p->flags & J1J2C_FLAG_PROFILE) != 0;
 
     auto cfail = [&](cudaError_t e, const char* what) {
@@ -708,10 +715,13 @@ int j1j2c_set_disorder(void* ctx, int32_t conf, const double* p, const int8_t* o
     CK(c, cudaMemcpy(c->d_nocc + conf, &nocc, sizeof(int), cudaMemcpyHostToDevice));
     c->nocc[conf] = nocc;
     c->conf_masks[conf] = anymask;
-    bool masks = false;
+    c->conf_vac[conf] = nocc < g.N;
+    bool masks = false, vac = false;
     for (int k : c->conf_masks) masks = masks || k;
-    if (masks != c->masks) {
+    for (int k : c->conf_vac) vac = vac || k;
+    if (masks != c->masks || vac != c->vac) {
         c->masks = masks;
+        c->vac = vac;
         free_graphs(c);
         for (auto& gr : c->G) {
             int rc = choose_variant(c, gr, c->P.precision == J1J2C_FP64_PLAIN, gr.var, gr.smem,

@@ -101,6 +101,7 @@ struct SweepVariant {
     int mode;      // kModeSweep / kModeAudit
     int fixed_nt;  // > 0: shape-specialised kernel with this many threads per CTA
     bool global;   // lattice in HBM, one launch per colour phase (too large for shared memory)
+    bool vac;      // some conf has vacancies (shape-specialised kernels: vacancy handling on)
 };
 
 // Global-memory path: one colour phase of sweep t of the cycle, and the observable reduction
@@ -111,9 +112,10 @@ cudaError_t launch_measure_global(const SweepArgs& a, const SweepVariant& v, int
                                   cudaStream_t st);
 
 // Shape-specialised kernels (sweep_fixed.cu): CTA sizes available for a shape, and the launch.
-int fixed_candidates(bool fp64, int L, int H, bool masks, int* nts, bool* stage_p, int cap);
-cudaError_t launch_fixed(const SweepArgs& a, bool fp64, int nt, int nblocks, size_t smem,
-                         cudaStream_t st, bool prepare);
+int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, int* nts, bool* stage_p,
+                     int cap);
+cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, int nt, int nblocks,
+                         size_t smem, cudaStream_t st, bool prepare);
 
 size_t sweep_smem_bytes(const Geo& g, const SweepVariant& v);
 cudaError_t prepare_sweep_variant(const SweepVariant& v, size_t smem);

@@ -704,7 +704,8 @@ cudaError_t prepare_sweep_variant(const SweepVariant& v, size_t smem)
 cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks, int nthreads,
                          size_t smem, cudaStream_t st)
 {
-    if (v.fixed_nt > 0) return launch_fixed(a, v.fp64, v.fixed_nt, nblocks, smem, st, false);
+    if (v.fixed_nt > 0)
+        return launch_fixed(a, v.fp64, v.vac, v.fixed_nt, nblocks, smem, st, false);
     return dispatch(a, v, nblocks, nthreads, smem, st, false);
 }
 

@@ -2,9 +2,11 @@
 // constants and the eight colour phases of a sweep are unrolled, so colour parities are
 // compile-time.  Each thread owns the same quad(s) in every colour class; the word offsets of the
 // quad's neighbours inside a colour block are computed once, and a colour phase addresses shared
-// memory as [offset + colour base], the base being an immediate.  Same arithmetic, Philox stream
-// and outputs as the generic quad kernel (kernels.cu), bit for bit.  One CTA owns one lattice,
-// staged in shared memory for the PTSWAPEVER fused sweeps of a PT cycle.
+// memory as [offset + colour base], the base being an immediate.  With two quads per thread both
+// quads' operands are loaded before either is updated (quads of one colour never neighbour each
+// other), which doubles the instruction-level parallelism of a thread.  Same arithmetic, Philox
+// stream and outputs as the generic quad kernel (kernels.cu), bit for bit.  One CTA owns one
+// lattice, staged in shared memory for the PTSWAPEVER fused sweeps of a PT cycle.
 #include "sweep_common.cuh"
 
 namespace j1j2 {
@@ -54,11 +56,18 @@ __device__ __forceinline__ QuadOff quad_offsets(int q)
     return o;
 }
 
-template <class Real, int LH, int HH, int C, bool MEASURE>
-__device__ __forceinline__ void quad_fixed(const SweepArgs& a, uint32_t* S32, const Real* P,
-                                           const QuadOff& o, uint32_t sweep, uint32_t rep,
-                                           uint32_t k0, uint32_t k1, double beta, float kb,
-                                           Acc& acc)
+// Operands of one quad in one colour phase
+template <class Real>
+struct QuadData {
+    int self;                                    // word offset of the quad in its colour block
+    uint32_t own, wxp, wxm, wyp, wym;            // spins: own, +-x, +-y
+    uint32_t wdpp, wdpm, wdmp, wdmm, wzp, wzm;   // diagonals (+x+y, -x+y, +x-y, -x-y), +-z
+    Real pown[4], pxa[4], pyp[4], pym[4], pextra;
+};
+
+template <class Real, int LH, int HH, int C>
+__device__ __forceinline__ QuadData<Real> load_quad(const uint32_t* S32, const Real* P,
+                                                    const QuadOff& o)
 {
     using Sh = Shape<LH, HH>;
     constexpr int px = C & 1, py = (C >> 1) & 1, pz = C >> 2;
@@ -71,96 +80,122 @@ __device__ __forceinline__ void quad_fixed(const SweepArgs& a, uint32_t* S32, co
     const int rYm_n = py ? xn : (px ? o.ym_xp : o.ym_xm);
     const int rZp = pz ? o.zp : o.self, rZm = pz ? o.self : o.zm;
 
-    const uint32_t own = S32[B0 + o.self];
-    uint32_t wxp, wxm, wdpp, wdpm, wdmp, wdmm;
-    x_pair(px, S32[B1 + o.self], S32[B1 + xn], wxp, wxm);
-    const uint32_t wyp = S32[B2 + rYp], wym = S32[B2 + rYm];
-    x_pair(px, S32[B3 + rYp], S32[B3 + rYp_n], wdpp, wdpm);
-    x_pair(px, S32[B3 + rYm], S32[B3 + rYm_n], wdmp, wdmm);
-    const uint32_t wzp = S32[B4 + rZp], wzm = S32[B4 + rZm];
-
-    Real pown[4], pxa[4], pyp[4], pym[4];
-    const Real pextra = P[4 * (B1 + xn) + (px ? 0 : 3)];
+    QuadData<Real> d;
+    d.self = o.self;
+    d.own = S32[B0 + o.self];
+    x_pair(px, S32[B1 + o.self], S32[B1 + xn], d.wxp, d.wxm);
+    d.wyp = S32[B2 + rYp];
+    d.wym = S32[B2 + rYm];
+    x_pair(px, S32[B3 + rYp], S32[B3 + rYp_n], d.wdpp, d.wdpm);
+    x_pair(px, S32[B3 + rYm], S32[B3 + rYm_n], d.wdmp, d.wdmm);
+    d.wzp = S32[B4 + rZp];
+    d.wzm = S32[B4 + rZm];
+    d.pextra = P[4 * (B1 + xn) + (px ? 0 : 3)];
     if constexpr (sizeof(Real) == 4) {
         const float4* P4 = reinterpret_cast<const float4*>(P);
         const float4 v0 = P4[B0 + o.self], v1 = P4[B1 + o.self];
         const float4 v2 = P4[B2 + rYp], v3 = P4[B2 + rYm];
-        pown[0] = v0.x, pown[1] = v0.y, pown[2] = v0.z, pown[3] = v0.w;
-        pxa[0] = v1.x, pxa[1] = v1.y, pxa[2] = v1.z, pxa[3] = v1.w;
-        pyp[0] = v2.x, pyp[1] = v2.y, pyp[2] = v2.z, pyp[3] = v2.w;
-        pym[0] = v3.x, pym[1] = v3.y, pym[2] = v3.z, pym[3] = v3.w;
+        d.pown[0] = v0.x, d.pown[1] = v0.y, d.pown[2] = v0.z, d.pown[3] = v0.w;
+        d.pxa[0] = v1.x, d.pxa[1] = v1.y, d.pxa[2] = v1.z, d.pxa[3] = v1.w;
+        d.pyp[0] = v2.x, d.pyp[1] = v2.y, d.pyp[2] = v2.z, d.pyp[3] = v2.w;
+        d.pym[0] = v3.x, d.pym[1] = v3.y, d.pym[2] = v3.z, d.pym[3] = v3.w;
     } else {
         const double2* P2 = reinterpret_cast<const double2*>(P);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const double2 v0 = P2[2 * (B0 + o.self) + h], v1 = P2[2 * (B1 + o.self) + h];
             const double2 v2 = P2[2 * (B2 + rYp) + h], v3 = P2[2 * (B2 + rYm) + h];
-            pown[2 * h] = v0.x, pown[2 * h + 1] = v0.y;
-            pxa[2 * h] = v1.x, pxa[2 * h + 1] = v1.y;
-            pyp[2 * h] = v2.x, pyp[2 * h + 1] = v2.y;
-            pym[2 * h] = v3.x, pym[2 * h + 1] = v3.y;
+            d.pown[2 * h] = v0.x, d.pown[2 * h + 1] = v0.y;
+            d.pxa[2 * h] = v1.x, d.pxa[2 * h + 1] = v1.y;
+            d.pyp[2 * h] = v2.x, d.pyp[2 * h + 1] = v2.y;
+            d.pym[2 * h] = v3.x, d.pym[2 * h + 1] = v3.y;
         }
     }
+    return d;
+}
 
+// Update (or measure) one quad from its loaded operands.  VAC: vacancies may be present (the
+// FP32 acceptance threshold is then scaled by s^2 so that a vacancy never flips).
+template <class Real, int LH, int HH, int C, bool MEASURE, bool VAC>
+__device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
+                                             const QuadData<Real>& d, uint32_t sweep,
+                                             uint32_t rep, uint32_t k0, uint32_t k1, double beta,
+                                             float kb, Acc& acc)
+{
+    using Sh = Shape<LH, HH>;
+    constexpr int px = C & 1, py = (C >> 1) & 1;
+    constexpr int B0 = C * Sh::CS;
     U4 rnd{0, 0, 0, 0};
     if constexpr (!MEASURE)
-        rnd = philox4x32_10(rep, sweep, (uint32_t)(B0 + o.self), kTagSweep, k0, k1);
-    const uint32_t dsum = wdpp + wdpm + wdmp + wdmm;  // bytewise, <= 8
-    const uint32_t zsum = wzp + wzm;                  // bytewise, <= 4
+        rnd = philox4x32_10(rep, sweep, (uint32_t)(B0 + d.self), kTagSweep, k0, k1);
     uint32_t flipmask = 0;
+    if constexpr (sizeof(Real) == 4) {
+        const uint32_t dsum = d.wdpp + d.wdpm + d.wdmp + d.wdmm;  // bytewise, <= 8
+        const uint32_t zsum = d.wzp + d.wzm;                      // bytewise, <= 4
+        int ehi = 0, elo = 0;  // fixed-point energy of the quad, split as in efix32_split
+        float nbf = 0.0f;      // nematic sum of the quad (exact small integers)
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const Real pxp = px ? (k < 3 ? pxa[k + 1] : pextra) : pxa[k];
-        const Real pxm = px ? pxa[k] : (k > 0 ? pxa[k - 1] : pextra);
-        if constexpr (sizeof(Real) == 4) {
+        for (int k = 0; k < 4; ++k) {
             Nbr32 nb;
-            nb.sxp = byte_off(wxp, k, 1.0f);
-            nb.sxm = byte_off(wxm, k, 1.0f);
-            nb.syp = byte_off(wyp, k, 1.0f);
-            nb.sym = byte_off(wym, k, 1.0f);
+            nb.sxp = byte_off(d.wxp, k, 1.0f);
+            nb.sxm = byte_off(d.wxm, k, 1.0f);
+            nb.syp = byte_off(d.wyp, k, 1.0f);
+            nb.sym = byte_off(d.wym, k, 1.0f);
             nb.D = byte_off(dsum, k, 4.0f);
             nb.Zs = byte_off(zsum, k, 2.0f);
-            nb.pxp = pxp;
-            nb.pxm = pxm;
-            nb.pyp = pyp[k];
-            nb.pym = pym[k];
-            const float f = field_fp32(nb, pown[k], a.J1hf, a.J1vf, a.J2f, a.J3f);
-            const float si = byte_off(own, k, 1.0f);
+            nb.pxp = px ? (k < 3 ? d.pxa[k + 1] : d.pextra) : d.pxa[k];
+            nb.pxm = px ? d.pxa[k] : (k > 0 ? d.pxa[k - 1] : d.pextra);
+            nb.pyp = d.pyp[k];
+            nb.pym = d.pym[k];
+            const float f = field_fp32(nb, d.pown[k], a.J1hf, a.J1vf, a.J2f, a.J3f);
+            const float si = byte_off(d.own, k, 1.0f);
             const float sf = __fmul_rn(si, f);
             if constexpr (MEASURE) {
-                const int s = (int)si;
-                acc.e += efix32_split(-sf);
-                acc.M += s;
-                acc.SX += px ? -s : s;
-                acc.SY += py ? -s : s;
-                acc.NB += s * (int)(nb.sxp + nb.sxm - nb.syp - nb.sym);
+                const float x = __fmul_rn(-sf, 65536.0f);
+                const float t = truncf(x);
+                ehi += __float2int_rz(t);
+                elo += __float2int_rn(__fmul_rn(__fsub_rn(x, t), 65536.0f));
+                nbf = __fmaf_rn(si, (nb.sxp + nb.sxm) - (nb.syp + nb.sym), nbf);
             } else {
-                // Metropolis test u < exp(-beta dE) as 2^(kb s f); vacancies (s = 0) never flip
-                // because the threshold is scaled by s^2 (FMA-pipe work instead of a compare)
-                const float thr = __fmul_rn(ex2_approx(__fmul_rn(kb, sf)), __fmul_rn(si, si));
+                // Metropolis test u < exp(-beta dE) as 2^(kb s f); with vacancies the threshold
+                // is scaled by s^2, so a vacancy (s = 0) never flips
+                float thr = ex2_approx(__fmul_rn(kb, sf));
+                if constexpr (VAC) thr = __fmul_rn(thr, __fmul_rn(si, si));
                 if (u01_f32(u4_word(rnd, k)) < thr) flipmask |= 2u << (8 * k);
             }
-        } else {
+        }
+        if constexpr (MEASURE) {
+            // magnetisation and stripe sums from the byte sum of the own word (s = b - 1)
+            const int mq = (int)((d.own * 0x01010101u) >> 24) - 4;
+            acc.M += mq;
+            acc.SX += px ? -mq : mq;
+            acc.SY += py ? -mq : mq;
+            acc.NB += (int)nbf;
+            acc.e += ((long long)ehi << 16) + (long long)elo;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
             const int sh = 8 * k;
-            const int b = (own >> sh) & 0xFF;
+            const int b = (d.own >> sh) & 0xFF;
             if (b == 1) continue;
             Nbr64 nb;
-            nb.s[0] = (int)((wyp >> sh) & 0xFF) - 1;
-            nb.s[1] = (int)((wym >> sh) & 0xFF) - 1;
-            nb.s[2] = (int)((wxp >> sh) & 0xFF) - 1;
-            nb.s[3] = (int)((wxm >> sh) & 0xFF) - 1;
-            nb.s[4] = (int)((wdpp >> sh) & 0xFF) - 1;
-            nb.s[5] = (int)((wdpm >> sh) & 0xFF) - 1;
-            nb.s[6] = (int)((wdmp >> sh) & 0xFF) - 1;
-            nb.s[7] = (int)((wdmm >> sh) & 0xFF) - 1;
-            nb.s[8] = (int)((wzp >> sh) & 0xFF) - 1;
-            nb.s[9] = (int)((wzm >> sh) & 0xFF) - 1;
-            nb.p1 = pyp[k];
-            nb.p2 = pym[k];
-            nb.p3 = pxp;
-            nb.p4 = pxm;
+            nb.s[0] = (int)((d.wyp >> sh) & 0xFF) - 1;
+            nb.s[1] = (int)((d.wym >> sh) & 0xFF) - 1;
+            nb.s[2] = (int)((d.wxp >> sh) & 0xFF) - 1;
+            nb.s[3] = (int)((d.wxm >> sh) & 0xFF) - 1;
+            nb.s[4] = (int)((d.wdpp >> sh) & 0xFF) - 1;
+            nb.s[5] = (int)((d.wdpm >> sh) & 0xFF) - 1;
+            nb.s[6] = (int)((d.wdmp >> sh) & 0xFF) - 1;
+            nb.s[7] = (int)((d.wdmm >> sh) & 0xFF) - 1;
+            nb.s[8] = (int)((d.wzp >> sh) & 0xFF) - 1;
+            nb.s[9] = (int)((d.wzm >> sh) & 0xFF) - 1;
+            nb.p1 = d.pyp[k];
+            nb.p2 = d.pym[k];
+            nb.p3 = px ? (k < 3 ? d.pxa[k + 1] : d.pextra) : d.pxa[k];
+            nb.p4 = px ? d.pxa[k] : (k > 0 ? d.pxa[k - 1] : d.pextra);
             nb.jv_own = nb.jv_m2 = nb.jh_own = nb.jh_m4 = 1;
-            const double f = field_fp64(nb, pown[k], a.J1h, a.J1v, a.J2, a.J3, nullptr);
+            const double f = field_fp64(nb, d.pown[k], a.J1h, a.J1v, a.J2, a.J3, nullptr);
             const int s = b - 1;
             if constexpr (MEASURE) {
                 acc.e += efix(-((double)s * f));
@@ -182,7 +217,7 @@ __device__ __forceinline__ void quad_fixed(const SweepArgs& a, uint32_t* S32, co
         }
     }
     if constexpr (!MEASURE) {
-        if (flipmask) S32[B0 + o.self] = own ^ flipmask;
+        if (flipmask) S32[B0 + d.self] = d.own ^ flipmask;
     }
 }
 
@@ -208,20 +243,47 @@ __device__ __forceinline__ QuadOff offsets_for(const OffsetCache<QPT>& oc, int j
     }
 }
 
-template <class Real, int LH, int HH, int NT, int QPT, bool MEASURE>
+template <class Real, int LH, int HH, int NT, int QPT, int C, bool MEASURE, bool VAC>
+__device__ __forceinline__ void colour_phase(const SweepArgs& a, uint32_t* S32, const Real* P,
+                                             const OffsetCache<QPT>& oc, uint32_t sweep,
+                                             uint32_t rep, uint32_t k0, uint32_t k1,
+                                             double beta, float kb, Acc& acc)
+{
+    constexpr int NQ = Shape<LH, HH>::CS;
+    if constexpr (QPT == 2) {
+        // both quads' loads first, then both updates (same-colour quads are independent)
+        const bool has1 = 2 * NT == NQ || (int)threadIdx.x + NT < NQ;
+        const QuadData<Real> d0 = load_quad<Real, LH, HH, C>(S32, P, oc.off[0]);
+        QuadData<Real> d1 = d0;
+        if (has1) d1 = load_quad<Real, LH, HH, C>(S32, P, oc.off[1]);
+        compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32, d0, sweep, rep, k0, k1, beta, kb,
+                                                    acc);
+        if (has1)
+            compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32, d1, sweep, rep, k0, k1, beta,
+                                                        kb, acc);
+    } else {
+#pragma unroll 2
+        for (int j = 0; j < QPT; ++j)
+            if (QPT * NT == NQ || (int)threadIdx.x + j * NT < NQ) {
+                const QuadData<Real> dj =
+                    load_quad<Real, LH, HH, C>(S32, P, offsets_for<LH, HH, NT, QPT>(oc, j));
+                compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32, dj, sweep, rep, k0, k1,
+                                                            beta, kb, acc);
+            }
+    }
+}
+
+template <class Real, int LH, int HH, int NT, int QPT, bool MEASURE, bool VAC>
 __device__ __forceinline__ void all_colours(const SweepArgs& a, uint32_t* S32, const Real* P,
                                             const OffsetCache<QPT>& oc, uint32_t sweep,
                                             uint32_t rep, uint32_t k0, uint32_t k1, double beta,
                                             float kb, Acc& acc)
 {
-    constexpr int NQ = Shape<LH, HH>::CS;
     // One barrier per colour.  The measurement only reads, but without the barrier the
     // instruction scheduler interleaves all eight read-only phases and runs out of registers.
-#define J1J2_PHASE(C)                                                                       \
-    _Pragma("unroll 2") for (int j = 0; j < QPT; ++j) if (QPT * NT == NQ ||                 \
-                                                          (int)threadIdx.x + j * NT < NQ)   \
-        quad_fixed<Real, LH, HH, C, MEASURE>(a, S32, P, offsets_for<LH, HH, NT, QPT>(oc, j), \
-                                             sweep, rep, k0, k1, beta, kb, acc);            \
+#define J1J2_PHASE(C)                                                                        \
+    colour_phase<Real, LH, HH, NT, QPT, C, MEASURE, VAC>(a, S32, P, oc, sweep, rep, k0, k1,  \
+                                                         beta, kb, acc);                     \
     __syncthreads();
     J1J2_PHASE(0)
     J1J2_PHASE(1)
@@ -234,7 +296,7 @@ __device__ __forceinline__ void all_colours(const SweepArgs& a, uint32_t* S32, c
 #undef J1J2_PHASE
 }
 
-template <class Real, int LH, int HH, int NT, int MINB, bool STAGE_P>
+template <class Real, int LH, int HH, int NT, int MINB, bool STAGE_P, bool VAC>
 __global__ void __launch_bounds__(NT, MINB) sweep_fixed_kernel(SweepArgs a)
 {
     using Sh = Shape<LH, HH>;
@@ -281,18 +343,18 @@ __global__ void __launch_bounds__(NT, MINB) sweep_fixed_kernel(SweepArgs a)
     Acc acc{0, 0, 0, 0, 0};
 #pragma unroll 1
     for (int t = 0; t < a.nsweeps; ++t)
-        all_colours<Real, LH, HH, NT, QPT, false>(a, S32, P, off, sweep0 + (uint32_t)t,
-                                                  (uint32_t)rep, k0, k1, beta, kb, acc);
-    all_colours<Real, LH, HH, NT, QPT, true>(a, S32, P, off, 0u, 0u, 0u, 0u, beta, kb, acc);
+        all_colours<Real, LH, HH, NT, QPT, false, VAC>(a, S32, P, off, sweep0 + (uint32_t)t,
+                                                       (uint32_t)rep, k0, k1, beta, kb, acc);
+    all_colours<Real, LH, HH, NT, QPT, true, VAC>(a, S32, P, off, 0u, 0u, 0u, 0u, beta, kb, acc);
     const Acc tot = block_reduce(acc);
     if (threadIdx.x == 0) store_obs(a.obs + lat, tot);
     block_copy16(Sg, S, Sh::NB);
 }
 
-template <class Real, int LH, int HH, int NT, int MINB, bool STAGE_P>
+template <class Real, int LH, int HH, int NT, int MINB, bool STAGE_P, bool VAC>
 cudaError_t run_fixed(const SweepArgs& a, int nblocks, size_t smem, cudaStream_t st, bool prep)
 {
-    auto k = sweep_fixed_kernel<Real, LH, HH, NT, MINB, STAGE_P>;
+    auto k = sweep_fixed_kernel<Real, LH, HH, NT, MINB, STAGE_P, VAC>;
     if (prep) return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<nblocks, NT, smem, st>>>(a);
     return cudaGetLastError();
@@ -304,33 +366,48 @@ struct FixedEntry {
     bool fp64;
     int L, H, nt;
     bool stage_p;
+    bool vac;  // handles vacancies (entries without it are only used for vacancy-free contexts)
     FixedFn fn;
 };
 
 // Shapes of the reference's configurations (L = 16, 24, 32, 48 with H = L) and the CTA sizes
-// the autotuner chooses from; the second number is the CTAs per SM that shared memory allows
-// (it bounds the registers per thread).
+// the autotuner chooses from; the MINB template argument is the CTAs per SM that shared memory
+// allows (it bounds the registers per thread).
 const FixedEntry kFixed[] = {
-    {false, 16, 16, 128, true, run_fixed<float, 8, 8, 128, 8, true>},
-    {false, 16, 16, 64, true, run_fixed<float, 8, 8, 64, 10, true>},
-    {false, 24, 24, 448, true, run_fixed<float, 12, 12, 448, 2, true>},
-    {false, 24, 24, 224, true, run_fixed<float, 12, 12, 224, 2, true>},
-    {false, 32, 32, 1024, true, run_fixed<float, 16, 16, 1024, 1, true>},
-    {false, 32, 32, 512, true, run_fixed<float, 16, 16, 512, 1, true>},
-    {false, 48, 48, 864, false, run_fixed<float, 24, 24, 864, 1, false>},
-    {false, 48, 48, 576, false, run_fixed<float, 24, 24, 576, 1, false>},
-    {true, 24, 24, 448, true, run_fixed<double, 12, 12, 448, 1, true>},
-    {true, 32, 32, 512, false, run_fixed<double, 16, 16, 512, 1, false>},
+    {false, 16, 16, 128, true, true, run_fixed<float, 8, 8, 128, 8, true, true>},
+    {false, 16, 16, 64, true, true, run_fixed<float, 8, 8, 64, 10, true, true>},
+    {false, 24, 24, 448, true, true, run_fixed<float, 12, 12, 448, 2, true, true>},
+    {false, 24, 24, 224, true, true, run_fixed<float, 12, 12, 224, 2, true, true>},
+    {false, 32, 32, 1024, true, false, run_fixed<float, 16, 16, 1024, 1, true, false>},
+    {false, 32, 32, 512, true, false, run_fixed<float, 16, 16, 512, 1, true, false>},
+    {false, 32, 32, 1024, true, true, run_fixed<float, 16, 16, 1024, 1, true, true>},
+    {false, 32, 32, 512, true, true, run_fixed<float, 16, 16, 512, 1, true, true>},
+    {false, 48, 48, 864, false, true, run_fixed<float, 24, 24, 864, 1, false, true>},
+    {false, 48, 48, 576, false, true, run_fixed<float, 24, 24, 576, 1, false, true>},
+    {true, 24, 24, 448, true, true, run_fixed<double, 12, 12, 448, 1, true, true>},
+    {true, 32, 32, 512, false, true, run_fixed<double, 16, 16, 512, 1, false, true>},
 };
+
+// Entries usable for a context: vacancy-free entries when it has no vacancy (where they exist),
+// else the vacancy-capable ones.
+bool usable(const FixedEntry& e, bool fp64, int L, int H, bool vac)
+{
+    if (e.fp64 != fp64 || e.L != L || e.H != H) return false;
+    if (vac) return e.vac;
+    for (const auto& f : kFixed)
+        if (f.fp64 == fp64 && f.L == L && f.H == H && !f.vac) return !e.vac;
+    return true;
+}
 
 }  // namespace
 
-int fixed_candidates(bool fp64, int L, int H, bool masks, int* nts, bool* stage_p, int cap)
+int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, int* nts, bool* stage_p,
+                     int cap)
 {
     if (masks) return 0;
     int n = 0;
     for (const auto& e : kFixed)
-        if (e.fp64 == fp64 && e.L == L && e.H == H && n < cap) {
+        if (usable(e, fp64, L, H, vac) && n < cap) {
             nts[n] = e.nt;
             stage_p[n] = e.stage_p;
             ++n;
@@ -338,11 +415,11 @@ int fixed_candidates(bool fp64, int L, int H, bool masks, int* nts, bool* stage_
     return n;
 }
 
-cudaError_t launch_fixed(const SweepArgs& a, bool fp64, int nt, int nblocks, size_t smem,
-                         cudaStream_t st, bool prepare)
+cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, int nt, int nblocks,
+                         size_t smem, cudaStream_t st, bool prepare)
 {
     for (const auto& e : kFixed)
-        if (e.fp64 == fp64 && e.L == a.g.L && e.H == a.g.H && e.nt == nt)
+        if (usable(e, fp64, a.g.L, a.g.H, vac) && e.nt == nt)
             return e.fn(a, nblocks, smem, st, prepare);
     return cudaErrorInvalidValue;
 }
