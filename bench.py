@@ -33,11 +33,26 @@ UNIT = "attempts/ns"
 B_PER_ATTEMPT_FP32 = 11.8  # full PT cycle model: 10 B per sweep attempt + 9 B/site measure / 5
 B_PER_ATTEMPT_FP64 = 21.4
 L2_FLUSH_BYTES = 256 << 20
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one sweep-kernel launch (5 sweeps
+# + measure of every lattice), from an ncu capture of the same workload
+TRAFFIC = {"batched_fp32_L32_64x32": 75592192 + 10054400}
 
+# name -> lattice-shape groups (L, nconf, nreplica), precision and options
 WORKLOADS = {
-    "batched_fp32_L32_64x32": dict(L=32, nconf=64, nrep=32, precision=1),
-    "plain_fp64_L24_1x16": dict(L=24, nconf=1, nrep=16, precision=0),
-    "batched_fp64_L32_64x32": dict(L=32, nconf=64, nrep=32, precision=0),
+    # L=32, 64 disorder configurations x 32-replica ladders (2048 lattices), FP32 sweep
+    "batched_fp32_L32_64x32": dict(groups=[(32, 64, 32)], precision=1),
+    # L=24, one disorder configuration, 16-replica PT ladder, FP64 sweep (plain form)
+    "plain_fp64_L24_1x16": dict(groups=[(24, 1, 16)], precision=0),
+    # the batched workload in the FP64 form (same seeds)
+    "batched_fp64_L32_64x32": dict(groups=[(32, 64, 32)], precision=0),
+    # uneven batch: L=16/24/32/48 with 128/64/32/8 configurations and 16/24/32/48 replicas
+    "mixed_L16_24_32_48": dict(groups=[(16, 128, 16), (24, 64, 24), (32, 32, 32), (48, 8, 48)],
+                               precision=1),
+    # L=96, 5 % site vacancies, 8 configurations x 48 replicas, one Wolff update per PT cycle
+    "large_L96_vac5_wolff_8x48": dict(groups=[(96, 8, 48)], precision=1, vacancies=0.05,
+                                      wolff=True),
+    # L=16 single-temperature local Metropolis (T=9.5, one sweep + measurement per cycle), FP64
+    "local_fp64_L16_T9.5": dict(groups=[(16, 1, 1)], precision=0, ptswapever=1, T=9.5),
 }
 
 
@@ -51,6 +66,20 @@ def peaks():
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def conf_base_of(rank, w):
+    """First global configuration index of a rank: every rank holds the workload's full set of
+    configurations, with disjoint disorder seeds (weak scaling, no data-path collective)."""
+    return rank * sum(n for _, n, _ in w["groups"])
+
+
+def max_over_ranks(dist, x, device):
+    """Maximum of a per-rank float (the timed interval) over all ranks."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 class Clocks:
@@ -104,17 +133,38 @@ class Clocks:
 
 
 def make_engine(jc, w, device, conf_base=0, flags=0, irinit=1):
-    L, nconf, nrep = w["L"], w["nconf"], w["nrep"]
-    eng = jc.Engine(L, L, nconf=nconf, nreplica=nrep, ptswapever=5, precision=w["precision"],
-                    seed=irinit, conf_base=conf_base, device=device, flags=flags)
-    betas = 1.0 / jc.ladder(nrep, 8.0, 11.5)
-    for k in range(nconf):
-        eng.set_disorder(k, jc.disorder(L, L, irinit + conf_base + k, 2.0, 3.0))
-    eng.set_ladder(-1, np.tile(betas, nconf))
-    for k in range(nconf):
+    """Engine of one workload: disorder of conf k from seed irinit + conf_base + k (PHI=2,
+    XI=3), optional Bernoulli site vacancies from the same seed, linear ladders over
+    T = 8.0-11.5 (or one temperature), HOT starts."""
+    ptswapever = w.get("ptswapever", 5)
+    if w.get("wolff"):
+        flags |= jc.FLAG_WOLFF
+    eng = jc.Engine(groups=[(L, L, n, r) for L, n, r in w["groups"]], ptswapever=ptswapever,
+                    precision=w["precision"], seed=irinit, conf_base=conf_base, device=device,
+                    flags=flags)
+    betas, k = [], 0
+    for L, n, r in w["groups"]:
+        b = np.full(r, 1.0 / w["T"]) if "T" in w else 1.0 / jc.ladder(r, 8.0, 11.5)
+        for _ in range(n):
+            seed = irinit + conf_base + k
+            occu = None
+            if w.get("vacancies"):
+                occu = jc.setup_vacancies(seed, L, L, w["vacancies"])[0]
+            eng.set_disorder(k, jc.disorder(L, L, seed, 2.0, 3.0), occu)
+            betas.append(b)
+            k += 1
+    betas = np.concatenate(betas)
+    eng.set_ladder(-1, betas)
+    for k in range(eng.nconf):
         eng.init_spins(k, jc.START_HOT)
     eng.reset_measurements()
     return eng, betas
+
+
+def attempts_per_cycle(eng):
+    """Occupied sites x replicas x sweeps of one PT cycle, summed over the configurations."""
+    reps = np.array([eng.nrep_of(k) for k in range(eng.nconf)], np.int64)
+    return int((eng.nocc * reps).sum()) * eng.ptswapever
 
 
 def time_steps(torch, eng, steps, warmup, flush):
@@ -139,6 +189,37 @@ def time_steps(torch, eng, steps, warmup, flush):
     return total_ms, eng.profile()[0] - prof0
 
 
+def time_workload(torch, jc, w, device, flush, steps):
+    """Device throughput of one workload (CUDA events per PT cycle, L2 flushed between)."""
+    eng, _ = make_engine(jc, w, device, flags=jc.FLAG_PROFILE)
+    ms, prof_ms = time_steps(torch, eng, steps, 3, flush)
+    att = attempts_per_cycle(eng)
+    out = {"value": round(att * steps / (ms * 1e6), 4), "unit": UNIT,
+           "ms_per_step": round(ms / steps, 4), "steps": steps, "attempts_per_step": att,
+           "sweep_ms_per_step": round(prof_ms / steps, 4),
+           "groups_L_nconf_nreplica": [list(g) for g in w["groups"]]}
+    cfg = eng.config()
+    out["block_threads"] = cfg["block_threads"]
+    eng.close()
+    return out
+
+
+def secondary_workloads(torch, jc, device, flush, steps):
+    """The other configurations of the same path, each timed alone on this GPU."""
+    res = {}
+    for name in ("batched_fp64_L32_64x32", "mixed_L16_24_32_48", "large_L96_vac5_wolff_8x48"):
+        res[name] = time_workload(torch, jc, WORKLOADS[name], device, flush, steps)
+    # per-L throughput of the uneven batch: each lattice-shape group alone
+    per_l = {}
+    for L, n, r in WORKLOADS["mixed_L16_24_32_48"]["groups"]:
+        w = dict(groups=[(L, n, r)], precision=1)
+        per_l[str(L)] = time_workload(torch, jc, w, device, flush, steps)["value"]
+    res["mixed_L16_24_32_48"]["per_L_alone"] = per_l
+    res["local_fp64_L16_T9.5"] = time_workload(torch, jc, WORKLOADS["local_fp64_L16_T9.5"],
+                                               device, flush, 4 * steps)
+    return res
+
+
 def run_ours(args):
     import torch
 
@@ -153,11 +234,10 @@ def run_ours(args):
 
     wname = args.workload
     w = WORKLOADS[wname]
-    eng, betas = make_engine(jc, w, local, conf_base=rank * w["nconf"],
-                             flags=jc.FLAG_PROFILE)
+    nconf = sum(n for _, n, _ in w["groups"])
+    eng, betas = make_engine(jc, w, local, conf_base=conf_base_of(rank, w), flags=jc.FLAG_PROFILE)
     cfg = eng.config()
-    occ = int(eng.nocc.sum()) * w["nrep"]
-    attempts_per_step = occ * 5
+    attempts_per_step = attempts_per_cycle(eng)
 
     if ws > 1:
         dist.barrier()
@@ -166,25 +246,22 @@ def run_ours(args):
         total_ms, prof_ms = time_steps(torch, eng, args.steps, args.warmup, flush)
     torch.cuda.synchronize()
     if ws > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(dist, total_ms, "cuda")
         dist.barrier()
     sweep_ms_avg = prof_ms / max(args.steps, 1)  # sweep kernel, per launch (timed steps)
     value = attempts_per_step * args.steps * ws / (total_ms * 1e6)
 
     # end to end through the public API with host buffers: ladder H2D, one cycle, all running
     # sums and observables D2H, every step
-    host_betas = np.tile(betas, w["nconf"])
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        eng.set_ladder(-1, host_betas)
+        eng.set_ladder(-1, betas)
         eng.run(1, measure=True, restart_swap_phase=False)
         sums, nm = eng.slot_sums(-1)
         obs = eng.observables(-1)
     e2e_s = time.perf_counter() - t0
     e2e = attempts_per_step * args.steps * ws / (e2e_s * 1e9)
-    h2d = host_betas.nbytes
+    h2d = betas.nbytes
     d2h = sums.nbytes + nm.nbytes + obs.nbytes
     assert np.isfinite(sums).all()
 
@@ -196,38 +273,41 @@ def run_ours(args):
     achieved = attempts_per_step * bpa / (sweep_ms_avg * 1e-3) / 1e9 if sweep_ms_avg > 0 else 0.0
 
     # FP64 plain form on the L=24, 16-replica PT configuration (the 10x target's denominator)
-    w64 = WORKLOADS["plain_fp64_L24_1x16"]
-    eng64, _ = make_engine(jc, w64, local)
-    s64 = max(4, args.steps // 4)
-    ms64, _ = time_steps(torch, eng64, s64, 3, flush)
-    fp64_val = int(eng64.nocc.sum()) * w64["nrep"] * 5 * s64 / (ms64 * 1e6)
-    eng64.close()
+    fp64 = time_workload(torch, jc, WORKLOADS["plain_fp64_L24_1x16"], local, flush,
+                         max(4, args.steps // 4))
+    extra = None
+    if not args.headline_only:
+        extra = secondary_workloads(torch, jc, local, flush, max(5, args.steps // 10))
 
     cpu = cpu_baseline() if (rank == 0 and not args.no_cpu) else None
     clocks = clk.summary()
+    g0 = w["groups"][0]
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if w["precision"] == 1 else "f64",
         "data": "synthetic (corr_rand_3d disorder from seeds IRINIT+k, HOT starts)",
-        "config": {"workload": wname, "L": w["L"], "H": w["L"], "nconf_per_gpu": w["nconf"],
-                   "nreplica": w["nrep"], "ptswapever": 5, "T": [8.0, 11.5], "phi": 2.0,
-                   "xi": 3.0, "lattices_per_gpu": w["nconf"] * w["nrep"],
+        "config": {"workload": wname, "L": g0[0], "H": g0[0], "nconf_per_gpu": nconf,
+                   "nreplica": g0[2], "ptswapever": eng.ptswapever, "T": [8.0, 11.5],
+                   "phi": 2.0, "xi": 3.0,
+                   "lattices_per_gpu": sum(n * r for _, n, r in w["groups"]),
                    "attempts_per_step": attempts_per_step * ws, "l2": "flushed before each step",
                    "block_threads": cfg["block_threads"], "sites_per_thread": cfg["sites_per_thread"],
                    "smem_bytes": cfg["smem_bytes"], "parallelism": f"confs x{ws}"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
-                     "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": None,
+                     "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": TRAFFIC.get(wname),
                      "peak_source": peak_src, "bytes_per_attempt": bpa,
                      "sweep_kernel_ms": round(sweep_ms_avg, 4)},
         "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "fp64_plain": {"value": round(fp64_val, 4), "unit": UNIT, "workload": "plain_fp64_L24_1x16",
-                       "ratio_fp32_over_fp64": round(value / fp64_val / ws, 2)},
+        "fp64_plain": dict(fp64, workload="plain_fp64_L24_1x16",
+                           ratio_fp32_over_fp64=round(value / fp64["value"] / ws, 2)),
         "gpu_launches": 2 * args.steps,
         "clocks": clocks,
     }
+    if extra is not None:
+        line["workloads"] = extra
     if cpu is not None:
         line["cpu_baseline"] = cpu
     eng.close()
@@ -297,6 +377,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched_fp32_L32_64x32", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the secondary workloads (batched FP64, mixed L, L=96, local)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

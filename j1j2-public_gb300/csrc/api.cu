@@ -283,7 +283,8 @@ cudaError_t enqueue_wolff(Ctx* c, const Group& grp, cudaStream_t st)
     cudaError_t e = cudaMemsetAsync(c->d_csize + grp.rep0, 0, sizeof(long long) * grp.nlat(), st);
     if (e != cudaSuccess) return e;
     return launch_wolff(a, grp.var.fp64, c->masks, grp.nlat(), c->d_labels + grp.lab_off,
-                        grp.lat_stride, c->d_csize + grp.rep0, c->d_err, st);
+                        grp.lat_stride, c->d_csize + grp.rep0, c->d_err, st,
+                        (c->P.flags & J1J2C_FLAG_GENERIC) != 0);
 }
 
 cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int nthreads,

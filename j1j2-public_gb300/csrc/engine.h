@@ -123,7 +123,9 @@ cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks,
                          size_t smem, cudaStream_t st);
 cudaError_t launch_swap(const SwapArgs& a, cudaStream_t st);
 cudaError_t launch_wolff(const SweepArgs& a, bool fp64, bool masks, int nlat, int* labels,
-                         long long lab_stride, long long* csize, int* err, cudaStream_t st);
+                         long long lab_stride, long long* csize, int* err, cudaStream_t st,
+                         bool per_site);
+int wolff_slab_planes(const Geo& g);  // planes per shared-memory slab of the Wolff labelling
 cudaError_t launch_init(const InitArgs& a, cudaStream_t st);
 
 }  // namespace j1j2

@@ -8,9 +8,19 @@
 // H = 2 a pair is reached from both sides and receives two trials, i.e. coupling 2K, exactly as
 // the doubled neighbour slots of the reference (J:564-574).
 //
-// Components are labelled in a scratch array (one int32 per site) by lock-free union-find:
-// hooking the larger root under the smaller with atomicCAS, path halving in find; then every
-// label is compressed to its root and the seed's component is flipped.
+// Components are labelled in a scratch array (one int32 per site, the compact index of a site of
+// the same component) by lock-free union-find: hooking the larger root under the smaller with
+// atomicCAS, path halving in find, so every pointer goes to a smaller compact index and every
+// root is the smallest compact index of its component.  Then the seed's component is flipped.
+//
+// Slab form (lattices up to 65536 sites per two planes): one CTA per slab of pz planes
+// (pz even, a divisor of H) stages the slab's spins in shared memory and runs the union-find on
+// 16-bit slab-local indices ordered like the compact layout (colour-major, each colour's planes
+// contiguous), which keeps the root of every slab-local component at its smallest compact index;
+// it writes every site's global label as that root.  A second kernel unites the +z bonds that
+// leave a slab in global memory, and the flip kernel finds roots on the fly.  Components, and so
+// the flipped cluster, are those of the site-per-thread global form, which stays as the path for
+// larger planes and for the per-site test mode.
 //
 // Streams (Philox4x32-10, key = (seed, conf_base + conf)):
 //   bond b of the site in group g: ctr = (replica, cycle, g, 3 + 16*b), word X & 3
@@ -82,6 +92,50 @@ __device__ __forceinline__ const Real* wfield(const SweepArgs& a, int conf)
         return a.pf + (long long)conf * a.p_stride;
 }
 
+// Weight w = K_ij s_i s_j of the bond of type b (coupling K_ij as in Compute_local_field); true
+// if the bond can be activated (w > 0).
+template <class Real>
+__device__ __forceinline__ bool bond_weight(const SweepArgs& a, int b, int si, int sj, int jh,
+                                            int jv, Real pi, Real pj, Real& w)
+{
+    Real K;
+    if constexpr (sizeof(Real) == 8) {
+        if (b == 0)
+            K = __dadd_rn(__dadd_rn(jh ? a.J1h : 0.0, pi), pj);
+        else if (b == 1)
+            K = __dsub_rn(__dsub_rn(jv ? a.J1v : 0.0, pi), pj);
+        else if (b < 4)
+            K = a.J2;
+        else
+            K = a.J3;
+    } else {
+        if (b == 0)
+            K = __fadd_rn(__fadd_rn(jh ? a.J1hf : 0.0f, pi), pj);
+        else if (b == 1)
+            K = __fsub_rn(__fsub_rn(jv ? a.J1vf : 0.0f, pi), pj);
+        else if (b < 4)
+            K = a.J2f;
+        else
+            K = a.J3f;
+    }
+    w = si * sj > 0 ? K : -K;
+    return w > Real(0);
+}
+
+// Activation trial of a bond of weight w > 0 with the uniform of word r: u < 1 - exp(-2 beta w)
+template <class Real>
+__device__ __forceinline__ bool bond_trial(Real w, double beta, uint32_t r)
+{
+    if constexpr (sizeof(Real) == 8) {
+        const double pa = __dsub_rn(1.0, own_exp(-__dmul_rn(__dmul_rn(2.0, w), beta)));
+        return u01_f64(r) < pa;
+    } else {
+        const float kb2 = (float)(-2.0 * beta * 1.4426950408889634);
+        const float pa = __fsub_rn(1.0f, ex2_approx(__fmul_rn(kb2, w)));
+        return u01_f32(r) < pa;
+    }
+}
+
 __global__ void wolff_init_kernel(int* labels, long long lab_stride, int N)
 {
     int* lab = labels + (long long)blockIdx.y * lab_stride;
@@ -119,77 +173,252 @@ __global__ void __launch_bounds__(256) wolff_bond_kernel(SweepArgs a, int* label
                        compact_of_xyz(g, xp, yp, s.z), compact_of_xyz(g, xm, yp, s.z),
                        compact_of_xyz(g, s.x, s.y, zp)};
     const int jh = MASKS ? (BM[ci] & 1) : 1, jv = MASKS ? ((BM[ci] >> 1) & 1) : 1;
+    const Real pi = P[ci];
 #pragma unroll
     for (int b = 0; b < 5; ++b) {
         const int cj = nb[b];
         const int sj = (int)S[cj] - 1;
         if (sj == 0) continue;
-        const int ss = si * sj;
-        bool active;
-        if constexpr (sizeof(Real) == 8) {
-            double K;
-            if (b == 0)
-                K = __dadd_rn(__dadd_rn(jh ? a.J1h : 0.0, P[ci]), P[cj]);
-            else if (b == 1)
-                K = __dsub_rn(__dsub_rn(jv ? a.J1v : 0.0, P[ci]), P[cj]);
-            else if (b < 4)
-                K = a.J2;
-            else
-                K = a.J3;
-            const double w = ss > 0 ? K : -K;
-            if (!(w > 0.0)) continue;
-            const uint32_t r = u4_word(
-                philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffBond + 16u * b, k0, k1), X & 3);
-            const double pa = __dsub_rn(1.0, own_exp(-__dmul_rn(__dmul_rn(2.0, w), beta)));
-            active = u01_f64(r) < pa;
-        } else {
-            float K;
-            if (b == 0)
-                K = __fadd_rn(__fadd_rn(jh ? a.J1hf : 0.0f, P[ci]), P[cj]);
-            else if (b == 1)
-                K = __fsub_rn(__fsub_rn(jv ? a.J1vf : 0.0f, P[ci]), P[cj]);
-            else if (b < 4)
-                K = a.J2f;
-            else
-                K = a.J3f;
-            const float w = ss > 0 ? K : -K;
-            if (!(w > 0.0f)) continue;
-            const uint32_t r = u4_word(
-                philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffBond + 16u * b, k0, k1), X & 3);
-            const float kb2 = (float)(-2.0 * beta * 1.4426950408889634);
-            const float pa = __fsub_rn(1.0f, ex2_approx(__fmul_rn(kb2, w)));
-            active = u01_f32(r) < pa;
-        }
-        if (active && !unite(lab, ci, cj)) atomicExch(err, 1);
+        Real w;
+        if (!bond_weight<Real>(a, b, si, sj, jh, jv, pi, b < 2 ? P[cj] : Real(0), w)) continue;
+        const uint32_t r = u4_word(
+            philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffBond + 16u * b, k0, k1), X & 3);
+        if (bond_trial<Real>(w, beta, r) && !unite(lab, ci, cj)) atomicExch(err, 1);
     }
 }
 
-__global__ void wolff_compress_kernel(int* labels, long long lab_stride, int N)
+// ---- slab form -------------------------------------------------------------------------------
+__device__ __forceinline__ int sfind(volatile uint16_t* lab, int x)
 {
-    volatile int* lab = labels + (long long)blockIdx.y * lab_stride;
-    for (int i = (int)(blockIdx.x * blockDim.x + threadIdx.x); i < N;
-         i += (int)(gridDim.x * blockDim.x))
-        lab[i] = find_root(lab, i);
+    int p = lab[x];
+    while (p != x) {
+        const int gp = lab[p];
+        if (gp != p) lab[x] = (uint16_t)gp;
+        x = p;
+        p = gp;
+    }
+    return x;
 }
 
-__global__ void wolff_flip_kernel(SweepArgs a, const int* labels, long long lab_stride,
+__device__ __forceinline__ bool sunite(volatile uint16_t* lab, int a, int b)
+{
+    for (int it = 0; it < (1 << 20); ++it) {
+        a = sfind(lab, a);
+        b = sfind(lab, b);
+        if (a == b) return true;
+        if (a < b) {
+            const int t = a;
+            a = b;
+            b = t;
+        }
+        if (atomicCAS(const_cast<unsigned short*>(reinterpret_cast<volatile unsigned short*>(lab)) + a,
+                      (unsigned short)a, (unsigned short)b) == (unsigned short)a)
+            return true;
+    }
+    return false;
+}
+
+// Slab geometry: pz planes starting at plane z0 = slab * pz (pz even); the slab holds Zh = pz/2
+// compact planes of each colour, local index ((c * Zh + Zl) * Lh + Y) * Lh + X.
+struct Slab {
+    int Zh, chunk, z0h;  // compact planes per colour, sites per colour chunk, first compact plane
+    bool wrap;           // the slab is the whole lattice (+z of its last plane stays inside)
+};
+
+__device__ __forceinline__ int slab_global(const Geo& g, const Slab& sl, int li)
+{
+    const int c = li / sl.chunk;
+    return c * g.Nc + sl.z0h * g.Lh * g.Lh + (li - c * sl.chunk);
+}
+
+// Slab-local index of the neighbour of bond b of the site (c, Zl, Y, X) (bond b never leaves
+// the slab here: +z bonds out of a slab that is not the whole lattice are the boundary kernel's)
+__device__ __forceinline__ int slab_nbr(const Geo& g, const Slab& sl, int c, int Zl, int Y, int X,
+                                        int b)
+{
+    const int px = c & 1, py = (c >> 1) & 1, pzb = c >> 2;
+    int cn = c, Zn = Zl, Yn = Y, Xn = X;
+    if (b == 0 || b == 2) Xn = px ? (X + 1 == g.Lh ? 0 : X + 1) : X;   // x + 1
+    if (b == 3) Xn = px ? X : (X == 0 ? g.Lh - 1 : X - 1);             // x - 1
+    if (b >= 1 && b <= 3) Yn = py ? (Y + 1 == g.Lh ? 0 : Y + 1) : Y;   // y + 1
+    if (b == 4) {
+        Zn = Zl + pzb;
+        if (Zn == sl.Zh) Zn = 0;
+    }
+    cn ^= b == 0 ? 1 : b == 1 ? 2 : b < 4 ? 3 : 4;
+    return ((cn * sl.Zh + Zn) * g.Lh + Yn) * g.Lh + Xn;
+}
+
+// Union-find of one slab of one lattice in shared memory; writes the label of every site.
+// Phase A computes the activated owned bonds of every site (bits 2..6 of its staged spin byte,
+// whose low two bits keep the biased spin), phase B unites along them, phase C compresses.
+template <class Real, bool MASKS>
+__global__ void __launch_bounds__(512, 2)
+    wolff_slab_kernel(SweepArgs a, int pz, int* labels, long long lab_stride, int* err)
+{
+    extern __shared__ __align__(16) unsigned char wsm[];
+    const Geo g = a.g;
+    const int lat = (int)blockIdx.y;
+    const int conf = lat / a.nrep, rep = lat - conf * a.nrep;
+    Slab sl;
+    sl.Zh = pz >> 1;
+    sl.chunk = sl.Zh * g.Lh * g.Lh;
+    sl.z0h = (int)blockIdx.x * sl.Zh;
+    sl.wrap = pz == g.H;
+    const int nsite = 8 * sl.chunk;
+    volatile uint16_t* slab = reinterpret_cast<uint16_t*>(wsm);
+    uint8_t* ss = wsm + 2 * (size_t)nsite;
+    const uint8_t* S = a.spins + (long long)lat * a.lat_stride;
+    const Real* P = wfield<Real>(a, conf);
+    const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
+    int* lab = labels + (long long)lat * lab_stride;
+    for (int li = (int)threadIdx.x; li < nsite; li += (int)blockDim.x) {
+        ss[li] = S[slab_global(g, sl, li)];
+        slab[li] = (uint16_t)li;
+    }
+    __syncthreads();
+
+    // phase A: activation bits, one Philox block per bond type and quad
+    const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+    const uint32_t cycle = a.ctl[0];
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    const int rowq = g.Lh * g.Qr;
+    const int nquad = 8 * sl.Zh * rowq;
+    const int dc = g.Nc - sl.chunk, goff = sl.z0h * g.Lh * g.Lh;  // local -> compact index
+    for (int q = (int)threadIdx.x; q < nquad; q += (int)blockDim.x) {
+        const int c = q / (sl.Zh * rowq);
+        int r = q - c * sl.Zh * rowq;
+        const int Zl = r / rowq;
+        r -= Zl * rowq;
+        const int Y = r / g.Qr, Xq = r - Y * g.Qr;
+        const uint32_t grp = (uint32_t)(((c * g.Hh + sl.z0h + Zl) * g.Lh + Y) * g.Qr + Xq);
+        const int row0 = ((c * sl.Zh + Zl) * g.Lh + Y) * g.Lh;
+        const bool zleave = (c >> 2) && Zl + 1 == sl.Zh && !sl.wrap;
+        unsigned act = 0;  // bit 5 * w + b
+#pragma unroll
+        for (int b = 0; b < 5; ++b) {
+            if (b == 4 && zleave) break;
+            unsigned want = 0;
+            Real wv[4];
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+                const int X = 4 * Xq + w;
+                if (X >= g.Lh) break;
+                const int li = row0 + X;
+                const int si = (int)(ss[li] & 3u) - 1;
+                if (si == 0) continue;
+                const int lj = slab_nbr(g, sl, c, Zl, Y, X, b);
+                const int sj = (int)(ss[lj] & 3u) - 1;
+                if (sj == 0) continue;
+                Real pi = Real(0), pj = Real(0);
+                int jh = 1, jv = 1;
+                if (b < 2) {
+                    const int gi = c * dc + goff + li;
+                    pi = P[gi];
+                    pj = P[(c ^ (b + 1)) * dc + goff + lj];
+                    if (MASKS) {
+                        jh = BM[gi] & 1;
+                        jv = (BM[gi] >> 1) & 1;
+                    }
+                }
+                if (bond_weight<Real>(a, b, si, sj, jh, jv, pi, pj, wv[w])) want |= 1u << w;
+            }
+            if (!want) continue;
+            const U4 rr = philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffBond + 16u * b, k0, k1);
+#pragma unroll
+            for (int w = 0; w < 4; ++w)
+                if (((want >> w) & 1u) && bond_trial<Real>(wv[w], beta, u4_word(rr, w)))
+                    act |= 1u << (5 * w + b);
+        }
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            const unsigned m = (act >> (5 * w)) & 31u;
+            if (m) ss[row0 + 4 * Xq + w] = (uint8_t)(ss[row0 + 4 * Xq + w] | (m << 2));
+        }
+    }
+    __syncthreads();
+
+    // phase B: unions along the activated bonds
+    bool ok = true;
+    for (int li = (int)threadIdx.x; li < nsite; li += (int)blockDim.x) {
+        unsigned m = (unsigned)ss[li] >> 2;
+        if (!m) continue;
+        const int c = li / sl.chunk;
+        int r = li - c * sl.chunk;
+        const int Zl = r / (g.Lh * g.Lh);
+        r -= Zl * g.Lh * g.Lh;
+        const int Y = r / g.Lh, X = r - Y * g.Lh;
+        while (m) {
+            const int b = __ffs((int)m) - 1;
+            m &= m - 1;
+            ok &= sunite(slab, li, slab_nbr(g, sl, c, Zl, Y, X, b));
+        }
+    }
+    if (!ok) atomicExch(err, 1);
+    __syncthreads();
+
+    // phase C: every site's label is the compact index of its slab-local root
+    for (int li = (int)threadIdx.x; li < nsite; li += (int)blockDim.x)
+        lab[slab_global(g, sl, li)] = slab_global(g, sl, sfind(slab, li));
+}
+
+// +z bonds from the last plane of every slab into the next slab (pz < H), united in global memory
+template <class Real>
+__global__ void __launch_bounds__(256) wolff_boundary_kernel(SweepArgs a, int pz, int* labels,
+                                                             long long lab_stride, int* err)
+{
+    const Geo g = a.g;
+    const int lat = (int)blockIdx.y;
+    const int conf = lat / a.nrep, rep = lat - conf * a.nrep;
+    const int nslab = g.H / pz;
+    const int per_slab = 4 * g.Lh * g.Qr;  // quads of the colours of odd z in one plane
+    const int item = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (item >= nslab * per_slab) return;
+    const int slab = item / per_slab;
+    int r = item - slab * per_slab;
+    const int c = 4 + r / (g.Lh * g.Qr);
+    r -= (c - 4) * g.Lh * g.Qr;
+    const int Y = r / g.Qr, Xq = r - Y * g.Qr;
+    const int Z = slab * (pz >> 1) + (pz >> 1) - 1;  // compact plane of z = z0 + pz - 1 (odd)
+    const int Zn = Z + 1 == g.Hh ? 0 : Z + 1;
+    const uint8_t* S = a.spins + (long long)lat * a.lat_stride;
+    volatile int* lab = labels + (long long)lat * lab_stride;
+    const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+    const uint32_t grp = (uint32_t)(((c * g.Hh + Z) * g.Lh + Y) * g.Qr + Xq);
+    const U4 rr = philox4x32_10((uint32_t)rep, a.ctl[0], grp, kTagWolffBond + 16u * 4u, a.seed,
+                                a.conf_base + (uint32_t)conf);
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        const int X = 4 * Xq + w;
+        if (X >= g.Lh) break;
+        const int ci = cidx(g, c, Z, Y, X), cj = cidx(g, c ^ 4, Zn, Y, X);
+        const int si = (int)S[ci] - 1, sj = (int)S[cj] - 1;
+        if (si == 0 || sj == 0) continue;
+        Real wv;
+        if (!bond_weight<Real>(a, 4, si, sj, 1, 1, Real(0), Real(0), wv)) continue;
+        if (bond_trial<Real>(wv, beta, u4_word(rr, w)) && !unite(lab, ci, cj)) atomicExch(err, 1);
+    }
+}
+
+// Flip the component of the seed site (roots found on the fly; labels of either form)
+__global__ void wolff_flip_kernel(SweepArgs a, int* labels, long long lab_stride,
                                   long long* csize)
 {
     const Geo g = a.g;
     const int lat = (int)blockIdx.y;
     const int conf = lat / a.nrep, rep = lat - conf * a.nrep;
     uint8_t* S = a.spins + (long long)lat * a.lat_stride;
-    const int* lab = labels + (long long)lat * lab_stride;
+    volatile int* lab = labels + (long long)lat * lab_stride;
     const uint32_t w = philox4x32_10((uint32_t)rep, a.ctl[0], 0xFFFFFFFFu, kTagWolffSeed, a.seed,
                                      a.conf_base + (uint32_t)conf).x;
     const int seed_site = (int)(((unsigned long long)w * (unsigned long long)g.N) >> 32);
     const int cs = compact_of_site(g, seed_site);
     int count = 0;
     if (S[cs] != 1) {
-        const int root = lab[cs];
+        const int root = find_root(lab, cs);
         for (int i = (int)(blockIdx.x * blockDim.x + threadIdx.x); i < g.N;
              i += (int)(gridDim.x * blockDim.x))
-            if (lab[i] == root) {
+            if (find_root(lab, i) == root) {
                 S[i] = (uint8_t)(2 - S[i]);
                 ++count;
             }
@@ -213,22 +442,62 @@ cudaError_t bonds(const SweepArgs& a, int* labels, long long ls, int* err, int n
 
 }  // namespace
 
+// Planes per slab of the shared-memory form: the largest even divisor pz of H whose slab fits
+// kSlabSites2 sites (two CTAs per SM), else kSlabSites1 (one CTA per SM); 0 if none does.
+constexpr int kSlabSites2 = 38912, kSlabSites1 = 65536, kSlabThreads = 512;
+
+int wolff_slab_planes(const Geo& g)
+{
+    for (const int cap : {kSlabSites2, kSlabSites1})
+        for (int pz = g.H; pz >= 2; pz -= 2)
+            if (g.H % pz == 0 && (long long)pz * g.L * g.L <= cap) return pz;
+    return 0;
+}
+
+namespace {
+template <class Real, bool MASKS>
+cudaError_t slab_launch(const SweepArgs& a, int pz, int nlat, int* labels, long long ls, int* err,
+                        cudaStream_t st)
+{
+    const size_t smem = 3 * (size_t)pz * a.g.L * a.g.L;
+    cudaError_t e = cudaFuncSetAttribute(wolff_slab_kernel<Real, MASKS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    wolff_slab_kernel<Real, MASKS>
+        <<<dim3((unsigned)(a.g.H / pz), (unsigned)nlat), kSlabThreads, smem, st>>>(a, pz, labels,
+                                                                                 ls, err);
+    if ((e = cudaGetLastError()) != cudaSuccess || pz == a.g.H) return e;
+    const int items = (a.g.H / pz) * 4 * a.g.Lh * a.g.Qr;
+    wolff_boundary_kernel<Real><<<dim3((unsigned)((items + 255) / 256), (unsigned)nlat), 256, 0,
+                                  st>>>(a, pz, labels, ls, err);
+    return cudaGetLastError();
+}
+}  // namespace
+
 // One Wolff update of every lattice of a group (the SweepArgs of the group, lat0 = 0): labels is
 // scratch of nlat x lab_stride ints, csize receives the flipped-cluster size per lattice (added;
-// the caller zeroes it), err is set on a union-find retry overflow.
+// the caller zeroes it), err is set on a union-find retry overflow.  per_site selects the
+// site-per-thread global form (also taken when no slab fits in shared memory).
 cudaError_t launch_wolff(const SweepArgs& a, bool fp64, bool masks, int nlat, int* labels,
-                         long long lab_stride, long long* csize, int* err, cudaStream_t st)
+                         long long lab_stride, long long* csize, int* err, cudaStream_t st,
+                         bool per_site)
 {
     const unsigned bx = (unsigned)((a.g.N + 255) / 256);
     const unsigned bxs = bx > 64 ? 64u : bx;
-    wolff_init_kernel<<<dim3(bxs, (unsigned)nlat), 256, 0, st>>>(labels, lab_stride, a.g.N);
-    cudaError_t e = cudaGetLastError();
+    const int pz = per_site ? 0 : wolff_slab_planes(a.g);
+    cudaError_t e;
+    if (pz > 0) {
+        e = fp64 ? (masks ? slab_launch<double, true>(a, pz, nlat, labels, lab_stride, err, st)
+                          : slab_launch<double, false>(a, pz, nlat, labels, lab_stride, err, st))
+                 : (masks ? slab_launch<float, true>(a, pz, nlat, labels, lab_stride, err, st)
+                          : slab_launch<float, false>(a, pz, nlat, labels, lab_stride, err, st));
+    } else {
+        wolff_init_kernel<<<dim3(bxs, (unsigned)nlat), 256, 0, st>>>(labels, lab_stride, a.g.N);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        e = fp64 ? bonds<double>(a, labels, lab_stride, err, nlat, masks, st)
+                 : bonds<float>(a, labels, lab_stride, err, nlat, masks, st);
+    }
     if (e != cudaSuccess) return e;
-    e = fp64 ? bonds<double>(a, labels, lab_stride, err, nlat, masks, st)
-             : bonds<float>(a, labels, lab_stride, err, nlat, masks, st);
-    if (e != cudaSuccess) return e;
-    wolff_compress_kernel<<<dim3(bxs, (unsigned)nlat), 256, 0, st>>>(labels, lab_stride, a.g.N);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     wolff_flip_kernel<<<dim3(bxs, (unsigned)nlat), 256, 0, st>>>(a, labels, lab_stride, csize);
     return cudaGetLastError();
 }
