@@ -225,11 +225,16 @@ struct Slab {
     bool wrap;           // the slab is the whole lattice (+z of its last plane stays inside)
 };
 
-__device__ __forceinline__ int slab_global(const Geo& g, const Slab& sl, int li)
-{
-    const int c = li / sl.chunk;
-    return c * g.Nc + sl.z0h * g.Lh * g.Lh + (li - c * sl.chunk);
-}
+// x / d for 0 <= x < 2^16, 1 <= d <= 2^16 by a multiply-high with m = floor((2^32 - 1) / d) + 1:
+// m*d - 2^32 < d and x*d < 2^32 keep the quotient exact.
+struct FastDiv {
+    uint32_t d, m;
+    __device__ explicit FastDiv(uint32_t dv) : d(dv), m(dv == 1u ? 0u : 0xFFFFFFFFu / dv + 1u) {}
+    __device__ __forceinline__ uint32_t operator()(uint32_t x) const
+    {
+        return d == 1u ? x : __umulhi(x, m);
+    }
+};
 
 // Slab-local index of the neighbour of bond b of the site (c, Zl, Y, X) (bond b never leaves
 // the slab here: +z bonds out of a slab that is not the whole lattice are the boundary kernel's)
@@ -237,7 +242,7 @@ __device__ __forceinline__ int slab_nbr(const Geo& g, const Slab& sl, int c, int
                                         int b)
 {
     const int px = c & 1, py = (c >> 1) & 1, pzb = c >> 2;
-    int cn = c, Zn = Zl, Yn = Y, Xn = X;
+    int Zn = Zl, Yn = Y, Xn = X;
     if (b == 0 || b == 2) Xn = px ? (X + 1 == g.Lh ? 0 : X + 1) : X;   // x + 1
     if (b == 3) Xn = px ? X : (X == 0 ? g.Lh - 1 : X - 1);             // x - 1
     if (b >= 1 && b <= 3) Yn = py ? (Y + 1 == g.Lh ? 0 : Y + 1) : Y;   // y + 1
@@ -245,13 +250,43 @@ __device__ __forceinline__ int slab_nbr(const Geo& g, const Slab& sl, int c, int
         Zn = Zl + pzb;
         if (Zn == sl.Zh) Zn = 0;
     }
-    cn ^= b == 0 ? 1 : b == 1 ? 2 : b < 4 ? 3 : 4;
+    const int cn = c ^ (b == 0 ? 1 : b == 1 ? 2 : b < 4 ? 3 : 4);
     return ((cn * sl.Zh + Zn) * g.Lh + Yn) * g.Lh + Xn;
 }
 
+// Exact integer form of the activation trial u < pa for a bond of uniform coupling: the
+// uniform's integer numerator (FP32: r mod 2^23 over 2^23; FP64: rotl(r, 9) over 2^32) is
+// below ceil(pa * 2^23) (resp. 2^32), pa * 2^k being exact.
+template <class Real>
+__device__ __forceinline__ unsigned long long uniform_threshold(Real K, double beta)
+{
+    if (!(K > Real(0))) return 0ull;
+    if constexpr (sizeof(Real) == 8) {
+        const double pa = __dsub_rn(1.0, own_exp(-__dmul_rn(__dmul_rn(2.0, K), beta)));
+        return (unsigned long long)ceil(__dmul_rn(pa, 4294967296.0));
+    } else {
+        const float kb2 = (float)(-2.0 * beta * 1.4426950408889634);
+        const float pa = __fsub_rn(1.0f, ex2_approx(__fmul_rn(kb2, K)));
+        return (unsigned long long)ceilf(__fmul_rn(pa, 8388608.0f));
+    }
+}
+
+template <class Real>
+__device__ __forceinline__ bool uniform_trial(unsigned long long thr, uint32_t r)
+{
+    if constexpr (sizeof(Real) == 8)
+        return (unsigned long long)((r << 9) | (r >> 23)) < thr;
+    else
+        return (unsigned long long)(r & 0x007FFFFFu) < thr;
+}
+
 // Union-find of one slab of one lattice in shared memory; writes the label of every site.
-// Phase A computes the activated owned bonds of every site (bits 2..6 of its staged spin byte,
-// whose low two bits keep the biased spin), phase B unites along them, phase C compresses.
+// Phase A evaluates the five owned bonds of every quad (the four sites of one Philox block) and
+// keeps the activated ones in bits 2..6 of each site's staged byte (bits 0..1 keep the biased
+// spin).  Phase B unites along them as a warp-synchronous state machine: in every round each lane
+// takes one step (fetch a bond, one find step with path halving, or one hook attempt), so lanes
+// never replay the union code for small subsets as nested divergent loops would.  Phase C writes
+// every site's label, the compact index of its slab-local root.
 template <class Real, bool MASKS>
 __global__ void __launch_bounds__(512, 2)
     wolff_slab_kernel(SweepArgs a, int pz, int* labels, long long lab_stride, int* err)
@@ -272,29 +307,52 @@ __global__ void __launch_bounds__(512, 2)
     const Real* P = wfield<Real>(a, conf);
     const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
     int* lab = labels + (long long)lat * lab_stride;
-    for (int li = (int)threadIdx.x; li < nsite; li += (int)blockDim.x) {
-        ss[li] = S[slab_global(g, sl, li)];
-        slab[li] = (uint16_t)li;
+    const int dc = g.Nc - sl.chunk, goff = sl.z0h * g.Lh * g.Lh;  // local li -> c*dc + goff + li
+    const int NT = (int)blockDim.x;
+    for (int c = 0; c < 8; ++c) {
+        const uint8_t* src = S + c * g.Nc + goff;
+        for (int k = (int)threadIdx.x; k < sl.chunk; k += NT) {
+            ss[c * sl.chunk + k] = src[k];
+            slab[c * sl.chunk + k] = (uint16_t)(c * sl.chunk + k);
+        }
     }
     __syncthreads();
 
-    // phase A: activation bits, one Philox block per bond type and quad
+    // ---- phase A: activated bonds --------------------------------------------------------
     const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
     const uint32_t cycle = a.ctl[0];
     const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    Real J2, J3;
+    if constexpr (sizeof(Real) == 8) {
+        J2 = a.J2;
+        J3 = a.J3;
+    } else {
+        J2 = a.J2f;
+        J3 = a.J3f;
+    }
+    const unsigned long long thr2 = uniform_threshold<Real>(J2 < Real(0) ? -J2 : J2, beta);
+    const unsigned long long thr3 = uniform_threshold<Real>(J3 < Real(0) ? -J3 : J3, beta);
+    const int s2 = J2 > Real(0) ? 1 : J2 < Real(0) ? -1 : 0;  // s_i s_j of a satisfied bond
+    const int s3 = J3 > Real(0) ? 1 : J3 < Real(0) ? -1 : 0;
     const int rowq = g.Lh * g.Qr;
-    const int nquad = 8 * sl.Zh * rowq;
-    const int dc = g.Nc - sl.chunk, goff = sl.z0h * g.Lh * g.Lh;  // local -> compact index
-    for (int q = (int)threadIdx.x; q < nquad; q += (int)blockDim.x) {
-        const int c = q / (sl.Zh * rowq);
-        int r = q - c * sl.Zh * rowq;
-        const int Zl = r / rowq;
+    const int cq = sl.Zh * rowq;
+    const int nquad = 8 * cq;
+    const FastDiv div_cq((uint32_t)cq), div_rq((uint32_t)rowq), div_qr((uint32_t)g.Qr);
+    for (int q = (int)threadIdx.x; q < nquad; q += NT) {
+        const int c = (int)div_cq((uint32_t)q);
+        int r = q - c * cq;
+        const int Zl = (int)div_rq((uint32_t)r);
         r -= Zl * rowq;
-        const int Y = r / g.Qr, Xq = r - Y * g.Qr;
-        const uint32_t grp = (uint32_t)(((c * g.Hh + sl.z0h + Zl) * g.Lh + Y) * g.Qr + Xq);
+        const int Y = (int)div_qr((uint32_t)r), Xq = r - Y * g.Qr;
+        const int X0 = 4 * Xq;
+        const int nw = g.Lh - X0 < 4 ? g.Lh - X0 : 4;
         const int row0 = ((c * sl.Zh + Zl) * g.Lh + Y) * g.Lh;
-        const bool zleave = (c >> 2) && Zl + 1 == sl.Zh && !sl.wrap;
-        unsigned act = 0;  // bit 5 * w + b
+        const bool zleave = (c >> 2) && Zl + 1 == sl.Zh && !sl.wrap;  // boundary kernel's bond
+        const uint32_t grp = (uint32_t)(((c * g.Hh + sl.z0h + Zl) * g.Lh + Y) * g.Qr + Xq);
+        int si[4];
+#pragma unroll
+        for (int w = 0; w < 4; ++w) si[w] = w < nw ? (int)(ss[row0 + X0 + w] & 3u) - 1 : 0;
+        unsigned act = 0;  // bit 5*w + b
 #pragma unroll
         for (int b = 0; b < 5; ++b) {
             if (b == 4 && zleave) break;
@@ -302,64 +360,128 @@ __global__ void __launch_bounds__(512, 2)
             Real wv[4];
 #pragma unroll
             for (int w = 0; w < 4; ++w) {
-                const int X = 4 * Xq + w;
-                if (X >= g.Lh) break;
-                const int li = row0 + X;
-                const int si = (int)(ss[li] & 3u) - 1;
-                if (si == 0) continue;
-                const int lj = slab_nbr(g, sl, c, Zl, Y, X, b);
-                const int sj = (int)(ss[lj] & 3u) - 1;
-                if (sj == 0) continue;
-                Real pi = Real(0), pj = Real(0);
-                int jh = 1, jv = 1;
+                wv[w] = Real(0);
+                if (si[w] == 0) continue;
+                const int lj = slab_nbr(g, sl, c, Zl, Y, X0 + w, b);
+                const int ssj = si[w] * ((int)(ss[lj] & 3u) - 1);
+                if (ssj == 0) continue;
                 if (b < 2) {
-                    const int gi = c * dc + goff + li;
-                    pi = P[gi];
-                    pj = P[(c ^ (b + 1)) * dc + goff + lj];
+                    const int gi = c * dc + goff + row0 + X0 + w;
+                    int jh = 1, jv = 1;
                     if (MASKS) {
                         jh = BM[gi] & 1;
                         jv = (BM[gi] >> 1) & 1;
                     }
+                    if (bond_weight<Real>(a, b, ssj, 1, jh, jv, P[gi],
+                                          P[(c ^ (b + 1)) * dc + goff + lj], wv[w]))
+                        want |= 1u << w;
+                } else if (ssj == (b < 4 ? s2 : s3)) {
+                    want |= 1u << w;
                 }
-                if (bond_weight<Real>(a, b, si, sj, jh, jv, pi, pj, wv[w])) want |= 1u << w;
             }
             if (!want) continue;
             const U4 rr = philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffBond + 16u * b, k0, k1);
 #pragma unroll
-            for (int w = 0; w < 4; ++w)
-                if (((want >> w) & 1u) && bond_trial<Real>(wv[w], beta, u4_word(rr, w)))
-                    act |= 1u << (5 * w + b);
+            for (int w = 0; w < 4; ++w) {
+                if (!((want >> w) & 1u)) continue;
+                const uint32_t word = u4_word(rr, w);
+                const bool on = b < 2 ? bond_trial<Real>(wv[w], beta, word)
+                                      : uniform_trial<Real>(b < 4 ? thr2 : thr3, word);
+                if (on) act |= 1u << (5 * w + b);
+            }
         }
 #pragma unroll
         for (int w = 0; w < 4; ++w) {
             const unsigned m = (act >> (5 * w)) & 31u;
-            if (m) ss[row0 + 4 * Xq + w] = (uint8_t)(ss[row0 + 4 * Xq + w] | (m << 2));
+            if (m) ss[row0 + X0 + w] = (uint8_t)(ss[row0 + X0 + w] | (m << 2));
         }
     }
     __syncthreads();
 
-    // phase B: unions along the activated bonds
-    bool ok = true;
-    for (int li = (int)threadIdx.x; li < nsite; li += (int)blockDim.x) {
-        unsigned m = (unsigned)ss[li] >> 2;
-        if (!m) continue;
-        const int c = li / sl.chunk;
-        int r = li - c * sl.chunk;
-        const int Zl = r / (g.Lh * g.Lh);
-        r -= Zl * g.Lh * g.Lh;
-        const int Y = r / g.Lh, X = r - Y * g.Lh;
-        while (m) {
-            const int b = __ffs((int)m) - 1;
-            m &= m - 1;
-            ok &= sunite(slab, li, slab_nbr(g, sl, c, Zl, Y, X, b));
+    // ---- phase B: unions, one step per lane per round -------------------------------------
+    {
+        enum { kFetch = 0, kFindA = 1, kFindB = 2, kHook = 3 };
+        const FastDiv div_chunk((uint32_t)sl.chunk), div_plane((uint32_t)(g.Lh * g.Lh)),
+            div_lh((uint32_t)g.Lh);
+        int li = (int)threadIdx.x - NT;  // site whose bonds are being united
+        unsigned m = 0;                  // its bonds still to unite
+        int c = 0, Zl = 0, Y = 0, X = 0;
+        int st = kFetch, ua = 0, ub = 0, x = 0, tries = 0;
+        bool alive = true, ok = true;
+        while (__any_sync(0xFFFFFFFFu, alive)) {
+            if (!alive) continue;
+            if (st == kFetch) {
+                if (m == 0) {
+                    li += NT;
+                    if (li >= nsite) {
+                        alive = false;
+                        continue;
+                    }
+                    m = (unsigned)ss[li] >> 2;
+                    c = (int)div_chunk((uint32_t)li);
+                    int r = li - c * sl.chunk;
+                    Zl = (int)div_plane((uint32_t)r);
+                    r -= Zl * g.Lh * g.Lh;
+                    Y = (int)div_lh((uint32_t)r);
+                    X = r - Y * g.Lh;
+                } else {
+                    const int b = __ffs((int)m) - 1;
+                    m &= m - 1;
+                    ua = li;
+                    ub = slab_nbr(g, sl, c, Zl, Y, X, b);
+                    x = ua;
+                    st = kFindA;
+                    tries = 0;
+                }
+            } else if (st != kHook) {  // one find step with path halving
+                const int p = slab[x];
+                if (p == x) {
+                    if (st == kFindA) {
+                        ua = x;
+                        x = ub;
+                        st = kFindB;
+                    } else {
+                        ub = x;
+                        st = kHook;
+                    }
+                } else {
+                    const int gp = slab[p];
+                    if (gp != p) slab[x] = (uint16_t)gp;
+                    x = p;
+                }
+            } else {  // hook the larger root under the smaller
+                if (ua == ub) {
+                    st = kFetch;
+                } else {
+                    const int hi = ua > ub ? ua : ub, lo = ua ^ ub ^ hi;
+                    const unsigned short old = atomicCAS(
+                        const_cast<unsigned short*>(reinterpret_cast<volatile unsigned short*>(slab)) + hi,
+                        (unsigned short)hi, (unsigned short)lo);
+                    if (old == (unsigned short)hi) {
+                        st = kFetch;
+                    } else if (++tries >= (1 << 20)) {  // retry budget spent: give up this bond
+                        ok = false;
+                        st = kFetch;
+                    } else {  // hi stopped being a root: find both roots again
+                        ua = hi;
+                        ub = lo;
+                        x = ua;
+                        st = kFindA;
+                    }
+                }
+            }
         }
+        if (!ok) atomicExch(err, 1);
     }
-    if (!ok) atomicExch(err, 1);
     __syncthreads();
 
-    // phase C: every site's label is the compact index of its slab-local root
-    for (int li = (int)threadIdx.x; li < nsite; li += (int)blockDim.x)
-        lab[slab_global(g, sl, li)] = slab_global(g, sl, sfind(slab, li));
+    // ---- phase C: labels -----------------------------------------------------------------
+    const FastDiv div_chunk((uint32_t)sl.chunk);
+    for (int c = 0; c < 8; ++c)
+        for (int k = (int)threadIdx.x; k < sl.chunk; k += NT) {
+            const int root = sfind(slab, c * sl.chunk + k);
+            lab[c * g.Nc + goff + k] = (int)div_chunk((uint32_t)root) * dc + goff + root;
+        }
 }
 
 // +z bonds from the last plane of every slab into the next slab (pz < H), united in global memory
