@@ -78,6 +78,16 @@ typedef struct {
     int64_t nmeasure;
 } j1j2c_slot_sums;
 
+/* Optional diagnostics of measured PT cycles (all off in a new context). */
+typedef struct j1j2c_diagnostics {
+    int32_t locnem_slot;  /* >= 0: per-site sums of s and of the local nematic term of the replica
+                             at this slot (PTMEASINDEX - 1) after every measured cycle; -1: off */
+    int32_t hist_bins;    /* > 0: per-slot energy histogram with this many bins (BINS); 0: off */
+    int32_t trace_cycles; /* > 0: record {mag, en, strx, stry, nbar} of every slot and temp_of_rep
+                             of every replica for the first trace_cycles measured cycles */
+    int32_t flip_counts;  /* 1: per-site accepted flips per temperature slot; 0: off */
+} j1j2c_diagnostics;
+
 /* ---------------------------------------------------------------------------------------------
  * Context life cycle
  * ------------------------------------------------------------------------------------------- */
@@ -131,6 +141,16 @@ int j1j2c_init_spins(void *ctx, int32_t conf, int32_t start, int32_t axis, const
  * reset best_en to +inf, as at the start of Pt_measurement_loop (J:1361-1389, J:1394-1395).
  * Swap counters run on across both loops, as cfg_ptswap_* do (reset by j1j2c_init_spins). */
 int j1j2c_reset_measurements(void *ctx, int32_t conf);
+
+/* Enable / disable the measurement diagnostics (replaces the WRITELOCNEM, WRITEHIST,
+ * WRITEBINDTIME / trace and WRITENUMFLIPS bookkeeping of J:1009-1025, J:1397-1477,
+ * J:1514-1523, J:1168-1177 and J:2575).  Every enabled diagnostic starts from zero.  Flip
+ * counting runs the generic sweep kernels (the shape-specialised ones do not count) and is
+ * charged 8 bytes of traffic per accepted flip; the others cost one small kernel or a few
+ * stores per measured cycle.  The local nematic sums and the histogram restart with
+ * j1j2c_reset_measurements (J:1388, J:1227-1230); flip counts restart with j1j2c_init_spins
+ * (J:1231-1232); the trace is indexed by the measured-cycle count. */
+int j1j2c_set_diagnostics(void *ctx, const j1j2c_diagnostics *diag);
 
 /* ---------------------------------------------------------------------------------------------
  * Hot path
@@ -193,6 +213,26 @@ int j1j2c_get_spins(void *ctx, int32_t conf, int32_t rep, int8_t *out);
  * (per occupied site; en includes the phi term, J:2835-2840; nbar as J:1028-1048);
  * conf < 0: every conf, nconf x NREPLICA x 5. */
 int j1j2c_get_observables(void *ctx, int32_t conf, double *out);
+
+/* Per-site sums of the local nematic average of one conf (N doubles each, site order, either
+ * may be NULL) and the number of cycles they hold: locspin_accum, locnem_accum and
+ * locnem_samples of Accumulate_local_nematic_average (J:1009-1025). */
+int j1j2c_get_locnem(void *ctx, int32_t conf, double *locspin, double *locnem, int64_t *samples);
+
+/* Energy histogram of every slot of a conf: counts (NREPLICA x bins; bin k holds the samples of
+ * J:1520-1522's histindex k+1, not yet divided by NMESS), lower edge and bin size per slot
+ * (hist_en_min_t, hist_bin_size_t; any output may be NULL). */
+int j1j2c_get_histogram(void *ctx, int32_t conf, double *counts, double *emin, double *binsize);
+
+/* Recorded trace of one conf: obs (cycles x NREPLICA x 5, by slot: mag, en, strx, stry, nbar),
+ * temp_of_rep (cycles x NREPLICA, by replica); *ncycles = rows written (<= trace_cycles).  The
+ * per-cycle data behind cfbt / cftr (J:1397-1475) and the LOCAL lists of Process_data. */
+int j1j2c_get_trace(void *ctx, int32_t conf, double *obs, int32_t *temp_of_rep, int64_t *ncycles);
+
+/* Accepted flips per site of every slot of a conf (NREPLICA x N int32, slot-major, site order;
+ * vacancies read -1 as Mark_vacancy_flipcounts sets them), counted since j1j2c_init_spins
+ * (confnumflips, J:109, J:2575). */
+int j1j2c_get_flip_counts(void *ctx, int32_t conf, int32_t *counts);
 
 /* Sweep-kernel timing accumulated under J1J2C_FLAG_PROFILE: milliseconds, launches, and the
  * attempts those launches made (occupied sites x sweeps). */

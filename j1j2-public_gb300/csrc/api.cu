@@ -92,6 +92,19 @@ struct Ctx {
     double prof_ms = 0.0;
     long long prof_launches = 0, prof_attempts = 0;
 
+    // optional diagnostics (j1j2c_set_diagnostics)
+    j1j2c_diagnostics diag{-1, 0, 0, 0};
+    long long spin_bytes = 0, mask_bytes = 0;
+    int* d_loc_s = nullptr;             // per-site sums of s (conf at mask offsets)
+    int* d_loc_n = nullptr;             // per-site sums of the local nematic term
+    long long* d_loc_samples = nullptr; // per conf
+    long long* d_hist = nullptr;        // [entries x bins]
+    double* d_hist_lo = nullptr;
+    double* d_hist_bs = nullptr;
+    double* d_trace = nullptr;          // [cycles x entries x 5]
+    int* d_trace_tor = nullptr;         // [cycles x entries]
+    int* d_flips = nullptr;             // flip counts, laid out like the spins
+
     uint32_t host_ctl[4] = {0, 1, 0, 0};
     std::string err;
 };
@@ -135,7 +148,9 @@ void release(Ctx* c)
     void* ptrs[] = {c->d_spins, c->d_pf,    c->d_pd,   c->d_bm,    c->d_occ,   c->d_beta,
                     c->d_rat,   c->d_tor,   c->d_obs,  c->d_sums,  c->d_nmeas, c->d_att,
                     c->d_acc,   c->d_vis,   c->d_last, c->d_ctl,   c->d_nocc,  c->d_rbase,
-                    c->d_nreps, c->d_audit, c->d_labels, c->d_csize, c->d_err};
+                    c->d_nreps, c->d_audit, c->d_labels, c->d_csize, c->d_err,
+                    c->d_loc_s, c->d_loc_n, c->d_loc_samples, c->d_hist, c->d_hist_lo,
+                    c->d_hist_bs, c->d_trace, c->d_trace_tor, c->d_flips};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto s : c->side) cudaStreamDestroy(s);
@@ -171,7 +186,9 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
     v.vac = c->vac;
     v.mode = kModeSweep;
     const bool quad_ok = (grp.g.Lh % 4 == 0) && !(fl & J1J2C_FLAG_GENERIC);
-    if (!(fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_GLOBAL))) {
+    // the shape-specialised kernels do not count flips
+    if (!(fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_GLOBAL)) &&
+        !c->diag.flip_counts) {
         int nts[8];
         bool sp[8];
         const int n = fixed_candidates(fp64, grp.g.L, grp.g.H, c->masks, c->vac, nts, sp, 8);
@@ -249,6 +266,7 @@ SweepArgs group_args(Ctx* c, const Group& grp)
     a.conf_base = c->P.conf_base + (uint32_t)grp.conf0;
     a.lat0 = 0;
     a.use_override = 0;
+    a.flips = c->d_flips ? c->d_flips + grp.spin_off : nullptr;
     return a;
 }
 
@@ -273,7 +291,36 @@ SwapArgs swap_args(Ctx* c, int measure)
     s.measure = measure;
     s.seed = c->P.seed;
     s.conf_base = c->P.conf_base;
+    s.hist_bins = c->d_hist ? c->diag.hist_bins : 0;
+    s.hist = c->d_hist;
+    s.hist_lo = c->d_hist_lo;
+    s.hist_bs = c->d_hist_bs;
+    s.trace_cap = c->d_trace ? c->diag.trace_cycles : 0;
+    s.entries = c->nentries;
+    s.trace = c->d_trace;
+    s.trace_tor = c->d_trace_tor;
     return s;
+}
+
+// Accumulate_local_nematic_average of every conf whose ladder has the diagnostic slot
+cudaError_t enqueue_locnem(Ctx* c, cudaStream_t st)
+{
+    for (const Group& grp : c->G) {
+        if (c->diag.locnem_slot >= grp.nrep) continue;
+        LocnemArgs a{};
+        a.g = grp.g;
+        a.spins = c->d_spins + grp.spin_off;
+        a.lat_stride = grp.lat_stride;
+        a.rat = c->d_rat + grp.rep0;
+        a.nrep = grp.nrep;
+        a.slot = c->diag.locnem_slot;
+        a.loc_s = c->d_loc_s + grp.mask_off;
+        a.loc_n = c->d_loc_n + grp.mask_off;
+        a.samples = c->d_loc_samples + grp.conf0;
+        cudaError_t e = launch_locnem(a, grp.nconf, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 // PTSWAPEVER sweeps and the observable reduction of lattices [lat0, lat0 + nlat) of a group
@@ -330,7 +377,9 @@ cudaError_t enqueue_cycle(Ctx* c, int measure, cudaStream_t st)
     if (c->profile &&
         (e = cudaEventRecordWithFlags(c->ev1, st, cudaEventRecordExternal)) != cudaSuccess)
         return e;
-    return launch_swap(swap_args(c, measure), st);
+    if ((e = launch_swap(swap_args(c, measure), st)) != cudaSuccess) return e;
+    if (measure && c->d_loc_s) return enqueue_locnem(c, st);
+    return cudaSuccess;
 }
 
 int build_graph(Ctx* c, int measure)
@@ -541,6 +590,8 @@ int j1j2c_create_multi(void** out, const j1j2c_params* groups, int32_t ngroups)
         c->nentries += grp.nlat();
         c->G.push_back(grp);
     }
+    c->spin_bytes = spin_bytes;
+    c->mask_bytes = mask_bytes;
     c->have_dis.assign(c->nconf, 0);
     c->have_ladder.assign(c->nconf, 0);
     c->have_spins.assign(c->nconf, 0);
@@ -798,8 +849,11 @@ int j1j2c_init_spins(void* ctx, int32_t conf, int32_t start, int32_t axis, const
         a.key1 = c->P.conf_base + (uint32_t)conf;
         CK(c, launch_init(a, c->st));
     }
-    // Initialize_pt_state: identity maps, swap counters zeroed (J:1222-1233)
+    // Initialize_pt_state: identity maps, swap counters and flip counts zeroed (J:1222-1233)
     const int rb = c->conf_rbase[conf];
+    if (c->d_flips)
+        CK(c, cudaMemsetAsync(c->d_flips + grp.spin_off + (size_t)lc * nrep * grp.lat_stride, 0,
+                              sizeof(int) * (size_t)nrep * grp.lat_stride, c->st));
     CK(c, cudaMemsetAsync(c->d_att + rb, 0, sizeof(long long) * nrep, c->st));
     CK(c, cudaMemsetAsync(c->d_acc + rb, 0, sizeof(long long) * nrep, c->st));
     std::vector<int> ident((size_t)nrep);
@@ -825,6 +879,179 @@ int j1j2c_reset_measurements(void* ctx, int32_t conf)
     CK(c, cudaMemcpy(c->d_sums + off * 22, sums.data(), sums.size() * 8, cudaMemcpyHostToDevice));
     CK(c, cudaMemset(c->d_nmeas + off, 0, n * sizeof(long long)));
     CK(c, cudaMemset(c->d_vis + off, 0, n));
+    // histograms start again (range from the next first sample, J:1227-1230) and so do the
+    // local nematic averages (Reset_local_nematic_average, J:1388)
+    if (c->d_hist) {
+        const size_t bins = (size_t)c->diag.hist_bins;
+        CK(c, cudaMemset(c->d_hist + off * bins, 0, n * bins * sizeof(long long)));
+        CK(c, cudaMemset(c->d_hist_bs + off, 0, n * sizeof(double)));
+        CK(c, cudaMemset(c->d_hist_lo + off, 0, n * sizeof(double)));
+    }
+    if (c->d_loc_s) {
+        size_t lo = 0, len = (size_t)c->mask_bytes;
+        if (conf >= 0) {
+            const Group& grp = c->G[c->conf_group[conf]];
+            lo = (size_t)grp.mask_off + (size_t)(conf - grp.conf0) * grp.lat_stride;
+            len = (size_t)grp.lat_stride;
+        }
+        CK(c, cudaMemset(c->d_loc_s + lo, 0, len * sizeof(int)));
+        CK(c, cudaMemset(c->d_loc_n + lo, 0, len * sizeof(int)));
+        CK(c, cudaMemset(c->d_loc_samples + (conf < 0 ? 0 : conf), 0,
+                         (conf < 0 ? (size_t)c->nconf : 1) * sizeof(long long)));
+    }
+    return J1J2C_OK;
+}
+
+int j1j2c_set_diagnostics(void* ctx, const j1j2c_diagnostics* d)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!d) return fail(c, J1J2C_EINVAL, "null diagnostics");
+    if (d->locnem_slot < -1 || d->hist_bins < 0 || d->hist_bins > (1 << 20) ||
+        d->trace_cycles < 0 || (d->flip_counts != 0 && d->flip_counts != 1))
+        return fail(c, J1J2C_EINVAL, "bad diagnostics settings");
+    CK(c, cudaStreamSynchronize(c->st));
+    free_graphs(c);
+    auto drop = [](auto*& p) {
+        if (p) cudaFree(p);
+        p = nullptr;
+    };
+    drop(c->d_loc_s);
+    drop(c->d_loc_n);
+    drop(c->d_loc_samples);
+    drop(c->d_hist);
+    drop(c->d_hist_lo);
+    drop(c->d_hist_bs);
+    drop(c->d_trace);
+    drop(c->d_trace_tor);
+    drop(c->d_flips);
+    const bool flips_changed = (d->flip_counts != 0) != (c->diag.flip_counts != 0);
+    c->diag = *d;
+    const size_t ne = (size_t)c->nentries;
+    if (d->locnem_slot >= 0) {
+        const size_t n = (size_t)c->mask_bytes;
+        CK(c, dalloc(&c->d_loc_s, n));
+        CK(c, dalloc(&c->d_loc_n, n));
+        CK(c, dalloc(&c->d_loc_samples, (size_t)c->nconf));
+        CK(c, cudaMemset(c->d_loc_s, 0, n * sizeof(int)));
+        CK(c, cudaMemset(c->d_loc_n, 0, n * sizeof(int)));
+        CK(c, cudaMemset(c->d_loc_samples, 0, (size_t)c->nconf * sizeof(long long)));
+    }
+    if (d->hist_bins > 0) {
+        CK(c, dalloc(&c->d_hist, ne * (size_t)d->hist_bins));
+        CK(c, dalloc(&c->d_hist_lo, ne));
+        CK(c, dalloc(&c->d_hist_bs, ne));
+        CK(c, cudaMemset(c->d_hist, 0, ne * (size_t)d->hist_bins * sizeof(long long)));
+        CK(c, cudaMemset(c->d_hist_lo, 0, ne * sizeof(double)));
+        CK(c, cudaMemset(c->d_hist_bs, 0, ne * sizeof(double)));
+    }
+    if (d->trace_cycles > 0) {
+        CK(c, dalloc(&c->d_trace, (size_t)d->trace_cycles * ne * 5));
+        CK(c, dalloc(&c->d_trace_tor, (size_t)d->trace_cycles * ne));
+    }
+    if (d->flip_counts) {
+        CK(c, dalloc(&c->d_flips, (size_t)c->spin_bytes));
+        CK(c, cudaMemset(c->d_flips, 0, (size_t)c->spin_bytes * sizeof(int)));
+    }
+    if (flips_changed)
+        for (auto& gr : c->G) {
+            int rc = choose_variant(c, gr, c->P.precision == J1J2C_FP64_PLAIN, gr.var, gr.smem,
+                                    gr.nthreads);
+            if (rc != J1J2C_OK) return rc;
+            gr.tuned = false;
+        }
+    return J1J2C_OK;
+}
+
+int j1j2c_get_locnem(void* ctx, int32_t conf, double* locspin, double* locnem, int64_t* samples)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!valid_conf(c, conf)) return fail(c, J1J2C_EINVAL, "conf out of range");
+    if (!c->d_loc_s) return fail(c, J1J2C_ESTATE, "local nematic averages are not enabled");
+    const Group& grp = c->G[c->conf_group[conf]];
+    const Geo& g = grp.g;
+    const size_t off = (size_t)grp.mask_off + (size_t)(conf - grp.conf0) * grp.lat_stride;
+    std::vector<int> vs((size_t)g.N), vn((size_t)g.N);
+    long long ns = 0;
+    CK(c, cudaStreamSynchronize(c->st));
+    CK(c, cudaMemcpy(vs.data(), c->d_loc_s + off, sizeof(int) * g.N, cudaMemcpyDeviceToHost));
+    CK(c, cudaMemcpy(vn.data(), c->d_loc_n + off, sizeof(int) * g.N, cudaMemcpyDeviceToHost));
+    CK(c, cudaMemcpy(&ns, c->d_loc_samples + conf, sizeof ns, cudaMemcpyDeviceToHost));
+    for (int st = 0; st < g.N; ++st) {
+        const int ci = compact_of_site(g, st);
+        if (locspin) locspin[st] = (double)vs[ci];
+        if (locnem) locnem[st] = (double)vn[ci];
+    }
+    if (samples) *samples = ns;
+    return J1J2C_OK;
+}
+
+int j1j2c_get_histogram(void* ctx, int32_t conf, double* counts, double* emin, double* binsize)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!valid_conf(c, conf)) return fail(c, J1J2C_EINVAL, "conf out of range");
+    if (!c->d_hist) return fail(c, J1J2C_ESTATE, "the energy histogram is not enabled");
+    const size_t off = (size_t)c->conf_rbase[conf], n = (size_t)c->conf_nrep[conf];
+    const size_t bins = (size_t)c->diag.hist_bins;
+    std::vector<long long> h(n * bins);
+    CK(c, cudaStreamSynchronize(c->st));
+    CK(c, cudaMemcpy(h.data(), c->d_hist + off * bins, h.size() * sizeof(long long),
+                     cudaMemcpyDeviceToHost));
+    if (counts)
+        for (size_t k = 0; k < h.size(); ++k) counts[k] = (double)h[k];
+    if (emin) CK(c, cudaMemcpy(emin, c->d_hist_lo + off, n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (binsize)
+        CK(c, cudaMemcpy(binsize, c->d_hist_bs + off, n * sizeof(double), cudaMemcpyDeviceToHost));
+    return J1J2C_OK;
+}
+
+int j1j2c_get_trace(void* ctx, int32_t conf, double* obs, int32_t* temp_of_rep, int64_t* ncycles)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!valid_conf(c, conf)) return fail(c, J1J2C_EINVAL, "conf out of range");
+    if (!c->d_trace) return fail(c, J1J2C_ESTATE, "the observable trace is not enabled");
+    const size_t off = (size_t)c->conf_rbase[conf], n = (size_t)c->conf_nrep[conf];
+    const size_t ne = (size_t)c->nentries;
+    long long nm = 0;
+    CK(c, cudaStreamSynchronize(c->st));
+    CK(c, cudaMemcpy(&nm, c->d_nmeas + off, sizeof nm, cudaMemcpyDeviceToHost));
+    const size_t rows = (size_t)(nm < c->diag.trace_cycles ? nm : c->diag.trace_cycles);
+    if (rows > 0 && obs)
+        CK(c, cudaMemcpy2D(obs, n * 5 * sizeof(double), c->d_trace + off * 5,
+                           ne * 5 * sizeof(double), n * 5 * sizeof(double), rows,
+                           cudaMemcpyDeviceToHost));
+    if (rows > 0 && temp_of_rep)
+        CK(c, cudaMemcpy2D(temp_of_rep, n * sizeof(int), c->d_trace_tor + off, ne * sizeof(int),
+                           n * sizeof(int), rows, cudaMemcpyDeviceToHost));
+    if (ncycles) *ncycles = (int64_t)rows;
+    return J1J2C_OK;
+}
+
+int j1j2c_get_flip_counts(void* ctx, int32_t conf, int32_t* counts)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!valid_conf(c, conf) || !counts) return fail(c, J1J2C_EINVAL, "bad conf or null output");
+    if (!c->d_flips) return fail(c, J1J2C_ESTATE, "flip counts are not enabled");
+    const Group& grp = c->G[c->conf_group[conf]];
+    const Geo& g = grp.g;
+    const int nrep = grp.nrep, lc = conf - grp.conf0;
+    std::vector<int> buf((size_t)nrep * grp.lat_stride);
+    std::vector<uint8_t> occ((size_t)g.N);
+    CK(c, cudaStreamSynchronize(c->st));
+    CK(c, cudaMemcpy(buf.data(), c->d_flips + grp.spin_off + (size_t)lc * nrep * grp.lat_stride,
+                     buf.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    CK(c, cudaMemcpy(occ.data(), c->d_occ + grp.mask_off + (size_t)lc * grp.lat_stride, g.N,
+                     cudaMemcpyDeviceToHost));
+    for (int sl = 0; sl < nrep; ++sl)
+        for (int st = 0; st < g.N; ++st) {
+            const int ci = compact_of_site(g, st);
+            // Mark_vacancy_flipcounts (J:1168-1177): vacancies read -1
+            counts[(size_t)sl * g.N + st] = occ[ci] ? buf[(size_t)sl * grp.lat_stride + ci] : -1;
+        }
     return J1J2C_OK;
 }
 

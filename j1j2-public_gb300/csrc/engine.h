@@ -42,6 +42,8 @@ struct SweepArgs {
     int use_override;        // 1: beta_override / sweep_override instead of ladder / cycle
     double beta_override;
     uint32_t sweep_override;
+    int* flips;              // accepted flips per site, row (conf * nrep + slot) of lat_stride
+                             // ints (nullptr: not counted; generic kernels only)
 };
 
 // Replica-indexed arrays are laid out conf by conf: conf c owns entries rbase[c] ..
@@ -63,7 +65,30 @@ struct SwapArgs {
     uint32_t* ctl;       // ctl[0] cycle, ctl[1] swap phase (1 or 2), ctl[2] CTA ticket
     int nconf, measure;
     uint32_t seed, conf_base;
+    // optional diagnostics of measured cycles
+    int hist_bins;          // > 0: energy histogram per slot (counts, range set by 1st sample)
+    long long* hist;        // [entries x hist_bins]
+    double* hist_lo;        // per slot: lower edge (valid once hist_bs > 0)
+    double* hist_bs;        // per slot: bin size, <= 0 until the first sample
+    long long trace_cap;    // > 0: record the first trace_cap measured cycles
+    int entries;            // replica-indexed entries of the context (trace row length)
+    double* trace;          // [trace_cap x entries x 5] observables by slot
+    int* trace_tor;         // [trace_cap x entries] temp_of_rep by replica
 };
+
+// Per-site accumulation of the replica at one temperature slot (Accumulate_local_nematic_average,
+// J:1009-1025) for every conf of a group.
+struct LocnemArgs {
+    Geo g;
+    const uint8_t* spins;    // group's first lattice
+    long long lat_stride;
+    const int* rat;          // rep_at_temp of the group's first entry
+    int nrep, slot;
+    int* loc_s;              // conf c at c * lat_stride (compact layout)
+    int* loc_n;
+    long long* samples;      // per conf of the group
+};
+cudaError_t launch_locnem(const LocnemArgs& a, int nconf, cudaStream_t st);
 
 struct InitArgs {
     Geo g;

@@ -30,7 +30,7 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint
                                           const Real* P, const uint8_t* BM, const float* Pf32,
                                           int c, int X, int Y, int Z, uint32_t sweep, uint32_t rep,
                                           uint32_t k0, uint32_t k1, double beta, float kb,
-                                          Acc& acc)
+                                          Acc& acc, int* fl = nullptr)
 {
     const int px = c & 1, py = (c >> 1) & 1, pz = c >> 2;
     const int Xp = px ? wrap_p(X, g.Lh) : X, Xm = px ? X : wrap_m(X, g.Lh);
@@ -139,11 +139,17 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint
             acc.M += 1;
             acc.SX += (flip32 != flip64);
         }
-        if (flip64) S[i] = (uint8_t)(2 - b);
+        if (flip64) {
+            S[i] = (uint8_t)(2 - b);
+            if (fl) fl[i] += 1;
+        }
     } else {
         r = u4_word(philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1), w);
         const float sf = __fmul_rn((float)s, f32);
-        if (u01_f32(r) < ex2_approx(__fmul_rn(kb, sf))) S[i] = (uint8_t)(2 - b);
+        if (u01_f32(r) < ex2_approx(__fmul_rn(kb, sf))) {
+            S[i] = (uint8_t)(2 - b);
+            if (fl) fl[i] += 1;
+        }
     }
 }
 
@@ -161,7 +167,7 @@ template <class Real, bool MASKS, bool MEASURE>
 __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, uint32_t* S32,
                                           const Real* P, const uint8_t* BM, int c, int q,
                                           uint32_t sweep, uint32_t rep, uint32_t k0, uint32_t k1,
-                                          double beta, float kb, Acc& acc)
+                                          double beta, float kb, Acc& acc, int* fl = nullptr)
 {
     const int Qr = g.Qr;
     const int row = q / Qr;
@@ -319,7 +325,14 @@ __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, uint
         }
     }
     if constexpr (!MEASURE) {
-        if (flipmask) S32[wown] = n.own ^ flipmask;
+        if (flipmask) {
+            S32[wown] = n.own ^ flipmask;
+            if (fl) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if ((flipmask >> (8 * k + 1)) & 1u) fl[bo + k] += 1;
+            }
+        }
     }
 }
 
@@ -366,6 +379,9 @@ __global__ void __launch_bounds__(1024) sweep_kernel(SweepArgs a)
     const float kb = (float)(-2.0 * beta * 1.4426950408889634);
     const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
     Acc acc{0, 0, 0, 0, 0};
+    int* fl = nullptr;  // flip counts of this replica's temperature slot
+    if (a.flips && !a.use_override && MODE == kModeSweep)
+        fl = a.flips + ((long long)conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]) * a.lat_stride;
 
     for (int t = 0; t < a.nsweeps; ++t) {
         const uint32_t sweep = sweep0 + (uint32_t)t;
@@ -375,13 +391,14 @@ __global__ void __launch_bounds__(1024) sweep_kernel(SweepArgs a)
                 const int nq = g.Nc >> 2;
                 for (int q = tid; q < nq; q += NT)
                     quad_step<Real, MASKS, false>(a, g, reinterpret_cast<uint32_t*>(S), P, BM, c,
-                                                  q, sweep, (uint32_t)rep, k0, k1, beta, kb, acc);
+                                                  q, sweep, (uint32_t)rep, k0, k1, beta, kb, acc,
+                                                  fl);
             } else {
                 for (int k = tid; k < g.Nc; k += NT) {
                     const int X = k % g.Lh, r = k / g.Lh;
                     const int Y = r % g.Lh, Z = r / g.Lh;
                     site_step<Real, MASKS, MODE, false>(a, g, S, P, BM, Pf32, c, X, Y, Z, sweep,
-                                                        (uint32_t)rep, k0, k1, beta, kb, acc);
+                                                        (uint32_t)rep, k0, k1, beta, kb, acc, fl);
                 }
             }
             __syncthreads();
@@ -483,10 +500,14 @@ __global__ void __launch_bounds__(32 * kSwapWarps) swap_kernel(SwapArgs a)
         }
         __syncwarp();
         if (a.measure) {
+            const long long trow = a.nmeas[base];  // measured cycles so far (every slot alike)
+            __syncwarp();
+            const bool tracing = trow < a.trace_cap;
             for (int rep = lane; rep < nrep; rep += 32) {
                 const int t = a.tor[base + rep];
                 if (t == 0) a.visited[base + rep] |= 1;
                 if (t == nrep - 1) a.visited[base + rep] |= 2;
+                if (tracing) a.trace_tor[trow * a.entries + base + rep] = t;
             }
             for (int sl = lane; sl < nrep; sl += 32) {
                 const double* o = a.last_obs + 5 * (base + a.rat[base + sl]);
@@ -520,6 +541,28 @@ __global__ void __launch_bounds__(32 * kSwapWarps) swap_kernel(SwapArgs a)
                 if (aen < S[20]) S[20] = aen;
                 S[21] = aen;
                 a.nmeas[base + sl] += 1;
+                if (tracing) {
+                    double* tr = a.trace + 5 * (trow * a.entries + base + sl);
+                    tr[0] = amag;
+                    tr[1] = aen;
+                    tr[2] = ax;
+                    tr[3] = ay;
+                    tr[4] = anb;
+                }
+                if (a.hist_bins > 0) {  // WRITEHIST, J:1514-1523
+                    const int e = base + sl;
+                    double lo = a.hist_lo[e], bs = a.hist_bs[e];
+                    if (bs <= 0.0) {
+                        const double w = __dadd_rn(fabs(aen), 1.0);
+                        lo = __dsub_rn(aen, w);
+                        bs = __ddiv_rn(__dsub_rn(__dadd_rn(aen, w), lo), (double)a.hist_bins);
+                        a.hist_lo[e] = lo;
+                        a.hist_bs[e] = bs;
+                    }
+                    int k = 1 + (int)__ddiv_rn(__dsub_rn(aen, lo), bs);
+                    k = k < 1 ? 1 : (k > a.hist_bins ? a.hist_bins : k);
+                    a.hist[(long long)e * a.hist_bins + k - 1] += 1;
+                }
             }
         }
     }
@@ -534,6 +577,34 @@ __global__ void __launch_bounds__(32 * kSwapWarps) swap_kernel(SwapArgs a)
             __threadfence();
         }
     }
+}
+
+// Accumulate_local_nematic_average (J:1009-1025) on the replica at one slot of every conf of a
+// group: per occupied site, s and s*(s_+x + s_-x - s_+y - s_-y) (vacant neighbours count 0).
+__global__ void __launch_bounds__(256) locnem_kernel(LocnemArgs a)
+{
+    const Geo g = a.g;
+    const int conf = (int)blockIdx.y;
+    const int rep = a.rat[conf * a.nrep + a.slot];
+    const uint8_t* S = a.spins + ((long long)conf * a.nrep + rep) * a.lat_stride;
+    int* ls = a.loc_s + (long long)conf * a.lat_stride;
+    int* ln = a.loc_n + (long long)conf * a.lat_stride;
+    for (int i = (int)(blockIdx.x * blockDim.x + threadIdx.x); i < g.N;
+         i += (int)(gridDim.x * blockDim.x)) {
+        const int s = (int)S[i] - 1;
+        if (s == 0) continue;
+        const int c = i / g.Nc, k = i - c * g.Nc;
+        const int X = k % g.Lh, r = k / g.Lh;
+        const int Y = r % g.Lh, Z = r / g.Lh;
+        const int px = c & 1, py = (c >> 1) & 1;
+        const int Xp = px ? wrap_p(X, g.Lh) : X, Xm = px ? X : wrap_m(X, g.Lh);
+        const int Yp = py ? wrap_p(Y, g.Lh) : Y, Ym = py ? Y : wrap_m(Y, g.Lh);
+        const int nx = (int)S[cidx(g, c ^ 1, Z, Y, Xp)] + (int)S[cidx(g, c ^ 1, Z, Y, Xm)] - 2;
+        const int ny = (int)S[cidx(g, c ^ 2, Z, Yp, X)] + (int)S[cidx(g, c ^ 2, Z, Ym, X)] - 2;
+        ls[i] += s;
+        ln[i] += s * (nx - ny);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.samples[conf] += 1;
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -565,16 +636,19 @@ __global__ void __launch_bounds__(256) sweep_global_kernel(SweepArgs a, int colo
     const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
     const int item = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     Acc acc{0, 0, 0, 0, 0};
+    int* fl = nullptr;  // flip counts of this replica's temperature slot
+    if (a.flips && !a.use_override)
+        fl = a.flips + ((long long)conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]) * a.lat_stride;
     if constexpr (QUAD) {
         if (item < (g.Nc >> 2))
             quad_step<Real, MASKS, false>(a, g, reinterpret_cast<uint32_t*>(S), P, BM, colour,
-                                          item, sweep, (uint32_t)rep, k0, k1, beta, kb, acc);
+                                          item, sweep, (uint32_t)rep, k0, k1, beta, kb, acc, fl);
     } else {
         if (item < g.Nc) {
             const int X = item % g.Lh, r = item / g.Lh;
             site_step<Real, MASKS, kModeSweep, false>(a, g, S, P, BM, nullptr, colour, X,
                                                       r % g.Lh, r / g.Lh, sweep, (uint32_t)rep,
-                                                      k0, k1, beta, kb, acc);
+                                                      k0, k1, beta, kb, acc, fl);
         }
     }
 }
@@ -755,6 +829,14 @@ cudaError_t launch_swap(const SwapArgs& a, cudaStream_t st)
 {
     const int nb = (a.nconf + kSwapWarps - 1) / kSwapWarps;
     swap_kernel<<<nb, 32 * kSwapWarps, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_locnem(const LocnemArgs& a, int nconf, cudaStream_t st)
+{
+    int bx = (a.g.N + 255) / 256;
+    if (bx > 512) bx = 512;
+    locnem_kernel<<<dim3((unsigned)bx, (unsigned)nconf), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -34,7 +34,9 @@ EXPORTS = ("j1j2c_create", "j1j2c_create_multi", "j1j2c_conf_shape", "j1j2c_dest
            "j1j2c_get_slot_sums", "j1j2c_get_pt_stats", "j1j2c_get_maps", "j1j2c_get_spins",
            "j1j2c_get_observables", "j1j2c_get_profile", "j1j2c_get_config",
            "j1j2c_corr_rand_3d", "j1j2c_setup_vacancies", "j1j2c_kiss_spins", "j1j2c_ladder",
-           "j1j2c_version", "j1j2c_wolff", "j1j2c_get_cluster_sizes", "j1j2c_enumerate_exact")
+           "j1j2c_version", "j1j2c_wolff", "j1j2c_get_cluster_sizes", "j1j2c_enumerate_exact",
+           "j1j2c_set_diagnostics", "j1j2c_get_locnem", "j1j2c_get_histogram", "j1j2c_get_trace",
+           "j1j2c_get_flip_counts")
 
 ENUM_FIELDS = ("lnZ", "e", "e2", "absm", "m2", "m4", "abssx", "sx2", "abssy", "sy2", "nbar",
                "nbar2")
@@ -56,6 +58,11 @@ class Params(C.Structure):
 
 class SlotSums(C.Structure):
     _fields_ = [(f, C.c_double) for f in SUM_FIELDS] + [("nmeasure", C.c_int64)]
+
+
+class Diagnostics(C.Structure):
+    _fields_ = [("locnem_slot", C.c_int32), ("hist_bins", C.c_int32),
+                ("trace_cycles", C.c_int32), ("flip_counts", C.c_int32)]
 
 
 _lib = None
@@ -185,6 +192,7 @@ class Engine:
         self.rbase = np.cumsum([0] + [s[2] for s in self.shapes])
         self.nentries = int(self.rbase[-1])
         self.nocc = np.array([s[0] * s[0] * s[1] for s in self.shapes], np.int64)
+        self.diag = Diagnostics(-1, 0, 0, 0)
 
     def _shape(self, conf):
         if not 0 <= conf < self.nconf:
@@ -270,6 +278,48 @@ class Engine:
         """One Wolff update of every lattice; returns the flipped-cluster sizes per replica."""
         out = np.zeros(self.nentries, np.int64)
         self._ck(lib().j1j2c_wolff(self._ctx, _p(out, C.c_int64)))
+        return out
+
+    # diagnostics -------------------------------------------------------------------------------
+    def set_diagnostics(self, locnem_slot=-1, hist_bins=0, trace_cycles=0, flip_counts=False):
+        """WRITELOCNEM (slot = PTMEASINDEX - 1), WRITEHIST (BINS), per-cycle traces and
+        WRITENUMFLIPS of the reference's measurement loop; everything off by default."""
+        d = Diagnostics(int(locnem_slot), int(hist_bins), int(trace_cycles), int(bool(flip_counts)))
+        self._ck(lib().j1j2c_set_diagnostics(self._ctx, C.byref(d)))
+        self.diag = d
+
+    def locnem(self, conf):
+        """(locspin_accum, locnem_accum, locnem_samples) of one conf in site order (J:1009-1025)."""
+        n = self.n_of(conf)
+        ls, ln = np.empty(n), np.empty(n)
+        ns = C.c_int64()
+        self._ck(lib().j1j2c_get_locnem(self._ctx, C.c_int32(conf), _p(ls, C.c_double),
+                                        _p(ln, C.c_double), C.byref(ns)))
+        return ls, ln, ns.value
+
+    def histogram(self, conf):
+        """(counts[nrep, bins], emin[nrep], binsize[nrep]) of one conf (J:1514-1523)."""
+        r = self.nrep_of(conf)
+        counts = np.empty((r, self.diag.hist_bins))
+        lo, bs = np.empty(r), np.empty(r)
+        self._ck(lib().j1j2c_get_histogram(self._ctx, C.c_int32(conf), _p(counts, C.c_double),
+                                           _p(lo, C.c_double), _p(bs, C.c_double)))
+        return counts, lo, bs
+
+    def trace(self, conf):
+        """(obs[cycles, nrep, 5] by slot, temp_of_rep[cycles, nrep]) of the recorded cycles."""
+        r, cap = self.nrep_of(conf), max(1, self.diag.trace_cycles)
+        obs = np.empty((cap, r, 5))
+        tor = np.empty((cap, r), np.int32)
+        n = C.c_int64()
+        self._ck(lib().j1j2c_get_trace(self._ctx, C.c_int32(conf), _p(obs, C.c_double),
+                                       _p(tor, C.c_int32), C.byref(n)))
+        return obs[:n.value], tor[:n.value]
+
+    def flip_counts(self, conf):
+        """confnumflips of one conf: nrep x N int32 by slot in site order, -1 at vacancies."""
+        out = np.empty((self.nrep_of(conf), self.n_of(conf)), np.int32)
+        self._ck(lib().j1j2c_get_flip_counts(self._ctx, C.c_int32(conf), _p(out, C.c_int32)))
         return out
 
     def cluster_sizes(self, conf=-1):
@@ -389,6 +439,25 @@ def finalize_slots(sums, nmeas, beta, nocc) -> SlotResult:
         USX=binder(strx4, strx2), USY=binder(stry4, stry2), UBN=binder(nbar4, nbar2),
         sph=(en2 - en ** 2) * nocc * beta ** 2, stripediff=strx ** 2 - stry ** 2,
         best_en=s[:, 20], final_en=s[:, 21])
+
+
+def local_histogram(enlist, bins):
+    """WRITEHIST of the LOCAL sampler (Process_data, J:2296-2352) from the measured per-site
+    energies of one temperature: the range spans the list's min..max widened by half the span on
+    either side (+-1e-6 when flat), a sample goes to bin NINT((e - min) / size) and samples
+    outside 1..bins are dropped.  Returns (counts[bins], min, size)."""
+    e = np.asarray(enlist, np.float64)
+    lo, hi = float(e.min()), float(e.max())
+    if hi > lo:
+        span = hi - lo
+        lo, hi = lo - 0.5 * span, hi + 0.5 * span
+    if hi <= lo:
+        lo, hi = lo - 1.0e-6, hi + 1.0e-6
+    size = (hi - lo) / bins
+    x = (e - lo) / size
+    k = np.where(x >= 0, np.floor(x + 0.5), -np.floor(-x + 0.5)).astype(np.int64)  # NINT
+    k = k[(k >= 1) & (k <= bins)]
+    return np.bincount(k - 1, minlength=bins).astype(np.float64), lo, size
 
 
 def pt_run(L, betas, nconf=1, neq=100, nmess=100, ptswapever=5, irinit=1, start=START_HOT,

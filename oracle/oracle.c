@@ -720,8 +720,9 @@ static inline void site_group(int32_t L, int32_t H, int32_t x, int32_t y, int32_
 #define TAG_SWAP 1u
 #define TAG_INIT 2u
 
+/* flipcounts (may be NULL): per-site accepted flips, as Metro_sweep's flipcounts (J:2575) */
 int64_t or_replay_sweeps(const or_lat *g, int8_t *s, double beta, uint32_t seed, uint32_t conf,
-                         uint32_t rep, uint32_t sweep0, int32_t nsweeps)
+                         uint32_t rep, uint32_t sweep0, int32_t nsweeps, int32_t *flipcounts)
 {
     const int32_t L = g->L, H = g->H, L2 = L * L;
     int64_t flips = 0;
@@ -751,6 +752,7 @@ int64_t or_replay_sweeps(const or_lat *g, int8_t *s, double beta, uint32_t seed,
                         if (flip) {
                             s[i] = (int8_t)(-s[i]);
                             flips++;
+                            if (flipcounts) flipcounts[i]++;
                         }
                     }
         }
@@ -802,7 +804,7 @@ void or_replay_pt(const or_lat *g, int32_t nrep, const double *beta, int32_t pts
                   int32_t ncycles, uint32_t cycle0, uint32_t seed, uint32_t conf, int32_t measure,
                   int32_t phase0, int8_t *spins, int32_t *rep_at_temp, int32_t *temp_of_rep,
                   double *sums, int64_t *nmeas, int64_t *attempts, int64_t *accepts,
-                  uint8_t *visited, double *obs_out)
+                  uint8_t *visited, double *obs_out, int32_t *flips)
 {
     const int32_t N = g->N;
     double *obs = (double *)malloc(sizeof(double) * 5 * nrep);
@@ -813,7 +815,8 @@ void or_replay_pt(const or_lat *g, int32_t nrep, const double *beta, int32_t pts
         for (int32_t rep = 0; rep < nrep; rep++) {
             double b = beta[temp_of_rep[rep]];
             or_replay_sweeps(g, spins + (size_t)rep * N, b, seed, conf, (uint32_t)rep,
-                             cycle * (uint32_t)ptswapever, ptswapever);
+                             cycle * (uint32_t)ptswapever, ptswapever,
+                             flips ? flips + (size_t)temp_of_rep[rep] * N : NULL);
             int64_t ints[4], acc;
             or_replay_measure(g, spins + (size_t)rep * N, ints, &acc, obs + 5 * rep);
             etot[rep] = (double)acc * 0x1p-33;

@@ -69,14 +69,14 @@ double or_bench_pt_ref(const or_lat *g, int32_t nthreads, int32_t nrep, const do
 void or_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 double or_dexp(double x);
 int64_t or_replay_sweeps(const or_lat *g, int8_t *s, double beta, uint32_t seed, uint32_t conf,
-                         uint32_t rep, uint32_t sweep0, int32_t nsweeps);
+                         uint32_t rep, uint32_t sweep0, int32_t nsweeps, int32_t *flipcounts);
 void or_replay_measure(const or_lat *g, const int8_t *s, int64_t ints[4], int64_t *eacc,
                        double obs[5]);
 void or_replay_pt(const or_lat *g, int32_t nrep, const double *beta, int32_t ptswapever,
                   int32_t ncycles, uint32_t cycle0, uint32_t seed, uint32_t conf, int32_t measure,
                   int32_t phase0, int8_t *spins, int32_t *rep_at_temp, int32_t *temp_of_rep,
                   double *sums, int64_t *nmeas, int64_t *attempts, int64_t *accepts,
-                  uint8_t *visited, double *obs_out);
+                  uint8_t *visited, double *obs_out, int32_t *flips);
 int64_t or_wolff_step(const or_lat *g, int8_t *s, double beta, uint32_t seed, uint32_t conf,
                       uint32_t rep, uint32_t cycle);
 void or_hot_spins_philox(int32_t L, int32_t H, uint32_t seed, uint32_t conf, uint32_t rep,

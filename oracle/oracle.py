@@ -184,10 +184,11 @@ class Model:
                                      C.c_int32(ncycles), C.c_int32(irinit))
 
     # device-engine replay --------------------------------------------------------------------
-    def replay_sweeps(self, s, beta, seed, conf, rep, sweep0, nsweeps):
+    def replay_sweeps(self, s, beta, seed, conf, rep, sweep0, nsweeps, flipcounts=None):
         return lib().or_replay_sweeps(self.ref(), _p(s, C.c_int8), C.c_double(beta),
                                       C.c_uint32(seed), C.c_uint32(conf), C.c_uint32(rep),
-                                      C.c_uint32(sweep0), C.c_int32(nsweeps))
+                                      C.c_uint32(sweep0), C.c_int32(nsweeps),
+                                      None if flipcounts is None else _p(flipcounts, C.c_int32))
 
     def wolff_step(self, s, beta, seed, conf, rep, cycle):
         """The engine's Wolff update restated (FP64 form); modifies s, returns the cluster size."""
@@ -203,8 +204,10 @@ class Model:
                                 _p(obs, C.c_double))
         return ints, acc.value, obs
 
-    def replay_pt(self, state, betas, ptswapever, ncycles, cycle0, seed, conf, measure, phase0):
-        """Advance ``state`` (dict of numpy arrays, modified in place) by ncycles PT cycles."""
+    def replay_pt(self, state, betas, ptswapever, ncycles, cycle0, seed, conf, measure, phase0,
+                  flips=None):
+        """Advance ``state`` (dict of numpy arrays, modified in place) by ncycles PT cycles;
+        ``flips`` (nrep x N int32, by temperature slot) accumulates accepted flips per site."""
         nrep = len(betas)
         b = np.ascontiguousarray(betas, np.float64)
         obs = np.empty((nrep, 5))
@@ -215,7 +218,7 @@ class Model:
                            _p(state["temp_of_rep"], C.c_int32), _p(state["sums"], C.c_double),
                            _p(state["nmeas"], C.c_int64), _p(state["attempts"], C.c_int64),
                            _p(state["accepts"], C.c_int64), _p(state["visited"], C.c_uint8),
-                           _p(obs, C.c_double))
+                           _p(obs, C.c_double), None if flips is None else _p(flips, C.c_int32))
         return obs
 
 
@@ -287,3 +290,58 @@ def ref_corr_rand_3d(n1, n2, n3, xi, seed, do_uniform=True, max_value=2.0) -> np
                                     C.c_double(xi), C.c_int(seed), C.c_int(int(do_uniform)),
                                     C.c_double(max_value))
     return out.reshape(n3, n2, n1)
+
+
+# ------------------------------------------------------------------------------------------------
+# Measurement-time diagnostics of the reference, restated for the tests
+# ------------------------------------------------------------------------------------------------
+def locnem_terms(s, occu, m):
+    """One call of Accumulate_local_nematic_average (J:1009-1025): the per-site additions to
+    locspin_accum and locnem_accum for spins s (site order), occupancy occu, neighbour table m
+    (m[k*N:(k+1)*N] = slot m(k+1))."""
+    N = s.size
+    s = s.astype(np.int64)
+    o = occu.astype(np.int64)
+    m1, m2, m3, m4 = (m[k * N:(k + 1) * N] for k in range(4))
+    ln = s * s[m3] * o[m3] - s * s[m1] * o[m1] + s * s[m4] * o[m4] - s * s[m2] * o[m2]
+    return np.where(o == 1, s, 0), np.where(o == 1, ln, 0)
+
+
+def pt_histogram(energies, bins):
+    """WRITEHIST of the PT measurement loop (J:1514-1523) for one temperature slot: the range is
+    set from the first measured energy, every sample lands in bin 1 + int((e - min) / size),
+    clamped to [1, bins].  Returns (counts[bins], min, size)."""
+    counts = np.zeros(bins)
+    lo = size = 0.0
+    for e in energies:
+        e = float(e)
+        if size <= 0.0:
+            lo = e - (abs(e) + 1.0)
+            hi = e + (abs(e) + 1.0)
+            size = (hi - lo) / bins
+        k = 1 + int((e - lo) / size)
+        k = max(1, min(bins, k))
+        counts[k - 1] += 1.0
+    return counts, lo, size
+
+
+def local_histogram_ref(enlist, bins):
+    """WRITEHIST of the LOCAL sampler's Process_data (J:2296-2352): range from the min and max of
+    the whole list widened by half the span (or +-1e-6 when flat), bin NINT((e - min) / size),
+    samples outside 1..bins dropped.  Returns (counts[bins], min, size)."""
+    lo, hi = float(min(enlist)), float(max(enlist))
+    if hi > lo:
+        span = hi - lo
+        lo -= 0.5 * span
+        hi += 0.5 * span
+    if hi <= lo:
+        lo -= 1.0e-6
+        hi += 1.0e-6
+    size = (hi - lo) / bins
+    counts = np.zeros(bins)
+    for e in enlist:
+        x = (float(e) - lo) / size
+        k = int(np.floor(x + 0.5)) if x >= 0 else -int(np.floor(-x + 0.5))
+        if 1 <= k <= bins:
+            counts[k - 1] += 1.0
+    return counts, lo, size

@@ -209,3 +209,26 @@ def test_ladder(oracle):
     np.testing.assert_allclose(t, 8.0 + 3.5 * np.arange(16) / 15, rtol=0, atol=1e-15)
     ts = oracle.ladder(11, 8.0, 11.5, split=True, tmid=9.5, tfrac=0.7)
     assert ts[0] == 8.0 and ts[-1] == 11.5 and ts[7] == 9.5
+
+
+def test_local_histogram_host_rule_matches_oracle(oracle):
+    """The product's LOCAL-histogram rule (Process_data, J:2296-2352) against the oracle's own
+    restatement, on random lists, a flat list and a two-value list."""
+    import j1j2cuda as jc
+    rng = np.random.default_rng(11)
+    cases = [rng.normal(-3.8, 0.05, 500), np.full(40, -2.5), np.array([-1.0, -2.0] * 10),
+             rng.uniform(-4.0, -3.0, 97)]
+    for e in cases:
+        for bins in (1, 7, 100):
+            c, lo, bs = jc.local_histogram(e, bins)
+            c_ref, lo_ref, bs_ref = oracle.local_histogram_ref(e, bins)
+            np.testing.assert_array_equal(c, c_ref)
+            assert lo == lo_ref and bs == bs_ref
+
+
+def test_pt_histogram_rule(oracle):
+    """J:1514-1523: the first sample fixes the range [e - (|e|+1), e + (|e|+1)] and later
+    samples clamp into the end bins."""
+    c, lo, bs = oracle.pt_histogram([-2.0, -2.0, -10.0, 5.0, -1.5], 4)
+    assert lo == -5.0 and bs == 1.5
+    assert c.tolist() == [1.0, 0.0, 3.0, 1.0]
