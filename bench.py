@@ -35,7 +35,7 @@ B_PER_ATTEMPT_FP64 = 21.4
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one sweep-kernel launch (5 sweeps
 # + measure of every lattice), from an ncu capture of the same workload
-TRAFFIC = {"batched_fp32_L32_64x32": 75592192 + 10054400}
+TRAFFIC = {"batched_fp32_L32_64x32": 75594240 + 9697280}
 
 # name -> lattice-shape groups (L, nconf, nreplica), precision and options
 WORKLOADS = {
@@ -50,6 +50,9 @@ WORKLOADS = {
                                precision=1),
     # L=96, 5 % site vacancies, 8 configurations x 48 replicas, one Wolff update per PT cycle
     "large_L96_vac5_wolff_8x48": dict(groups=[(96, 8, 48)], precision=1, vacancies=0.05,
+                                      wolff=True),
+    # the same with one configuration (48 lattices): the small case for ncu captures
+    "large_L96_vac5_wolff_1x48": dict(groups=[(96, 1, 48)], precision=1, vacancies=0.05,
                                       wolff=True),
     # L=16 single-temperature local Metropolis (T=9.5, one sweep + measurement per cycle), FP64
     "local_fp64_L16_T9.5": dict(groups=[(16, 1, 1)], precision=0, ptswapever=1, T=9.5),
