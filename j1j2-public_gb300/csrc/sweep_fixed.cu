@@ -21,6 +21,54 @@ struct Shape {
     static constexpr int NB = (N + 15) & ~15;
 };
 
+// Packed FP32 pairs (Blackwell add/sub/mul/fma .f32x2: two IEEE round-to-nearest operations per
+// instruction, element by element)
+using f2 = unsigned long long;
+
+__device__ __forceinline__ f2 f2_pack(float lo, float hi)
+{
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ f2 f2_splat(float v) { return f2_pack(v, v); }
+__device__ __forceinline__ float f2_get(f2 v, int e)
+{
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+    return e ? hi : lo;
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b)
+{
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b)
+{
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
+{
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c)
+{
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+// bytes k and k+1 of w as 2^23 + byte (exact floats; subtract 2^23 + offset afterwards)
+__device__ __forceinline__ f2 byte_pair(uint32_t w, int k)
+{
+    return f2_pack(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)k)),
+                   __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7541u + (uint32_t)k)));
+}
+
 // Word offsets (within a colour block) of a quad and of the words its neighbours live in:
 // same row; row Y+1 / Y-1; plane Z+1 / Z-1; and the words one step along x in those rows.
 struct QuadOff {
@@ -130,38 +178,66 @@ __device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
         rnd = philox4x32_10(rep, sweep, (uint32_t)(B0 + d.self), kTagSweep, k0, k1);
     uint32_t flipmask = 0;
     if constexpr (sizeof(Real) == 4) {
+        // Sites in pairs (0,1), (2,3) with packed FP32x2 arithmetic: every element follows
+        // field_fp32's operations and rounding (the -y terms enter as products with the negated
+        // spins, the J1v term as (pi - J1v) * (-sy): the same products, exactly).
         const uint32_t dsum = d.wdpp + d.wdpm + d.wdmp + d.wdmm;  // bytewise, <= 8
         const uint32_t zsum = d.wzp + d.wzm;                      // bytewise, <= 4
+        const f2 c1 = f2_splat(8388609.0f), c2 = f2_splat(8388610.0f), c4 = f2_splat(8388612.0f);
+        const f2 j3 = f2_splat(a.J3f), j2 = f2_splat(a.J2f), j1h = f2_splat(a.J1hf),
+                 j1v = f2_splat(a.J1vf);
         int ehi = 0, elo = 0;  // fixed-point energy of the quad, split as in efix32_split
         float nbf = 0.0f;      // nematic sum of the quad (exact small integers)
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            Nbr32 nb;
-            nb.sxp = byte_off(d.wxp, k, 1.0f);
-            nb.sxm = byte_off(d.wxm, k, 1.0f);
-            nb.syp = byte_off(d.wyp, k, 1.0f);
-            nb.sym = byte_off(d.wym, k, 1.0f);
-            nb.D = byte_off(dsum, k, 4.0f);
-            nb.Zs = byte_off(zsum, k, 2.0f);
-            nb.pxp = px ? (k < 3 ? d.pxa[k + 1] : d.pextra) : d.pxa[k];
-            nb.pxm = px ? d.pxa[k] : (k > 0 ? d.pxa[k - 1] : d.pextra);
-            nb.pyp = d.pyp[k];
-            nb.pym = d.pym[k];
-            const float f = field_fp32(nb, d.pown[k], a.J1hf, a.J1vf, a.J2f, a.J3f);
-            const float si = byte_off(d.own, k, 1.0f);
-            const float sf = __fmul_rn(si, f);
+        for (int h = 0; h < 2; ++h) {
+            const int k = 2 * h;
+            const f2 sxp = f2_sub(byte_pair(d.wxp, k), c1);
+            const f2 sxm = f2_sub(byte_pair(d.wxm, k), c1);
+            const f2 nsyp = f2_sub(c1, byte_pair(d.wyp, k));   // -s at +y
+            const f2 nsym = f2_sub(c1, byte_pair(d.wym, k));   // -s at -y
+            const f2 D = f2_sub(byte_pair(dsum, k), c4);
+            const f2 Zs = f2_sub(byte_pair(zsum, k), c2);
+            const f2 si = f2_sub(byte_pair(d.own, k), c1);
+            const f2 pi = f2_pack(d.pown[k], d.pown[k + 1]);
+            const f2 pxp = px ? f2_pack(d.pxa[k + 1], k + 1 < 3 ? d.pxa[k + 2] : d.pextra)
+                              : f2_pack(d.pxa[k], d.pxa[k + 1]);
+            const f2 pxm = px ? f2_pack(d.pxa[k], d.pxa[k + 1])
+                              : f2_pack(k > 0 ? d.pxa[k - 1] : d.pextra, d.pxa[k]);
+            const f2 pyp = f2_pack(d.pyp[k], d.pyp[k + 1]);
+            const f2 pym = f2_pack(d.pym[k], d.pym[k + 1]);
+            const f2 sx = f2_add(sxp, sxm), nsy = f2_add(nsyp, nsym);
+            f2 f = f2_mul(j3, Zs);
+            f = f2_fma(j2, D, f);
+            f = f2_fma(f2_add(j1h, pi), sx, f);
+            f = f2_fma(f2_sub(pi, j1v), nsy, f);
+            f = f2_fma(pxp, sxp, f);
+            f = f2_fma(pxm, sxm, f);
+            f = f2_fma(pyp, nsyp, f);
+            f = f2_fma(pym, nsym, f);
+            const f2 sf = f2_mul(si, f);
             if constexpr (MEASURE) {
-                const float x = __fmul_rn(-sf, 65536.0f);
-                const float t = truncf(x);
-                ehi += __float2int_rz(t);
-                elo += __float2int_rn(__fmul_rn(__fsub_rn(x, t), 65536.0f));
-                nbf = __fmaf_rn(si, (nb.sxp + nb.sxm) - (nb.syp + nb.sym), nbf);
+                const f2 x2 = f2_mul(sf, f2_splat(-65536.0f));
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const float x = f2_get(x2, e);
+                    const float t = truncf(x);
+                    ehi += __float2int_rz(t);
+                    elo += __float2int_rn(__fmul_rn(__fsub_rn(x, t), 65536.0f));
+                }
+                const f2 nb = f2_mul(si, f2_add(sx, nsy));
+                nbf = __fadd_rn(__fadd_rn(nbf, f2_get(nb, 0)), f2_get(nb, 1));
             } else {
                 // Metropolis test u < exp(-beta dE) as 2^(kb s f); with vacancies the threshold
                 // is scaled by s^2, so a vacancy (s = 0) never flips
-                float thr = ex2_approx(__fmul_rn(kb, sf));
-                if constexpr (VAC) thr = __fmul_rn(thr, __fmul_rn(si, si));
-                if (u01_f32(u4_word(rnd, k)) < thr) flipmask |= 2u << (8 * k);
+                const f2 arg = f2_mul(f2_splat(kb), sf);
+                f2 thr = f2_pack(ex2_approx(f2_get(arg, 0)), ex2_approx(f2_get(arg, 1)));
+                if constexpr (VAC) thr = f2_mul(thr, f2_mul(si, si));
+                const f2 u = f2_sub(
+                    f2_pack(__uint_as_float(0x3F800000u | (u4_word(rnd, k) & 0x007FFFFFu)),
+                            __uint_as_float(0x3F800000u | (u4_word(rnd, k + 1) & 0x007FFFFFu))),
+                    f2_splat(1.0f));
+                if (f2_get(u, 0) < f2_get(thr, 0)) flipmask |= 2u << (8 * k);
+                if (f2_get(u, 1) < f2_get(thr, 1)) flipmask |= 2u << (8 * k + 8);
             }
         }
         if constexpr (MEASURE) {
