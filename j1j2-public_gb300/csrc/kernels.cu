@@ -240,97 +240,165 @@ __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, uint
     uint32_t flipmask = 0;
     const uint32_t dsum = n.dpp + n.dpm + n.dmp + n.dmm;  // bytewise, <= 8 each
     const uint32_t zsum = n.zp + n.zm;                    // bytewise, <= 4 each
+    if constexpr (sizeof(Real) == 4 && !MEASURE) {
+        // Sweep in pairs of sites with packed FP32x2 arithmetic, element by element the
+        // operations and rounding of field_fp32 / field_fp32_masked (-y terms as products with
+        // the negated spins, exactly).
+        const f2 c1 = f2_splat(8388609.0f), c2 = f2_splat(8388610.0f), c4 = f2_splat(8388612.0f);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int sh = 8 * k;
-        const int b = (n.own >> sh) & 0xFF;
-        const Real pxp = px ? (k < 3 ? pxa[k + 1] : pextra) : pxa[k];
-        const Real pxm = px ? pxa[k] : (k > 0 ? pxa[k - 1] : pextra);
-        const int jh_own = (mown >> sh) & 1, jv_own = (mown >> (sh + 1)) & 1;
-        const int jh_m4 = (mxm >> sh) & 1, jv_m2 = (mym >> (sh + 1)) & 1;
-        if constexpr (sizeof(Real) == 4) {
-            Nbr32 nb;
-            nb.sxp = byte_f(n.xp, k) - 1.0f;
-            nb.sxm = byte_f(n.xm, k) - 1.0f;
-            nb.syp = byte_f(n.yp, k) - 1.0f;
-            nb.sym = byte_f(n.ym, k) - 1.0f;
-            nb.D = byte_f(dsum, k) - 4.0f;
-            nb.Zs = byte_f(zsum, k) - 2.0f;
-            nb.pxp = pxp;
-            nb.pxm = pxm;
-            nb.pyp = pyp[k];
-            nb.pym = pym[k];
-            float f;
-            if constexpr (MASKS)
-                f = field_fp32_masked(nb, pown[k], a.J1hf, a.J1vf, a.J2f, a.J3f, (float)jh_own,
-                                      (float)jh_m4, (float)jv_own, (float)jv_m2);
-            else
-                f = field_fp32(nb, pown[k], a.J1hf, a.J1vf, a.J2f, a.J3f);
-            const float sf = __fmul_rn((float)(b - 1), f);
-            if constexpr (MEASURE) {
-                const int s = b - 1;
-                acc.e += efix32(-sf);
-                acc.M += s;
-                acc.SX += px ? -s : s;
-                acc.SY += py ? -s : s;
-                acc.NB += s * ((int)((n.xp >> sh) & 0xFF) + (int)((n.xm >> sh) & 0xFF) -
-                               (int)((n.yp >> sh) & 0xFF) - (int)((n.ym >> sh) & 0xFF));
+        for (int h = 0; h < 2; ++h) {
+            const int k = 2 * h;
+            const f2 sxp = f2_sub(byte_pair(n.xp, k), c1);
+            const f2 sxm = f2_sub(byte_pair(n.xm, k), c1);
+            const f2 nsyp = f2_sub(c1, byte_pair(n.yp, k));
+            const f2 nsym = f2_sub(c1, byte_pair(n.ym, k));
+            const f2 D = f2_sub(byte_pair(dsum, k), c4);
+            const f2 Zs = f2_sub(byte_pair(zsum, k), c2);
+            const f2 si = f2_sub(byte_pair(n.own, k), c1);
+            const f2 pi = f2_pack(pown[k], pown[k + 1]);
+            const f2 pxp = px ? f2_pack(pxa[k + 1], k + 1 < 3 ? pxa[k + 2] : pextra)
+                              : f2_pack(pxa[k], pxa[k + 1]);
+            const f2 pxm = px ? f2_pack(pxa[k], pxa[k + 1])
+                              : f2_pack(k > 0 ? pxa[k - 1] : pextra, pxa[k]);
+            const f2 pyp2 = f2_pack(pyp[k], pyp[k + 1]);
+            const f2 pym2 = f2_pack(pym[k], pym[k + 1]);
+            const f2 sx = f2_add(sxp, sxm), nsy = f2_add(nsyp, nsym);
+            f2 f = f2_mul(f2_splat(a.J3f), Zs);
+            f = f2_fma(f2_splat(a.J2f), D, f);
+            if constexpr (MASKS) {
+                const int sh0 = 8 * k, sh1 = 8 * k + 8;
+                const f2 jho = f2_pack((float)((mown >> sh0) & 1), (float)((mown >> sh1) & 1));
+                const f2 jhm = f2_pack((float)((mxm >> sh0) & 1), (float)((mxm >> sh1) & 1));
+                const f2 jvo = f2_pack((float)((mown >> (sh0 + 1)) & 1),
+                                       (float)((mown >> (sh1 + 1)) & 1));
+                const f2 jvm = f2_pack((float)((mym >> (sh0 + 1)) & 1),
+                                       (float)((mym >> (sh1 + 1)) & 1));
+                const f2 hx = f2_fma(jho, sxp, f2_mul(jhm, sxm));
+                const f2 nhy = f2_fma(jvo, nsyp, f2_mul(jvm, nsym));  // -hy
+                f = f2_fma(f2_splat(a.J1hf), hx, f);
+                f = f2_fma(f2_splat(-a.J1vf), nhy, f);
+                f = f2_fma(pi, f2_add(sx, nsy), f);
             } else {
-                // vacancies (s = 0) never flip: the threshold is scaled by s^2
-                const float s2 = byte_f(n.own, k) - 1.0f;
-                const bool flip = u01_f32(u4_word(rnd, k)) <
-                                  __fmul_rn(ex2_approx(__fmul_rn(kb, sf)), __fmul_rn(s2, s2));
-                flipmask |= flip ? (2u << sh) : 0u;
+                f = f2_fma(f2_add(f2_splat(a.J1hf), pi), sx, f);
+                f = f2_fma(f2_sub(pi, f2_splat(a.J1vf)), nsy, f);
             }
-        } else {
-            if (b == 1) continue;
-            Nbr64 nb;
-            nb.s[0] = (int)((n.yp >> sh) & 0xFF) - 1;
-            nb.s[1] = (int)((n.ym >> sh) & 0xFF) - 1;
-            nb.s[2] = (int)((n.xp >> sh) & 0xFF) - 1;
-            nb.s[3] = (int)((n.xm >> sh) & 0xFF) - 1;
-            nb.s[4] = (int)((n.dpp >> sh) & 0xFF) - 1;
-            nb.s[5] = (int)((n.dpm >> sh) & 0xFF) - 1;
-            nb.s[6] = (int)((n.dmp >> sh) & 0xFF) - 1;
-            nb.s[7] = (int)((n.dmm >> sh) & 0xFF) - 1;
-            nb.s[8] = (int)((n.zp >> sh) & 0xFF) - 1;
-            nb.s[9] = (int)((n.zm >> sh) & 0xFF) - 1;
-            nb.p1 = pyp[k];
-            nb.p2 = pym[k];
-            nb.p3 = pxp;
-            nb.p4 = pxm;
-            nb.jv_own = jv_own;
-            nb.jv_m2 = jv_m2;
-            nb.jh_own = jh_own;
-            nb.jh_m4 = jh_m4;
-            const double f = field_fp64(nb, pown[k], a.J1h, a.J1v, a.J2, a.J3, nullptr);
-            const int s = b - 1;
-            if constexpr (MEASURE) {
-                acc.e += efix(-((double)s * f));
-                acc.M += s;
-                acc.SX += px ? -s : s;
-                acc.SY += py ? -s : s;
-                acc.NB += s * (nb.s[2] + nb.s[3] - nb.s[0] - nb.s[1]);
-            } else {
-                bool flip;
-                if (s == 1 ? f <= 0.0 : f >= 0.0) {
-                    flip = true;
-                } else {
-                    const double u = u01_f64(u4_word(rnd, k));
-                    const double t2 = __dmul_rn(__dmul_rn(2.0, f), beta);
-                    flip = u < own_exp(s == 1 ? -t2 : t2);
-                }
-                flipmask |= flip ? (2u << sh) : 0u;
-            }
+            f = f2_fma(pxp, sxp, f);
+            f = f2_fma(pxm, sxm, f);
+            f = f2_fma(pyp2, nsyp, f);
+            f = f2_fma(pym2, nsym, f);
+            const f2 sf = f2_mul(si, f);
+            const f2 arg = f2_mul(f2_splat(kb), sf);
+            // vacancies (s = 0) never flip: the threshold is scaled by s^2
+            const f2 thr = f2_mul(f2_pack(ex2_approx(f2_get(arg, 0)), ex2_approx(f2_get(arg, 1))),
+                                  f2_mul(si, si));
+            const f2 u = f2_sub(
+                f2_pack(__uint_as_float(0x3F800000u | (u4_word(rnd, k) & 0x007FFFFFu)),
+                        __uint_as_float(0x3F800000u | (u4_word(rnd, k + 1) & 0x007FFFFFu))),
+                f2_splat(1.0f));
+            if (f2_get(u, 0) < f2_get(thr, 0)) flipmask |= 2u << (8 * k);
+            if (f2_get(u, 1) < f2_get(thr, 1)) flipmask |= 2u << (8 * k + 8);
         }
-    }
-    if constexpr (!MEASURE) {
         if (flipmask) {
             S32[wown] = n.own ^ flipmask;
             if (fl) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
                     if ((flipmask >> (8 * k + 1)) & 1u) fl[bo + k] += 1;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int sh = 8 * k;
+            const int b = (n.own >> sh) & 0xFF;
+            const Real pxp = px ? (k < 3 ? pxa[k + 1] : pextra) : pxa[k];
+            const Real pxm = px ? pxa[k] : (k > 0 ? pxa[k - 1] : pextra);
+            const int jh_own = (mown >> sh) & 1, jv_own = (mown >> (sh + 1)) & 1;
+            const int jh_m4 = (mxm >> sh) & 1, jv_m2 = (mym >> (sh + 1)) & 1;
+            if constexpr (sizeof(Real) == 4) {
+                Nbr32 nb;
+                nb.sxp = byte_f(n.xp, k) - 1.0f;
+                nb.sxm = byte_f(n.xm, k) - 1.0f;
+                nb.syp = byte_f(n.yp, k) - 1.0f;
+                nb.sym = byte_f(n.ym, k) - 1.0f;
+                nb.D = byte_f(dsum, k) - 4.0f;
+                nb.Zs = byte_f(zsum, k) - 2.0f;
+                nb.pxp = pxp;
+                nb.pxm = pxm;
+                nb.pyp = pyp[k];
+                nb.pym = pym[k];
+                float f;
+                if constexpr (MASKS)
+                    f = field_fp32_masked(nb, pown[k], a.J1hf, a.J1vf, a.J2f, a.J3f, (float)jh_own,
+                                          (float)jh_m4, (float)jv_own, (float)jv_m2);
+                else
+                    f = field_fp32(nb, pown[k], a.J1hf, a.J1vf, a.J2f, a.J3f);
+                const float sf = __fmul_rn((float)(b - 1), f);
+                if constexpr (MEASURE) {
+                    const int s = b - 1;
+                    acc.e += efix32(-sf);
+                    acc.M += s;
+                    acc.SX += px ? -s : s;
+                    acc.SY += py ? -s : s;
+                    acc.NB += s * ((int)((n.xp >> sh) & 0xFF) + (int)((n.xm >> sh) & 0xFF) -
+                                   (int)((n.yp >> sh) & 0xFF) - (int)((n.ym >> sh) & 0xFF));
+                } else {
+                    // vacancies (s = 0) never flip: the threshold is scaled by s^2
+                    const float s2 = byte_f(n.own, k) - 1.0f;
+                    const bool flip = u01_f32(u4_word(rnd, k)) <
+                                      __fmul_rn(ex2_approx(__fmul_rn(kb, sf)), __fmul_rn(s2, s2));
+                    flipmask |= flip ? (2u << sh) : 0u;
+                }
+            } else {
+                if (b == 1) continue;
+                Nbr64 nb;
+                nb.s[0] = (int)((n.yp >> sh) & 0xFF) - 1;
+                nb.s[1] = (int)((n.ym >> sh) & 0xFF) - 1;
+                nb.s[2] = (int)((n.xp >> sh) & 0xFF) - 1;
+                nb.s[3] = (int)((n.xm >> sh) & 0xFF) - 1;
+                nb.s[4] = (int)((n.dpp >> sh) & 0xFF) - 1;
+                nb.s[5] = (int)((n.dpm >> sh) & 0xFF) - 1;
+                nb.s[6] = (int)((n.dmp >> sh) & 0xFF) - 1;
+                nb.s[7] = (int)((n.dmm >> sh) & 0xFF) - 1;
+                nb.s[8] = (int)((n.zp >> sh) & 0xFF) - 1;
+                nb.s[9] = (int)((n.zm >> sh) & 0xFF) - 1;
+                nb.p1 = pyp[k];
+                nb.p2 = pym[k];
+                nb.p3 = pxp;
+                nb.p4 = pxm;
+                nb.jv_own = jv_own;
+                nb.jv_m2 = jv_m2;
+                nb.jh_own = jh_own;
+                nb.jh_m4 = jh_m4;
+                const double f = field_fp64(nb, pown[k], a.J1h, a.J1v, a.J2, a.J3, nullptr);
+                const int s = b - 1;
+                if constexpr (MEASURE) {
+                    acc.e += efix(-((double)s * f));
+                    acc.M += s;
+                    acc.SX += px ? -s : s;
+                    acc.SY += py ? -s : s;
+                    acc.NB += s * (nb.s[2] + nb.s[3] - nb.s[0] - nb.s[1]);
+                } else {
+                    bool flip;
+                    if (s == 1 ? f <= 0.0 : f >= 0.0) {
+                        flip = true;
+                    } else {
+                        const double u = u01_f64(u4_word(rnd, k));
+                        const double t2 = __dmul_rn(__dmul_rn(2.0, f), beta);
+                        flip = u < own_exp(s == 1 ? -t2 : t2);
+                    }
+                    flipmask |= flip ? (2u << sh) : 0u;
+                }
+            }
+        }
+        if constexpr (!MEASURE) {
+            if (flipmask) {
+                S32[wown] = n.own ^ flipmask;
+                if (fl) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if ((flipmask >> (8 * k + 1)) & 1u) fl[bo + k] += 1;
+                }
             }
         }
     }

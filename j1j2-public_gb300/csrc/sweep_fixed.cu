@@ -21,54 +21,6 @@ struct Shape {
     static constexpr int NB = (N + 15) & ~15;
 };
 
-// Packed FP32 pairs (Blackwell add/sub/mul/fma .f32x2: two IEEE round-to-nearest operations per
-// instruction, element by element)
-using f2 = unsigned long long;
-
-__device__ __forceinline__ f2 f2_pack(float lo, float hi)
-{
-    f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ f2 f2_splat(float v) { return f2_pack(v, v); }
-__device__ __forceinline__ float f2_get(f2 v, int e)
-{
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-    return e ? hi : lo;
-}
-__device__ __forceinline__ f2 f2_add(f2 a, f2 b)
-{
-    f2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 f2_sub(f2 a, f2 b)
-{
-    f2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
-{
-    f2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c)
-{
-    f2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-// bytes k and k+1 of w as 2^23 + byte (exact floats; subtract 2^23 + offset afterwards)
-__device__ __forceinline__ f2 byte_pair(uint32_t w, int k)
-{
-    return f2_pack(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)k)),
-                   __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7541u + (uint32_t)k)));
-}
-
 // Word offsets (within a colour block) of a quad and of the words its neighbours live in:
 // same row; row Y+1 / Y-1; plane Z+1 / Z-1; and the words one step along x in those rows.
 struct QuadOff {
