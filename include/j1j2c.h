@@ -214,6 +214,12 @@ int j1j2c_get_spins(void *ctx, int32_t conf, int32_t rep, int8_t *out);
  * conf < 0: every conf, nconf x NREPLICA x 5. */
 int j1j2c_get_observables(void *ctx, int32_t conf, double *out);
 
+/* Current diagnostics settings of the context. */
+int j1j2c_get_diagnostics(void *ctx, j1j2c_diagnostics *out);
+
+/* Occupied sites of one conf (N - nimp of its disorder; N before j1j2c_set_disorder). */
+int j1j2c_get_occupied(void *ctx, int32_t conf, int32_t *nocc);
+
 /* Per-site sums of the local nematic average of one conf (N doubles each, site order, either
  * may be NULL) and the number of cycles they hold: locspin_accum, locnem_accum and
  * locnem_samples of Accumulate_local_nematic_average (J:1009-1025). */
@@ -233,6 +239,25 @@ int j1j2c_get_trace(void *ctx, int32_t conf, double *obs, int32_t *temp_of_rep, 
  * vacancies read -1 as Mark_vacancy_flipcounts sets them), counted since j1j2c_init_spins
  * (confnumflips, J:109, J:2575). */
 int j1j2c_get_flip_counts(void *ctx, int32_t conf, int32_t *counts);
+
+/* ---------------------------------------------------------------------------------------------
+ * Checkpoint / resume (no reference counterpart: the reference restarts runs from scratch)
+ * ------------------------------------------------------------------------------------------- */
+
+/* Bytes of the state blob of this context. */
+int j1j2c_state_size(void *ctx, int64_t *bytes);
+
+/* Copy the whole device state into buf (at least j1j2c_state_size bytes): spins, disorder,
+ * ladders, slot maps, swap counters, running sums, visit flags, last observables, cluster
+ * sizes, the PT cycle counter and swap phase, and the enabled diagnostics.  Continuing a run
+ * from the blob (j1j2c_load_state into a context created with the same parameters) reproduces
+ * the uninterrupted run bit for bit. */
+int j1j2c_save_state(void *ctx, void *buf, int64_t size);
+
+/* Restore a blob written by j1j2c_save_state.  The context must have been created with the
+ * same lattice-shape groups, couplings, precision, ptswapever, seed and conf_base
+ * (J1J2C_EINVAL otherwise); the blob's diagnostics settings replace the context's. */
+int j1j2c_load_state(void *ctx, const void *buf, int64_t size);
 
 /* Sweep-kernel timing accumulated under J1J2C_FLAG_PROFILE: milliseconds, launches, and the
  * attempts those launches made (occupied sites x sweeps). */

@@ -94,7 +94,7 @@ struct Ctx {
 
     // optional diagnostics (j1j2c_set_diagnostics)
     j1j2c_diagnostics diag{-1, 0, 0, 0};
-    long long spin_bytes = 0, mask_bytes = 0;
+    long long spin_bytes = 0, mask_bytes = 0, p_elems = 0;
     int* d_loc_s = nullptr;             // per-site sums of s (conf at mask offsets)
     int* d_loc_n = nullptr;             // per-site sums of the local nematic term
     long long* d_loc_samples = nullptr; // per conf
@@ -592,6 +592,7 @@ int j1j2c_create_multi(void** out, const j1j2c_params* groups, int32_t ngroups)
     }
     c->spin_bytes = spin_bytes;
     c->mask_bytes = mask_bytes;
+    c->p_elems = p_elems;
     c->have_dis.assign(c->nconf, 0);
     c->have_ladder.assign(c->nconf, 0);
     c->have_spins.assign(c->nconf, 0);
@@ -960,6 +961,22 @@ int j1j2c_set_diagnostics(void* ctx, const j1j2c_diagnostics* d)
             if (rc != J1J2C_OK) return rc;
             gr.tuned = false;
         }
+    return J1J2C_OK;
+}
+
+int j1j2c_get_diagnostics(void* ctx, j1j2c_diagnostics* out)
+{
+    if (!ctx || !out) return J1J2C_EINVAL;
+    *out = static_cast<Ctx*>(ctx)->diag;
+    return J1J2C_OK;
+}
+
+int j1j2c_get_occupied(void* ctx, int32_t conf, int32_t* nocc)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!valid_conf(c, conf) || !nocc) return fail(c, J1J2C_EINVAL, "bad conf or null output");
+    *nocc = c->nocc[conf];
     return J1J2C_OK;
 }
 
@@ -1403,6 +1420,211 @@ int j1j2c_get_config(void* ctx, int32_t* block_threads, int32_t* sites_per_threa
     if (block_threads) *block_threads = grp.nthreads;
     if (sites_per_thread) *sites_per_thread = grp.var.quad ? 4 : 1;
     if (smem_bytes) *smem_bytes = (int32_t)grp.smem;
+    return J1J2C_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------------------
+// Checkpoint / resume: the whole device state of a context as one host byte blob
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+struct StateHeader {
+    char magic[8];
+    uint32_t version, ngroups;
+    int32_t nconf, nentries, precision, ptswapever;
+    uint32_t seed, conf_base;
+    double J1h, J1v, J2, J3;
+    int64_t spin_bytes, p_elems, mask_bytes;
+    uint32_t cycle, phase;
+    j1j2c_diagnostics diag;
+};
+constexpr char kStateMagic[8] = {'J', '1', 'J', '2', 'C', 'S', 'T', '1'};
+
+// Walks the sections of the blob in a fixed order; mode 0 counts, 1 saves (device -> blob),
+// 2 loads (blob -> device).
+struct StateIO {
+    int mode;
+    uint8_t* buf;
+    size_t off = 0;
+    cudaError_t err = cudaSuccess;
+    void dev(void* d, size_t bytes)
+    {
+        if (mode == 1 && err == cudaSuccess && bytes)
+            err = cudaMemcpy(buf + off, d, bytes, cudaMemcpyDeviceToHost);
+        if (mode == 2 && err == cudaSuccess && bytes)
+            err = cudaMemcpy(d, buf + off, bytes, cudaMemcpyHostToDevice);
+        off += bytes;
+    }
+    void host(void* h, size_t bytes)
+    {
+        if (mode == 1 && bytes) std::memcpy(buf + off, h, bytes);
+        if (mode == 2 && bytes) std::memcpy(h, buf + off, bytes);
+        off += bytes;
+    }
+};
+
+void state_sections(Ctx* c, StateIO& io)
+{
+    const size_t ne = (size_t)c->nentries, nc = (size_t)c->nconf;
+    io.dev(c->d_spins, (size_t)c->spin_bytes);
+    io.dev(c->d_pf, (size_t)c->p_elems * sizeof(float));
+    io.dev(c->d_pd, (size_t)c->p_elems * sizeof(double));
+    io.dev(c->d_bm, (size_t)c->mask_bytes);
+    io.dev(c->d_occ, (size_t)c->mask_bytes);
+    io.dev(c->d_nocc, nc * sizeof(int));
+    io.dev(c->d_beta, ne * sizeof(double));
+    io.dev(c->d_rat, ne * sizeof(int));
+    io.dev(c->d_tor, ne * sizeof(int));
+    io.dev(c->d_obs, ne * sizeof(LatObs));
+    io.dev(c->d_sums, ne * 22 * sizeof(double));
+    io.dev(c->d_nmeas, ne * sizeof(long long));
+    io.dev(c->d_att, ne * sizeof(long long));
+    io.dev(c->d_acc, ne * sizeof(long long));
+    io.dev(c->d_vis, ne);
+    io.dev(c->d_last, ne * 5 * sizeof(double));
+    io.dev(c->d_csize, ne * sizeof(long long));
+    io.host(c->have_dis.data(), nc);
+    io.host(c->have_ladder.data(), nc);
+    io.host(c->have_spins.data(), nc);
+    io.host(c->nocc.data(), nc * sizeof(int));
+    io.host(c->conf_masks.data(), nc * sizeof(int));
+    io.host(c->conf_vac.data(), nc * sizeof(int));
+    if (c->d_loc_s) {
+        io.dev(c->d_loc_s, (size_t)c->mask_bytes * sizeof(int));
+        io.dev(c->d_loc_n, (size_t)c->mask_bytes * sizeof(int));
+        io.dev(c->d_loc_samples, nc * sizeof(long long));
+    }
+    if (c->d_hist) {
+        io.dev(c->d_hist, ne * (size_t)c->diag.hist_bins * sizeof(long long));
+        io.dev(c->d_hist_lo, ne * sizeof(double));
+        io.dev(c->d_hist_bs, ne * sizeof(double));
+    }
+    if (c->d_trace) {
+        io.dev(c->d_trace, (size_t)c->diag.trace_cycles * ne * 5 * sizeof(double));
+        io.dev(c->d_trace_tor, (size_t)c->diag.trace_cycles * ne * sizeof(int));
+    }
+    if (c->d_flips) io.dev(c->d_flips, (size_t)c->spin_bytes * sizeof(int));
+}
+
+StateHeader make_header(Ctx* c)
+{
+    StateHeader h{};
+    std::memcpy(h.magic, kStateMagic, 8);
+    h.version = 1;
+    h.ngroups = (uint32_t)c->G.size();
+    h.nconf = c->nconf;
+    h.nentries = c->nentries;
+    h.precision = c->P.precision;
+    h.ptswapever = c->P.ptswapever;
+    h.seed = c->P.seed;
+    h.conf_base = c->P.conf_base;
+    h.J1h = c->P.J1h;
+    h.J1v = c->P.J1v;
+    h.J2 = c->P.J2;
+    h.J3 = c->P.J3;
+    h.spin_bytes = c->spin_bytes;
+    h.p_elems = c->p_elems;
+    h.mask_bytes = c->mask_bytes;
+    h.cycle = c->host_ctl[0];
+    h.phase = c->host_ctl[1];
+    h.diag = c->diag;
+    return h;
+}
+
+size_t state_bytes(Ctx* c)
+{
+    StateIO io{0, nullptr};
+    state_sections(c, io);
+    return sizeof(StateHeader) + c->G.size() * 4 * sizeof(int32_t) + io.off;
+}
+
+}  // namespace
+
+extern "C" {
+
+int j1j2c_state_size(void* ctx, int64_t* bytes)
+{
+    if (!ctx || !bytes) return J1J2C_EINVAL;
+    *bytes = (int64_t)state_bytes(static_cast<Ctx*>(ctx));
+    return J1J2C_OK;
+}
+
+int j1j2c_save_state(void* ctx, void* buf, int64_t size)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!buf || size < (int64_t)state_bytes(c))
+        return fail(c, J1J2C_EINVAL, "state buffer missing or smaller than j1j2c_state_size");
+    CK(c, cudaStreamSynchronize(c->st));
+    CK(c, cudaMemcpy(c->host_ctl, c->d_ctl, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    uint8_t* b = static_cast<uint8_t*>(buf);
+    StateHeader h = make_header(c);
+    std::memcpy(b, &h, sizeof h);
+    size_t off = sizeof h;
+    for (const Group& grp : c->G) {
+        const int32_t shape[4] = {grp.g.L, grp.g.H, grp.nconf, grp.nrep};
+        std::memcpy(b + off, shape, sizeof shape);
+        off += sizeof shape;
+    }
+    StateIO io{1, b + off};
+    state_sections(c, io);
+    if (io.err != cudaSuccess) return cuda_fail(c, io.err, "saving the state");
+    return J1J2C_OK;
+}
+
+int j1j2c_load_state(void* ctx, const void* buf, int64_t size)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!buf || size < (int64_t)sizeof(StateHeader)) return fail(c, J1J2C_EINVAL, "state blob too small");
+    const uint8_t* b = static_cast<const uint8_t*>(buf);
+    StateHeader h;
+    std::memcpy(&h, b, sizeof h);
+    const StateHeader mine = make_header(c);
+    if (std::memcmp(h.magic, kStateMagic, 8) != 0 || h.version != 1)
+        return fail(c, J1J2C_EINVAL, "not a libj1j2cuda state blob");
+    if (h.ngroups != mine.ngroups || h.nconf != mine.nconf || h.nentries != mine.nentries ||
+        h.precision != mine.precision || h.ptswapever != mine.ptswapever || h.seed != mine.seed ||
+        h.conf_base != mine.conf_base || h.J1h != mine.J1h || h.J1v != mine.J1v ||
+        h.J2 != mine.J2 || h.J3 != mine.J3 || h.spin_bytes != mine.spin_bytes)
+        return fail(c, J1J2C_EINVAL, "state blob from a context with other parameters");
+    size_t off = sizeof h;
+    for (const Group& grp : c->G) {
+        int32_t shape[4];
+        std::memcpy(shape, b + off, sizeof shape);
+        off += sizeof shape;
+        if (shape[0] != grp.g.L || shape[1] != grp.g.H || shape[2] != grp.nconf ||
+            shape[3] != grp.nrep)
+            return fail(c, J1J2C_EINVAL, "state blob from a context with other lattice shapes");
+    }
+    // the blob's diagnostics decide which optional buffers exist
+    int rc = j1j2c_set_diagnostics(ctx, &h.diag);
+    if (rc != J1J2C_OK) return rc;
+    if (size < (int64_t)state_bytes(c)) return fail(c, J1J2C_EINVAL, "state blob truncated");
+    CK(c, cudaStreamSynchronize(c->st));
+    StateIO io{2, const_cast<uint8_t*>(b) + off};
+    state_sections(c, io);
+    if (io.err != cudaSuccess) return cuda_fail(c, io.err, "loading the state");
+    c->host_ctl[0] = h.cycle;
+    c->host_ctl[1] = h.phase;
+    c->host_ctl[2] = 0;
+    CK(c, cudaMemcpy(c->d_ctl, c->host_ctl, 4 * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    bool masks = false, vac = false;
+    for (int k : c->conf_masks) masks = masks || k;
+    for (int k : c->conf_vac) vac = vac || k;
+    free_graphs(c);
+    c->masks = masks;
+    c->vac = vac;
+    for (auto& gr : c->G) {
+        rc = choose_variant(c, gr, c->P.precision == J1J2C_FP64_PLAIN, gr.var, gr.smem,
+                            gr.nthreads);
+        if (rc != J1J2C_OK) return rc;
+        gr.tuned = false;
+    }
+    c->occ_total = 0;
+    for (int k = 0; k < c->nconf; ++k) c->occ_total += (long long)c->nocc[k] * c->conf_nrep[k];
     return J1J2C_OK;
 }
 

@@ -36,7 +36,8 @@ EXPORTS = ("j1j2c_create", "j1j2c_create_multi", "j1j2c_conf_shape", "j1j2c_dest
            "j1j2c_corr_rand_3d", "j1j2c_setup_vacancies", "j1j2c_kiss_spins", "j1j2c_ladder",
            "j1j2c_version", "j1j2c_wolff", "j1j2c_get_cluster_sizes", "j1j2c_enumerate_exact",
            "j1j2c_set_diagnostics", "j1j2c_get_locnem", "j1j2c_get_histogram", "j1j2c_get_trace",
-           "j1j2c_get_flip_counts")
+           "j1j2c_get_flip_counts", "j1j2c_state_size", "j1j2c_save_state", "j1j2c_load_state",
+           "j1j2c_get_diagnostics", "j1j2c_get_occupied")
 
 ENUM_FIELDS = ("lnZ", "e", "e2", "absm", "m2", "m4", "abssx", "sx2", "abssy", "sy2", "nbar",
                "nbar2")
@@ -321,6 +322,28 @@ class Engine:
         out = np.empty((self.nrep_of(conf), self.n_of(conf)), np.int32)
         self._ck(lib().j1j2c_get_flip_counts(self._ctx, C.c_int32(conf), _p(out, C.c_int32)))
         return out
+
+    # checkpoint / resume -----------------------------------------------------------------------
+    def save_state(self) -> np.ndarray:
+        """The whole device state as a byte array (write it to a file to checkpoint)."""
+        n = C.c_int64()
+        self._ck(lib().j1j2c_state_size(self._ctx, C.byref(n)))
+        buf = np.empty(n.value, np.uint8)
+        self._ck(lib().j1j2c_save_state(self._ctx, _p(buf, C.c_uint8), C.c_int64(buf.size)))
+        return buf
+
+    def load_state(self, buf):
+        """Resume from save_state()'s bytes (a context created with the same parameters)."""
+        b = np.ascontiguousarray(np.frombuffer(buf, np.uint8) if isinstance(buf, (bytes, bytearray))
+                                 else buf, np.uint8)
+        self._ck(lib().j1j2c_load_state(self._ctx, _p(b, C.c_uint8), C.c_int64(b.size)))
+        d = Diagnostics()
+        self._ck(lib().j1j2c_get_diagnostics(self._ctx, C.byref(d)))
+        self.diag = d
+        n = C.c_int32()
+        for k in range(self.nconf):
+            self._ck(lib().j1j2c_get_occupied(self._ctx, C.c_int32(k), C.byref(n)))
+            self.nocc[k] = n.value
 
     def cluster_sizes(self, conf=-1):
         out = np.zeros(self.nentries if conf < 0 else self.nrep_of(conf), np.int64)
