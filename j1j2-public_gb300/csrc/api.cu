@@ -70,7 +70,7 @@ struct Ctx {
     int* d_rbase = nullptr;
     int* d_nreps = nullptr;
     unsigned long long* d_audit = nullptr;
-    int* d_labels = nullptr;        // Wolff union-find scratch, one int per site
+    int* d_labels = nullptr;        // Wolff union-find labels / cluster list, one int per site
     long long* d_csize = nullptr;   // Wolff cluster size of the last update, per replica
     int* d_err = nullptr;           // device error word (union-find retry overflow)
     long long lab_ints = 0;
@@ -329,9 +329,12 @@ cudaError_t enqueue_wolff(Ctx* c, const Group& grp, cudaStream_t st)
     SweepArgs a = group_args(c, grp);
     cudaError_t e = cudaMemsetAsync(c->d_csize + grp.rep0, 0, sizeof(long long) * grp.nlat(), st);
     if (e != cudaSuccess) return e;
+    // default: seed-cluster growth; the labelling forms stay selectable for cross-checks
+    const WolffForm form = (c->P.flags & J1J2C_FLAG_GENERIC)    ? kWolffSite
+                           : (c->P.flags & J1J2C_FLAG_NO_FIXED) ? kWolffSlab
+                                                                : kWolffGrow;
     return launch_wolff(a, grp.var.fp64, c->masks, grp.nlat(), c->d_labels + grp.lab_off,
-                        grp.lat_stride, c->d_csize + grp.rep0, c->d_err, st,
-                        (c->P.flags & J1J2C_FLAG_GENERIC) != 0);
+                        grp.lat_stride, c->d_csize + grp.rep0, c->d_err, st, form);
 }
 
 cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int nthreads,

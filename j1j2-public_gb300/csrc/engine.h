@@ -147,9 +147,12 @@ cudaError_t prepare_sweep_variant(const SweepVariant& v, size_t smem);
 cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks, int nthreads,
                          size_t smem, cudaStream_t st);
 cudaError_t launch_swap(const SwapArgs& a, cudaStream_t st);
+// Wolff forms: seed-cluster growth (default), slab union-find labelling in shared memory,
+// per-site union-find labelling in global memory; all three flip the same cluster.
+enum WolffForm { kWolffGrow = 0, kWolffSlab = 1, kWolffSite = 2 };
 cudaError_t launch_wolff(const SweepArgs& a, bool fp64, bool masks, int nlat, int* labels,
                          long long lab_stride, long long* csize, int* err, cudaStream_t st,
-                         bool per_site);
+                         WolffForm form);
 int wolff_slab_planes(const Geo& g);  // planes per shared-memory slab of the Wolff labelling
 cudaError_t launch_init(const InitArgs& a, cudaStream_t st);
 

@@ -550,6 +550,186 @@ __global__ void wolff_flip_kernel(SweepArgs a, int* labels, long long lab_stride
     if ((threadIdx.x & 31) == 0 && count) atomicAdd((unsigned long long*)(csize + lat), count);
 }
 
+// ---- seed-cluster growth ----------------------------------------------------------------------
+// One CTA per lattice grows the seed's cluster breadth-first.  A bond is tested when the growth
+// first reaches it, with the same owner-site Philox word, coupling and arithmetic as the
+// labelling forms, so the flipped cluster is the same component; only the bonds of the cluster
+// and of its boundary are evaluated.  A site joins by setting bit 2 of its spin byte with an
+// atomic OR on the word holding it: the old word tells whether it had already joined and gives
+// its original spin, so one round trip both claims and reads it.  The winner flips the spin
+// (atomic XOR of bit 1) and appends (compact coordinates c:3 Z:9 Y:9 X:9 bits, original byte:
+// 2 bits) to the cluster list; level k of the
+// breadth-first search is the list segment appended during level k - 1, kept in a shared-memory
+// ring while it fits.  A test that reads a neighbour already claimed by a concurrent winner sees
+// bit 2 (or loses the claim), so nothing changes.  The join bits are cleared at the end.
+constexpr int kGrowThreads = 256;
+constexpr int kGrowRing = 8192;  // queue entries kept in shared memory (32 KiB)
+
+template <class Real, bool MASKS>
+__global__ void __launch_bounds__(kGrowThreads, 3)
+    wolff_grow_kernel(SweepArgs a, int* list, long long list_stride, long long* csize)
+{
+    const Geo g = a.g;
+    const int lat = (int)blockIdx.x;
+    const int conf = lat / a.nrep, rep = lat - conf * a.nrep;
+    const int tid = (int)threadIdx.x, NT = (int)blockDim.x;
+    uint8_t* S = a.spins + (long long)lat * a.lat_stride;
+    uint32_t* S32 = reinterpret_cast<uint32_t*>(S);
+    const Real* P = wfield<Real>(a, conf);
+    const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
+    int* Q = list + (long long)lat * list_stride;
+    __shared__ int ring[kGrowRing];
+    __shared__ int s_head, s_end, s_tail, s_rlim, s_wlim;
+
+    const uint32_t cycle = a.ctl[0];
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    if (tid == 0) {
+        const uint32_t w =
+            philox4x32_10((uint32_t)rep, cycle, 0xFFFFFFFFu, kTagWolffSeed, k0, k1).x;
+        const int seed_site = (int)(((unsigned long long)w * (unsigned long long)g.N) >> 32);
+        const int cs = compact_of_site(g, seed_site);
+        s_head = s_end = s_tail = 0;
+        s_rlim = s_wlim = kGrowRing;
+        const int b = S[cs];
+        if (b != 1) {  // a vacant seed flips nothing
+            S[cs] = (uint8_t)((2 - b) | 4);
+            const int x = seed_site % g.L, y = (seed_site / g.L) % g.L, z = seed_site / (g.L * g.L);
+            const int cc = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+            Q[0] = ring[0] = (int)(((uint32_t)cc << 29) | ((uint32_t)(z >> 1) << 20) |
+                                   ((uint32_t)(y >> 1) << 11) | ((uint32_t)(x >> 1) << 2) |
+                                   (uint32_t)b);
+            s_end = s_tail = 1;
+        }
+    }
+    __syncthreads();
+
+    const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+    Real J2, J3;
+    if constexpr (sizeof(Real) == 8) {
+        J2 = a.J2;
+        J3 = a.J3;
+    } else {
+        J2 = a.J2f;
+        J3 = a.J3f;
+    }
+    const unsigned long long thr2 = uniform_threshold<Real>(J2 < Real(0) ? -J2 : J2, beta);
+    const unsigned long long thr3 = uniform_threshold<Real>(J3 < Real(0) ? -J3 : J3, beta);
+    const int s2 = J2 > Real(0) ? 1 : J2 < Real(0) ? -1 : 0;  // s_i s_j of a satisfied bond
+    const int s3 = J3 > Real(0) ? 1 : J3 < Real(0) ? -1 : 0;
+
+    for (int level = 0; level < g.N; ++level) {  // at most N levels: every site joins once
+        const int head = s_head, end = s_end, rlim = s_rlim, wlim = s_wlim;
+        if (head == end) break;
+        for (int idx = head + tid; idx < end; idx += NT) {
+            // entry: compact coordinates and original spin byte of a cluster site
+            const uint32_t e = (uint32_t)(idx < rlim ? ring[idx & (kGrowRing - 1)] : Q[idx]);
+            const int c = (int)(e >> 29), Z = (int)((e >> 20) & 511), Y = (int)((e >> 11) & 511),
+                      X = (int)((e >> 2) & 511);
+            const int si = (int)(e & 3u) - 1;  // original spin
+            const int i = cidx(g, c, Z, Y, X);
+            const int px = c & 1, py = (c >> 1) & 1, pz = c >> 2;
+            const int Xp = px ? (X + 1 == g.Lh ? 0 : X + 1) : X;   // column of x + 1
+            const int Xm = px ? X : (X == 0 ? g.Lh - 1 : X - 1);   // column of x - 1
+            const int Yp = py ? (Y + 1 == g.Lh ? 0 : Y + 1) : Y;
+            const int Ym = py ? Y : (Y == 0 ? g.Lh - 1 : Y - 1);
+            const int Zp = pz ? (Z + 1 == g.Hh ? 0 : Z + 1) : Z;
+            const int Zm = pz ? Z : (Z == 0 ? g.Hh - 1 : Z - 1);
+            // neighbour d: +x, +y, (+x,+y), (-x,+y), +z own the bond (b = d); -x, -y, (-x,-y),
+            // (+x,-y), -z are the bonds b = d - 5 owned by the neighbour
+            auto cof = [&](int d) { return c ^ (d % 5 == 0 ? 1 : d % 5 == 1 ? 2 : d % 5 == 4 ? 4 : 3); };
+            auto xof = [&](int d) {
+                return (d == 0 || d == 2 || d == 8) ? Xp : (d == 3 || d == 5 || d == 7) ? Xm : X;
+            };
+            auto yof = [&](int d) {
+                return (d == 1 || d == 2 || d == 3) ? Yp : (d == 6 || d == 7 || d == 8) ? Ym : Y;
+            };
+            auto zof = [&](int d) { return d == 4 ? Zp : d == 9 ? Zm : Z; };
+            int jn[10], bn[10];
+#pragma unroll
+            for (int d = 0; d < 10; ++d) jn[d] = cidx(g, cof(d), zof(d), yof(d), xof(d));
+            // every load first (independent, in flight together)
+#pragma unroll
+            for (int d = 0; d < 10; ++d) bn[d] = S[jn[d]];
+            const Real p_i = P[i], p0 = P[jn[0]], p1 = P[jn[1]], p5 = P[jn[5]], p6 = P[jn[6]];
+            int m_i = 3, m5 = 3, m6 = 3;
+            if (MASKS) {
+                m_i = BM[i];
+                m5 = BM[jn[5]];
+                m6 = BM[jn[6]];
+            }
+            // the ten bonds' Philox words as independent chains while the loads are in flight
+            uint32_t word[10];
+#pragma unroll
+            for (int d = 0; d < 10; ++d) {
+                const int b = d < 5 ? d : d - 5;
+                const int co = d < 5 ? c : cof(d), Zo = d < 5 ? Z : zof(d);
+                const int Yo = d < 5 ? Y : yof(d), Xo = d < 5 ? X : xof(d);
+                const uint32_t grp =
+                    (uint32_t)(((co * g.Hh + Zo) * g.Lh + Yo) * g.Qr + (Xo >> 2));
+                word[d] = u4_word(
+                    philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffBond + 16u * b, k0, k1),
+                    Xo & 3);
+            }
+            unsigned act = 0;
+#pragma unroll
+            for (int d = 0; d < 10; ++d) {
+                const int sj = (bn[d] & 3) - 1;
+                if (sj == 0 || (bn[d] & 4)) continue;  // vacancy, or joined already
+                const int b = d < 5 ? d : d - 5;
+                bool on;
+                if (b < 2) {
+                    const int mo = d < 5 ? m_i : (d == 5 ? m5 : m6);
+                    const Real po = d < 5 ? p_i : (d == 5 ? p5 : p6);
+                    const Real pt = d == 0 ? p0 : d == 1 ? p1 : p_i;
+                    Real wv;
+                    on = bond_weight<Real>(a, b, si, sj, mo & 1, (mo >> 1) & 1, po, pt, wv) &&
+                         bond_trial<Real>(wv, beta, word[d]);
+                } else {
+                    on = si * sj == (b < 4 ? s2 : s3) &&
+                         uniform_trial<Real>(b < 4 ? thr2 : thr3, word[d]);
+                }
+                if (on) act |= 1u << d;
+            }
+            // claims: every atomic issued before any result is used
+            uint32_t old[10];
+#pragma unroll
+            for (int d = 0; d < 10; ++d)
+                old[d] = ((act >> d) & 1u) ? atomicOr(&S32[jn[d] >> 2], 4u << (8 * (jn[d] & 3)))
+                                           : 4u << (8 * (jn[d] & 3));
+#pragma unroll
+            for (int d = 0; d < 10; ++d) {
+                const int sh = 8 * (jn[d] & 3);
+                if ((old[d] >> sh) & 4u) continue;  // not active, or joined meanwhile
+                atomicXor(&S32[jn[d] >> 2], 2u << sh);
+                const int pos = atomicAdd(&s_tail, 1);
+                const int entry = (int)(((uint32_t)cof(d) << 29) | ((uint32_t)zof(d) << 20) |
+                                        ((uint32_t)yof(d) << 11) | ((uint32_t)xof(d) << 2) |
+                                        ((old[d] >> sh) & 3u));
+                Q[pos] = entry;
+                if (pos < wlim) ring[pos & (kGrowRing - 1)] = entry;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            s_rlim = wlim;
+            s_head = end;
+            s_end = s_tail;
+            s_wlim = end + kGrowRing;
+        }
+        __syncthreads();
+    }
+    // clear the join bits of the cluster; atomically, at L2, where the flips were made (a plain
+    // read-modify-write could see a line cached before the flip)
+    const int n = s_tail;
+    for (int k = tid; k < n; k += NT) {
+        const uint32_t e = (uint32_t)Q[k];
+        const int i = cidx(g, (int)(e >> 29), (int)((e >> 20) & 511), (int)((e >> 11) & 511),
+                           (int)((e >> 2) & 511));
+        atomicAnd(&S32[i >> 2], ~(4u << (8 * (i & 3))));
+    }
+    if (tid == 0) csize[lat] += n;
+}
+
 template <class Real>
 cudaError_t bonds(const SweepArgs& a, int* labels, long long ls, int* err, int nlat, bool masks,
                   cudaStream_t st)
@@ -597,17 +777,31 @@ cudaError_t slab_launch(const SweepArgs& a, int pz, int nlat, int* labels, long 
 }  // namespace
 
 // One Wolff update of every lattice of a group (the SweepArgs of the group, lat0 = 0): labels is
-// scratch of nlat x lab_stride ints, csize receives the flipped-cluster size per lattice (added;
-// the caller zeroes it), err is set on a union-find retry overflow.  per_site selects the
-// site-per-thread global form (also taken when no slab fits in shared memory).
+// scratch of nlat x lab_stride ints (labels, or the cluster list of the growth form), csize
+// receives the flipped-cluster size per lattice (added; the caller zeroes it), err is set on a
+// union-find retry overflow.
 cudaError_t launch_wolff(const SweepArgs& a, bool fp64, bool masks, int nlat, int* labels,
                          long long lab_stride, long long* csize, int* err, cudaStream_t st,
-                         bool per_site)
+                         WolffForm form)
 {
     const unsigned bx = (unsigned)((a.g.N + 255) / 256);
     const unsigned bxs = bx > 64 ? 64u : bx;
-    const int pz = per_site ? 0 : wolff_slab_planes(a.g);
     cudaError_t e;
+    if (form == kWolffGrow) {
+        const dim3 grid((unsigned)nlat);
+        if (fp64)
+            masks ? wolff_grow_kernel<double, true><<<grid, kGrowThreads, 0, st>>>(
+                        a, labels, lab_stride, csize)
+                  : wolff_grow_kernel<double, false><<<grid, kGrowThreads, 0, st>>>(
+                        a, labels, lab_stride, csize);
+        else
+            masks ? wolff_grow_kernel<float, true><<<grid, kGrowThreads, 0, st>>>(
+                        a, labels, lab_stride, csize)
+                  : wolff_grow_kernel<float, false><<<grid, kGrowThreads, 0, st>>>(
+                        a, labels, lab_stride, csize);
+        return cudaGetLastError();
+    }
+    const int pz = form == kWolffSlab ? wolff_slab_planes(a.g) : 0;
     if (pz > 0) {
         e = fp64 ? (masks ? slab_launch<double, true>(a, pz, nlat, labels, lab_stride, err, st)
                           : slab_launch<double, false>(a, pz, nlat, labels, lab_stride, err, st))

@@ -33,15 +33,17 @@ def _engine(jc, L, H, nconf, nrep, precision, flags=0, pp=0.0, bonds=0.0, betas=
     return eng, dis, betas
 
 
-# Shapes cover every labelling form: one shared-memory slab per lattice (8..10, 48 x 16 planes
-# would be 3 slabs), several slabs with the +z boundary merge (48^3: 3 slabs of 16 planes;
-# 96 x 8: 2 slabs of 4), one-CTA-per-SM slabs (160 x 4: 2 slabs of 2 planes), the per-site
-# global form (200 x 4: a slab of 2 planes does not fit; flags 4 forces it at 8 x 4).
+# Forms: flags 0 / 16 the seed-cluster growth (default), 8 the shared-memory slab labelling,
+# 4 the per-site global labelling.  Slab shapes: one slab per lattice (8 x 4), several slabs with
+# the +z boundary merge (48^3: 3 slabs of 16 planes; 96 x 8: 2 slabs of 4), one-CTA-per-SM slabs
+# (160 x 4: 2 slabs of 2 planes), no slab fits (200 x 4: the per-site form is used).
 @pytest.mark.parametrize("L,H,pp,bonds,flags", [(8, 4, 0.1, 0.2, 0), (10, 6, 0.0, 0.0, 0),
                                                  (4, 2, 0.0, 0.0, 0), (8, 8, 0.05, 0.0, 16),
-                                                 (8, 4, 0.1, 0.2, 4), (48, 48, 0.05, 0.0, 0),
-                                                 (96, 8, 0.1, 0.2, 0), (160, 4, 0.0, 0.0, 0),
-                                                 (200, 4, 0.05, 0.0, 0)])
+                                                 (8, 4, 0.1, 0.2, 4), (8, 4, 0.1, 0.2, 8),
+                                                 (48, 48, 0.05, 0.0, 0), (48, 48, 0.05, 0.0, 8),
+                                                 (96, 8, 0.1, 0.2, 0), (96, 8, 0.1, 0.2, 8),
+                                                 (160, 4, 0.0, 0.0, 8), (200, 4, 0.05, 0.0, 8),
+                                                 (2, 2, 0.0, 0.0, 0)])
 def test_wolff_step_bit_identical(engine_mod, oracle, L, H, pp, bonds, flags):
     jc = engine_mod
     eng, dis, betas = _engine(jc, L, H, 2, 3, jc.FP64_PLAIN, flags, pp, bonds)
@@ -65,22 +67,24 @@ def test_wolff_step_bit_identical(engine_mod, oracle, L, H, pp, bonds, flags):
 
 @pytest.mark.parametrize("L,H,pp,bonds", [(96, 8, 0.1, 0.2), (48, 48, 0.05, 0.0),
                                           (32, 32, 0.0, 0.0), (160, 4, 0.05, 0.0)])
-def test_wolff_fp32_slab_equals_per_site(engine_mod, oracle, L, H, pp, bonds):
-    """FP32: the shared-memory slab labelling flips exactly the clusters of the per-site global
-    union-find (same activated bonds, same components), after sweeps and over several cycles."""
+def test_wolff_fp32_forms_agree(engine_mod, oracle, L, H, pp, bonds):
+    """FP32: the seed-cluster growth, the shared-memory slab labelling and the per-site global
+    union-find flip exactly the same clusters (same activated bonds, same component of the seed),
+    after sweeps and over several cycles."""
     jc = engine_mod
     out = []
-    for flags in (jc.FLAG_WOLFF, jc.FLAG_WOLFF | jc.FLAG_GENERIC):
+    for flags in (jc.FLAG_WOLFF, jc.FLAG_WOLFF | jc.FLAG_NO_FIXED, jc.FLAG_WOLFF | jc.FLAG_GENERIC):
         eng, _, _ = _engine(jc, L, H, 2, 3, jc.FP32_BATCHED, flags, pp, bonds)
         sizes = [eng.wolff().copy()]
         eng.run(3, measure=True)
         sizes.append(eng.cluster_sizes().copy())
         out.append(([eng.spins(k, r).copy() for k in range(2) for r in range(3)], sizes))
         eng.close()
-    for a, b in zip(out[0][0], out[1][0]):
-        np.testing.assert_array_equal(a, b)
-    for a, b in zip(out[0][1], out[1][1]):
-        np.testing.assert_array_equal(a, b)
+    for other in out[1:]:
+        for a, b in zip(out[0][0], other[0]):
+            np.testing.assert_array_equal(a, b)
+        for a, b in zip(out[0][1], other[1]):
+            np.testing.assert_array_equal(a, b)
     assert sum(int(x.sum()) for x in out[0][1]) > 0
 
 
