@@ -248,6 +248,7 @@ SweepArgs group_args(Ctx* c, const Group& grp)
     a.p_stride = grp.p_stride;
     a.beta = c->d_beta + grp.rep0;
     a.temp_of_rep = c->d_tor + grp.rep0;
+    a.rep_at_temp = c->d_rat + grp.rep0;
     a.ctl = c->d_ctl;
     a.obs = c->d_obs + grp.rep0;
     a.audit = c->d_audit;

@@ -29,6 +29,7 @@ struct SweepArgs {
     long long p_stride;      // elements, multiple of 4
     const double* beta;      // [nconf*nrep], by slot
     const int* temp_of_rep;  // [nconf*nrep]
+    const int* rep_at_temp;  // [nconf*nrep]
     const uint32_t* ctl;     // ctl[0] = PT cycle counter
     LatObs* obs;             // [nlat]
     unsigned long long* audit;  // [2]: attempts, mismatches (audit mode)

@@ -562,16 +562,19 @@ __global__ void wolff_flip_kernel(SweepArgs a, int* labels, long long lab_stride
 // breadth-first search is the list segment appended during level k - 1, kept in a shared-memory
 // ring while it fits.  A test that reads a neighbour already claimed by a concurrent winner sees
 // bit 2 (or loses the claim), so nothing changes.  The join bits are cleared at the end.
-constexpr int kGrowThreads = 256;
+constexpr int kGrowThreads = 1024;
 constexpr int kGrowRing = 8192;  // queue entries kept in shared memory (32 KiB)
 
 template <class Real, bool MASKS>
-__global__ void __launch_bounds__(kGrowThreads, 3)
+__global__ void __launch_bounds__(kGrowThreads, 1)
     wolff_grow_kernel(SweepArgs a, int* list, long long list_stride, long long* csize)
 {
     const Geo g = a.g;
-    const int lat = (int)blockIdx.x;
-    const int conf = lat / a.nrep, rep = lat - conf * a.nrep;
+    // coldest slots first: their clusters are the largest, so they start in the first wave
+    const int nconf = (int)gridDim.x / a.nrep;
+    const int slot = (int)blockIdx.x / nconf, conf = (int)blockIdx.x - slot * nconf;
+    const int rep = a.rep_at_temp[conf * a.nrep + slot];
+    const int lat = conf * a.nrep + rep;
     const int tid = (int)threadIdx.x, NT = (int)blockDim.x;
     uint8_t* S = a.spins + (long long)lat * a.lat_stride;
     uint32_t* S32 = reinterpret_cast<uint32_t*>(S);
