@@ -161,6 +161,9 @@ void release(Ctx* c)
     if (c->own) cudaStreamDestroy(c->own);
 }
 
+// Shared memory of a cluster-path CTA that still lets two CTAs share an SM
+constexpr size_t kClusterCtaSmem = 112 * 1024;
+
 size_t smem_budget(Ctx* c)
 {
     int optin = 0;
@@ -217,6 +220,19 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
     if (smem > budget) {
         v.stage_p = false;
         smem = sweep_smem_bytes(grp.g, v);
+    }
+    if (smem > budget && !(fl & J1J2C_FLAG_GLOBAL) && v.quad) {
+        // the lattice in the distributed shared memory of a thread-block cluster: prefer CTAs
+        // small enough for two per SM
+        int cs = cluster_size_for(grp.g, fp64, c->masks, kClusterCtaSmem);
+        if (cs == 0) cs = cluster_size_for(grp.g, fp64, c->masks, budget);
+        if (cs > 0) {
+            v.cluster = cs;
+            v.stage_p = false;
+            smem = (size_t)grp.g.N / (size_t)cs;
+            nthreads = 512;
+            return J1J2C_OK;
+        }
     }
     if (smem > budget || (fl & J1J2C_FLAG_GLOBAL)) {
         v.global = true;
@@ -343,6 +359,11 @@ cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int n
 {
     cudaError_t e;
     if (cycle && c->wolff && (e = enqueue_wolff(c, grp, st)) != cudaSuccess) return e;
+    if (v.cluster > 0) {
+        if ((e = cudaMemsetAsync(a.obs + a.lat0, 0, sizeof(LatObs) * nlat, st)) != cudaSuccess)
+            return e;
+        return launch_sweep_cluster(a, v, nlat, st);
+    }
     if (!v.global) return launch_sweep(a, v, nlat, nthreads, smem, st);
     for (int t = 0; t < a.nsweeps; ++t)
         for (int col = 0; col < 8; ++col)
@@ -411,10 +432,82 @@ bool valid_conf(Ctx* c, int conf) { return conf >= 0 && conf < c->nconf; }
 std::mutex g_tune_mu;
 std::map<std::tuple<bool, int, int, int>, int> g_tune_cache;
 
+// Cluster path or one launch per colour phase for a lattice that does not fit one CTA: both run
+// on a scratch copy of the group's lattices (3 cycles each, live state untouched) and the faster
+// is kept, cached per (precision, L, H, lattice count, bond dilution).
+std::map<std::tuple<bool, int, int, int, bool>, bool> g_cluster_cache;
+
+int tune_cluster(Ctx* c, Group& grp)
+{
+    const int nlat = grp.nlat();
+    const auto key = std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, nlat, c->masks);
+    bool use_cluster = true;
+    bool known = false;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_cluster_cache.find(key);
+        if (it != g_cluster_cache.end()) {
+            use_cluster = it->second;
+            known = true;
+        }
+    }
+    if (!known) {
+        uint8_t* tmp = nullptr;
+        LatObs* tobs = nullptr;
+        const size_t bytes = (size_t)nlat * grp.lat_stride;
+        CK(c, cudaMalloc(&tmp, bytes));
+        if (cudaMalloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess) {
+            cudaFree(tmp);
+            return fail(c, J1J2C_ENOMEM, "autotuner scratch");
+        }
+        cudaError_t e = cudaMemcpyAsync(tmp, c->d_spins + grp.spin_off, bytes,
+                                        cudaMemcpyDeviceToDevice, c->own);
+        SweepArgs a = group_args(c, grp);
+        a.spins = tmp;
+        a.obs = tobs;
+        a.use_override = 1;
+        a.beta_override = 1.0 / 9.5;
+        a.sweep_override = 0x5EED0000u;
+        a.flips = nullptr;
+        SweepVariant vg = grp.var;
+        vg.cluster = 0;
+        vg.global = true;
+        float ms[2] = {0.0f, 0.0f};
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+            const SweepVariant& v = k == 0 ? grp.var : vg;
+            const size_t sm = k == 0 ? grp.smem : 0;
+            const int nt = k == 0 ? grp.nthreads : 256;
+            e = enqueue_group(c, grp, v, nt, sm, a, nlat, c->own, false);  // warm-up
+            if (e == cudaSuccess) e = cudaEventRecord(c->ev0, c->own);
+            for (int r = 0; r < 3 && e == cudaSuccess; ++r)
+                e = enqueue_group(c, grp, v, nt, sm, a, nlat, c->own, false);
+            if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->own);
+            if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[k], c->ev0, c->ev1);
+        }
+        cudaStreamSynchronize(c->own);
+        cudaFree(tmp);
+        cudaFree(tobs);
+        if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the large-lattice path");
+        use_cluster = ms[0] <= ms[1];
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_cluster_cache[key] = use_cluster;
+    }
+    if (!use_cluster) {
+        grp.var.cluster = 0;
+        grp.var.global = true;
+        grp.smem = 0;
+        grp.nthreads = 256;
+        free_graphs(c);
+    }
+    return J1J2C_OK;
+}
+
 int autotune(Ctx* c, Group& grp)
 {
     if (grp.tuned) return J1J2C_OK;
     grp.tuned = true;
+    if (grp.var.cluster > 0 && grp.block_threads == 0) return tune_cluster(c, grp);
     if (grp.var.fixed_nt == 0 || grp.block_threads > 0) return J1J2C_OK;
     int nts[8];
     bool sp[8];

@@ -128,6 +128,7 @@ struct SweepVariant {
     int fixed_nt;  // > 0: shape-specialised kernel with this many threads per CTA
     bool global;   // lattice in HBM, one launch per colour phase (too large for shared memory)
     bool vac;      // some conf has vacancies (shape-specialised kernels: vacancy handling on)
+    int cluster;   // > 0: thread-block cluster of this many CTAs per lattice (distributed smem)
 };
 
 // Global-memory path: one colour phase of sweep t of the cycle, and the observable reduction
@@ -136,6 +137,12 @@ cudaError_t launch_sweep_global(const SweepArgs& a, const SweepVariant& v, int c
                                 int nlat, cudaStream_t st);
 cudaError_t launch_measure_global(const SweepArgs& a, const SweepVariant& v, int nlat,
                                   cudaStream_t st);
+
+// Cluster path: CTAs per lattice for a shape (0: not available), and the launch (PTSWAPEVER
+// sweeps and the observables, added into a.obs, which the caller zeroes first).
+int cluster_size_for(const Geo& g, bool fp64, bool masks, size_t max_smem);
+cudaError_t launch_sweep_cluster(const SweepArgs& a, const SweepVariant& v, int nlat,
+                                 cudaStream_t st);
 
 // Shape-specialised kernels (sweep_fixed.cu): CTA sizes available for a shape, and the launch.
 int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, int* nts, bool* stage_p,

@@ -8,7 +8,11 @@
 //                 Pt_attempt_swaps (J:1303-1338), visit flags and the per-slot running sums of
 //                 Pt_measurement_loop (J:1440-1513).
 //   init_kernel   HOT/FER/STR starts (Initialize_spin_array J:1179-1209) on the device.
+#include <cooperative_groups.h>
+
 #include "sweep_common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace j1j2 {
 namespace {
@@ -163,8 +167,26 @@ struct QuadNbr {
     uint32_t own, xp, xm, yp, ym, dpp, dpm, dmp, dmm, zp, zm;
 };
 
-template <class Real, bool MASKS, bool MEASURE>
-__device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, uint32_t* S32,
+// Spin words of a lattice held whole in one array of the compact layout (shared or global memory)
+struct CompactSpins {
+    uint32_t* S32;
+    int rowstride, colstride, Qr;  // words per compact z-plane, per colour, per row
+    __device__ __forceinline__ CompactSpins(uint32_t* s, const Geo& g)
+        : S32(s), rowstride(g.Lh * g.Qr), colstride(g.Hh * g.Lh * g.Qr), Qr(g.Qr)
+    {
+    }
+    __device__ __forceinline__ uint32_t word(int cc, int ZZ, int YY, int qq) const
+    {
+        return S32[cc * colstride + ZZ * rowstride + YY * Qr + qq];
+    }
+    __device__ __forceinline__ void put(int cc, int ZZ, int YY, int qq, uint32_t v) const
+    {
+        S32[cc * colstride + ZZ * rowstride + YY * Qr + qq] = v;
+    }
+};
+
+template <class Real, bool MASKS, bool MEASURE, class Spins>
+__device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, const Spins& sp,
                                           const Real* P, const uint8_t* BM, int c, int q,
                                           uint32_t sweep, uint32_t rep, uint32_t k0, uint32_t k1,
                                           double beta, float kb, Acc& acc, int* fl = nullptr)
@@ -185,14 +207,14 @@ __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, uint
     };
     QuadNbr n;
     const int wown = W(c, Z, Y, qx);
-    n.own = S32[wown];
-    x_pair(px, S32[W(c ^ 1, Z, Y, qx)], S32[W(c ^ 1, Z, Y, qn)], n.xp, n.xm);
-    n.yp = S32[W(c ^ 2, Z, Yp, qx)];
-    n.ym = S32[W(c ^ 2, Z, Ym, qx)];
-    x_pair(px, S32[W(c ^ 3, Z, Yp, qx)], S32[W(c ^ 3, Z, Yp, qn)], n.dpp, n.dpm);
-    x_pair(px, S32[W(c ^ 3, Z, Ym, qx)], S32[W(c ^ 3, Z, Ym, qn)], n.dmp, n.dmm);
-    n.zp = S32[W(c ^ 4, Zp, Y, qx)];
-    n.zm = S32[W(c ^ 4, Zm, Y, qx)];
+    n.own = sp.word(c, Z, Y, qx);
+    x_pair(px, sp.word(c ^ 1, Z, Y, qx), sp.word(c ^ 1, Z, Y, qn), n.xp, n.xm);
+    n.yp = sp.word(c ^ 2, Z, Yp, qx);
+    n.ym = sp.word(c ^ 2, Z, Ym, qx);
+    x_pair(px, sp.word(c ^ 3, Z, Yp, qx), sp.word(c ^ 3, Z, Yp, qn), n.dpp, n.dpm);
+    x_pair(px, sp.word(c ^ 3, Z, Ym, qx), sp.word(c ^ 3, Z, Ym, qn), n.dmp, n.dmm);
+    n.zp = sp.word(c ^ 4, Zp, Y, qx);
+    n.zm = sp.word(c ^ 4, Zm, Y, qx);
 
     uint32_t mown = 0xFFFFFFFFu, mxm = 0xFFFFFFFFu, mym = 0xFFFFFFFFu;
     if constexpr (MASKS) {
@@ -299,7 +321,7 @@ __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, uint
             if (f2_get(u, 1) < f2_get(thr, 1)) flipmask |= 2u << (8 * k + 8);
         }
         if (flipmask) {
-            S32[wown] = n.own ^ flipmask;
+            sp.put(c, Z, Y, qx, n.own ^ flipmask);
             if (fl) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
@@ -393,7 +415,7 @@ __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, uint
         }
         if constexpr (!MEASURE) {
             if (flipmask) {
-                S32[wown] = n.own ^ flipmask;
+                sp.put(c, Z, Y, qx, n.own ^ flipmask);
                 if (fl) {
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
@@ -458,7 +480,7 @@ __global__ void __launch_bounds__(1024) sweep_kernel(SweepArgs a)
             if constexpr (QUAD) {
                 const int nq = g.Nc >> 2;
                 for (int q = tid; q < nq; q += NT)
-                    quad_step<Real, MASKS, false>(a, g, reinterpret_cast<uint32_t*>(S), P, BM, c,
+                    quad_step<Real, MASKS, false>(a, g, CompactSpins(reinterpret_cast<uint32_t*>(S), g), P, BM, c,
                                                   q, sweep, (uint32_t)rep, k0, k1, beta, kb, acc,
                                                   fl);
             } else {
@@ -489,7 +511,7 @@ __global__ void __launch_bounds__(1024) sweep_kernel(SweepArgs a)
         if constexpr (QUAD) {
             const int nq = g.Nc >> 2;
             for (int q = tid; q < nq; q += NT)
-                quad_step<Real, MASKS, true>(a, g, reinterpret_cast<uint32_t*>(S), P, BM, c, q, 0u,
+                quad_step<Real, MASKS, true>(a, g, CompactSpins(reinterpret_cast<uint32_t*>(S), g), P, BM, c, q, 0u,
                                              0u, 0u, 0u, beta, kb, acc);
         } else {
             for (int k = tid; k < g.Nc; k += NT) {
@@ -709,7 +731,7 @@ __global__ void __launch_bounds__(256) sweep_global_kernel(SweepArgs a, int colo
         fl = a.flips + ((long long)conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]) * a.lat_stride;
     if constexpr (QUAD) {
         if (item < (g.Nc >> 2))
-            quad_step<Real, MASKS, false>(a, g, reinterpret_cast<uint32_t*>(S), P, BM, colour,
+            quad_step<Real, MASKS, false>(a, g, CompactSpins(reinterpret_cast<uint32_t*>(S), g), P, BM, colour,
                                           item, sweep, (uint32_t)rep, k0, k1, beta, kb, acc, fl);
     } else {
         if (item < g.Nc) {
@@ -736,7 +758,7 @@ __global__ void __launch_bounds__(256) measure_global_kernel(SweepArgs a)
     if (item < 8 * per) {
         const int c = item / per, k = item - c * per;
         if constexpr (QUAD) {
-            quad_step<Real, MASKS, true>(a, g, reinterpret_cast<uint32_t*>(S), P, BM, c, k, 0u, 0u,
+            quad_step<Real, MASKS, true>(a, g, CompactSpins(reinterpret_cast<uint32_t*>(S), g), P, BM, c, k, 0u, 0u,
                                          0u, 0u, 0.0, 0.0f, acc);
         } else {
             const int X = k % g.Lh, r = k / g.Lh;
@@ -878,6 +900,198 @@ cudaError_t global_dispatch(const SweepArgs& a, const SweepVariant& v, int colou
                    : global_pass<Real, false, false>(a, colour, t, nlat, st, measure);
 }
 }  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// Lattices too large for one CTA's shared memory but not for a thread-block cluster's (L = 96:
+// 864 KiB of spins over 8 CTAs of 108 KiB): CTA r of a lattice's cluster holds compact planes
+// [z0, z0 + zpc) of every colour; a colour phase reads only the plane below and the plane above
+// from the neighbouring CTAs' shared memory, and a cluster barrier separates the colour phases.
+// All PTSWAPEVER sweeps and the observable reduction run in one launch.  The random field stays in
+// global memory (L2-resident, shared by a configuration's replicas).
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+constexpr int kClusterThreads = 512;
+
+struct ClusterSpins {
+    uint32_t* local;     // this CTA's planes: [colour][plane][row][word]
+    const uint32_t* lo;  // the CTA holding plane z0 - 1
+    const uint32_t* hi;  // the CTA holding plane z0 + zpc
+    int z0, zpc, Hh, rowstride, colstride, Qr;
+    __device__ __forceinline__ uint32_t word(int cc, int ZZ, int YY, int qq) const
+    {
+        int d = ZZ - z0;
+        if (d < 0) d += Hh;
+        const int off = YY * Qr + qq;
+        if (d < zpc) return local[cc * colstride + d * rowstride + off];
+        if (d == zpc) return hi[cc * colstride + off];              // first plane above
+        return lo[cc * colstride + (zpc - 1) * rowstride + off];    // last plane below
+    }
+    __device__ __forceinline__ void put(int cc, int ZZ, int YY, int qq, uint32_t v) const
+    {
+        local[cc * colstride + (ZZ - z0) * rowstride + YY * Qr + qq] = v;
+    }
+};
+
+template <class Real, bool MASKS>
+__global__ void __launch_bounds__(kClusterThreads, 2) sweep_cluster_kernel(SweepArgs a, int cs)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    cg::cluster_group cl = cg::this_cluster();
+    const Geo g = a.g;
+    const int rank = (int)cl.block_rank();
+    const int lat = a.lat0 + (int)blockIdx.x / cs;
+    const int conf = lat / a.nrep;
+    const int rep = lat - conf * a.nrep;
+    const int tid = (int)threadIdx.x, NT = (int)blockDim.x;
+    const int zpc = g.Hh / cs, z0 = rank * zpc;
+    const int plane_words = g.Lh * g.Qr;     // one word = one quad
+    const int chunk_words = zpc * plane_words;  // this CTA's quads of one colour
+    uint32_t* local = reinterpret_cast<uint32_t*>(smem);
+    uint8_t* Sg = a.spins + (long long)lat * a.lat_stride;
+    const size_t plane_bytes = (size_t)g.Lh * g.Lh;
+#pragma unroll 1
+    for (int c = 0; c < 8; ++c) {
+        const uint4* src = reinterpret_cast<const uint4*>(Sg + (size_t)c * g.Nc + z0 * plane_bytes);
+        uint4* dst = reinterpret_cast<uint4*>(local + c * chunk_words);
+        for (int k = tid; k < chunk_words / 4; k += NT) dst[k] = src[k];
+    }
+    ClusterSpins sp;
+    sp.local = local;
+    sp.lo = cl.map_shared_rank(local, (rank + cs - 1) % cs);
+    sp.hi = cl.map_shared_rank(local, (rank + 1) % cs);
+    sp.z0 = z0;
+    sp.zpc = zpc;
+    sp.Hh = g.Hh;
+    sp.rowstride = plane_words;
+    sp.colstride = chunk_words;
+    sp.Qr = g.Qr;
+    cl.sync();
+
+    const Real* P = field_base<Real>(a, conf);
+    const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
+    double beta;
+    uint32_t sweep0;
+    if (a.use_override) {
+        beta = a.beta_override;
+        sweep0 = a.sweep_override;
+    } else {
+        beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+        sweep0 = a.ctl[0] * (uint32_t)a.ptswapever;
+    }
+    const float kb = (float)(-2.0 * beta * 1.4426950408889634);
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    int* fl = nullptr;  // flip counts of this replica's temperature slot
+    if (a.flips && !a.use_override)
+        fl = a.flips + ((long long)conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]) * a.lat_stride;
+    Acc acc{0, 0, 0, 0, 0};
+    const int q0 = z0 * plane_words;
+    for (int t = 0; t < a.nsweeps; ++t) {
+        const uint32_t sweep = sweep0 + (uint32_t)t;
+#pragma unroll 1
+        for (int c = 0; c < 8; ++c) {
+            for (int lq = tid; lq < chunk_words; lq += NT)
+                quad_step<Real, MASKS, false>(a, g, sp, P, BM, c, q0 + lq, sweep, (uint32_t)rep,
+                                              k0, k1, beta, kb, acc, fl);
+            cl.sync();
+        }
+    }
+    // observables of the new configuration
+#pragma unroll 1
+    for (int c = 0; c < 8; ++c)
+        for (int lq = tid; lq < chunk_words; lq += NT)
+            quad_step<Real, MASKS, true>(a, g, sp, P, BM, c, q0 + lq, 0u, 0u, 0u, 0u, beta, kb,
+                                         acc);
+    const Acc tot = block_reduce(acc);
+    if (tid == 0) {
+        LatObs* o = a.obs + lat;
+        atomicAdd(reinterpret_cast<unsigned long long*>(&o->eacc), (unsigned long long)tot.e);
+        atomicAdd(&o->M, tot.M);
+        atomicAdd(&o->SX, tot.SX);
+        atomicAdd(&o->SY, tot.SY);
+        atomicAdd(&o->NB, tot.NB);
+    }
+#pragma unroll 1
+    for (int c = 0; c < 8; ++c) {
+        uint4* dst = reinterpret_cast<uint4*>(Sg + (size_t)c * g.Nc + z0 * plane_bytes);
+        const uint4* src = reinterpret_cast<const uint4*>(local + c * chunk_words);
+        for (int k = tid; k < chunk_words / 4; k += NT) dst[k] = src[k];
+    }
+    cl.sync();  // every CTA has finished reading its neighbours' shared memory
+}
+
+template <class Real, bool MASKS>
+cudaError_t cluster_launch(const SweepArgs& a, int nlat, int cs, cudaStream_t st, bool prepare)
+{
+    auto kern = sweep_cluster_kernel<Real, MASKS>;
+    const size_t smem = (size_t)a.g.N / (size_t)cs;
+    if (prepare)
+        return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nlat * cs));
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, a, cs);
+}
+
+template <class Real, bool MASKS>
+int cluster_fits(const Geo& g, int cs)
+{
+    auto kern = sweep_cluster_kernel<Real, MASKS>;
+    const size_t smem = (size_t)g.N / (size_t)cs;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)cs);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) return 0;
+    return n;
+}
+
+}  // namespace
+
+// CTAs per lattice of the cluster path for a shape (0: none): the smallest of 2, 4, 8 that
+// divides H/2 and keeps a CTA's planes within max_smem bytes, if such clusters can be resident.
+int cluster_size_for(const Geo& g, bool fp64, bool masks, size_t max_smem)
+{
+    if (g.Lh % 4 != 0) return 0;
+    for (const int cs : {2, 4, 8}) {
+        if (g.Hh % cs != 0 || (size_t)g.N / (size_t)cs > max_smem) continue;
+        const int n = fp64 ? (masks ? cluster_fits<double, true>(g, cs) : cluster_fits<double, false>(g, cs))
+                           : (masks ? cluster_fits<float, true>(g, cs) : cluster_fits<float, false>(g, cs));
+        if (n > 0) return cs;
+    }
+    return 0;
+}
+
+cudaError_t launch_sweep_cluster(const SweepArgs& a, const SweepVariant& v, int nlat,
+                                 cudaStream_t st)
+{
+    const int cs = v.cluster;
+    if (v.fp64)
+        return v.masks ? cluster_launch<double, true>(a, nlat, cs, st, false)
+                       : cluster_launch<double, false>(a, nlat, cs, st, false);
+    return v.masks ? cluster_launch<float, true>(a, nlat, cs, st, false)
+                   : cluster_launch<float, false>(a, nlat, cs, st, false);
+}
 
 cudaError_t launch_sweep_global(const SweepArgs& a, const SweepVariant& v, int colour, int t,
                                 int nlat, cudaStream_t st)

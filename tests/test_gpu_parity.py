@@ -19,9 +19,9 @@ def _betas(nrep, tmin=8.0, tmax=11.5):
 
 
 def _setup(jc, O, L, H, nconf, nrep, precision, pp=0.0, bonds=0.0, flags=0, start=0, axis=0,
-           seed=SEED, conf_base=0, ptswapever=5, betas=None):
+           seed=SEED, conf_base=0, ptswapever=5, betas=None, block_threads=0):
     eng = jc.Engine(L, H, nconf=nconf, nreplica=nrep, ptswapever=ptswapever, precision=precision,
-                    seed=seed, conf_base=conf_base, flags=flags)
+                    seed=seed, conf_base=conf_base, flags=flags, block_threads=block_threads)
     betas = _betas(nrep) if betas is None else betas
     models = []
     for k in range(nconf):
@@ -283,3 +283,51 @@ def test_invalid_calls_fail_cleanly(engine_mod, oracle):
     with pytest.raises(jc.J1J2CError):
         eng.set_ladder(0, np.array([1.0, np.nan, 2.0]))
     eng.close()
+
+
+def test_cluster_path_fp64_bit_identical(engine_mod, oracle):
+    """A lattice too large for one CTA's shared memory (64^3: 256 KiB of spins) runs on the
+    thread-block-cluster kernel (4 CTAs of 64 KiB, distributed shared memory; a fixed CTA size
+    keeps the autotuner from switching to the global path); FP64 with vacancies and diluted bonds
+    equals the oracle's replay bit for bit."""
+    jc = engine_mod
+    L = H = 64
+    eng, models, betas = _setup(jc, oracle, L, H, 1, 2, jc.FP64_PLAIN, pp=0.05, bonds=0.1,
+                                block_threads=512)
+    cfg = eng.config()
+    assert cfg["block_threads"] == 512 and cfg["smem_bytes"] == L * L * H // 4
+    st = oracle.new_pt_state(np.stack([oracle.hot_spins_philox(L, H, SEED, 0, q) * models[0].occu
+                                       for q in range(2)]))
+    eng.run(2, measure=False)
+    eng.reset_measurements()
+    eng.run(2, measure=True)
+    M = models[0]
+    M.replay_pt(st, betas, 5, 2, 0, SEED, 0, False, 1)
+    M.replay_pt(st, betas, 5, 2, 2, SEED, 0, True, 1)
+    for r in range(2):
+        np.testing.assert_array_equal(eng.spins(0, r), st["spins"][r])
+    np.testing.assert_array_equal(eng.slot_sums(0)[0], st["sums"])
+    np.testing.assert_array_equal(eng.maps(0)[0], st["rep_at_temp"])
+    eng.close()
+
+
+@pytest.mark.parametrize("pp,bonds", [(0.05, 0.0), (0.0, 0.1)])
+def test_cluster_path_fp32_equals_global_path(engine_mod, oracle, pp, bonds):
+    """FP32, 96 x 96 x 32 (the cluster kernel, 4 CTAs per lattice) against the one-launch-per-
+    colour global-memory kernel: bitwise equal spins, sums and observables."""
+    jc = engine_mod
+    out = []
+    for flags in (0, jc.FLAG_GLOBAL):
+        eng, _, _ = _setup(jc, oracle, 96, 32, 2, 2, jc.FP32_BATCHED, pp=pp, bonds=bonds,
+                           flags=flags, block_threads=512)
+        eng.run(3, measure=True)
+        out.append(([eng.spins(k, r) for k in range(2) for r in range(2)],
+                    [eng.slot_sums(k)[0] for k in range(2)], eng.observables(-1),
+                    eng.config()["smem_bytes"]))
+        eng.close()
+    assert out[0][3] == 96 * 96 * 32 // 4 and out[1][3] == 0
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    for a, b in zip(out[0][1], out[1][1]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(out[0][2], out[1][2])
