@@ -244,6 +244,24 @@ __device__ __forceinline__ float ex2_approx(float x)
     return y;
 }
 
+// FP64 Metropolis test u < own_exp(x) (x <= 0), decided from an FP32 estimate of exp(x) unless u
+// lies inside the estimate's error band, where own_exp decides: the result is exactly that of
+// u < own_exp(x).  Error of the estimate 2^(x log2e) for -80 <= x <= 0 (no FP32 underflow):
+// rounding x and the product to FP32 shifts the exponent by at most |x| (2^-24 + 2^-23), and the
+// SFU's ex2 is taken at 2^-20 relative (above its documented accuracy); the band
+// e (|x| 2^-20 + 2^-18) is four times the sum.
+__device__ __forceinline__ bool accept_fp64(double u, double x)
+{
+    if (x >= -80.0) {
+        const float xf = __double2float_rn(x);
+        const float e = ex2_approx(__fmul_rn(xf, 1.44269504f));
+        const float band = __fmul_rn(e, __fmaf_rn(fabsf(xf), 0x1p-20f, 0x1p-18f));
+        if (u < (double)__fsub_rn(e, band)) return true;
+        if (u > (double)__fadd_rn(e, band)) return false;
+    }
+    return u < own_exp(x);
+}
+
 // FP64 uniform in [0, 1) from a Philox word: the word rotated left by 9 bits, times 2^-32.  Its
 // top 23 bits are the word's low 23 bits, i.e. exactly the FP32 uniform below, so both forms
 // test the same random number (to 2^-23) in the deterministic FP32-vs-FP64 replay.

@@ -134,7 +134,7 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint
             r = u4_word(philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1), w);
             const double u = u01_f64(r);
             const double t2 = __dmul_rn(__dmul_rn(2.0, f64), beta);
-            flip64 = u < own_exp(s == 1 ? -t2 : t2);
+            flip64 = accept_fp64(u, s == 1 ? -t2 : t2);
         }
         if constexpr (MODE == kModeAudit) {
             r = u4_word(philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1), w);
@@ -407,7 +407,7 @@ __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, cons
                     } else {
                         const double u = u01_f64(u4_word(rnd, k));
                         const double t2 = __dmul_rn(__dmul_rn(2.0, f), beta);
-                        flip = u < own_exp(s == 1 ? -t2 : t2);
+                        flip = accept_fp64(u, s == 1 ? -t2 : t2);
                     }
                     flipmask |= flip ? (2u << sh) : 0u;
                 }

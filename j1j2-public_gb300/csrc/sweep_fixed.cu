@@ -238,7 +238,7 @@ __device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
                 } else {
                     const double u = u01_f64(u4_word(rnd, k));
                     const double t2 = __dmul_rn(__dmul_rn(2.0, f), beta);
-                    flip = u < own_exp(s == 1 ? -t2 : t2);
+                    flip = accept_fp64(u, s == 1 ? -t2 : t2);
                 }
                 flipmask |= flip ? (2u << sh) : 0u;
             }
