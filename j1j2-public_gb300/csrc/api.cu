@@ -189,6 +189,18 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
     v.vac = c->vac;
     v.mode = kModeSweep;
     const bool quad_ok = (grp.g.Lh % 4 == 0) && !(fl & J1J2C_FLAG_GENERIC);
+    if ((fl & J1J2C_FLAG_CLUSTER) && quad_ok) {
+        int cs[16];
+        const int n = cluster_sizes(grp.g, fp64, c->masks, budget, cs, 16);
+        if (n > 0) {
+            v.quad = true;
+            v.cluster = cs[n - 1];
+            v.stage_p = false;
+            smem = (size_t)grp.g.N / (size_t)cs[n - 1];
+            nthreads = 512;
+            return J1J2C_OK;
+        }
+    }
     // the shape-specialised kernels do not count flips
     if (!(fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_GLOBAL)) &&
         !c->diag.flip_counts) {
@@ -432,17 +444,50 @@ bool valid_conf(Ctx* c, int conf) { return conf >= 0 && conf < c->nconf; }
 std::mutex g_tune_mu;
 std::map<std::tuple<bool, int, int, int>, int> g_tune_cache;
 
-// Cluster path or one launch per colour phase for a lattice that does not fit one CTA: both run
-// on a scratch copy of the group's lattices (3 cycles each, live state untouched) and the faster
-// is kept, cached per (precision, L, H, lattice count, bond dilution).
+// Device time of 3 PT-cycle sweep launches of a group with kernel variant v, on a scratch copy of
+// its lattices (the live state is not touched; one warm-up launch first).
+int time_variant(Ctx* c, Group& grp, const SweepVariant& v, int nthreads, size_t smem, float& ms)
+{
+    const int nlat = grp.nlat();
+    uint8_t* tmp = nullptr;
+    LatObs* tobs = nullptr;
+    const size_t bytes = (size_t)nlat * grp.lat_stride;
+    CK(c, cudaMalloc(&tmp, bytes));
+    if (cudaMalloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess) {
+        cudaFree(tmp);
+        return fail(c, J1J2C_ENOMEM, "autotuner scratch");
+    }
+    cudaError_t e =
+        cudaMemcpyAsync(tmp, c->d_spins + grp.spin_off, bytes, cudaMemcpyDeviceToDevice, c->own);
+    SweepArgs a = group_args(c, grp);
+    a.spins = tmp;
+    a.obs = tobs;
+    a.use_override = 1;
+    a.beta_override = 1.0 / 9.5;
+    a.sweep_override = 0x5EED0000u;
+    a.flips = nullptr;
+    if (e == cudaSuccess) e = enqueue_group(c, grp, v, nthreads, smem, a, nlat, c->own, false);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev0, c->own);
+    for (int r = 0; r < 3 && e == cudaSuccess; ++r)
+        e = enqueue_group(c, grp, v, nthreads, smem, a, nlat, c->own, false);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->own);
+    if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    cudaStreamSynchronize(c->own);
+    cudaFree(tmp);
+    cudaFree(tobs);
+    if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the sweep path");
+    return J1J2C_OK;
+}
+
+// Cluster path or one launch per colour phase for a lattice that does not fit one CTA: both are
+// timed and the faster kept, cached per (precision, L, H, lattice count, bond dilution).
 std::map<std::tuple<bool, int, int, int, bool>, bool> g_cluster_cache;
 
 int tune_cluster(Ctx* c, Group& grp)
 {
-    const int nlat = grp.nlat();
-    const auto key = std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, nlat, c->masks);
-    bool use_cluster = true;
-    bool known = false;
+    const auto key = std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks);
+    bool use_cluster = true, known = false;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_cluster_cache.find(key);
@@ -452,44 +497,14 @@ int tune_cluster(Ctx* c, Group& grp)
         }
     }
     if (!known) {
-        uint8_t* tmp = nullptr;
-        LatObs* tobs = nullptr;
-        const size_t bytes = (size_t)nlat * grp.lat_stride;
-        CK(c, cudaMalloc(&tmp, bytes));
-        if (cudaMalloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess) {
-            cudaFree(tmp);
-            return fail(c, J1J2C_ENOMEM, "autotuner scratch");
-        }
-        cudaError_t e = cudaMemcpyAsync(tmp, c->d_spins + grp.spin_off, bytes,
-                                        cudaMemcpyDeviceToDevice, c->own);
-        SweepArgs a = group_args(c, grp);
-        a.spins = tmp;
-        a.obs = tobs;
-        a.use_override = 1;
-        a.beta_override = 1.0 / 9.5;
-        a.sweep_override = 0x5EED0000u;
-        a.flips = nullptr;
         SweepVariant vg = grp.var;
         vg.cluster = 0;
         vg.global = true;
-        float ms[2] = {0.0f, 0.0f};
-        for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
-            const SweepVariant& v = k == 0 ? grp.var : vg;
-            const size_t sm = k == 0 ? grp.smem : 0;
-            const int nt = k == 0 ? grp.nthreads : 256;
-            e = enqueue_group(c, grp, v, nt, sm, a, nlat, c->own, false);  // warm-up
-            if (e == cudaSuccess) e = cudaEventRecord(c->ev0, c->own);
-            for (int r = 0; r < 3 && e == cudaSuccess; ++r)
-                e = enqueue_group(c, grp, v, nt, sm, a, nlat, c->own, false);
-            if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->own);
-            if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[k], c->ev0, c->ev1);
-        }
-        cudaStreamSynchronize(c->own);
-        cudaFree(tmp);
-        cudaFree(tobs);
-        if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the large-lattice path");
-        use_cluster = ms[0] <= ms[1];
+        float ms_c = 0.0f, ms_g = 0.0f;
+        int rc = time_variant(c, grp, grp.var, grp.nthreads, grp.smem, ms_c);
+        if (rc == J1J2C_OK) rc = time_variant(c, grp, vg, 256, 0, ms_g);
+        if (rc != J1J2C_OK) return rc;
+        use_cluster = ms_c <= ms_g;
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_cluster_cache[key] = use_cluster;
     }
@@ -503,17 +518,115 @@ int tune_cluster(Ctx* c, Group& grp)
     return J1J2C_OK;
 }
 
+// The small-batch search applies to the default kernel choice only (the test flags pin a path)
+bool small_batch_ok(Ctx* c, const Group& grp)
+{
+    return grp.block_threads == 0 && grp.var.mode == kModeSweep &&
+           !(c->P.flags & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_GLOBAL |
+                           J1J2C_FLAG_CLUSTER));
+}
+
+// Small batches (fewer lattices than half the SMs): one CTA per lattice leaves most SMs idle, so
+// every cluster size that divides H/2 is timed against the chosen one-CTA kernel and the fastest
+// kept, cached per (precision, L, H, lattice count, bond dilution, vacancies).
+std::map<std::tuple<bool, int, int, int, bool, bool>, int> g_small_cache;
+
+int tune_small_batch(Ctx* c, Group& grp)
+{
+    int nsm = 0;
+    CK(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->P.device));
+    if (2 * grp.nlat() > nsm) return J1J2C_OK;
+    const auto key =
+        std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks, c->vac);
+    int best = -1;  // after the search: 0 keep, -2 one site per thread, > 0 cluster size
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_small_cache.find(key);
+        if (it != g_small_cache.end()) best = it->second;
+    }
+    if (best == -1) {
+        int cs[16];
+        const int n = cluster_sizes(grp.g, grp.var.fp64, c->masks, smem_budget(c), cs, 16);
+        best = 0;
+        float best_ms = 0.0f;
+        int rc = time_variant(c, grp, grp.var, grp.nthreads, grp.smem, best_ms);
+        if (rc != J1J2C_OK) return rc;
+        // one site per thread (the latency of a colour phase is one site's arithmetic, not a
+        // quad's: what counts for a handful of lattices)
+        SweepVariant vs;
+        size_t sm_s = 0;
+        int nt_s = 0;
+        {
+            const uint32_t keep = c->P.flags;
+            c->P.flags |= J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED;
+            rc = choose_variant(c, grp, grp.var.fp64, vs, sm_s, nt_s);
+            c->P.flags = keep;
+            if (rc != J1J2C_OK) return rc;
+        }
+        if (!vs.global && !vs.quad) {
+            nt_s = ((grp.g.Nc + 31) / 32) * 32;
+            if (nt_s > 1024) nt_s = 1024;
+            float ms = 0.0f;
+            rc = time_variant(c, grp, vs, nt_s, sm_s, ms);
+            if (rc != J1J2C_OK) return rc;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = -2;  // per-site
+            }
+        }
+        if (n > 0) {
+            for (int k = 0; k < n; ++k) {
+                SweepVariant v = grp.var;
+                v.cluster = cs[k];
+                v.fixed_nt = 0;
+                v.global = false;
+                v.stage_p = false;
+                float ms = 0.0f;
+                rc = time_variant(c, grp, v, 512, (size_t)grp.g.N / (size_t)cs[k], ms);
+                if (rc != J1J2C_OK) return rc;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = cs[k];
+                }
+            }
+        }
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_small_cache[key] = best;
+    }
+    if (best > 0) {
+        grp.var.cluster = best;
+        grp.var.fixed_nt = 0;
+        grp.var.global = false;
+        grp.var.stage_p = false;
+        grp.smem = (size_t)grp.g.N / (size_t)best;
+        grp.nthreads = 512;
+        free_graphs(c);
+    } else if (best == -2) {
+        const uint32_t keep = c->P.flags;
+        c->P.flags |= J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED;
+        const int rc = choose_variant(c, grp, grp.var.fp64, grp.var, grp.smem, grp.nthreads);
+        c->P.flags = keep;
+        if (rc != J1J2C_OK) return rc;
+        grp.nthreads = ((grp.g.Nc + 31) / 32) * 32;
+        if (grp.nthreads > 1024) grp.nthreads = 1024;
+        free_graphs(c);
+    }
+    return J1J2C_OK;
+}
+
 int autotune(Ctx* c, Group& grp)
 {
     if (grp.tuned) return J1J2C_OK;
     grp.tuned = true;
+    if (c->P.flags & J1J2C_FLAG_CLUSTER) return J1J2C_OK;
     if (grp.var.cluster > 0 && grp.block_threads == 0) return tune_cluster(c, grp);
-    if (grp.var.fixed_nt == 0 || grp.block_threads > 0) return J1J2C_OK;
+    if (grp.block_threads > 0) return J1J2C_OK;
+    if (grp.var.fixed_nt == 0) return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
     int nts[8];
     bool sp[8];
     const int n =
         fixed_candidates(grp.var.fp64, grp.g.L, grp.g.H, c->masks, c->vac, nts, sp, 8);
-    if (n <= 1) return J1J2C_OK;
+    if (n <= 1) return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
     const int nlat = grp.nlat();
     const auto key = std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, nlat);
     int best_nt = 0;
@@ -584,7 +697,7 @@ int autotune(Ctx* c, Group& grp)
                                true));
         }
     free_graphs(c);
-    return J1J2C_OK;
+    return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
 }
 
 int check_params(const j1j2c_params* p, std::string& why)

@@ -141,6 +141,7 @@ cudaError_t launch_measure_global(const SweepArgs& a, const SweepVariant& v, int
 // Cluster path: CTAs per lattice for a shape (0: not available), and the launch (PTSWAPEVER
 // sweeps and the observables, added into a.obs, which the caller zeroes first).
 int cluster_size_for(const Geo& g, bool fp64, bool masks, size_t max_smem);
+int cluster_sizes(const Geo& g, bool fp64, bool masks, size_t max_smem, int* out, int cap);
 cudaError_t launch_sweep_cluster(const SweepArgs& a, const SweepVariant& v, int nlat,
                                  cudaStream_t st);
 

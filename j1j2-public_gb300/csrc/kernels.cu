@@ -809,8 +809,7 @@ cudaError_t do_launch(const SweepArgs& a, int nblocks, int nthreads, size_t smem
                       cudaStream_t st, bool prepare)
 {
     auto k = sweep_kernel<Real, QUAD, STAGE_P, MASKS, MODE>;
-    if (prepare)
-        return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (prepare) return raise_smem_limit(k);  // one instantiation serves every shape
     k<<<nblocks, nthreads, smem, st>>>(a);
     return cudaGetLastError();
 }
@@ -1020,13 +1019,25 @@ __global__ void __launch_bounds__(kClusterThreads, 2) sweep_cluster_kernel(Sweep
     cl.sync();  // every CTA has finished reading its neighbours' shared memory
 }
 
+// The kernels' dynamic shared memory limit is the most the device allows, so every cluster size
+// (and every shape in one context) launches whatever was probed last.
+template <class Real, bool MASKS>
+cudaError_t cluster_prepare()
+{
+    cudaError_t e = raise_smem_limit(sweep_cluster_kernel<Real, MASKS>);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(sweep_cluster_kernel<Real, MASKS>,
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return e;
+}
+
 template <class Real, bool MASKS>
 cudaError_t cluster_launch(const SweepArgs& a, int nlat, int cs, cudaStream_t st, bool prepare)
 {
     auto kern = sweep_cluster_kernel<Real, MASKS>;
     const size_t smem = (size_t)a.g.N / (size_t)cs;
-    if (prepare)
-        return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e0 = cluster_prepare<Real, MASKS>();
+    if (prepare || e0 != cudaSuccess) return e0;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(nlat * cs));
     cfg.blockDim = dim3(kClusterThreads);
@@ -1047,9 +1058,10 @@ int cluster_fits(const Geo& g, int cs)
 {
     auto kern = sweep_cluster_kernel<Real, MASKS>;
     const size_t smem = (size_t)g.N / (size_t)cs;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
+    if (cluster_prepare<Real, MASKS>() != cudaSuccess) {
+        (void)cudaGetLastError();
         return 0;
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)cs);
     cfg.blockDim = dim3(kClusterThreads);
@@ -1062,8 +1074,17 @@ int cluster_fits(const Geo& g, int cs)
     cfg.attrs = at;
     cfg.numAttrs = 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0;
+    }
     return n;
+}
+
+int cluster_fits_any(const Geo& g, int cs, bool fp64, bool masks)
+{
+    return fp64 ? (masks ? cluster_fits<double, true>(g, cs) : cluster_fits<double, false>(g, cs))
+                : (masks ? cluster_fits<float, true>(g, cs) : cluster_fits<float, false>(g, cs));
 }
 
 }  // namespace
@@ -1075,11 +1096,22 @@ int cluster_size_for(const Geo& g, bool fp64, bool masks, size_t max_smem)
     if (g.Lh % 4 != 0) return 0;
     for (const int cs : {2, 4, 8}) {
         if (g.Hh % cs != 0 || (size_t)g.N / (size_t)cs > max_smem) continue;
-        const int n = fp64 ? (masks ? cluster_fits<double, true>(g, cs) : cluster_fits<double, false>(g, cs))
-                           : (masks ? cluster_fits<float, true>(g, cs) : cluster_fits<float, false>(g, cs));
-        if (n > 0) return cs;
+        if (cluster_fits_any(g, cs, fp64, masks) > 0) return cs;
     }
     return 0;
+}
+
+// Every cluster size from 2 to 16 that divides H/2 and can be resident (for small batches, where
+// spreading a lattice over several SMs beats one CTA per lattice); returns the count.
+int cluster_sizes(const Geo& g, bool fp64, bool masks, size_t max_smem, int* out, int cap)
+{
+    int n = 0;
+    if (g.Lh % 4 != 0) return 0;
+    for (int cs = 2; cs <= 16 && n < cap; ++cs) {
+        if (g.Hh % cs != 0 || (size_t)g.N / (size_t)cs > max_smem) continue;
+        if (cluster_fits_any(g, cs, fp64, masks) > 0) out[n++] = cs;
+    }
+    return n;
 }
 
 cudaError_t launch_sweep_cluster(const SweepArgs& a, const SweepVariant& v, int nlat,

@@ -100,6 +100,22 @@ __device__ __forceinline__ f2 byte_pair(uint32_t w, int k)
                    __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7541u + (uint32_t)k)));
 }
 
+// Raise a kernel's dynamic shared memory limit to the most the device allows next to its static
+// shared memory (one instantiation may serve several shapes and sizes in one context).
+template <class Kernel>
+inline cudaError_t raise_smem_limit(Kernel kern)
+{
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa{};
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kern);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 optin - (int)fa.sharedSizeBytes);
+    return e;
+}
+
 // byte k of w minus off, as an exact float (one PRMT into a 2^23 exponent field, one FADD)
 __device__ __forceinline__ float byte_off(uint32_t w, int k, float off)
 {

@@ -765,8 +765,8 @@ cudaError_t slab_launch(const SweepArgs& a, int pz, int nlat, int* labels, long 
                         cudaStream_t st)
 {
     const size_t smem = 3 * (size_t)pz * a.g.L * a.g.L;
-    cudaError_t e = cudaFuncSetAttribute(wolff_slab_kernel<Real, MASKS>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the limit is the most the device allows, valid for every slab size in one context
+    cudaError_t e = raise_smem_limit(wolff_slab_kernel<Real, MASKS>);
     if (e != cudaSuccess) return e;
     wolff_slab_kernel<Real, MASKS>
         <<<dim3((unsigned)(a.g.H / pz), (unsigned)nlat), kSlabThreads, smem, st>>>(a, pz, labels,

@@ -331,3 +331,42 @@ def test_cluster_path_fp32_equals_global_path(engine_mod, oracle, pp, bonds):
     for a, b in zip(out[0][1], out[1][1]):
         np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("L,H,nconf,nrep,pp", [(24, 24, 1, 16, 0.0), (16, 16, 1, 1, 0.05),
+                                                (32, 8, 2, 2, 0.1)])
+def test_small_batch_cluster_path_fp64_bit_identical(engine_mod, oracle, L, H, nconf, nrep, pp):
+    """Small batches may run one lattice over a cluster of up to 16 CTAs (the autotuner's
+    small-batch choice; flag 64 pins the largest cluster): FP64 equals the replay bit for bit,
+    including the PT SERIAL configuration (24^3, 16 replicas) and a single-lattice LOCAL-style run."""
+    jc = engine_mod
+    eng, models, betas = _setup(jc, oracle, L, H, nconf, nrep, jc.FP64_PLAIN, pp=pp,
+                                flags=jc.FLAG_CLUSTER)
+    assert eng.config()["block_threads"] == 512
+    eng.run(2, measure=False)
+    eng.reset_measurements()
+    eng.run(3, measure=True)
+    for k in range(nconf):
+        st = oracle.new_pt_state(np.stack([oracle.hot_spins_philox(L, H, SEED, k, q) *
+                                           models[k].occu for q in range(nrep)]))
+        models[k].replay_pt(st, betas, 5, 2, 0, SEED, k, False, 1)
+        models[k].replay_pt(st, betas, 5, 3, 2, SEED, k, True, 1)
+        for r in range(nrep):
+            np.testing.assert_array_equal(eng.spins(k, r), st["spins"][r])
+        np.testing.assert_array_equal(eng.slot_sums(k)[0], st["sums"])
+    eng.close()
+
+
+def test_small_batch_cluster_path_fp32_bitwise(engine_mod, oracle):
+    jc = engine_mod
+    out = []
+    for flags in (jc.FLAG_CLUSTER, jc.FLAG_NO_FIXED):
+        eng, _, _ = _setup(jc, oracle, 32, 32, 2, 3, jc.FP32_BATCHED, pp=0.05, flags=flags)
+        eng.run(3, measure=True)
+        out.append(([eng.spins(k, r) for k in range(2) for r in range(3)], eng.slot_sums(-1)[0],
+                    eng.observables(-1)))
+        eng.close()
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    np.testing.assert_array_equal(out[0][2], out[1][2])
