@@ -281,6 +281,12 @@ int j1j2c_get_config(void *ctx, int32_t *block_threads, int32_t *sites_per_threa
 int j1j2c_corr_rand_3d(int32_t n1, int32_t n2, int32_t n3, double xi, int32_t seed,
                        int32_t do_uniform, double max_value, double *out);
 
+/* Same as j1j2c_corr_rand_3d with the three 3-D transforms, the filter and the crop on the current
+ * GPU (cuFFT); the white noise is drawn on the host in the reference's order and the uniform map
+ * is applied on the host.  Agrees with the host form to the rounding of the transforms. */
+int j1j2c_corr_rand_3d_gpu(int32_t n1, int32_t n2, int32_t n3, double xi, int32_t seed,
+                           int32_t do_uniform, double max_value, double *out);
+
 /* Setup_vacancies (J:1111-1165) after kissinit(seed): mode 0 = RAN (Bernoulli pp per site),
  * 1 = COR (anticorrelated); then bond masks with pph / ppv.  Returns the vacancy count (>= 0). */
 int j1j2c_setup_vacancies(int32_t seed, int32_t L, int32_t H, double pp, double pph, double ppv,

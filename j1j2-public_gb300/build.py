@@ -29,7 +29,8 @@ def _nvcc() -> str:
 
 def _sources():
     cu = [os.path.join(CSRC, f)
-          for f in ("sweep_fixed.cu", "kernels.cu", "wolff.cu", "enumerate.cu", "api.cu")]
+          for f in ("sweep_fixed.cu", "kernels.cu", "wolff.cu", "enumerate.cu", "disorder.cu",
+                    "api.cu")]
     cpp = [os.path.join(CSRC, "host_model.cpp")]
     hdr = [os.path.join(CSRC, f) for f in ("device_common.cuh", "engine.h", "sweep_common.cuh")]
     hdr.append(os.path.join(ROOT, "include", "j1j2c.h"))
@@ -69,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         for log in logs:
             sys.stdout.write(log)
     tmp = LIB + ".tmp"
-    _compile([nvcc, ARCH, "-shared", "-o", tmp] + objs + ["-lcudart"])
+    _compile([nvcc, ARCH, "-shared", "-o", tmp] + objs + ["-lcufft", "-lcudart"])
     os.replace(tmp, LIB)
     return LIB
 

@@ -146,6 +146,22 @@ void fft3(std::vector<cplx>& a, int f1, int f2, int f3, int sign)
 
 }  // namespace
 
+namespace j1j2 {
+// gkiss05 white noise after gkissinit(seed), n deviates in the reference's order (CR:256, 280-287)
+void gauss_fill(int32_t seed, size_t n, double* out)
+{
+    Gauss gs;
+    gs.k.seed(seed);
+    for (size_t t = 0; t < n; ++t) out[t] = gs.next();
+}
+
+// the uniform map of CR:333-341 (x -> (2 (1 - erfcc(x / sqrt 2) / 2) - 1) * max_value)
+double uniform_map(double v, double max_value)
+{
+    return (2.0 * (1.0 - 0.5 * erfcc(v / std::sqrt(2.0))) - 1.0) * max_value;
+}
+}  // namespace j1j2
+
 extern "C" {
 
 int j1j2c_corr_rand_3d(int32_t n1, int32_t n2, int32_t n3, double xi, int32_t seed,

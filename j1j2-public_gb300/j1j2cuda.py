@@ -38,7 +38,7 @@ EXPORTS = ("j1j2c_create", "j1j2c_create_multi", "j1j2c_conf_shape", "j1j2c_dest
            "j1j2c_version", "j1j2c_wolff", "j1j2c_get_cluster_sizes", "j1j2c_enumerate_exact",
            "j1j2c_set_diagnostics", "j1j2c_get_locnem", "j1j2c_get_histogram", "j1j2c_get_trace",
            "j1j2c_get_flip_counts", "j1j2c_state_size", "j1j2c_save_state", "j1j2c_load_state",
-           "j1j2c_get_diagnostics", "j1j2c_get_occupied")
+           "j1j2c_get_diagnostics", "j1j2c_get_occupied", "j1j2c_corr_rand_3d_gpu")
 
 ENUM_FIELDS = ("lnZ", "e", "e2", "absm", "m2", "m4", "abssx", "sx2", "abssy", "sy2", "nbar",
                "nbar2")
@@ -102,13 +102,15 @@ def _check(ctx, rc):
 # ------------------------------------------------------------------------------------------------
 # host helpers (no GPU)
 # ------------------------------------------------------------------------------------------------
-def corr_rand_3d(n1, n2, n3, xi, seed, do_uniform=True, max_value=2.0) -> np.ndarray:
-    """make_corr_rand_3d (CR:191-386); returns x[k, j, i] = x(i, j, k), i.e. site order."""
+def corr_rand_3d(n1, n2, n3, xi, seed, do_uniform=True, max_value=2.0,
+                 gpu=False) -> np.ndarray:
+    """make_corr_rand_3d (CR:191-386); returns x[k, j, i] = x(i, j, k), i.e. site order.
+    gpu=True runs the transforms on the current GPU (cuFFT)."""
     out = np.empty(n1 * n2 * n3, np.float64)
-    _check(None, lib().j1j2c_corr_rand_3d(C.c_int32(n1), C.c_int32(n2), C.c_int32(n3),
-                                          C.c_double(xi), C.c_int32(seed),
-                                          C.c_int32(int(do_uniform)), C.c_double(max_value),
-                                          _p(out, C.c_double)))
+    fn = lib().j1j2c_corr_rand_3d_gpu if gpu else lib().j1j2c_corr_rand_3d
+    _check(None, fn(C.c_int32(n1), C.c_int32(n2), C.c_int32(n3), C.c_double(xi),
+                    C.c_int32(seed), C.c_int32(int(do_uniform)), C.c_double(max_value),
+                    _p(out, C.c_double)))
     return out.reshape(n3, n2, n1)
 
 
@@ -158,9 +160,9 @@ def enumerate_exact(L, H, p, betas, occu=None, jh=None, jv=None, J1h=1.0, J1v=1.
     return out
 
 
-def disorder(L, H, seed, phi=2.0, xi=3.0, map_uniform=True) -> np.ndarray:
+def disorder(L, H, seed, phi=2.0, xi=3.0, map_uniform=True, gpu=False) -> np.ndarray:
     """Setup_phi_table (J:590-633): p(site) for disorder seed IRINIT + iconf - 1."""
-    return corr_rand_3d(L, L, H, xi, seed, map_uniform, phi).reshape(-1)
+    return corr_rand_3d(L, L, H, xi, seed, map_uniform, phi, gpu).reshape(-1)
 
 
 # ------------------------------------------------------------------------------------------------
