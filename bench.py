@@ -254,18 +254,25 @@ def run_ours(args):
     sweep_ms_avg = prof_ms / max(args.steps, 1)  # sweep kernel, per launch (timed steps)
     value = attempts_per_step * args.steps * ws / (total_ms * 1e6)
 
-    # end to end through the public API with host buffers: ladder H2D, one cycle, all running
-    # sums and observables D2H, every step
+    # end to end through the public API with pinned host buffers: ladder H2D, one cycle, all
+    # running sums and observables D2H, every step
+    def pinned(nbytes):
+        return torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+
+    h_betas = pinned(betas.nbytes).view(np.float64)
+    h_betas[:] = betas
+    h_sums = pinned(eng.nentries * eng.SLOT_DTYPE.itemsize).view(eng.SLOT_DTYPE)
+    h_obs = pinned(eng.nentries * 5 * 8).view(np.float64).reshape(eng.nentries, 5)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        eng.set_ladder(-1, betas)
+        eng.set_ladder(-1, h_betas)
         eng.run(1, measure=True, restart_swap_phase=False)
-        sums, nm = eng.slot_sums(-1)
-        obs = eng.observables(-1)
+        sums, nm = eng.slot_sums(-1, out=h_sums)
+        obs = eng.observables(-1, out=h_obs)
     e2e_s = time.perf_counter() - t0
     e2e = attempts_per_step * args.steps * ws / (e2e_s * 1e9)
-    h2d = betas.nbytes
-    d2h = sums.nbytes + nm.nbytes + obs.nbytes
+    h2d = h_betas.nbytes
+    d2h = h_sums.nbytes + h_obs.nbytes
     assert np.isfinite(sums).all()
 
     pk = peaks()

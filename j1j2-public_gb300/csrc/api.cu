@@ -1440,17 +1440,13 @@ int j1j2c_get_slot_sums(void* ctx, int32_t conf, j1j2c_slot_sums* out)
     if (conf >= c->nconf || !out) return fail(c, J1J2C_EINVAL, "bad conf or null output");
     const size_t off = conf < 0 ? 0 : (size_t)c->conf_rbase[conf];
     const int nr = conf < 0 ? c->nentries : c->conf_nrep[conf];
-    std::vector<double> sums((size_t)nr * 22);
-    std::vector<long long> nm((size_t)nr);
-    CK(c, cudaMemcpyAsync(sums.data(), c->d_sums + off * 22, sums.size() * 8,
-                          cudaMemcpyDeviceToHost, c->st));
-    CK(c, cudaMemcpyAsync(nm.data(), c->d_nmeas + off, nm.size() * 8, cudaMemcpyDeviceToHost,
-                          c->st));
+    // straight into the caller's records (two strided copies; DMA when the buffer is pinned)
+    CK(c, cudaMemcpy2DAsync(out, sizeof(j1j2c_slot_sums), c->d_sums + off * 22, 22 * sizeof(double),
+                            22 * sizeof(double), (size_t)nr, cudaMemcpyDeviceToHost, c->st));
+    CK(c, cudaMemcpy2DAsync(&out[0].nmeasure, sizeof(j1j2c_slot_sums), c->d_nmeas + off,
+                            sizeof(long long), sizeof(long long), (size_t)nr,
+                            cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaStreamSynchronize(c->st));
-    for (int r = 0; r < nr; ++r) {
-        std::memcpy(&out[r], &sums[(size_t)r * 22], 22 * sizeof(double));
-        out[r].nmeasure = nm[r];
-    }
     return J1J2C_OK;
 }
 

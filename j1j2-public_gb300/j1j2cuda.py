@@ -360,13 +360,19 @@ class Engine:
         return att.value, mis.value
 
     # outputs -----------------------------------------------------------------------------------
-    def slot_sums(self, conf):
+    SLOT_DTYPE = np.dtype([("s", np.float64, 22), ("n", np.int64)])
+
+    def slot_sums(self, conf, out=None):
         """(nrep, 22) running sums in SUM_FIELDS order and the (nrep,) measurement counts;
-        conf < 0 returns every conf, (nconf*nrep, 22) and (nconf*nrep,)."""
+        conf < 0 returns every conf, (nconf*nrep, 22) and (nconf*nrep,).  out: a record array
+        of SLOT_DTYPE to fill (e.g. in pinned memory); the result is then views into it."""
         n = self.nentries if conf < 0 else self.nrep_of(conf)
-        raw = np.zeros(n, dtype=np.dtype([("s", np.float64, 22), ("n", np.int64)]))
+        raw = np.zeros(n, dtype=self.SLOT_DTYPE) if out is None else out
+        assert raw.dtype == self.SLOT_DTYPE and raw.size == n and raw.flags.c_contiguous
         self._ck(lib().j1j2c_get_slot_sums(self._ctx, C.c_int32(conf),
                                            raw.ctypes.data_as(C.c_void_p)))
+        if out is not None:
+            return raw["s"], raw["n"]
         return raw["s"].copy(), raw["n"].copy()
 
     def pt_stats(self, conf):
@@ -391,8 +397,13 @@ class Engine:
                                        _p(s, C.c_int8)))
         return s
 
-    def observables(self, conf):
-        out = np.empty((self.nentries if conf < 0 else self.nrep_of(conf), 5))
+    def observables(self, conf, out=None):
+        """{mag, en, strx, stry, nbar} of every replica after the last cycle; out: an array of
+        that shape to fill (e.g. in pinned memory)."""
+        shape = (self.nentries if conf < 0 else self.nrep_of(conf), 5)
+        if out is None:
+            out = np.empty(shape)
+        assert out.shape == shape and out.dtype == np.float64 and out.flags.c_contiguous
         self._ck(lib().j1j2c_get_observables(self._ctx, C.c_int32(conf), _p(out, C.c_double)))
         return out
 
