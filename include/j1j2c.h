@@ -80,6 +80,23 @@ typedef struct {
     int64_t nmeasure;
 } j1j2c_slot_sums;
 
+/* Run description for the reference-format output files (the parameters Write_files prints,
+ * J:43-96); strings are the reference's values, e.g. impmode "RAN", start "HOT", straxis "X",
+ * samplermode "PT   ", updateorder "SEQ", tempprotocol "INDEP", ptstartmode "COMMON",
+ * ptladdermode "LINEAR". */
+typedef struct j1j2c_run_info {
+    int32_t L, H;
+    double J1, deltaJ1, J2, J3, phi, xi, pp;
+    const char *impmode, *start, *straxis, *samplermode, *updateorder, *tempprotocol,
+        *ptstartmode, *ptladdermode;
+    int32_t nreplica, ptswapever, ptmeasindex, nconf, neq, nmess, irinit;
+    double tladdermid, tladderfrac;
+    int32_t bins;            /* BINS: > 0 writes the histogram file cfhs */
+    int32_t write_strip;     /* WRITESTRIP: per-configuration stripe file cfxy */
+    int32_t write_numflips;  /* WRITENUMFLIPS: per-site flip counts cfnu */
+    int32_t write_phitable;  /* WRITEPHITABLE: random field table cfph */
+} j1j2c_run_info;
+
 /* Optional diagnostics of measured PT cycles (all off in a new context). */
 typedef struct j1j2c_diagnostics {
     int32_t locnem_slot;  /* >= 0: per-site sums of s and of the local nematic term of the replica
@@ -261,7 +278,33 @@ int j1j2c_save_state(void *ctx, void *buf, int64_t size);
  * (J1J2C_EINVAL otherwise); the blob's diagnostics settings replace the context's. */
 int j1j2c_load_state(void *ctx, const void *buf, int64_t size);
 
-/* Sweep-kernel timing accumulated under J1J2C_FLAG_PROFILE: milliseconds, launches, and the
+/* ---------------------------------------------------------------------------------------------
+ * Results in the reference's file formats (host side; replaces the per-configuration
+ * finalisation J:1542-1684, Collect_data J:2917-3207 and Write_files J:3210-3575)
+ * ------------------------------------------------------------------------------------------- */
+
+/* An accumulator of disorder averages for a run of NREPLICA temperatures temps[] (T of each slot). */
+int j1j2c_results_create(void **res, const j1j2c_run_info *info, const double *temps);
+
+/* Add one disorder configuration: its slot sums (NREPLICA records, j1j2c_get_slot_sums), occupied
+ * sites (L3 - nimp), swap attempts / accepts (NREPLICA - 1 each, may be NULL), replicas that
+ * visited both ladder ends, and optionally the histogram (NREPLICA x bins counts with per-slot
+ * lower edge and bin size, j1j2c_get_histogram), the flip counts (NREPLICA x N,
+ * j1j2c_get_flip_counts) and the random field (N). */
+int j1j2c_results_add_conf(void *res, const j1j2c_slot_sums *sums, int32_t nocc,
+                           const int64_t *swap_attempts, const int64_t *swap_accepts,
+                           int32_t visited_both, const double *hist_counts,
+                           const double *hist_min, const double *hist_bin,
+                           const int32_t *flip_counts, const double *p);
+
+/* Write cfen / cfma / cfnm / cfst / cfnd (always), cfhs (bins > 0), cfxy (write_strip),
+ * cfnu (write_numflips), cfpt (PT sampler), cfph (write_phitable) into directory dir, named as
+ * the reference names them (e.g. cfen00320032.dat for L = H = 32). */
+int j1j2c_results_write(void *res, const char *dir);
+
+void j1j2c_results_destroy(void *res);
+
+/* Sweep-kernel timing accumulated under J1J2C_FLAG_PROFILE/* Sweep-kernel timing accumulated under J1J2C_FLAG_PROFILE: milliseconds, launches, and the
  * attempts those launches made (occupied sites x sweeps). */
 int j1j2c_get_profile(void *ctx, double *sweep_ms, int64_t *sweep_launches, int64_t *attempts);
 

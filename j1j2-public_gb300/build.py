@@ -31,7 +31,7 @@ def _sources():
     cu = [os.path.join(CSRC, f)
           for f in ("sweep_fixed.cu", "kernels.cu", "wolff.cu", "enumerate.cu", "disorder.cu",
                     "api.cu")]
-    cpp = [os.path.join(CSRC, "host_model.cpp")]
+    cpp = [os.path.join(CSRC, f) for f in ("host_model.cpp", "results.cpp")]
     hdr = [os.path.join(CSRC, f) for f in ("device_common.cuh", "engine.h", "sweep_common.cuh")]
     hdr.append(os.path.join(ROOT, "include", "j1j2c.h"))
     return cu, cpp, hdr

@@ -38,7 +38,9 @@ EXPORTS = ("j1j2c_create", "j1j2c_create_multi", "j1j2c_conf_shape", "j1j2c_dest
            "j1j2c_version", "j1j2c_wolff", "j1j2c_get_cluster_sizes", "j1j2c_enumerate_exact",
            "j1j2c_set_diagnostics", "j1j2c_get_locnem", "j1j2c_get_histogram", "j1j2c_get_trace",
            "j1j2c_get_flip_counts", "j1j2c_state_size", "j1j2c_save_state", "j1j2c_load_state",
-           "j1j2c_get_diagnostics", "j1j2c_get_occupied", "j1j2c_corr_rand_3d_gpu")
+           "j1j2c_get_diagnostics", "j1j2c_get_occupied", "j1j2c_corr_rand_3d_gpu",
+           "j1j2c_results_create", "j1j2c_results_add_conf", "j1j2c_results_write",
+           "j1j2c_results_destroy")
 
 ENUM_FIELDS = ("lnZ", "e", "e2", "absm", "m2", "m4", "abssx", "sx2", "abssy", "sy2", "nbar",
                "nbar2")
@@ -62,6 +64,17 @@ class SlotSums(C.Structure):
     _fields_ = [(f, C.c_double) for f in SUM_FIELDS] + [("nmeasure", C.c_int64)]
 
 
+class RunInfo(C.Structure):
+    _fields_ = [("L", C.c_int32), ("H", C.c_int32)] + \
+        [(f, C.c_double) for f in ("J1", "deltaJ1", "J2", "J3", "phi", "xi", "pp")] + \
+        [(f, C.c_char_p) for f in ("impmode", "start", "straxis", "samplermode", "updateorder",
+                                    "tempprotocol", "ptstartmode", "ptladdermode")] + \
+        [(f, C.c_int32) for f in ("nreplica", "ptswapever", "ptmeasindex", "nconf", "neq",
+                                   "nmess", "irinit")] + \
+        [("tladdermid", C.c_double), ("tladderfrac", C.c_double)] + \
+        [(f, C.c_int32) for f in ("bins", "write_strip", "write_numflips", "write_phitable")]
+
+
 class Diagnostics(C.Structure):
     _fields_ = [("locnem_slot", C.c_int32), ("hist_bins", C.c_int32),
                 ("trace_cycles", C.c_int32), ("flip_counts", C.c_int32)]
@@ -83,6 +96,8 @@ def lib():
         L.j1j2c_last_error.argtypes = [C.c_void_p]
         L.j1j2c_version.restype = C.c_char_p
         L.j1j2c_destroy.restype = None
+        L.j1j2c_results_destroy.restype = None
+        L.j1j2c_results_destroy.argtypes = [C.c_void_p]
         L.j1j2c_destroy.argtypes = [C.c_void_p]
         _lib = L
     return _lib
@@ -495,6 +510,80 @@ def local_histogram(enlist, bins):
     k = np.where(x >= 0, np.floor(x + 0.5), -np.floor(-x + 0.5)).astype(np.int64)  # NINT
     k = k[(k >= 1) & (k <= bins)]
     return np.bincount(k - 1, minlength=bins).astype(np.float64), lo, size
+
+
+class Results:
+    """Disorder averages of a run written in the reference's file formats (Collect_data,
+    J:2917-3207, and Write_files, J:3210-3575): cfen, cfma, cfnm, cfst, cfnd, and cfhs / cfxy /
+    cfnu / cfpt / cfph as enabled."""
+
+    def __init__(self, L, H, temps, nconf, neq, nmess, irinit=1, J1=1.0, deltaJ1=0.0, J2=-1.0,
+                 J3=1.0, phi=2.0, xi=3.0, pp=0.0, impmode="RAN", start="HOT", straxis="X",
+                 samplermode="PT   ", updateorder="SEQ", tempprotocol="INDEP",
+                 ptstartmode="COMMON", ptladdermode="LINEAR", ptswapever=5, ptmeasindex=1,
+                 tladdermid=9.5, tladderfrac=0.7, bins=0, write_strip=True,
+                 write_numflips=False, write_phitable=False):
+        self.temps = np.ascontiguousarray(temps, np.float64)
+        self._strings = [x.encode() for x in (impmode, start, straxis, samplermode, updateorder,
+                                              tempprotocol, ptstartmode, ptladdermode)]
+        info = RunInfo(L, H, J1, deltaJ1, J2, J3, phi, xi, pp, *self._strings,
+                       self.temps.size, ptswapever, ptmeasindex, nconf, neq, nmess, irinit,
+                       tladdermid, tladderfrac, bins, int(write_strip), int(write_numflips),
+                       int(write_phitable))
+        self.N = L * L * H
+        self.bins = bins
+        self._res = C.c_void_p()
+        _check(None, lib().j1j2c_results_create(C.byref(self._res), C.byref(info),
+                                                _p(self.temps, C.c_double)))
+
+    def add_conf(self, sums, nocc, attempts=None, accepts=None, visited_both=0, hist=None,
+                 hist_min=None, hist_bin=None, flips=None, p=None):
+        """sums: SLOT_DTYPE records (nrep) or a (22-column sums, counts) pair."""
+        if isinstance(sums, tuple):
+            rec = np.zeros(len(sums[1]), Engine.SLOT_DTYPE)
+            rec["s"], rec["n"] = sums
+            sums = rec
+        arrs = []
+
+        def ptr(a, dt, ct):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dt)
+            arrs.append(a)
+            return _p(a, ct)
+        _check(None, lib().j1j2c_results_add_conf(
+            self._res, sums.ctypes.data_as(C.c_void_p), C.c_int32(int(nocc)),
+            ptr(attempts, np.int64, C.c_int64), ptr(accepts, np.int64, C.c_int64),
+            C.c_int32(int(visited_both)), ptr(hist, np.float64, C.c_double),
+            ptr(hist_min, np.float64, C.c_double), ptr(hist_bin, np.float64, C.c_double),
+            ptr(flips, np.int32, C.c_int32), ptr(p, np.float64, C.c_double)))
+
+    def add_engine_conf(self, eng, conf, p=None):
+        """Pull one configuration's results from an Engine (diagnostics as enabled there)."""
+        raw = np.zeros(eng.nrep_of(conf), Engine.SLOT_DTYPE)
+        eng.slot_sums(conf, out=raw)
+        att, acc, vb = eng.pt_stats(conf)
+        hist = hmin = hbin = flips = None
+        if self.bins > 0 and eng.diag.hist_bins == self.bins:
+            hist, hmin, hbin = eng.histogram(conf)
+        if eng.diag.flip_counts:
+            flips = eng.flip_counts(conf)
+        self.add_conf(raw, eng.nocc[conf], att, acc, vb, hist, hmin, hbin, flips, p)
+
+    def write(self, directory):
+        os.makedirs(directory, exist_ok=True)
+        _check(None, lib().j1j2c_results_write(self._res, os.fsencode(directory)))
+
+    def close(self):
+        if self._res:
+            lib().j1j2c_results_destroy(self._res)
+            self._res = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def pt_run(L, betas, nconf=1, neq=100, nmess=100, ptswapever=5, irinit=1, start=START_HOT,

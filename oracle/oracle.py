@@ -345,3 +345,81 @@ def local_histogram_ref(enlist, bins):
         if 1 <= k <= bins:
             counts[k - 1] += 1.0
     return counts, lo, size
+
+
+def results_ref(sums_list, nmeas_list, nocc_list, temps):
+    """Write_files' columns restated from the reference (J:1542-1684 per configuration, the sums
+    of Collect_data, the formulas of Write_files J:3210-3575) for slot sums in SUM_FIELDS order.
+    Returns {file stem: list of rows}; per-configuration files list (iconf, slot) rows."""
+    temps = np.asarray(temps, np.float64)
+    beta = 1.0 / temps
+    per = []
+    for S, nm, nocc in zip(sums_list, nmeas_list, nocc_list):
+        n = np.asarray(nm, np.float64)
+        f = {k: S[:, i] / n for i, k in enumerate(SUM_FIELDS[:20])}
+        absmag, mag2, mag4, en, en2 = f["absmag"], f["mag2"], f["mag4"], f["en"], f["en2"]
+        strx, stry = f["strx_abs"], f["stry_abs"]
+        q = dict(absmag=absmag, mag2=mag2, mag4=mag4, en=en, strx=strx, stry=stry,
+                 strx2=f["strx2"], strx4=f["strx4"], stry2=f["stry2"], stry4=f["stry4"],
+                 str2=f["str2"], str4=f["str4"], absstr=f["absstr"], nem=f["nem"],
+                 nbar=f["nbar"], nbarabs=f["nbarabs"], nbar2=f["nbar2"], nbar4=f["nbar4"])
+
+        def b4(x4, x2):
+            return np.where(x2 > 0, 1.0 - x4 / np.where(x2 > 0, 3.0 * x2 ** 2, 1.0), 0.0)
+        q["susc"] = (mag2 - absmag ** 2) * nocc * beta
+        q["suscstr"] = (q["str2"] - q["absstr"] ** 2) * nocc * beta
+        q["UL"] = b4(mag4, mag2)
+        q["US"] = np.where(q["str2"] > 0, 2.0 - q["str4"] / np.where(q["str2"] > 0, q["str2"] ** 2, 1), 0)
+        q["USX"], q["USY"], q["UBN"] = b4(q["strx4"], q["strx2"]), b4(q["stry4"], q["stry2"]), \
+            b4(q["nbar4"], q["nbar2"])
+        q["sph"] = (en2 - en ** 2) * nocc * beta ** 2
+        q["logmag"] = np.log(np.where(absmag > 0, absmag, np.finfo(float).tiny))
+        q["stripediff"] = strx ** 2 - stry ** 2
+        q["besten"], q["finalen"] = S[:, 20], S[:, 21]
+        per.append(q)
+    nf = len(per)
+
+    def mean(k):
+        return sum(p[k] for p in per) / nf
+
+    def err(k):
+        return np.sqrt(sum(p[k] ** 2 for p in per) / nf - mean(k) ** 2) / np.sqrt(nf)
+
+    def coex(x, y):
+        d = x * x + y * y
+        return np.where(d > 0, 4 * x * x * y * y / np.where(d > 0, d * d, 1), 0.0)
+    out = {}
+    out["cfen"] = np.column_stack([temps, mean("en"), err("en"), mean("sph"), err("sph")])
+    out["cfma"] = np.column_stack([temps, mean("absmag"), sum(p["absmag"] ** 2 for p in per) / nf,
+                                   err("absmag"), mean("susc"), err("susc"), mean("UL"), err("UL"),
+                                   mean("logmag"), 1 - mean("mag4") / (3 * mean("mag2") ** 2)])
+    nb = mean("nbar")
+    mabs = sum(np.abs(p["nbar"]) for p in per) / nf
+    mabserr = np.sqrt(np.maximum(0, sum((np.abs(p["nbar"]) - mabs) ** 2 for p in per) / nf)) / np.sqrt(nf)
+    nabs = mean("nbarabs")
+    nabserr = np.sqrt(np.maximum(0, sum((p["nbarabs"] - nabs) ** 2 for p in per) / nf)) / np.sqrt(nf)
+    n2, n4 = mean("nbar2"), mean("nbar4")
+    out["cfnm"] = np.column_stack([temps, nb, mabs, nabs,
+                                   np.sqrt(np.maximum(0, sum(p["nbar"] ** 2 for p in per) / nf - nb ** 2)) / np.sqrt(nf),
+                                   mabserr, nabserr, n2, n4,
+                                   np.where(n2 > 0, 1 - n4 / (3 * n2 ** 2), 0), mean("UBN"), err("UBN")])
+    cp = sum(p["strx"] * p["stry"] for p in per) / nf
+    cp2 = sum((p["strx"] * p["stry"]) ** 2 for p in per) / nf
+    ca = sum(coex(p["strx"], p["stry"]) for p in per) / nf
+    ca2 = sum(coex(p["strx"], p["stry"]) ** 2 for p in per) / nf
+    s2, s4 = mean("str2"), mean("str4")
+    out["cfst"] = np.column_stack([temps, mean("absstr"), s2, s4, mean("nem"), 2 - s4 / s2 ** 2,
+                                   mean("suscstr"), mean("US"), err("US"),
+                                   np.sqrt(sum(p["absstr"] ** 2 for p in per) / nf - mean("absstr") ** 2) / np.sqrt(nf),
+                                   err("suscstr"), mean("strx"), mean("strx2"), mean("strx4"),
+                                   mean("USX"), err("USX"), mean("stry"), mean("stry2"),
+                                   mean("stry4"), mean("USY"), err("USY"), cp,
+                                   np.sqrt(cp2 - cp ** 2) / np.sqrt(nf), ca,
+                                   np.sqrt(ca2 - ca ** 2) / np.sqrt(nf)])
+    out["cfxy"] = [[k + 1, temps[t], p["strx"][t], p["stry"][t], p["absstr"][t],
+                    p["stripediff"][t], p["besten"][t], p["finalen"][t],
+                    p["strx"][t] * p["stry"][t], float(coex(p["strx"][t], p["stry"][t]))]
+                   for k, p in enumerate(per) for t in range(len(temps))]
+    out["cfnd"] = [[k + 1, temps[t], p["nbar"][t], p["nbarabs"][t], p["nbar2"][t],
+                    p["nbar4"][t], p["UBN"][t]] for k, p in enumerate(per) for t in range(len(temps))]
+    return out
