@@ -116,3 +116,41 @@ def test_diagnostics_errors(engine_mod):
     ls, ln, ns = eng.locnem(0)
     assert ns == 0 and not ls.any() and not ln.any()
     eng.close()
+
+
+def test_results_files_from_an_engine_run(engine_mod, oracle, tmp_path):
+    """A PT run's results written in the reference's formats: the energy column of cfen is the
+    disorder average of the slots' mean energies, cfpt holds the engine's swap counts and cfhs
+    the engine's histograms divided by NMESS."""
+    jc = engine_mod
+    L, H, nconf, nrep, nmess, bins = 8, 8, 3, 4, 20, 10
+    betas = _betas(nrep)
+    eng = jc.Engine(L, H, nconf=nconf, nreplica=nrep, precision=jc.FP32_BATCHED, seed=SEED)
+    eng.set_diagnostics(hist_bins=bins, flip_counts=True)
+    for k in range(nconf):
+        eng.set_disorder(k, jc.disorder(L, H, SEED + k))
+        eng.set_ladder(k, betas)
+        eng.init_spins(k, jc.START_HOT)
+    eng.run(10, measure=False)
+    eng.reset_measurements()
+    eng.run(nmess, measure=True)
+    res = jc.Results(L, H, 1.0 / betas, nconf=nconf, neq=10, nmess=nmess, bins=bins,
+                     write_numflips=True)
+    for k in range(nconf):
+        res.add_engine_conf(eng, k)
+    res.write(str(tmp_path))
+    en = np.mean([eng.slot_sums(k)[0][:, 4] / nmess for k in range(nconf)], axis=0)
+    rows = [ln for ln in open(tmp_path / "cfen00080008.dat").read().splitlines()
+            if ln.startswith("   ") and "E" in ln]
+    np.testing.assert_allclose([float(r.split()[1]) for r in rows], en, rtol=1e-13)
+    pt = open(tmp_path / "cfpt00080008.dat").read().splitlines()
+    att = sum(eng.pt_stats(k)[0] for k in range(nconf))
+    assert [int(ln.split()[3]) for ln in pt[1:nrep]] == list(att)
+    hs = [ln for ln in open(tmp_path / "cfhs00080008.dat").read().splitlines()
+          if ln.startswith(" 0.") and len(ln.split()) == 4]
+    h = np.mean([eng.histogram(k)[0] for k in range(nconf)], axis=0) / nmess
+    np.testing.assert_allclose([float(r.split()[3]) for r in hs], h[:, :bins - 1].reshape(-1),
+                               rtol=1e-5, atol=1e-7)
+    assert (tmp_path / "cfnu00080008.dat").exists()
+    res.close()
+    eng.close()
