@@ -193,8 +193,11 @@ int j1j2c_metro_sweep_fp64(void *ctx, int32_t conf, int32_t rep, double beta,
 
 /* One Wolff cluster update of every lattice at its slot's beta: bonds with K s_i s_j > 0 are
  * activated with probability 1 - exp(-2 beta K s_i s_j) (K the per-bond coupling of
- * Compute_local_field, J:2498-2541), components are labelled by union-find in a scratch array
- * the context allocates on first use, and the component of a Philox-chosen seed site is flipped.
+ * Compute_local_field, J:2498-2541) and the cluster of a Philox-chosen seed site is flipped.
+ * By default one CTA per lattice grows the seed's cluster breadth-first; J1J2C_FLAG_NO_FIXED
+ * selects shared-memory slab union-find labelling and J1J2C_FLAG_GENERIC per-site global
+ * union-find labelling (scratch the context allocates on first use); all three flip the same
+ * cluster.
  * The random stream is indexed by the PT cycle counter (a cycle with J1J2C_FLAG_WOLFF runs this
  * before its sweeps).  cluster_sizes (NULL or nconf x NREPLICA) receives the flipped sizes.
  * Replaces the Wolff update named in the reference's header (J:7), which it never implements. */

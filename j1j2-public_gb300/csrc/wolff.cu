@@ -8,8 +8,13 @@
 // H = 2 a pair is reached from both sides and receives two trials, i.e. coupling 2K, exactly as
 // the doubled neighbour slots of the reference (J:564-574).
 //
-// Components are labelled in a scratch array (one int32 per site, the compact index of a site of
-// the same component) by lock-free union-find: hooking the larger root under the smaller with
+// Three forms flip the same cluster.  The default grows the seed's cluster breadth-first (one CTA
+// per lattice, only the bonds of the cluster and its boundary are tested; see the growth kernel
+// below).  The two labelling forms label every component and then flip the seed's; they are kept
+// as cross-checks and selectable by flags.
+//
+// Labelling: components are labelled in a scratch array (one int32 per site, the compact index
+// of a site of the same component) by lock-free union-find: hooking the larger root under the smaller with
 // atomicCAS, path halving in find, so every pointer goes to a smaller compact index and every
 // root is the smallest compact index of its component.  Then the seed's component is flipped.
 //
