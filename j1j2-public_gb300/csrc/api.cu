@@ -173,6 +173,16 @@ size_t smem_budget(Ctx* c)
     return (size_t)optin - 2048;  // static shared memory of the reduction
 }
 
+// CTA size of the shape-specialised kernel for a group whose lattices stay in HBM (0: the
+// generic global-memory kernel).  Like the shared-memory ones it counts no flips and handles no
+// bond dilution; the test flags GENERIC and NO_FIXED pin the generic kernel.
+int hbm_fixed_threads(const Ctx* c, const Group& grp, bool fp64)
+{
+    if ((c->P.flags & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED)) || c->diag.flip_counts)
+        return 0;
+    return fixed_hbm_threads(fp64, grp.g.L, grp.g.H, c->masks);
+}
+
 // Kernel shape for a group: the shape-specialised kernel when one exists for (precision, L, H)
 // and no bond is diluted (its CTA size autotuned at the first run unless block_threads names
 // one); else the generic CTA-per-lattice kernel with the lattice in shared memory (quad path when
@@ -249,8 +259,10 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
     if (smem > budget || (fl & J1J2C_FLAG_GLOBAL)) {
         v.global = true;
         v.stage_p = false;
+        v.fixed_nt = hbm_fixed_threads(c, grp, fp64);
+        v.rpt = grp.nrep % 4 == 0 ? 4 : grp.nrep % 2 == 0 ? 2 : 1;
         smem = 0;
-        nthreads = 256;
+        nthreads = v.fixed_nt > 0 ? v.fixed_nt : 256;
         return J1J2C_OK;
     }
     if (grp.block_threads > 0) {
@@ -480,39 +492,59 @@ int time_variant(Ctx* c, Group& grp, const SweepVariant& v, int nthreads, size_t
     return J1J2C_OK;
 }
 
-// Cluster path or one launch per colour phase for a lattice that does not fit one CTA: both are
-// timed and the faster kept, cached per (precision, L, H, lattice count, bond dilution).
-std::map<std::tuple<bool, int, int, int, bool>, bool> g_cluster_cache;
+// Cluster path or one launch per colour phase for a lattice that does not fit one CTA: the
+// cluster kernel and the HBM kernel (shape-specialised form with 1, 2 or 4 replicas per thread
+// where it exists, else the generic one) are timed and the fastest kept, cached per (precision,
+// L, H, lattice count, bond dilution, HBM kernel).  Choice: 0 cluster, -1 generic HBM kernel,
+// r > 0 shape-specialised HBM kernel with r replicas per thread.
+std::map<std::tuple<bool, int, int, int, bool, int>, int> g_cluster_cache;
 
 int tune_cluster(Ctx* c, Group& grp)
 {
-    const auto key = std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks);
-    bool use_cluster = true, known = false;
+    const int hbm_nt = hbm_fixed_threads(c, grp, grp.var.fp64);
+    const auto key =
+        std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks, hbm_nt);
+    int choice = 0;
+    bool known = false;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_cluster_cache.find(key);
         if (it != g_cluster_cache.end()) {
-            use_cluster = it->second;
+            choice = it->second;
             known = true;
         }
     }
     if (!known) {
+        float best_ms = 0.0f;
+        int rc = time_variant(c, grp, grp.var, grp.nthreads, grp.smem, best_ms);
+        if (rc != J1J2C_OK) return rc;
         SweepVariant vg = grp.var;
         vg.cluster = 0;
         vg.global = true;
-        float ms_c = 0.0f, ms_g = 0.0f;
-        int rc = time_variant(c, grp, grp.var, grp.nthreads, grp.smem, ms_c);
-        if (rc == J1J2C_OK) rc = time_variant(c, grp, vg, 256, 0, ms_g);
-        if (rc != J1J2C_OK) return rc;
-        use_cluster = ms_c <= ms_g;
+        vg.stage_p = false;
+        vg.fixed_nt = hbm_nt;
+        for (int r = 1; r <= (hbm_nt > 0 ? 4 : 1); r *= 2) {
+            if (grp.nrep % r) continue;
+            vg.rpt = r;
+            float ms = 0.0f;
+            rc = time_variant(c, grp, vg, hbm_nt > 0 ? hbm_nt : 256, 0, ms);
+            if (rc != J1J2C_OK) return rc;
+            if (ms < best_ms) {
+                best_ms = ms;
+                choice = hbm_nt > 0 ? r : -1;
+            }
+        }
         std::lock_guard<std::mutex> lk(g_tune_mu);
-        g_cluster_cache[key] = use_cluster;
+        g_cluster_cache[key] = choice;
     }
-    if (!use_cluster) {
+    if (choice != 0) {
         grp.var.cluster = 0;
         grp.var.global = true;
+        grp.var.stage_p = false;
+        grp.var.fixed_nt = choice > 0 ? hbm_nt : 0;
+        grp.var.rpt = choice > 0 ? choice : 1;
         grp.smem = 0;
-        grp.nthreads = 256;
+        grp.nthreads = choice > 0 ? hbm_nt : 256;
         free_graphs(c);
     }
     return J1J2C_OK;
@@ -620,6 +652,7 @@ int autotune(Ctx* c, Group& grp)
     grp.tuned = true;
     if (c->P.flags & J1J2C_FLAG_CLUSTER) return J1J2C_OK;
     if (grp.var.cluster > 0 && grp.block_threads == 0) return tune_cluster(c, grp);
+    if (grp.var.global && grp.var.fixed_nt > 0) return J1J2C_OK;
     if (grp.block_threads > 0) return J1J2C_OK;
     if (grp.var.fixed_nt == 0) return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
     int nts[8];

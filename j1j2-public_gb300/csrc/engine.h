@@ -126,9 +126,11 @@ struct SweepVariant {
     bool masks;    // bond dilution present
     int mode;      // kModeSweep / kModeAudit
     int fixed_nt;  // > 0: shape-specialised kernel with this many threads per CTA
-    bool global;   // lattice in HBM, one launch per colour phase (too large for shared memory)
+    bool global;   // lattice in HBM, one launch per colour phase (too large for shared memory;
+                   // with fixed_nt > 0 the shape-specialised form)
     bool vac;      // some conf has vacancies (shape-specialised kernels: vacancy handling on)
     int cluster;   // > 0: thread-block cluster of this many CTAs per lattice (distributed smem)
+    int rpt;       // shape-specialised HBM kernel: replicas per thread (1, 2 or 4)
 };
 
 // Global-memory path: one colour phase of sweep t of the cycle, and the observable reduction
@@ -150,6 +152,16 @@ int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, int* nts, bo
                      int cap);
 cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, int nt, int nblocks,
                          size_t smem, cudaStream_t st, bool prepare);
+
+// Shape-specialised kernels for lattices in HBM (one launch per colour phase): CTA size for a
+// shape (0: none), and one colour phase (colour >= 0) or the observable reduction (colour < 0,
+// added into a.obs, which the caller zeroes first).
+// With rpt = 2 or 4 each thread updates its quad in that many replicas of one configuration
+// (sharing the field loads); the launch falls back to 1 when the range is not whole
+// configurations or rpt does not divide the replica count.
+int fixed_hbm_threads(bool fp64, int L, int H, bool masks);
+cudaError_t launch_fixed_hbm(const SweepArgs& a, bool fp64, int colour, int t, int nlat, int rpt,
+                             cudaStream_t st);
 
 size_t sweep_smem_bytes(const Geo& g, const SweepVariant& v);
 cudaError_t prepare_sweep_variant(const SweepVariant& v, size_t smem);

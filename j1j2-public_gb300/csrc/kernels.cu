@@ -17,15 +17,6 @@ namespace cg = cooperative_groups;
 namespace j1j2 {
 namespace {
 
-template <class Real>
-__device__ __forceinline__ const Real* field_base(const SweepArgs& a, int conf)
-{
-    if constexpr (sizeof(Real) == 8)
-        return a.pd + (long long)conf * a.p_stride;
-    else
-        return a.pf + (long long)conf * a.p_stride;
-}
-
 // ------------------------------------------------------------------------------------------------
 // Per-site path (any even L, H): one site per thread per colour phase.
 // ------------------------------------------------------------------------------------------------
@@ -1128,6 +1119,7 @@ cudaError_t launch_sweep_cluster(const SweepArgs& a, const SweepVariant& v, int 
 cudaError_t launch_sweep_global(const SweepArgs& a, const SweepVariant& v, int colour, int t,
                                 int nlat, cudaStream_t st)
 {
+    if (v.fixed_nt > 0) return launch_fixed_hbm(a, v.fp64, colour, t, nlat, v.rpt, st);
     return v.fp64 ? global_dispatch<double>(a, v, colour, t, nlat, st, false)
                   : global_dispatch<float>(a, v, colour, t, nlat, st, false);
 }
@@ -1135,6 +1127,7 @@ cudaError_t launch_sweep_global(const SweepArgs& a, const SweepVariant& v, int c
 cudaError_t launch_measure_global(const SweepArgs& a, const SweepVariant& v, int nlat,
                                   cudaStream_t st)
 {
+    if (v.fixed_nt > 0) return launch_fixed_hbm(a, v.fp64, -1, 0, nlat, 1, st);
     return v.fp64 ? global_dispatch<double>(a, v, 0, 0, nlat, st, true)
                   : global_dispatch<float>(a, v, 0, 0, nlat, st, true);
 }

@@ -6,6 +6,16 @@
 
 namespace j1j2 {
 
+// random field of configuration conf (compact layout)
+template <class Real>
+__device__ __forceinline__ const Real* field_base(const SweepArgs& a, int conf)
+{
+    if constexpr (sizeof(Real) == 8)
+        return a.pd + (long long)conf * a.p_stride;
+    else
+        return a.pf + (long long)conf * a.p_stride;
+}
+
 struct Acc {
     long long e;  // fixed-point energy, sum of llrint(-s*field * 2^32)
     int M, SX, SY, NB;

@@ -65,36 +65,58 @@ struct QuadData {
     Real pown[4], pxa[4], pyp[4], pym[4], pextra;
 };
 
+// Neighbour rows of a quad for colour C's parities (J:540-584): odd parity steps +1, even -1
+template <int C>
+struct QuadRows {
+    int yp, ym, xn, yp_n, ym_n, zp, zm;
+    __device__ __forceinline__ explicit QuadRows(const QuadOff& o)
+    {
+        constexpr int px = C & 1, py = (C >> 1) & 1, pz = C >> 2;
+        yp = py ? o.yp : o.self;  // +y / -y rows, word qx
+        ym = py ? o.self : o.ym;
+        xn = px ? o.xp : o.xm;    // same row, shifted word
+        yp_n = py ? (px ? o.yp_xp : o.yp_xm) : xn;
+        ym_n = py ? xn : (px ? o.ym_xp : o.ym_xm);
+        zp = pz ? o.zp : o.self;
+        zm = pz ? o.self : o.zm;
+    }
+};
+
+// Spin words of a quad and its neighbours
 template <class Real, int LH, int HH, int C>
-__device__ __forceinline__ QuadData<Real> load_quad(const uint32_t* S32, const Real* P,
-                                                    const QuadOff& o)
+__device__ __forceinline__ void load_quad_spins(const uint32_t* S32, const QuadOff& o,
+                                                QuadData<Real>& d)
 {
     using Sh = Shape<LH, HH>;
-    constexpr int px = C & 1, py = (C >> 1) & 1, pz = C >> 2;
+    constexpr int px = C & 1;
     constexpr int B0 = C * Sh::CS, B1 = (C ^ 1) * Sh::CS, B2 = (C ^ 2) * Sh::CS;
     constexpr int B3 = (C ^ 3) * Sh::CS, B4 = (C ^ 4) * Sh::CS;
-    // neighbour rows for this colour's parities (J:540-584): odd parity steps +1, even -1
-    const int rYp = py ? o.yp : o.self, rYm = py ? o.self : o.ym;  // +y / -y rows, word qx
-    const int xn = px ? o.xp : o.xm;                                 // same row, shifted word
-    const int rYp_n = py ? (px ? o.yp_xp : o.yp_xm) : xn;
-    const int rYm_n = py ? xn : (px ? o.ym_xp : o.ym_xm);
-    const int rZp = pz ? o.zp : o.self, rZm = pz ? o.self : o.zm;
-
-    QuadData<Real> d;
+    const QuadRows<C> r(o);
     d.self = o.self;
     d.own = S32[B0 + o.self];
-    x_pair(px, S32[B1 + o.self], S32[B1 + xn], d.wxp, d.wxm);
-    d.wyp = S32[B2 + rYp];
-    d.wym = S32[B2 + rYm];
-    x_pair(px, S32[B3 + rYp], S32[B3 + rYp_n], d.wdpp, d.wdpm);
-    x_pair(px, S32[B3 + rYm], S32[B3 + rYm_n], d.wdmp, d.wdmm);
-    d.wzp = S32[B4 + rZp];
-    d.wzm = S32[B4 + rZm];
-    d.pextra = P[4 * (B1 + xn) + (px ? 0 : 3)];
+    x_pair(px, S32[B1 + o.self], S32[B1 + r.xn], d.wxp, d.wxm);
+    d.wyp = S32[B2 + r.yp];
+    d.wym = S32[B2 + r.ym];
+    x_pair(px, S32[B3 + r.yp], S32[B3 + r.yp_n], d.wdpp, d.wdpm);
+    x_pair(px, S32[B3 + r.ym], S32[B3 + r.ym_n], d.wdmp, d.wdmm);
+    d.wzp = S32[B4 + r.zp];
+    d.wzm = S32[B4 + r.zm];
+}
+
+// Random-field values of a quad and of its +-x and +-y neighbours
+template <class Real, int LH, int HH, int C>
+__device__ __forceinline__ void load_quad_field(const Real* P, const QuadOff& o,
+                                                QuadData<Real>& d)
+{
+    using Sh = Shape<LH, HH>;
+    constexpr int px = C & 1;
+    constexpr int B0 = C * Sh::CS, B1 = (C ^ 1) * Sh::CS, B2 = (C ^ 2) * Sh::CS;
+    const QuadRows<C> r(o);
+    d.pextra = P[4 * (B1 + r.xn) + (px ? 0 : 3)];
     if constexpr (sizeof(Real) == 4) {
         const float4* P4 = reinterpret_cast<const float4*>(P);
         const float4 v0 = P4[B0 + o.self], v1 = P4[B1 + o.self];
-        const float4 v2 = P4[B2 + rYp], v3 = P4[B2 + rYm];
+        const float4 v2 = P4[B2 + r.yp], v3 = P4[B2 + r.ym];
         d.pown[0] = v0.x, d.pown[1] = v0.y, d.pown[2] = v0.z, d.pown[3] = v0.w;
         d.pxa[0] = v1.x, d.pxa[1] = v1.y, d.pxa[2] = v1.z, d.pxa[3] = v1.w;
         d.pyp[0] = v2.x, d.pyp[1] = v2.y, d.pyp[2] = v2.z, d.pyp[3] = v2.w;
@@ -104,13 +126,22 @@ __device__ __forceinline__ QuadData<Real> load_quad(const uint32_t* S32, const R
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const double2 v0 = P2[2 * (B0 + o.self) + h], v1 = P2[2 * (B1 + o.self) + h];
-            const double2 v2 = P2[2 * (B2 + rYp) + h], v3 = P2[2 * (B2 + rYm) + h];
+            const double2 v2 = P2[2 * (B2 + r.yp) + h], v3 = P2[2 * (B2 + r.ym) + h];
             d.pown[2 * h] = v0.x, d.pown[2 * h + 1] = v0.y;
             d.pxa[2 * h] = v1.x, d.pxa[2 * h + 1] = v1.y;
             d.pyp[2 * h] = v2.x, d.pyp[2 * h + 1] = v2.y;
             d.pym[2 * h] = v3.x, d.pym[2 * h + 1] = v3.y;
         }
     }
+}
+
+template <class Real, int LH, int HH, int C>
+__device__ __forceinline__ QuadData<Real> load_quad(const uint32_t* S32, const Real* P,
+                                                    const QuadOff& o)
+{
+    QuadData<Real> d;
+    load_quad_spins<Real, LH, HH, C>(S32, o, d);
+    load_quad_field<Real, LH, HH, C>(P, o, d);
     return d;
 }
 
@@ -336,11 +367,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_fixed_kernel(SweepArgs a)
     uint8_t* S = smem;
     Real* Ps = reinterpret_cast<Real*>(smem + Sh::NB);
     uint8_t* Sg = a.spins + (long long)lat * a.lat_stride;
-    const Real* Pg;
-    if constexpr (sizeof(Real) == 8)
-        Pg = a.pd + (long long)conf * a.p_stride;
-    else
-        Pg = a.pf + (long long)conf * a.p_stride;
+    const Real* Pg = field_base<Real>(a, conf);
 
     block_copy16(S, Sg, Sh::NB);
     if constexpr (STAGE_P)
@@ -427,6 +454,159 @@ bool usable(const FixedEntry& e, bool fp64, int L, int H, bool vac)
     return true;
 }
 
+// ---- lattices in HBM --------------------------------------------------------------------------
+// Lattices too large for one CTA's shared memory (L = 96: 864 KiB of spins) keep spins and field
+// in HBM / L2 and run one launch per colour phase; the kernel boundary is the barrier between
+// colours.  One thread per quad with the same compile-time offsets, operand loads and arithmetic
+// as the shared-memory kernel above, so the results are those of every other kernel bit for bit.
+// Grid: (quads of a colour / NT, lattices).
+// One colour phase of quad o in RPT replicas of one configuration: the field operands are loaded
+// once and shared, the spin operands of every replica are loaded before any is updated.
+template <class Real, int LH, int HH, int C, int RPT, bool VAC>
+__device__ __forceinline__ void hbm_phase(const SweepArgs& a, const Real* P, const QuadOff& o,
+                                          int lat, int conf, int rep, uint32_t sweep,
+                                          uint32_t k0, uint32_t k1)
+{
+    QuadData<Real> d[RPT];
+    load_quad_field<Real, LH, HH, C>(P, o, d[0]);
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+        if (r > 0) d[r] = d[0];
+        load_quad_spins<Real, LH, HH, C>(
+            reinterpret_cast<const uint32_t*>(a.spins + (long long)(lat + r) * a.lat_stride), o,
+            d[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+        const double beta = a.use_override
+                                ? a.beta_override
+                                : a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep + r]];
+        const float kb = (float)(-2.0 * beta * 1.4426950408889634);
+        Acc none{0, 0, 0, 0, 0};
+        compute_quad<Real, LH, HH, C, false, VAC>(
+            a, reinterpret_cast<uint32_t*>(a.spins + (long long)(lat + r) * a.lat_stride), d[r],
+            sweep, (uint32_t)(rep + r), k0, k1, beta, kb, none);
+    }
+}
+
+// Grid: (quads of a colour / NT, lattices / RPT); with RPT > 1 the launcher guarantees that the
+// RPT lattices of a block row are replicas of one configuration.
+template <class Real, int LH, int HH, int NT, int RPT, bool VAC>
+__global__ void __launch_bounds__(NT) sweep_fixed_hbm_kernel(SweepArgs a, int colour, int t)
+{
+    using Sh = Shape<LH, HH>;
+    const int q = (int)(blockIdx.x * NT + threadIdx.x);
+    if (q >= Sh::CS) return;
+    const int lat = a.lat0 + (int)blockIdx.y * RPT;
+    const int conf = lat / a.nrep;
+    const int rep = lat - conf * a.nrep;
+    const Real* P = field_base<Real>(a, conf);
+    const uint32_t sweep = (a.use_override ? a.sweep_override
+                                           : a.ctl[0] * (uint32_t)a.ptswapever) + (uint32_t)t;
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    const QuadOff o = quad_offsets<LH, HH>(q);
+    switch (colour) {
+#define J1J2_HBM_PHASE(C)                                                                     \
+    case C:                                                                                   \
+        hbm_phase<Real, LH, HH, C, RPT, VAC>(a, P, o, lat, conf, rep, sweep, k0, k1);         \
+        break;
+        J1J2_HBM_PHASE(0)
+        J1J2_HBM_PHASE(1)
+        J1J2_HBM_PHASE(2)
+        J1J2_HBM_PHASE(3)
+        J1J2_HBM_PHASE(4)
+        J1J2_HBM_PHASE(5)
+        J1J2_HBM_PHASE(6)
+        J1J2_HBM_PHASE(7)
+#undef J1J2_HBM_PHASE
+        default:
+            break;
+    }
+}
+
+// Observables: one thread per quad, grid.z = colour; per-CTA sums are added into the lattice's
+// (zeroed) observables with atomics (integer sums: order-independent).
+template <class Real, int LH, int HH, int NT, bool VAC>
+__global__ void __launch_bounds__(NT) measure_fixed_hbm_kernel(SweepArgs a)
+{
+    using Sh = Shape<LH, HH>;
+    const int q = (int)(blockIdx.x * NT + threadIdx.x);
+    const int lat = a.lat0 + (int)blockIdx.y;
+    const int conf = lat / a.nrep;
+    uint32_t* S32 = reinterpret_cast<uint32_t*>(a.spins + (long long)lat * a.lat_stride);
+    const Real* P = field_base<Real>(a, conf);
+    Acc acc{0, 0, 0, 0, 0};
+    if (q < Sh::CS) {
+        const QuadOff o = quad_offsets<LH, HH>(q);
+        switch (blockIdx.z) {
+#define J1J2_HBM_MEASURE(C)                                                                    \
+    case C: {                                                                                  \
+        const QuadData<Real> d = load_quad<Real, LH, HH, C>(S32, P, o);                        \
+        compute_quad<Real, LH, HH, C, true, VAC>(a, S32, d, 0u, 0u, 0u, 0u, 0.0, 0.0f, acc);   \
+        break;                                                                                 \
+    }
+            J1J2_HBM_MEASURE(0)
+            J1J2_HBM_MEASURE(1)
+            J1J2_HBM_MEASURE(2)
+            J1J2_HBM_MEASURE(3)
+            J1J2_HBM_MEASURE(4)
+            J1J2_HBM_MEASURE(5)
+            J1J2_HBM_MEASURE(6)
+            J1J2_HBM_MEASURE(7)
+#undef J1J2_HBM_MEASURE
+            default:
+                break;
+        }
+    }
+    const Acc tot = block_reduce(acc);
+    if (threadIdx.x == 0) {
+        LatObs* ob = a.obs + lat;
+        atomicAdd(reinterpret_cast<unsigned long long*>(&ob->eacc), (unsigned long long)tot.e);
+        atomicAdd(&ob->M, tot.M);
+        atomicAdd(&ob->SX, tot.SX);
+        atomicAdd(&ob->SY, tot.SY);
+        atomicAdd(&ob->NB, tot.NB);
+    }
+}
+
+template <class Real, int LH, int HH, int NT>
+cudaError_t run_hbm(const SweepArgs& a, int colour, int t, int nlat, int rpt, cudaStream_t st)
+{
+    constexpr int CS = Shape<LH, HH>::CS;
+    const unsigned gx = (unsigned)((CS + NT - 1) / NT);
+    if (colour < 0) {
+        measure_fixed_hbm_kernel<Real, LH, HH, NT, true>
+            <<<dim3(gx, (unsigned)nlat, 8u), NT, 0, st>>>(a);
+    } else if (rpt == 4) {
+        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 4, true>
+            <<<dim3(gx, (unsigned)(nlat / 4)), NT, 0, st>>>(a, colour, t);
+    } else if (rpt == 2) {
+        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 2, true>
+            <<<dim3(gx, (unsigned)(nlat / 2)), NT, 0, st>>>(a, colour, t);
+    } else {
+        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 1, true>
+            <<<dim3(gx, (unsigned)nlat), NT, 0, st>>>(a, colour, t);
+    }
+    return cudaGetLastError();
+}
+
+using HbmFn = cudaError_t (*)(const SweepArgs&, int, int, int, int, cudaStream_t);
+
+struct HbmEntry {
+    bool fp64;
+    int L, H, nt;
+    HbmFn fn;
+};
+
+// L = 96 (the reference's largest configuration) and L = 32 (a cheap cross-check of the same
+// code against the shared-memory kernels); vacancy handling always on.
+const HbmEntry kHbm[] = {
+    {false, 96, 96, 256, run_hbm<float, 48, 48, 256>},
+    {true, 96, 96, 256, run_hbm<double, 48, 48, 256>},
+    {false, 32, 32, 256, run_hbm<float, 16, 16, 256>},
+    {true, 32, 32, 256, run_hbm<double, 16, 16, 256>},
+};
+
 }  // namespace
 
 int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, int* nts, bool* stage_p,
@@ -449,6 +629,27 @@ cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, int nt, int nb
     for (const auto& e : kFixed)
         if (usable(e, fp64, a.g.L, a.g.H, vac) && e.nt == nt)
             return e.fn(a, nblocks, smem, st, prepare);
+    return cudaErrorInvalidValue;
+}
+
+int fixed_hbm_threads(bool fp64, int L, int H, bool masks)
+{
+    if (masks) return 0;
+    for (const auto& e : kHbm)
+        if (e.fp64 == fp64 && e.L == L && e.H == H) return e.nt;
+    return 0;
+}
+
+cudaError_t launch_fixed_hbm(const SweepArgs& a, bool fp64, int colour, int t, int nlat, int rpt,
+                             cudaStream_t st)
+{
+    // replicas per thread only over whole configurations (RPT lattices of one block row share
+    // their configuration's field)
+    if (rpt > 1 && (a.nrep % rpt != 0 || a.lat0 % a.nrep != 0 || nlat % a.nrep != 0)) rpt = 1;
+    if (rpt != 2 && rpt != 4) rpt = 1;
+    for (const auto& e : kHbm)
+        if (e.fp64 == fp64 && e.L == a.g.L && e.H == a.g.H)
+            return e.fn(a, colour, t, nlat, rpt, st);
     return cudaErrorInvalidValue;
 }
 

@@ -65,6 +65,31 @@ def test_wolff_step_bit_identical(engine_mod, oracle, L, H, pp, bonds, flags):
     eng.close()
 
 
+@pytest.mark.parametrize("nconf", [40, 80])
+def test_wolff_growth_many_lattices(engine_mod, oracle, nconf):
+    """More lattices than SMs (160 and 320 lattices: two and three waves of growth CTAs, coldest
+    slots first): the flipped clusters equal the oracle's in the first, middle and last
+    configuration."""
+    jc = engine_mod
+    L, H, nrep = 16, 16, 4
+    eng, dis, betas = _engine(jc, L, H, nconf, nrep, jc.FP64_PLAIN, 0, 0.05)
+    eng.run(2, measure=False)
+    check = (0, nconf // 2, nconf - 1)
+    before = {(k, r): eng.spins(k, r).copy() for k in check for r in range(nrep)}
+    tors = {k: eng.maps(k)[1] for k in check}
+    sizes = eng.wolff()
+    assert len(sizes) == nconf * nrep and sizes.sum() > 0
+    for k in check:
+        p, occu, _, _ = dis[k]
+        M = oracle.Model(L, H, p, occu)
+        for r in range(nrep):
+            s = before[(k, r)].copy()
+            n = M.wolff_step(s, betas[tors[k][r]], SEED, k, r, 2)
+            np.testing.assert_array_equal(eng.spins(k, r), s)
+            assert sizes[nrep * k + r] == n
+    eng.close()
+
+
 @pytest.mark.parametrize("L,H,pp,bonds", [(96, 8, 0.1, 0.2), (48, 48, 0.05, 0.0),
                                           (32, 32, 0.0, 0.0), (160, 4, 0.05, 0.0)])
 def test_wolff_fp32_forms_agree(engine_mod, oracle, L, H, pp, bonds):

@@ -56,6 +56,7 @@ def test_hot_start_is_the_philox_stream(engine_mod, oracle, L, H):
     (12, 6, 0.05, 0.1, 0),      # per-site path with dilution
     (16, 8, 0.05, 0.0, 4),      # per-site path forced on a quad-capable shape
     (24, 24, 0.0, 0.0, 0),      # config-2 lattice
+    (32, 32, 0.05, 0.0, 16),    # shape-specialised kernel on lattices in HBM
 ])
 def test_fp64_sweep_bit_identical_to_replay(engine_mod, oracle, L, H, pp, bonds, flags):
     jc = engine_mod
@@ -85,6 +86,8 @@ def test_fp64_sweep_bit_identical_to_replay(engine_mod, oracle, L, H, pp, bonds,
     (16, 4, 1, 1, 0.0, 0),  # LOCAL sampler: one replica, no swaps
     (24, 24, 1, 2, 0.0, 0),  # shape-specialised FP64 kernel (config-2 lattice)
     (8, 4, 3, 4, 0.1, 16),   # global-memory path
+    (32, 32, 1, 2, 0.05, 16),  # shape-specialised kernel on lattices in HBM
+    (32, 32, 1, 2, 0.05, 24),  # generic global-memory kernel on the same shape
 ])
 def test_fp64_pt_run_bit_identical_to_replay(engine_mod, oracle, L, H, nconf, nrep, pp, flags):
     jc = engine_mod
@@ -142,7 +145,8 @@ def test_specialised_kernels_agree_bitwise(engine_mod, oracle, precision, L):
     nts = {16: [128, 64], 24: [448, 224], 32: [1024, 512]}[L] if precision == 1 else \
         {24: [448], 32: [512]}[L]
     runs = []
-    for flags, bt in [(jc.FLAG_NO_FIXED, 0), (jc.FLAG_GENERIC, 0), (jc.FLAG_GLOBAL, 0)] + \
+    for flags, bt in [(jc.FLAG_NO_FIXED, 0), (jc.FLAG_GENERIC, 0), (jc.FLAG_GLOBAL, 0),
+                      (jc.FLAG_GLOBAL | jc.FLAG_NO_FIXED, 0)] + \
             [(0, nt) for nt in nts]:
         eng = jc.Engine(L, L, nconf=2, nreplica=3, precision=precision, seed=SEED, flags=flags,
                         block_threads=bt)
@@ -331,6 +335,69 @@ def test_cluster_path_fp32_equals_global_path(engine_mod, oracle, pp, bonds):
     for a, b in zip(out[0][1], out[1][1]):
         np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("precision,nrep", [(0, 4), (1, 4), (1, 2), (1, 3)])
+def test_hbm_kernel_replicas_per_thread(engine_mod, oracle, precision, nrep):
+    """The HBM kernel with 4, 2 or 1 replicas per thread (chosen from the replica count under
+    the global-memory flag) against the shared-memory kernel: bitwise equal, 32^3 with
+    vacancies."""
+    jc = engine_mod
+    out = []
+    for flags in (0, jc.FLAG_GLOBAL):
+        eng, _, _ = _setup(jc, oracle, 32, 32, 2, nrep, precision, pp=0.05, flags=flags)
+        eng.run(2, measure=False)
+        eng.run(3, measure=True)
+        out.append(([eng.spins(k, r) for k in range(2) for r in range(nrep)],
+                    eng.slot_sums(-1)[0], eng.observables(-1), eng.config()["smem_bytes"]))
+        eng.close()
+    assert out[0][3] > 0 and out[1][3] == 0
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    np.testing.assert_array_equal(out[0][2], out[1][2])
+
+
+def test_hbm_kernel_L96_fp64_bit_identical_to_replay(engine_mod, oracle):
+    """96^3 with 5 % vacancies (the reference's largest configuration) through the shape-
+    specialised kernel that keeps lattices in HBM: spins, maps and running sums equal the replay."""
+    jc = engine_mod
+    L, nrep = 96, 2
+    eng, models, betas = _setup(jc, oracle, L, L, 1, nrep, jc.FP64_PLAIN, pp=0.05,
+                                flags=jc.FLAG_GLOBAL)
+    assert eng.config()["smem_bytes"] == 0 and eng.config()["block_threads"] == 256
+    st = oracle.new_pt_state(np.stack([eng.spins(0, r) for r in range(nrep)]))
+    eng.run(1, measure=False, restart_swap_phase=True)
+    eng.reset_measurements()
+    eng.run(2, measure=True, restart_swap_phase=True)
+    M = models[0]
+    M.replay_pt(st, betas, 5, 1, 0, SEED, 0, False, 1)
+    obs = M.replay_pt(st, betas, 5, 2, 1, SEED, 0, True, 1)
+    for r in range(nrep):
+        np.testing.assert_array_equal(eng.spins(0, r), st["spins"][r])
+    np.testing.assert_array_equal(eng.slot_sums(0)[0], st["sums"])
+    np.testing.assert_array_equal(eng.maps(0)[0], st["rep_at_temp"])
+    np.testing.assert_array_equal(eng.observables(0), obs)
+    eng.close()
+
+
+def test_hbm_kernel_L96_fp32_equals_other_paths(engine_mod, oracle):
+    """FP32 96^3 with vacancies: the shape-specialised HBM kernel, the generic global-memory
+    kernel and the default choice (thread-block cluster or HBM kernel, whichever the autotuner
+    keeps) give bitwise equal spins, sums and observables."""
+    jc = engine_mod
+    out = []
+    for flags in (jc.FLAG_GLOBAL, jc.FLAG_GLOBAL | jc.FLAG_NO_FIXED, 0):
+        eng, _, _ = _setup(jc, oracle, 96, 96, 1, 3, jc.FP32_BATCHED, pp=0.05, flags=flags)
+        eng.run(2, measure=True)
+        out.append(([eng.spins(0, r) for r in range(3)], eng.slot_sums(0)[0],
+                    eng.observables(-1)))
+        eng.close()
+    for other in out[1:]:
+        for a, b in zip(out[0][0], other[0]):
+            np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(out[0][1], other[1])
+        np.testing.assert_array_equal(out[0][2], other[2])
 
 
 @pytest.mark.parametrize("L,H,nconf,nrep,pp", [(24, 24, 1, 16, 0.0), (16, 16, 1, 1, 0.05),
