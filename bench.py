@@ -55,7 +55,10 @@ WORKLOADS = {
     "large_L96_vac5_wolff_1x48": dict(groups=[(96, 1, 48)], precision=1, vacancies=0.05,
                                       wolff=True),
     # L=16 single-temperature local Metropolis (T=9.5, one sweep + measurement per cycle), FP64
-    "local_fp64_L16_T9.5": dict(groups=[(16, 1, 1)], precision=0, ptswapever=1, T=9.5),
+    # LOCAL: one sweep + measurement per cycle, 100 back-to-back cycles per step (a LOCAL run of
+    # the reference is 10^4 + 10^4 such sweeps in one call)
+    "local_fp64_L16_T9.5": dict(groups=[(16, 1, 1)], precision=0, ptswapever=1, T=9.5,
+                                cycles_per_step=100),
 }
 
 
@@ -170,9 +173,9 @@ def attempts_per_cycle(eng):
     return int((eng.nocc * reps).sum()) * eng.ptswapever
 
 
-def time_steps(torch, eng, steps, warmup, flush):
-    """Device time of `steps` PT cycles (CUDA events on the engine's stream), L2 flushed
-    before every step outside the timed interval."""
+def time_steps(torch, eng, steps, warmup, flush, cycles=1):
+    """Device time of `steps` steps of `cycles` PT cycles each (CUDA events on the engine's
+    stream), L2 flushed before every step outside the timed interval."""
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
     eng.run(warmup, measure=True, restart_swap_phase=True)
@@ -184,7 +187,7 @@ def time_steps(torch, eng, steps, warmup, flush):
     for k in range(steps):
         flush.zero_()
         ev[k][0].record(stream)
-        eng.run(1, measure=True, restart_swap_phase=False)
+        eng.run(cycles, measure=True, restart_swap_phase=False)
         ev[k][1].record(stream)
     torch.cuda.synchronize()
     for a, b in ev:
@@ -195,12 +198,15 @@ def time_steps(torch, eng, steps, warmup, flush):
 def time_workload(torch, jc, w, device, flush, steps):
     """Device throughput of one workload (CUDA events per PT cycle, L2 flushed between)."""
     eng, _ = make_engine(jc, w, device, flags=jc.FLAG_PROFILE)
-    ms, prof_ms = time_steps(torch, eng, steps, 3, flush)
-    att = attempts_per_cycle(eng)
+    cycles = w.get("cycles_per_step", 1)
+    ms, prof_ms = time_steps(torch, eng, steps, 3, flush, cycles)
+    att = attempts_per_cycle(eng) * cycles
     out = {"value": round(att * steps / (ms * 1e6), 4), "unit": UNIT,
            "ms_per_step": round(ms / steps, 4), "steps": steps, "attempts_per_step": att,
            "sweep_ms_per_step": round(prof_ms / steps, 4),
            "groups_L_nconf_nreplica": [list(g) for g in w["groups"]]}
+    if cycles > 1:
+        out["cycles_per_step"] = cycles
     cfg = eng.config()
     out["block_threads"] = cfg["block_threads"]
     eng.close()
@@ -219,7 +225,7 @@ def secondary_workloads(torch, jc, device, flush, steps):
         per_l[str(L)] = time_workload(torch, jc, w, device, flush, steps)["value"]
     res["mixed_L16_24_32_48"]["per_L_alone"] = per_l
     res["local_fp64_L16_T9.5"] = time_workload(torch, jc, WORKLOADS["local_fp64_L16_T9.5"],
-                                               device, flush, 4 * steps)
+                                               device, flush, steps)
     return res
 
 
@@ -240,13 +246,14 @@ def run_ours(args):
     nconf = sum(n for _, n, _ in w["groups"])
     eng, betas = make_engine(jc, w, local, conf_base=conf_base_of(rank, w), flags=jc.FLAG_PROFILE)
     cfg = eng.config()
-    attempts_per_step = attempts_per_cycle(eng)
+    cycles = w.get("cycles_per_step", 1)
+    attempts_per_step = attempts_per_cycle(eng) * cycles
 
     if ws > 1:
         dist.barrier()
     torch.cuda.synchronize()
     with Clocks(local) as clk:
-        total_ms, prof_ms = time_steps(torch, eng, args.steps, args.warmup, flush)
+        total_ms, prof_ms = time_steps(torch, eng, args.steps, args.warmup, flush, cycles)
     torch.cuda.synchronize()
     if ws > 1:
         total_ms = max_over_ranks(dist, total_ms, "cuda")
@@ -266,7 +273,7 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         eng.set_ladder(-1, h_betas)
-        eng.run(1, measure=True, restart_swap_phase=False)
+        eng.run(cycles, measure=True, restart_swap_phase=False)
         sums, nm = eng.slot_sums(-1, out=h_sums)
         obs = eng.observables(-1, out=h_obs)
     e2e_s = time.perf_counter() - t0
