@@ -550,6 +550,20 @@ int tune_cluster(Ctx* c, Group& grp)
     return J1J2C_OK;
 }
 
+// Generic global-memory kernels, one site per thread, nt threads per CTA
+SweepVariant global_site_variant(const Ctx* c, bool fp64, int nt)
+{
+    SweepVariant v{};
+    v.fp64 = fp64;
+    v.masks = c->masks;
+    v.vac = c->vac;
+    v.mode = kModeSweep;
+    v.global = true;
+    v.rpt = 1;
+    v.global_nt = nt;
+    return v;
+}
+
 // The small-batch search applies to the default kernel choice only (the test flags pin a path)
 bool small_batch_ok(Ctx* c, const Group& grp)
 {
@@ -570,7 +584,9 @@ int tune_small_batch(Ctx* c, Group& grp)
     if (2 * grp.nlat() > nsm) return J1J2C_OK;
     const auto key =
         std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks, c->vac);
-    int best = -1;  // after the search: 0 keep, -2 one site per thread, > 0 cluster size
+    // after the search: 0 keep, -2 one site per thread, > 0 cluster size, <= -100 one launch
+    // per colour phase with one site per thread and -(best + 100) threads per CTA
+    int best = -1;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_small_cache.find(key);
@@ -622,6 +638,19 @@ int tune_small_batch(Ctx* c, Group& grp)
                 }
             }
         }
+        // one launch per colour phase, one site per thread, small CTAs: the colour phase of a
+        // handful of lattices spread over many SMs (the FP64 form is bound by each SM's FP64
+        // rate, so the sites per SM, not per lattice, set its time)
+        for (int nt = 32; nt <= 256; nt *= 2) {
+            SweepVariant v = global_site_variant(c, grp.var.fp64, nt);
+            float ms = 0.0f;
+            rc = time_variant(c, grp, v, nt, 0, ms);
+            if (rc != J1J2C_OK) return rc;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = -(100 + nt);
+            }
+        }
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_small_cache[key] = best;
     }
@@ -632,6 +661,11 @@ int tune_small_batch(Ctx* c, Group& grp)
         grp.var.stage_p = false;
         grp.smem = (size_t)grp.g.N / (size_t)best;
         grp.nthreads = 512;
+        free_graphs(c);
+    } else if (best <= -100) {
+        grp.var = global_site_variant(c, grp.var.fp64, -(best + 100));
+        grp.smem = 0;
+        grp.nthreads = -(best + 100);
         free_graphs(c);
     } else if (best == -2) {
         const uint32_t keep = c->P.flags;

@@ -162,28 +162,33 @@ struct Nbr64 {
     int jv_own, jv_m2, jh_own, jh_m4;
 };
 
+// s * c for a spin s in {-1, 0, +1}: the product is exact, so it is a selection rather than an
+// FP64 multiplication (GB300's FP64 rate is 2 operations per clock per SM).  A vacancy's zero is
+// +0; since no partial sum is -0, adding it leaves the sum as IEEE multiplication's signed zero
+// would.
+__device__ __forceinline__ double spin_mul(int s, double c)
+{
+    return s > 0 ? c : (s < 0 ? -c : 0.0);
+}
+
 __device__ __forceinline__ double field_fp64(const Nbr64& n, double pi, double J1h, double J1v,
                                              double J2, double J3, double* nem_out)
 {
-    double f = 0.0, nm = 0.0;
-    const double s1 = (double)n.s[0], s2 = (double)n.s[1], s3 = (double)n.s[2],
-                 s4 = (double)n.s[3];
-    f = __dadd_rn(f, n.jv_own ? __dmul_rn(s1, J1v) : 0.0);
-    nm = __dsub_rn(nm, s1);
-    f = __dsub_rn(f, __dmul_rn(n.p1, s1));
-    f = __dadd_rn(f, n.jv_m2 ? __dmul_rn(s2, J1v) : 0.0);
-    nm = __dsub_rn(nm, s2);
-    f = __dsub_rn(f, __dmul_rn(n.p2, s2));
-    f = __dadd_rn(f, n.jh_own ? __dmul_rn(s3, J1h) : 0.0);
-    nm = __dadd_rn(nm, s3);
-    f = __dadd_rn(f, __dmul_rn(n.p3, s3));
-    f = __dadd_rn(f, n.jh_m4 ? __dmul_rn(s4, J1h) : 0.0);
-    nm = __dadd_rn(nm, s4);
-    f = __dadd_rn(f, __dmul_rn(n.p4, s4));
+    double f = 0.0;
+    f = __dadd_rn(f, n.jv_own ? spin_mul(n.s[0], J1v) : 0.0);
+    f = __dsub_rn(f, spin_mul(n.s[0], n.p1));
+    f = __dadd_rn(f, n.jv_m2 ? spin_mul(n.s[1], J1v) : 0.0);
+    f = __dsub_rn(f, spin_mul(n.s[1], n.p2));
+    f = __dadd_rn(f, n.jh_own ? spin_mul(n.s[2], J1h) : 0.0);
+    f = __dadd_rn(f, spin_mul(n.s[2], n.p3));
+    f = __dadd_rn(f, n.jh_m4 ? spin_mul(n.s[3], J1h) : 0.0);
+    f = __dadd_rn(f, spin_mul(n.s[3], n.p4));
 #pragma unroll
-    for (int k = 4; k < 8; ++k) f = __dadd_rn(f, __dmul_rn((double)n.s[k], J2));
+    for (int k = 4; k < 8; ++k) f = __dadd_rn(f, spin_mul(n.s[k], J2));
 #pragma unroll
-    for (int k = 8; k < 10; ++k) f = __dadd_rn(f, __dmul_rn((double)n.s[k], J3));
+    for (int k = 8; k < 10; ++k) f = __dadd_rn(f, spin_mul(n.s[k], J3));
+    // the nematic sum -s1 - s2 + s3 + s4 is an exact small integer in any order
+    const double nm = (double)(n.s[2] + n.s[3] - n.s[0] - n.s[1]);
     f = __dadd_rn(f, __dmul_rn(pi, nm));
     if (nem_out) *nem_out = nm;
     return f;
@@ -244,30 +249,47 @@ __device__ __forceinline__ float ex2_approx(float x)
     return y;
 }
 
-// FP64 Metropolis test u < own_exp(x) (x <= 0), decided from an FP32 estimate of exp(x) unless u
-// lies inside the estimate's error band, where own_exp decides: the result is exactly that of
-// u < own_exp(x).  Error of the estimate 2^(x log2e) for -80 <= x <= 0 (no FP32 underflow):
-// rounding x and the product to FP32 shifts the exponent by at most |x| (2^-24 + 2^-23), and the
-// SFU's ex2 is taken at 2^-20 relative (above its documented accuracy); the band
-// e (|x| 2^-20 + 2^-18) is four times the sum.
-__device__ __forceinline__ bool accept_fp64(double u, double x)
-{
-    if (x >= -80.0) {
-        const float xf = __double2float_rn(x);
-        const float e = ex2_approx(__fmul_rn(xf, 1.44269504f));
-        const float band = __fmul_rn(e, __fmaf_rn(fabsf(xf), 0x1p-20f, 0x1p-18f));
-        if (u < (double)__fsub_rn(e, band)) return true;
-        if (u > (double)__fadd_rn(e, band)) return false;
-    }
-    return u < own_exp(x);
-}
-
 // FP64 uniform in [0, 1) from a Philox word: the word rotated left by 9 bits, times 2^-32.  Its
 // top 23 bits are the word's low 23 bits, i.e. exactly the FP32 uniform below, so both forms
 // test the same random number (to 2^-23) in the deterministic FP32-vs-FP64 replay.
 __host__ __device__ __forceinline__ double u01_f64(uint32_t r)
 {
     return (double)((r << 9) | (r >> 23)) * 0x1p-32;
+}
+
+// FP64 Metropolis test u < own_exp(x) for u = u01_f64(r) and x < 0, decided from an FP32
+// estimate of exp(x) unless u lies inside the estimate's error band, where own_exp decides: the
+// result is exactly that of u01_f64(r) < own_exp(x).  Error of the estimate 2^(x log2e) for
+// -80 <= x <= 0 (no FP32 underflow; the cut is taken on x rounded to FP32, which moves it by
+// 2^-18 at most): rounding x and the product to FP32 shifts the exponent by at most
+// |x| (2^-24 + 2^-23), and the SFU's ex2 is taken at 2^-20 relative (above its documented
+// accuracy); the band e (|x| 2^-20 + 2^-18) is four times the sum.  The comparisons with the
+// band's ends need no FP64 arithmetic (GB300 runs 2 FP64 operations per clock per SM): u is the
+// integer v = rotl(r, 9) times 2^-32, and for a float y >= 0 (y 2^32 exact in FP32)
+// u < y  <=>  v < ceil(y 2^32)  and  u > y  <=>  v > floor(y 2^32); the conversions saturate
+// at 2^32 - 1, where the first test is settled by y >= 1 beforehand and the second is false, as
+// u > y is for y >= 1.
+__device__ __forceinline__ bool accept_fp64(uint32_t r, double x)
+{
+    const float xf = __double2float_rn(x);
+    if (xf >= -80.0f) {
+        const uint32_t v = (r << 9) | (r >> 23);
+        const float e = ex2_approx(__fmul_rn(xf, 1.44269504f));
+        const float band = __fmul_rn(e, __fmaf_rn(fabsf(xf), 0x1p-20f, 0x1p-18f));
+        const float lo = __fsub_rn(e, band), hi = __fadd_rn(e, band);
+        if (lo >= 1.0f || v < __float2uint_ru(__fmul_rn(lo, 0x1p32f))) return true;
+        if (v > __float2uint_rd(__fmul_rn(hi, 0x1p32f))) return false;
+    }
+    return u01_f64(r) < own_exp(x);
+}
+
+// x = -2 f beta * s for the spin s = +-1 of a site whose field f is nonzero (and, as a sum of
+// couplings of order one, normal): the doubling is exact, so it is an exponent increment
+__device__ __forceinline__ double metropolis_arg(double f, double beta, int s)
+{
+    const double f2 = __hiloint2double(__double2hiint(f) + 0x00100000, __double2loint(f));
+    const double t2 = __dmul_rn(f2, beta);
+    return s == 1 ? -t2 : t2;
 }
 
 // FP32 uniform in [0, 1) from a Philox word: its low 23 bits as a mantissa, (r mod 2^23) * 2^-23

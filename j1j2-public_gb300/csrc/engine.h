@@ -131,6 +131,7 @@ struct SweepVariant {
     bool vac;      // some conf has vacancies (shape-specialised kernels: vacancy handling on)
     int cluster;   // > 0: thread-block cluster of this many CTAs per lattice (distributed smem)
     int rpt;       // shape-specialised HBM kernel: replicas per thread (1, 2 or 4)
+    int global_nt; // generic global-memory kernels: threads per CTA (0: 256)
 };
 
 // Global-memory path: one colour phase of sweep t of the cycle, and the observable reduction

@@ -79,7 +79,7 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint
         n.jh_m4 = jh_m4;
         f64 = field_fp64(n, P[i], a.J1h, a.J1v, a.J2, a.J3, nullptr);
         if constexpr (MEASURE) {
-            acc.e += efix(-((double)s * f64));
+            acc.e += efix(-spin_mul(s, f64));
             return;
         }
     }
@@ -123,9 +123,7 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint
             flip64 = true;
         } else {
             r = u4_word(philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1), w);
-            const double u = u01_f64(r);
-            const double t2 = __dmul_rn(__dmul_rn(2.0, f64), beta);
-            flip64 = accept_fp64(u, s == 1 ? -t2 : t2);
+            flip64 = accept_fp64(r, metropolis_arg(f64, beta, s));
         }
         if constexpr (MODE == kModeAudit) {
             r = u4_word(philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1), w);
@@ -386,7 +384,7 @@ __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, cons
                 const double f = field_fp64(nb, pown[k], a.J1h, a.J1v, a.J2, a.J3, nullptr);
                 const int s = b - 1;
                 if constexpr (MEASURE) {
-                    acc.e += efix(-((double)s * f));
+                    acc.e += efix(-spin_mul(s, f));
                     acc.M += s;
                     acc.SX += px ? -s : s;
                     acc.SY += py ? -s : s;
@@ -396,9 +394,7 @@ __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, cons
                     if (s == 1 ? f <= 0.0 : f >= 0.0) {
                         flip = true;
                     } else {
-                        const double u = u01_f64(u4_word(rnd, k));
-                        const double t2 = __dmul_rn(__dmul_rn(2.0, f), beta);
-                        flip = accept_fp64(u, s == 1 ? -t2 : t2);
+                        flip = accept_fp64(u4_word(rnd, k), metropolis_arg(f, beta, s));
                     }
                     flipmask |= flip ? (2u << sh) : 0u;
                 }
@@ -865,16 +861,16 @@ cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks,
 
 namespace {
 template <class Real, bool QUAD, bool MASKS>
-cudaError_t global_pass(const SweepArgs& a, int colour, int t, int nlat, cudaStream_t st,
+cudaError_t global_pass(const SweepArgs& a, int colour, int t, int nlat, int nt, cudaStream_t st,
                         bool measure)
 {
     const int per = QUAD ? (a.g.Nc >> 2) : a.g.Nc;
     if (measure) {
-        dim3 grid((unsigned)((8 * per + 255) / 256), (unsigned)nlat);
-        measure_global_kernel<Real, QUAD, MASKS><<<grid, 256, 0, st>>>(a);
+        dim3 grid((unsigned)((8 * per + nt - 1) / nt), (unsigned)nlat);
+        measure_global_kernel<Real, QUAD, MASKS><<<grid, nt, 0, st>>>(a);
     } else {
-        dim3 grid((unsigned)((per + 255) / 256), (unsigned)nlat);
-        sweep_global_kernel<Real, QUAD, MASKS><<<grid, 256, 0, st>>>(a, colour, t);
+        dim3 grid((unsigned)((per + nt - 1) / nt), (unsigned)nlat);
+        sweep_global_kernel<Real, QUAD, MASKS><<<grid, nt, 0, st>>>(a, colour, t);
     }
     return cudaGetLastError();
 }
@@ -883,11 +879,13 @@ template <class Real>
 cudaError_t global_dispatch(const SweepArgs& a, const SweepVariant& v, int colour, int t,
                             int nlat, cudaStream_t st, bool measure)
 {
+    const int nt = v.global_nt > 0 ? v.global_nt : 256;
+    if (nt > 256 || nt % 32) return cudaErrorInvalidValue;
     if (v.quad)
-        return v.masks ? global_pass<Real, true, true>(a, colour, t, nlat, st, measure)
-                       : global_pass<Real, true, false>(a, colour, t, nlat, st, measure);
-    return v.masks ? global_pass<Real, false, true>(a, colour, t, nlat, st, measure)
-                   : global_pass<Real, false, false>(a, colour, t, nlat, st, measure);
+        return v.masks ? global_pass<Real, true, true>(a, colour, t, nlat, nt, st, measure)
+                       : global_pass<Real, true, false>(a, colour, t, nlat, nt, st, measure);
+    return v.masks ? global_pass<Real, false, true>(a, colour, t, nlat, nt, st, measure)
+                   : global_pass<Real, false, false>(a, colour, t, nlat, nt, st, measure);
 }
 }  // namespace
 

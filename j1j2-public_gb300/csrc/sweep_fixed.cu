@@ -257,7 +257,7 @@ __device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
             const double f = field_fp64(nb, d.pown[k], a.J1h, a.J1v, a.J2, a.J3, nullptr);
             const int s = b - 1;
             if constexpr (MEASURE) {
-                acc.e += efix(-((double)s * f));
+                acc.e += efix(-spin_mul(s, f));
                 acc.M += s;
                 acc.SX += px ? -s : s;
                 acc.SY += py ? -s : s;
@@ -267,9 +267,7 @@ __device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
                 if (s == 1 ? f <= 0.0 : f >= 0.0) {
                     flip = true;
                 } else {
-                    const double u = u01_f64(u4_word(rnd, k));
-                    const double t2 = __dmul_rn(__dmul_rn(2.0, f), beta);
-                    flip = accept_fp64(u, s == 1 ? -t2 : t2);
+                    flip = accept_fp64(u4_word(rnd, k), metropolis_arg(f, beta, s));
                 }
                 flipmask |= flip ? (2u << sh) : 0u;
             }

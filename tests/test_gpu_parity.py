@@ -340,11 +340,11 @@ def test_cluster_path_fp32_equals_global_path(engine_mod, oracle, pp, bonds):
 @pytest.mark.parametrize("precision,nrep", [(0, 4), (1, 4), (1, 2), (1, 3)])
 def test_hbm_kernel_replicas_per_thread(engine_mod, oracle, precision, nrep):
     """The HBM kernel with 4, 2 or 1 replicas per thread (chosen from the replica count under
-    the global-memory flag) against the shared-memory kernel: bitwise equal, 32^3 with
+    the global-memory flag) against the generic shared-memory kernel: bitwise equal, 32^3 with
     vacancies."""
     jc = engine_mod
     out = []
-    for flags in (0, jc.FLAG_GLOBAL):
+    for flags in (jc.FLAG_NO_FIXED, jc.FLAG_GLOBAL):
         eng, _, _ = _setup(jc, oracle, 32, 32, 2, nrep, precision, pp=0.05, flags=flags)
         eng.run(2, measure=False)
         eng.run(3, measure=True)
