@@ -50,7 +50,7 @@ extern "C" {
 #define J1J2C_FLAG_NO_FIXED 8u   /* skip the shape-specialised kernels (testing)                  */
 #define J1J2C_FLAG_GLOBAL 16u    /* force the global-memory (one launch per colour) path (testing) */
 #define J1J2C_FLAG_CLUSTER 64u   /* force the thread-block-cluster path, largest cluster that fits
-                                    (testing)                                                     */
+                                    (testing; with J1J2C_FLAG_GENERIC one site per thread)        */
 #define J1J2C_FLAG_WOLFF 32u     /* one Wolff cluster update at the start of every PT cycle       */
 
 /* Run parameters: the compile-time constants of J:43-96 that the hot path consumes. */

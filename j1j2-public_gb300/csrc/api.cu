@@ -173,6 +173,13 @@ size_t smem_budget(Ctx* c)
     return (size_t)optin - 2048;  // static shared memory of the reduction
 }
 
+// threads of a per-site cluster CTA: its sites of one colour, in whole warps, at most 512
+int cluster_site_threads(const Group& grp, int cs)
+{
+    int nt = ((grp.g.Nc / cs + 31) / 32) * 32;
+    return nt > 512 ? 512 : nt;
+}
+
 // CTA size of the shape-specialised kernel for a group whose lattices stay in HBM (0: the
 // generic global-memory kernel).  Like the shared-memory ones it counts no flips and handles no
 // bond dilution; the test flags GENERIC and NO_FIXED pin the generic kernel.
@@ -199,15 +206,17 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
     v.vac = c->vac;
     v.mode = kModeSweep;
     const bool quad_ok = (grp.g.Lh % 4 == 0) && !(fl & J1J2C_FLAG_GENERIC);
-    if ((fl & J1J2C_FLAG_CLUSTER) && quad_ok) {
+    if ((fl & J1J2C_FLAG_CLUSTER) && grp.g.Lh % 4 == 0) {
+        // the largest cluster; with the GENERIC flag one site per thread
         int cs[16];
         const int n = cluster_sizes(grp.g, fp64, c->masks, budget, cs, 16);
         if (n > 0) {
-            v.quad = true;
+            v.quad = quad_ok;
             v.cluster = cs[n - 1];
             v.stage_p = false;
             smem = (size_t)grp.g.N / (size_t)cs[n - 1];
-            nthreads = 512;
+            nthreads = quad_ok ? 512 : cluster_site_threads(grp, cs[n - 1]);
+            v.threads = nthreads;
             return J1J2C_OK;
         }
     }
@@ -457,7 +466,9 @@ std::mutex g_tune_mu;
 std::map<std::tuple<bool, int, int, int>, int> g_tune_cache;
 
 // Device time of 3 PT-cycle sweep launches of a group with kernel variant v, on a scratch copy of
-// its lattices (the live state is not touched; one warm-up launch first).
+// its lattices (the live state is not touched; one warm-up launch first).  The launches are
+// replays of a captured graph, as in a run, unless the context runs without graphs: variants with
+// many small launches per cycle are timed as they run.
 int time_variant(Ctx* c, Group& grp, const SweepVariant& v, int nthreads, size_t smem, float& ms)
 {
     const int nlat = grp.nlat();
@@ -478,14 +489,30 @@ int time_variant(Ctx* c, Group& grp, const SweepVariant& v, int nthreads, size_t
     a.beta_override = 1.0 / 9.5;
     a.sweep_override = 0x5EED0000u;
     a.flips = nullptr;
-    if (e == cudaSuccess) e = enqueue_group(c, grp, v, nthreads, smem, a, nlat, c->own, false);
+    cudaGraphExec_t exec = nullptr;
+    if (e == cudaSuccess && !(c->P.flags & J1J2C_FLAG_NO_GRAPH)) {
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamBeginCapture(c->own, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const cudaError_t e1 = enqueue_group(c, grp, v, nthreads, smem, a, nlat, c->own, false);
+            e = cudaStreamEndCapture(c->own, &graph);
+            if (e1 != cudaSuccess) e = e1;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+    }
+    auto once = [&]() {
+        return exec ? cudaGraphLaunch(exec, c->own)
+                    : enqueue_group(c, grp, v, nthreads, smem, a, nlat, c->own, false);
+    };
+    if (e == cudaSuccess) e = once();
     if (e == cudaSuccess) e = cudaEventRecord(c->ev0, c->own);
-    for (int r = 0; r < 3 && e == cudaSuccess; ++r)
-        e = enqueue_group(c, grp, v, nthreads, smem, a, nlat, c->own, false);
+    for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = once();
     if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->own);
     if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     cudaStreamSynchronize(c->own);
+    if (exec) cudaGraphExecDestroy(exec);
     cudaFree(tmp);
     cudaFree(tobs);
     if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the sweep path");
@@ -560,7 +587,7 @@ SweepVariant global_site_variant(const Ctx* c, bool fp64, int nt)
     v.mode = kModeSweep;
     v.global = true;
     v.rpt = 1;
-    v.global_nt = nt;
+    v.threads = nt;
     return v;
 }
 
@@ -573,9 +600,39 @@ bool small_batch_ok(Ctx* c, const Group& grp)
 }
 
 // Small batches (fewer lattices than half the SMs): one CTA per lattice leaves most SMs idle, so
-// every cluster size that divides H/2 is timed against the chosen one-CTA kernel and the fastest
-// kept, cached per (precision, L, H, lattice count, bond dilution, vacancies).
-std::map<std::tuple<bool, int, int, int, bool, bool>, int> g_small_cache;
+// the chosen one-CTA kernel is timed against one site per thread in one CTA, every cluster size
+// that divides H/2 (four sites or one site per thread), and one launch per colour phase with one
+// site per thread in CTAs of 32-256 threads; the fastest is kept, cached per (precision, L, H,
+// lattice count, bond dilution, vacancies).
+enum SmallKind { kKeep = 0, kSiteCta = 1, kClusterQuad = 2, kClusterSite = 3, kGlobalSite = 4 };
+struct SmallChoice {
+    int kind, cs, nt;
+};
+std::map<std::tuple<bool, int, int, int, bool, bool>, SmallChoice> g_small_cache;
+
+// One site per thread in one CTA per lattice (the generic kernel)
+int site_cta_variant(Ctx* c, Group& grp, SweepVariant& v, size_t& smem, int& nt)
+{
+    const uint32_t keep = c->P.flags;
+    c->P.flags |= J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED;
+    const int rc = choose_variant(c, grp, grp.var.fp64, v, smem, nt);
+    c->P.flags = keep;
+    nt = ((grp.g.Nc + 31) / 32) * 32;
+    if (nt > 1024) nt = 1024;
+    return rc;
+}
+
+SweepVariant cluster_variant(const SweepVariant& base, int cs, bool quad, int nt)
+{
+    SweepVariant v = base;
+    v.cluster = cs;
+    v.quad = quad;
+    v.threads = nt;
+    v.fixed_nt = 0;
+    v.global = false;
+    v.stage_p = false;
+    return v;
+}
 
 int tune_small_batch(Ctx* c, Group& grp)
 {
@@ -584,99 +641,82 @@ int tune_small_batch(Ctx* c, Group& grp)
     if (2 * grp.nlat() > nsm) return J1J2C_OK;
     const auto key =
         std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks, c->vac);
-    // after the search: 0 keep, -2 one site per thread, > 0 cluster size, <= -100 one launch
-    // per colour phase with one site per thread and -(best + 100) threads per CTA
-    int best = -1;
+    SmallChoice best{kKeep, 0, 0};
+    bool known = false;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_small_cache.find(key);
-        if (it != g_small_cache.end()) best = it->second;
+        if (it != g_small_cache.end()) {
+            best = it->second;
+            known = true;
+        }
     }
-    if (best == -1) {
-        int cs[16];
-        const int n = cluster_sizes(grp.g, grp.var.fp64, c->masks, smem_budget(c), cs, 16);
-        best = 0;
+    if (!known) {
         float best_ms = 0.0f;
         int rc = time_variant(c, grp, grp.var, grp.nthreads, grp.smem, best_ms);
         if (rc != J1J2C_OK) return rc;
+        auto consider = [&](const SweepVariant& v, int nt, size_t smem, SmallChoice ch) {
+            float ms = 0.0f;
+            const int r = time_variant(c, grp, v, nt, smem, ms);
+            if (r == J1J2C_OK && ms < best_ms) {
+                best_ms = ms;
+                best = ch;
+            }
+            return r;
+        };
         // one site per thread (the latency of a colour phase is one site's arithmetic, not a
         // quad's: what counts for a handful of lattices)
         SweepVariant vs;
         size_t sm_s = 0;
         int nt_s = 0;
-        {
-            const uint32_t keep = c->P.flags;
-            c->P.flags |= J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED;
-            rc = choose_variant(c, grp, grp.var.fp64, vs, sm_s, nt_s);
-            c->P.flags = keep;
+        if ((rc = site_cta_variant(c, grp, vs, sm_s, nt_s)) != J1J2C_OK) return rc;
+        if (!vs.global && !vs.quad &&
+            (rc = consider(vs, nt_s, sm_s, SmallChoice{kSiteCta, 0, nt_s})) != J1J2C_OK)
+            return rc;
+        int cs[16];
+        const int n = cluster_sizes(grp.g, grp.var.fp64, c->masks, smem_budget(c), cs, 16);
+        for (int k = 0; k < n; ++k) {
+            const size_t sm = (size_t)grp.g.N / (size_t)cs[k];
+            rc = consider(cluster_variant(grp.var, cs[k], true, 0), 512, sm,
+                          SmallChoice{kClusterQuad, cs[k], 512});
             if (rc != J1J2C_OK) return rc;
-        }
-        if (!vs.global && !vs.quad) {
-            nt_s = ((grp.g.Nc + 31) / 32) * 32;
-            if (nt_s > 1024) nt_s = 1024;
-            float ms = 0.0f;
-            rc = time_variant(c, grp, vs, nt_s, sm_s, ms);
+            const int nt = cluster_site_threads(grp, cs[k]);
+            rc = consider(cluster_variant(grp.var, cs[k], false, nt), nt, sm,
+                          SmallChoice{kClusterSite, cs[k], nt});
             if (rc != J1J2C_OK) return rc;
-            if (ms < best_ms) {
-                best_ms = ms;
-                best = -2;  // per-site
-            }
-        }
-        if (n > 0) {
-            for (int k = 0; k < n; ++k) {
-                SweepVariant v = grp.var;
-                v.cluster = cs[k];
-                v.fixed_nt = 0;
-                v.global = false;
-                v.stage_p = false;
-                float ms = 0.0f;
-                rc = time_variant(c, grp, v, 512, (size_t)grp.g.N / (size_t)cs[k], ms);
-                if (rc != J1J2C_OK) return rc;
-                if (ms < best_ms) {
-                    best_ms = ms;
-                    best = cs[k];
-                }
-            }
         }
         // one launch per colour phase, one site per thread, small CTAs: the colour phase of a
         // handful of lattices spread over many SMs (the FP64 form is bound by each SM's FP64
         // rate, so the sites per SM, not per lattice, set its time)
         for (int nt = 32; nt <= 256; nt *= 2) {
-            SweepVariant v = global_site_variant(c, grp.var.fp64, nt);
-            float ms = 0.0f;
-            rc = time_variant(c, grp, v, nt, 0, ms);
+            rc = consider(global_site_variant(c, grp.var.fp64, nt), nt, 0,
+                          SmallChoice{kGlobalSite, 0, nt});
             if (rc != J1J2C_OK) return rc;
-            if (ms < best_ms) {
-                best_ms = ms;
-                best = -(100 + nt);
-            }
         }
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_small_cache[key] = best;
     }
-    if (best > 0) {
-        grp.var.cluster = best;
-        grp.var.fixed_nt = 0;
-        grp.var.global = false;
-        grp.var.stage_p = false;
-        grp.smem = (size_t)grp.g.N / (size_t)best;
-        grp.nthreads = 512;
-        free_graphs(c);
-    } else if (best <= -100) {
-        grp.var = global_site_variant(c, grp.var.fp64, -(best + 100));
-        grp.smem = 0;
-        grp.nthreads = -(best + 100);
-        free_graphs(c);
-    } else if (best == -2) {
-        const uint32_t keep = c->P.flags;
-        c->P.flags |= J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED;
-        const int rc = choose_variant(c, grp, grp.var.fp64, grp.var, grp.smem, grp.nthreads);
-        c->P.flags = keep;
-        if (rc != J1J2C_OK) return rc;
-        grp.nthreads = ((grp.g.Nc + 31) / 32) * 32;
-        if (grp.nthreads > 1024) grp.nthreads = 1024;
-        free_graphs(c);
+    switch (best.kind) {
+        case kClusterQuad:
+        case kClusterSite:
+            grp.var = cluster_variant(grp.var, best.cs, best.kind == kClusterQuad, best.nt);
+            grp.smem = (size_t)grp.g.N / (size_t)best.cs;
+            grp.nthreads = best.nt;
+            break;
+        case kGlobalSite:
+            grp.var = global_site_variant(c, grp.var.fp64, best.nt);
+            grp.smem = 0;
+            grp.nthreads = best.nt;
+            break;
+        case kSiteCta: {
+            const int rc = site_cta_variant(c, grp, grp.var, grp.smem, grp.nthreads);
+            if (rc != J1J2C_OK) return rc;
+            break;
+        }
+        default:
+            return J1J2C_OK;
     }
+    free_graphs(c);
     return J1J2C_OK;
 }
 

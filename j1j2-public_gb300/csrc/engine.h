@@ -129,9 +129,11 @@ struct SweepVariant {
     bool global;   // lattice in HBM, one launch per colour phase (too large for shared memory;
                    // with fixed_nt > 0 the shape-specialised form)
     bool vac;      // some conf has vacancies (shape-specialised kernels: vacancy handling on)
-    int cluster;   // > 0: thread-block cluster of this many CTAs per lattice (distributed smem)
+    int cluster;   // > 0: thread-block cluster of this many CTAs per lattice (distributed smem;
+                   // quad: four sites per thread, else one)
     int rpt;       // shape-specialised HBM kernel: replicas per thread (1, 2 or 4)
-    int global_nt; // generic global-memory kernels: threads per CTA (0: 256)
+    int threads;   // threads per CTA of the generic global-memory kernels (0: 256) and of the
+                   // cluster kernel (0: 512)
 };
 
 // Global-memory path: one colour phase of sweep t of the cycle, and the observable reduction

@@ -20,8 +20,17 @@ namespace {
 // ------------------------------------------------------------------------------------------------
 // Per-site path (any even L, H): one site per thread per colour phase.
 // ------------------------------------------------------------------------------------------------
-template <class Real, bool MASKS, int MODE, bool MEASURE>
-__device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint8_t* S,
+// Spin bytes of a lattice held whole in one array of the compact layout (shared or global
+// memory); site_step reads and writes spins through such an accessor (the cluster path's reaches
+// into the neighbouring CTAs' shared memory).
+struct FlatBytes {
+    uint8_t* S;
+    __device__ __forceinline__ int get(int i, int, int, int, int) const { return S[i]; }
+    __device__ __forceinline__ void set(int i, int, int, int, int, uint8_t v) const { S[i] = v; }
+};
+
+template <class Real, bool MASKS, int MODE, bool MEASURE, class Bytes>
+__device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, const Bytes& S,
                                           const Real* P, const uint8_t* BM, const float* Pf32,
                                           int c, int X, int Y, int Z, uint32_t sweep, uint32_t rep,
                                           uint32_t k0, uint32_t k1, double beta, float kb,
@@ -32,13 +41,18 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint
     const int Yp = py ? wrap_p(Y, g.Lh) : Y, Ym = py ? Y : wrap_m(Y, g.Lh);
     const int Zp = pz ? wrap_p(Z, g.Hh) : Z, Zm = pz ? Z : wrap_m(Z, g.Hh);
     const int i = cidx(g, c, Z, Y, X);
-    const int b = S[i];
+    const int b = S.get(i, c, Z, Y, X);
     if (b == 1) return;  // vacancy: no attempt and no measured term (J:2563, J:2825)
     const int i1 = cidx(g, c ^ 2, Z, Yp, X), i2 = cidx(g, c ^ 2, Z, Ym, X);
     const int i3 = cidx(g, c ^ 1, Z, Y, Xp), i4 = cidx(g, c ^ 1, Z, Y, Xm);
     const int i5 = cidx(g, c ^ 3, Z, Yp, Xp), i6 = cidx(g, c ^ 3, Z, Yp, Xm);
     const int i7 = cidx(g, c ^ 3, Z, Ym, Xp), i8 = cidx(g, c ^ 3, Z, Ym, Xm);
     const int i9 = cidx(g, c ^ 4, Zp, Y, X), i10 = cidx(g, c ^ 4, Zm, Y, X);
+    const int b1 = S.get(i1, c ^ 2, Z, Yp, X), b2 = S.get(i2, c ^ 2, Z, Ym, X);
+    const int b3 = S.get(i3, c ^ 1, Z, Y, Xp), b4 = S.get(i4, c ^ 1, Z, Y, Xm);
+    const int b5 = S.get(i5, c ^ 3, Z, Yp, Xp), b6 = S.get(i6, c ^ 3, Z, Yp, Xm);
+    const int b7 = S.get(i7, c ^ 3, Z, Ym, Xp), b8 = S.get(i8, c ^ 3, Z, Ym, Xm);
+    const int b9 = S.get(i9, c ^ 4, Zp, Y, X), b10 = S.get(i10, c ^ 4, Zm, Y, X);
     const int s = b - 1;
     int jh_own = 1, jh_m4 = 1, jv_own = 1, jv_m2 = 1;
     if constexpr (MASKS) {
@@ -52,23 +66,23 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint
         acc.M += s;
         acc.SX += px ? -s : s;
         acc.SY += py ? -s : s;
-        acc.NB += s * ((int)S[i3] + (int)S[i4] - (int)S[i1] - (int)S[i2]);
+        acc.NB += s * (b3 + b4 - b1 - b2);
     }
 
     bool flip64 = false;
     double f64 = 0.0;
     if constexpr (sizeof(Real) == 8) {
         Nbr64 n;
-        n.s[0] = (int)S[i1] - 1;
-        n.s[1] = (int)S[i2] - 1;
-        n.s[2] = (int)S[i3] - 1;
-        n.s[3] = (int)S[i4] - 1;
-        n.s[4] = (int)S[i5] - 1;
-        n.s[5] = (int)S[i6] - 1;
-        n.s[6] = (int)S[i7] - 1;
-        n.s[7] = (int)S[i8] - 1;
-        n.s[8] = (int)S[i9] - 1;
-        n.s[9] = (int)S[i10] - 1;
+        n.s[0] = b1 - 1;
+        n.s[1] = b2 - 1;
+        n.s[2] = b3 - 1;
+        n.s[3] = b4 - 1;
+        n.s[4] = b5 - 1;
+        n.s[5] = b6 - 1;
+        n.s[6] = b7 - 1;
+        n.s[7] = b8 - 1;
+        n.s[8] = b9 - 1;
+        n.s[9] = b10 - 1;
         n.p1 = P[i1];
         n.p2 = P[i2];
         n.p3 = P[i3];
@@ -93,12 +107,12 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint
         else
             Q = Pf32;
         Nbr32 n;
-        n.syp = (float)((int)S[i1] - 1);
-        n.sym = (float)((int)S[i2] - 1);
-        n.sxp = (float)((int)S[i3] - 1);
-        n.sxm = (float)((int)S[i4] - 1);
-        n.D = (float)((int)S[i5] + (int)S[i6] + (int)S[i7] + (int)S[i8] - 4);
-        n.Zs = (float)((int)S[i9] + (int)S[i10] - 2);
+        n.syp = (float)(b1 - 1);
+        n.sym = (float)(b2 - 1);
+        n.sxp = (float)(b3 - 1);
+        n.sxm = (float)(b4 - 1);
+        n.D = (float)(b5 + b6 + b7 + b8 - 4);
+        n.Zs = (float)(b9 + b10 - 2);
         n.pyp = Q[i1];
         n.pym = Q[i2];
         n.pxp = Q[i3];
@@ -133,14 +147,14 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, uint
             acc.SX += (flip32 != flip64);
         }
         if (flip64) {
-            S[i] = (uint8_t)(2 - b);
+            S.set(i, c, Z, Y, X, (uint8_t)(2 - b));
             if (fl) fl[i] += 1;
         }
     } else {
         r = u4_word(philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1), w);
         const float sf = __fmul_rn((float)s, f32);
         if (u01_f32(r) < ex2_approx(__fmul_rn(kb, sf))) {
-            S[i] = (uint8_t)(2 - b);
+            S.set(i, c, Z, Y, X, (uint8_t)(2 - b));
             if (fl) fl[i] += 1;
         }
     }
@@ -474,7 +488,7 @@ __global__ void __launch_bounds__(1024) sweep_kernel(SweepArgs a)
                 for (int k = tid; k < g.Nc; k += NT) {
                     const int X = k % g.Lh, r = k / g.Lh;
                     const int Y = r % g.Lh, Z = r / g.Lh;
-                    site_step<Real, MASKS, MODE, false>(a, g, S, P, BM, Pf32, c, X, Y, Z, sweep,
+                    site_step<Real, MASKS, MODE, false>(a, g, FlatBytes{S}, P, BM, Pf32, c, X, Y, Z, sweep,
                                                         (uint32_t)rep, k0, k1, beta, kb, acc, fl);
                 }
             }
@@ -504,7 +518,7 @@ __global__ void __launch_bounds__(1024) sweep_kernel(SweepArgs a)
             for (int k = tid; k < g.Nc; k += NT) {
                 const int X = k % g.Lh, r = k / g.Lh;
                 const int Y = r % g.Lh, Z = r / g.Lh;
-                site_step<Real, MASKS, MODE, true>(a, g, S, P, BM, Pf32, c, X, Y, Z, 0u, 0u, 0u,
+                site_step<Real, MASKS, MODE, true>(a, g, FlatBytes{S}, P, BM, Pf32, c, X, Y, Z, 0u, 0u, 0u,
                                                    0u, beta, kb, acc);
             }
         }
@@ -723,7 +737,7 @@ __global__ void __launch_bounds__(256) sweep_global_kernel(SweepArgs a, int colo
     } else {
         if (item < g.Nc) {
             const int X = item % g.Lh, r = item / g.Lh;
-            site_step<Real, MASKS, kModeSweep, false>(a, g, S, P, BM, nullptr, colour, X,
+            site_step<Real, MASKS, kModeSweep, false>(a, g, FlatBytes{S}, P, BM, nullptr, colour, X,
                                                       r % g.Lh, r / g.Lh, sweep, (uint32_t)rep,
                                                       k0, k1, beta, kb, acc, fl);
         }
@@ -749,7 +763,7 @@ __global__ void __launch_bounds__(256) measure_global_kernel(SweepArgs a)
                                          0u, 0u, 0.0, 0.0f, acc);
         } else {
             const int X = k % g.Lh, r = k / g.Lh;
-            site_step<Real, MASKS, kModeSweep, true>(a, g, S, P, BM, nullptr, c, X, r % g.Lh,
+            site_step<Real, MASKS, kModeSweep, true>(a, g, FlatBytes{S}, P, BM, nullptr, c, X, r % g.Lh,
                                                      r / g.Lh, 0u, 0u, 0u, 0u, 0.0, 0.0f, acc);
         }
     }
@@ -879,7 +893,7 @@ template <class Real>
 cudaError_t global_dispatch(const SweepArgs& a, const SweepVariant& v, int colour, int t,
                             int nlat, cudaStream_t st, bool measure)
 {
-    const int nt = v.global_nt > 0 ? v.global_nt : 256;
+    const int nt = v.threads > 0 ? v.threads : 256;
     if (nt > 256 || nt % 32) return cudaErrorInvalidValue;
     if (v.quad)
         return v.masks ? global_pass<Real, true, true>(a, colour, t, nlat, nt, st, measure)
@@ -921,7 +935,30 @@ struct ClusterSpins {
     }
 };
 
-template <class Real, bool MASKS>
+// The same planes as bytes, for one site per thread
+struct ClusterBytes {
+    uint8_t* local;
+    const uint8_t* lo;
+    const uint8_t* hi;
+    int z0, zpc, Hh, Lh, plane, colstride;  // bytes per compact plane and per colour chunk
+    __device__ __forceinline__ int get(int, int cc, int ZZ, int YY, int XX) const
+    {
+        int d = ZZ - z0;
+        if (d < 0) d += Hh;
+        const int off = YY * Lh + XX;
+        if (d < zpc) return local[cc * colstride + d * plane + off];
+        if (d == zpc) return hi[cc * colstride + off];
+        return lo[cc * colstride + (zpc - 1) * plane + off];
+    }
+    __device__ __forceinline__ void set(int, int cc, int ZZ, int YY, int XX, uint8_t v) const
+    {
+        local[cc * colstride + (ZZ - z0) * plane + YY * Lh + XX] = v;
+    }
+};
+
+// QUAD: four sites (one spin word) per thread per colour phase; else one site per thread, for
+// small batches where a colour phase's latency is one site's arithmetic (the FP64 form)
+template <class Real, bool MASKS, bool QUAD>
 __global__ void __launch_bounds__(kClusterThreads, 2) sweep_cluster_kernel(SweepArgs a, int cs)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -954,6 +991,17 @@ __global__ void __launch_bounds__(kClusterThreads, 2) sweep_cluster_kernel(Sweep
     sp.rowstride = plane_words;
     sp.colstride = chunk_words;
     sp.Qr = g.Qr;
+    ClusterBytes sb;
+    sb.local = reinterpret_cast<uint8_t*>(sp.local);
+    sb.lo = reinterpret_cast<const uint8_t*>(sp.lo);
+    sb.hi = reinterpret_cast<const uint8_t*>(sp.hi);
+    sb.z0 = z0;
+    sb.zpc = zpc;
+    sb.Hh = g.Hh;
+    sb.Lh = g.Lh;
+    sb.plane = 4 * plane_words;
+    sb.colstride = 4 * chunk_words;
+    const int chunk_sites = 4 * chunk_words;  // this CTA's sites of one colour
     cl.sync();
 
     const Real* P = field_base<Real>(a, conf);
@@ -978,18 +1026,37 @@ __global__ void __launch_bounds__(kClusterThreads, 2) sweep_cluster_kernel(Sweep
         const uint32_t sweep = sweep0 + (uint32_t)t;
 #pragma unroll 1
         for (int c = 0; c < 8; ++c) {
-            for (int lq = tid; lq < chunk_words; lq += NT)
-                quad_step<Real, MASKS, false>(a, g, sp, P, BM, c, q0 + lq, sweep, (uint32_t)rep,
-                                              k0, k1, beta, kb, acc, fl);
+            if constexpr (QUAD) {
+                for (int lq = tid; lq < chunk_words; lq += NT)
+                    quad_step<Real, MASKS, false>(a, g, sp, P, BM, c, q0 + lq, sweep,
+                                                  (uint32_t)rep, k0, k1, beta, kb, acc, fl);
+            } else {
+                for (int ls = tid; ls < chunk_sites; ls += NT) {
+                    const int X = ls % g.Lh, r = ls / g.Lh;
+                    site_step<Real, MASKS, kModeSweep, false>(
+                        a, g, sb, P, BM, nullptr, c, X, r % g.Lh, z0 + r / g.Lh, sweep,
+                        (uint32_t)rep, k0, k1, beta, kb, acc, fl);
+                }
+            }
             cl.sync();
         }
     }
     // observables of the new configuration
 #pragma unroll 1
-    for (int c = 0; c < 8; ++c)
-        for (int lq = tid; lq < chunk_words; lq += NT)
-            quad_step<Real, MASKS, true>(a, g, sp, P, BM, c, q0 + lq, 0u, 0u, 0u, 0u, beta, kb,
-                                         acc);
+    for (int c = 0; c < 8; ++c) {
+        if constexpr (QUAD) {
+            for (int lq = tid; lq < chunk_words; lq += NT)
+                quad_step<Real, MASKS, true>(a, g, sp, P, BM, c, q0 + lq, 0u, 0u, 0u, 0u, beta,
+                                             kb, acc);
+        } else {
+            for (int ls = tid; ls < chunk_sites; ls += NT) {
+                const int X = ls % g.Lh, r = ls / g.Lh;
+                site_step<Real, MASKS, kModeSweep, true>(a, g, sb, P, BM, nullptr, c, X,
+                                                         r % g.Lh, z0 + r / g.Lh, 0u, 0u, 0u, 0u,
+                                                         beta, kb, acc);
+            }
+        }
+    }
     const Acc tot = block_reduce(acc);
     if (tid == 0) {
         LatObs* o = a.obs + lat;
@@ -1010,26 +1077,29 @@ __global__ void __launch_bounds__(kClusterThreads, 2) sweep_cluster_kernel(Sweep
 
 // The kernels' dynamic shared memory limit is the most the device allows, so every cluster size
 // (and every shape in one context) launches whatever was probed last.
-template <class Real, bool MASKS>
+template <class Real, bool MASKS, bool QUAD>
 cudaError_t cluster_prepare()
 {
-    cudaError_t e = raise_smem_limit(sweep_cluster_kernel<Real, MASKS>);
+    cudaError_t e = raise_smem_limit(sweep_cluster_kernel<Real, MASKS, QUAD>);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(sweep_cluster_kernel<Real, MASKS>,
+        e = cudaFuncSetAttribute(sweep_cluster_kernel<Real, MASKS, QUAD>,
                                  cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     return e;
 }
 
-template <class Real, bool MASKS>
-cudaError_t cluster_launch(const SweepArgs& a, int nlat, int cs, cudaStream_t st, bool prepare)
+template <class Real, bool MASKS, bool QUAD>
+cudaError_t cluster_launch(const SweepArgs& a, int nlat, int cs, int nt, cudaStream_t st,
+                           bool prepare)
 {
-    auto kern = sweep_cluster_kernel<Real, MASKS>;
+    auto kern = sweep_cluster_kernel<Real, MASKS, QUAD>;
     const size_t smem = (size_t)a.g.N / (size_t)cs;
-    cudaError_t e0 = cluster_prepare<Real, MASKS>();
+    cudaError_t e0 = cluster_prepare<Real, MASKS, QUAD>();
     if (prepare || e0 != cudaSuccess) return e0;
+    if (nt <= 0) nt = kClusterThreads;
+    if (nt > kClusterThreads || nt % 32) return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(nlat * cs));
-    cfg.blockDim = dim3(kClusterThreads);
+    cfg.blockDim = dim3((unsigned)nt);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute at[1];
@@ -1045,9 +1115,9 @@ cudaError_t cluster_launch(const SweepArgs& a, int nlat, int cs, cudaStream_t st
 template <class Real, bool MASKS>
 int cluster_fits(const Geo& g, int cs)
 {
-    auto kern = sweep_cluster_kernel<Real, MASKS>;
+    auto kern = sweep_cluster_kernel<Real, MASKS, true>;
     const size_t smem = (size_t)g.N / (size_t)cs;
-    if (cluster_prepare<Real, MASKS>() != cudaSuccess) {
+    if (cluster_prepare<Real, MASKS, true>() != cudaSuccess) {
         (void)cudaGetLastError();
         return 0;
     }
@@ -1106,12 +1176,19 @@ int cluster_sizes(const Geo& g, bool fp64, bool masks, size_t max_smem, int* out
 cudaError_t launch_sweep_cluster(const SweepArgs& a, const SweepVariant& v, int nlat,
                                  cudaStream_t st)
 {
-    const int cs = v.cluster;
+    const int cs = v.cluster, nt = v.threads;
+    if (v.quad) {
+        if (v.fp64)
+            return v.masks ? cluster_launch<double, true, true>(a, nlat, cs, nt, st, false)
+                           : cluster_launch<double, false, true>(a, nlat, cs, nt, st, false);
+        return v.masks ? cluster_launch<float, true, true>(a, nlat, cs, nt, st, false)
+                       : cluster_launch<float, false, true>(a, nlat, cs, nt, st, false);
+    }
     if (v.fp64)
-        return v.masks ? cluster_launch<double, true>(a, nlat, cs, st, false)
-                       : cluster_launch<double, false>(a, nlat, cs, st, false);
-    return v.masks ? cluster_launch<float, true>(a, nlat, cs, st, false)
-                   : cluster_launch<float, false>(a, nlat, cs, st, false);
+        return v.masks ? cluster_launch<double, true, false>(a, nlat, cs, nt, st, false)
+                       : cluster_launch<double, false, false>(a, nlat, cs, nt, st, false);
+    return v.masks ? cluster_launch<float, true, false>(a, nlat, cs, nt, st, false)
+                   : cluster_launch<float, false, false>(a, nlat, cs, nt, st, false);
 }
 
 cudaError_t launch_sweep_global(const SweepArgs& a, const SweepVariant& v, int colour, int t,

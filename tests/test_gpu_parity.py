@@ -424,6 +424,48 @@ def test_small_batch_cluster_path_fp64_bit_identical(engine_mod, oracle, L, H, n
     eng.close()
 
 
+@pytest.mark.parametrize("L,H,nconf,nrep,pp", [(16, 16, 1, 1, 0.05), (24, 24, 1, 4, 0.0),
+                                                (32, 8, 2, 2, 0.1)])
+def test_small_batch_site_cluster_fp64_bit_identical(engine_mod, oracle, L, H, nconf, nrep, pp):
+    """One site per thread over a thread-block cluster (flags CLUSTER + GENERIC; a small-batch
+    choice of the autotuner): FP64 equals the replay bit for bit, the LOCAL shape included."""
+    jc = engine_mod
+    eng, models, betas = _setup(jc, oracle, L, H, nconf, nrep, jc.FP64_PLAIN, pp=pp,
+                                flags=jc.FLAG_CLUSTER | jc.FLAG_GENERIC)
+    cfg = eng.config()
+    assert cfg["sites_per_thread"] == 1 and 0 < cfg["smem_bytes"] < L * L * H
+    eng.run(2, measure=False)
+    eng.reset_measurements()
+    eng.run(3, measure=True)
+    for k in range(nconf):
+        st = oracle.new_pt_state(np.stack([oracle.hot_spins_philox(L, H, SEED, k, q) *
+                                           models[k].occu for q in range(nrep)]))
+        models[k].replay_pt(st, betas, 5, 2, 0, SEED, k, False, 1)
+        obs = models[k].replay_pt(st, betas, 5, 3, 2, SEED, k, True, 1)
+        for r in range(nrep):
+            np.testing.assert_array_equal(eng.spins(k, r), st["spins"][r])
+        np.testing.assert_array_equal(eng.slot_sums(k)[0], st["sums"])
+        np.testing.assert_array_equal(eng.observables(k), obs)
+    eng.close()
+
+
+def test_small_batch_site_cluster_fp32_bitwise(engine_mod, oracle):
+    """FP32: one site per thread over a cluster equals the shared-memory kernels bit for bit."""
+    jc = engine_mod
+    out = []
+    for flags in (jc.FLAG_NO_FIXED, jc.FLAG_CLUSTER | jc.FLAG_GENERIC):
+        eng, _, _ = _setup(jc, oracle, 32, 16, 2, 3, jc.FP32_BATCHED, pp=0.05, flags=flags)
+        eng.run(4, measure=True)
+        out.append(([eng.spins(k, r) for k in range(2) for r in range(3)],
+                    eng.slot_sums(-1)[0], eng.observables(-1), eng.config()))
+        eng.close()
+    assert out[1][3]["sites_per_thread"] == 1
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    np.testing.assert_array_equal(out[0][2], out[1][2])
+
+
 def test_small_batch_cluster_path_fp32_bitwise(engine_mod, oracle):
     jc = engine_mod
     out = []
