@@ -162,13 +162,33 @@ struct Nbr64 {
     int jv_own, jv_m2, jh_own, jh_m4;
 };
 
-// s * c for a spin s in {-1, 0, +1}: the product is exact, so it is a selection rather than an
-// FP64 multiplication (GB300's FP64 rate is 2 operations per clock per SM).  A vacancy's zero is
-// +0; since no partial sum is -0, adding it leaves the sum as IEEE multiplication's signed zero
-// would.
+// s * c for a spin s in {-1, 0, +1}: the product is exact, so it is a selection of c's bits with
+// the sign flipped for s = -1, in integer operations rather than on the FP64 pipe (GB300 runs 2
+// FP64 operations per clock per SM; a negation there would cost as much as the addition).  A
+// vacancy's zero is +0; since no partial sum is -0, adding it leaves the sum as IEEE
+// multiplication's signed zero would.
 __device__ __forceinline__ double spin_mul(int s, double c)
 {
-    return s > 0 ? c : (s < 0 ? -c : 0.0);
+    const int hi = __double2hiint(c) ^ (s < 0 ? (int)0x80000000 : 0);
+    return __hiloint2double(s == 0 ? 0 : hi, s == 0 ? 0 : __double2loint(c));
+}
+
+// A small integer n (|n| <= 15) as a double, built from its bits (no FP64 conversion)
+__device__ __forceinline__ double small_int_double(int n)
+{
+    const int m = n < 0 ? -n : n;
+    if (m == 0) return 0.0;
+    const int e = 31 - __clz(m);  // m = 2^e (1 + f)
+    const int hi = ((1023 + e) << 20) | ((m << (20 - e)) & 0xFFFFF);
+    return __hiloint2double(n < 0 ? hi | (int)0x80000000 : hi, 0);
+}
+
+// s f <= 0 for a spin s = +-1: the Metropolis move is downhill (or level) and accepted without a
+// random number; read off the sign bit of f (and f = +-0) without an FP64 comparison
+__device__ __forceinline__ bool downhill(double f, int s)
+{
+    const long long b = __double_as_longlong(f);
+    return (b << 1) == 0 || ((b < 0) == (s == 1));
 }
 
 __device__ __forceinline__ double field_fp64(const Nbr64& n, double pi, double J1h, double J1v,
@@ -188,7 +208,7 @@ __device__ __forceinline__ double field_fp64(const Nbr64& n, double pi, double J
 #pragma unroll
     for (int k = 8; k < 10; ++k) f = __dadd_rn(f, spin_mul(n.s[k], J3));
     // the nematic sum -s1 - s2 + s3 + s4 is an exact small integer in any order
-    const double nm = (double)(n.s[2] + n.s[3] - n.s[0] - n.s[1]);
+    const double nm = small_int_double(n.s[2] + n.s[3] - n.s[0] - n.s[1]);
     f = __dadd_rn(f, __dmul_rn(pi, nm));
     if (nem_out) *nem_out = nm;
     return f;
@@ -288,8 +308,7 @@ __device__ __forceinline__ bool accept_fp64(uint32_t r, double x)
 __device__ __forceinline__ double metropolis_arg(double f, double beta, int s)
 {
     const double f2 = __hiloint2double(__double2hiint(f) + 0x00100000, __double2loint(f));
-    const double t2 = __dmul_rn(f2, beta);
-    return s == 1 ? -t2 : t2;
+    return spin_mul(-s, __dmul_rn(f2, beta));
 }
 
 // FP32 uniform in [0, 1) from a Philox word: its low 23 bits as a mantissa, (r mod 2^23) * 2^-23

@@ -93,7 +93,7 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, cons
         n.jh_m4 = jh_m4;
         f64 = field_fp64(n, P[i], a.J1h, a.J1v, a.J2, a.J3, nullptr);
         if constexpr (MEASURE) {
-            acc.e += efix(-spin_mul(s, f64));
+            acc.e += efix(spin_mul(-s, f64));
             return;
         }
     }
@@ -133,7 +133,7 @@ __device__ __forceinline__ void site_step(const SweepArgs& a, const Geo& g, cons
     uint32_t r = 0;
     if constexpr (sizeof(Real) == 8) {
         // FP64 acceptance, J:2572-2604: no uniform is needed when dE <= 0
-        if (s == 1 ? f64 <= 0.0 : f64 >= 0.0) {
+        if (downhill(f64, s)) {
             flip64 = true;
         } else {
             r = u4_word(philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1), w);
@@ -398,14 +398,14 @@ __device__ __forceinline__ void quad_step(const SweepArgs& a, const Geo& g, cons
                 const double f = field_fp64(nb, pown[k], a.J1h, a.J1v, a.J2, a.J3, nullptr);
                 const int s = b - 1;
                 if constexpr (MEASURE) {
-                    acc.e += efix(-spin_mul(s, f));
+                    acc.e += efix(spin_mul(-s, f));
                     acc.M += s;
                     acc.SX += px ? -s : s;
                     acc.SY += py ? -s : s;
                     acc.NB += s * (nb.s[2] + nb.s[3] - nb.s[0] - nb.s[1]);
                 } else {
                     bool flip;
-                    if (s == 1 ? f <= 0.0 : f >= 0.0) {
+                    if (downhill(f, s)) {
                         flip = true;
                     } else {
                         flip = accept_fp64(u4_word(rnd, k), metropolis_arg(f, beta, s));

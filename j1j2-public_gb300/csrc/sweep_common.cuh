@@ -24,10 +24,26 @@ struct Acc {
 __device__ __forceinline__ int wrap_p(int v, int n) { return v + 1 == n ? 0 : v + 1; }
 __device__ __forceinline__ int wrap_m(int v, int n) { return v == 0 ? n - 1 : v - 1; }
 
-// fixed-point energy contribution of one site: llrint(e * 2^32)
+// fixed-point energy contribution of one site: llrint(e * 2^32) for |e| < 2^30, rounded from
+// e's bits in integer arithmetic (no FP64 operation): e 2^32 = m 2^(ex - 1043) with m the 53-bit
+// significand, rounded to nearest, ties to even, when the shift drops bits
 __device__ __forceinline__ long long efix(double e)
 {
-    return __double2ll_rn(__dmul_rn(e, 4294967296.0));
+    const long long bits = __double_as_longlong(e);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    if (ex == 0) return 0;  // zero, or subnormal (|e 2^32| < 2^-990)
+    const long long m = (bits & 0xFFFFFFFFFFFFFLL) | 0x10000000000000LL;
+    const int sh = 1043 - ex;
+    long long v;
+    if (sh <= 0) {
+        v = m << (-sh);  // integral
+    } else if (sh > 53) {
+        v = 0;           // below 1/2
+    } else {
+        const long long q = m >> sh, r = m & ((1LL << sh) - 1), half = 1LL << (sh - 1);
+        v = q + ((r > half || (r == half && (q & 1))) ? 1 : 0);
+    }
+    return bits < 0 ? -v : v;
 }
 // same value for an FP32 energy term: e * 2^32 is exact in FP32, so no FP64 operation is needed
 __device__ __forceinline__ long long efix32(float e)

@@ -257,14 +257,14 @@ __device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
             const double f = field_fp64(nb, d.pown[k], a.J1h, a.J1v, a.J2, a.J3, nullptr);
             const int s = b - 1;
             if constexpr (MEASURE) {
-                acc.e += efix(-spin_mul(s, f));
+                acc.e += efix(spin_mul(-s, f));
                 acc.M += s;
                 acc.SX += px ? -s : s;
                 acc.SY += py ? -s : s;
                 acc.NB += s * (nb.s[2] + nb.s[3] - nb.s[0] - nb.s[1]);
             } else {
                 bool flip;
-                if (s == 1 ? f <= 0.0 : f >= 0.0) {
+                if (downhill(f, s)) {
                     flip = true;
                 } else {
                     flip = accept_fp64(u4_word(rnd, k), metropolis_arg(f, beta, s));
