@@ -35,7 +35,7 @@ B_PER_ATTEMPT_FP64 = 21.4
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one sweep-kernel launch (5 sweeps
 # + measure of every lattice), from an ncu capture of the same workload
-TRAFFIC = {"batched_fp32_L32_64x32": 75594240 + 9697280}
+TRAFFIC = {"batched_fp32_L32_64x32": 75578112 + 10685696}
 
 # name -> lattice-shape groups (L, nconf, nreplica), precision and options
 WORKLOADS = {
@@ -243,8 +243,11 @@ def run_ours(args):
 
     wname = args.workload
     w = WORKLOADS[wname]
+    if args.nconf:  # a smaller case of the same kernels (profiling captures)
+        w = dict(w, groups=[(L, args.nconf, r) for L, _, r in w["groups"]])
     nconf = sum(n for _, n, _ in w["groups"])
-    eng, betas = make_engine(jc, w, local, conf_base=conf_base_of(rank, w), flags=jc.FLAG_PROFILE)
+    eng, betas = make_engine(jc, w, local, conf_base=conf_base_of(rank, w),
+                             flags=jc.FLAG_PROFILE | args.flags)
     cfg = eng.config()
     cycles = w.get("cycles_per_step", 1)
     attempts_per_step = attempts_per_cycle(eng) * cycles
@@ -313,7 +316,8 @@ def run_ours(args):
                    "block_threads": cfg["block_threads"], "sites_per_thread": cfg["sites_per_thread"],
                    "smem_bytes": cfg["smem_bytes"], "parallelism": f"confs x{ws}"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
-                     "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": TRAFFIC.get(wname),
+                     "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                     "traffic": None if args.nconf else TRAFFIC.get(wname),
                      "peak_source": peak_src, "bytes_per_attempt": bpa,
                      "sweep_kernel_ms": round(sweep_ms_avg, 4)},
         "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
@@ -394,6 +398,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched_fp32_L32_64x32", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--flags", type=int, default=0,
+                    help="engine flags added to the run (e.g. 16 pins the one-launch-per-colour "
+                         "HBM path; for profiling captures)")
+    ap.add_argument("--nconf", type=int, default=0,
+                    help="configurations per lattice shape instead of the workload's (a smaller "
+                         "case for profiling captures; 0: the workload's)")
     ap.add_argument("--headline-only", action="store_true",
                     help="skip the secondary workloads (batched FP64, mixed L, L=96, local)")
     args = ap.parse_args()

@@ -490,7 +490,8 @@ __device__ __forceinline__ void hbm_phase(const SweepArgs& a, const Real* P, con
 // Grid: (quads of a colour / NT, lattices / RPT); with RPT > 1 the launcher guarantees that the
 // RPT lattices of a block row are replicas of one configuration.
 template <class Real, int LH, int HH, int NT, int RPT, bool VAC>
-__global__ void __launch_bounds__(NT) sweep_fixed_hbm_kernel(SweepArgs a, int colour, int t)
+__global__ void __launch_bounds__(NT, sizeof(Real) == 8 ? 1 : RPT == 4 ? 768 / NT : 1024 / NT)
+    sweep_fixed_hbm_kernel(SweepArgs a, int colour, int t)
 {
     using Sh = Shape<LH, HH>;
     const int q = (int)(blockIdx.x * NT + threadIdx.x);
