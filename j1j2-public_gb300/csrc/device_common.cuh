@@ -194,8 +194,8 @@ __device__ __forceinline__ bool downhill(double f, int s)
 __device__ __forceinline__ double field_fp64(const Nbr64& n, double pi, double J1h, double J1v,
                                              double J2, double J3, double* nem_out)
 {
-    double f = 0.0;
-    f = __dadd_rn(f, n.jv_own ? spin_mul(n.s[0], J1v) : 0.0);
+    // 0 + t = t exactly (up to the sign of a zero, which no later sum or test can see)
+    double f = n.jv_own ? spin_mul(n.s[0], J1v) : 0.0;
     f = __dsub_rn(f, spin_mul(n.s[0], n.p1));
     f = __dadd_rn(f, n.jv_m2 ? spin_mul(n.s[1], J1v) : 0.0);
     f = __dsub_rn(f, spin_mul(n.s[1], n.p2));
