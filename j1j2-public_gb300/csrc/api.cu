@@ -41,6 +41,7 @@ struct Group {
     int nthreads = 0;
     size_t smem = 0;
     bool tuned = false;
+    int wolff_cs = 0;  // CTAs per lattice of the Wolff growth kernel (0: not tuned, 1)
     int nlat() const { return nconf * nrep; }
 };
 
@@ -373,6 +374,14 @@ cudaError_t enqueue_locnem(Ctx* c, cudaStream_t st)
     return cudaSuccess;
 }
 
+// CTAs per lattice of the Wolff growth kernel: pinned by a test flag, else the tuned count
+int wolff_cs_of(const Ctx* c, const Group& grp)
+{
+    if (c->P.flags & J1J2C_FLAG_WOLFF_CS4) return 4;
+    if (c->P.flags & J1J2C_FLAG_WOLFF_CS2) return 2;
+    return grp.wolff_cs > 0 ? grp.wolff_cs : 1;
+}
+
 // PTSWAPEVER sweeps and the observable reduction of lattices [lat0, lat0 + nlat) of a group
 cudaError_t enqueue_wolff(Ctx* c, const Group& grp, cudaStream_t st)
 {
@@ -384,7 +393,8 @@ cudaError_t enqueue_wolff(Ctx* c, const Group& grp, cudaStream_t st)
                            : (c->P.flags & J1J2C_FLAG_NO_FIXED) ? kWolffSlab
                                                                 : kWolffGrow;
     return launch_wolff(a, grp.var.fp64, c->masks, grp.nlat(), c->d_labels + grp.lab_off,
-                        grp.lat_stride, c->d_csize + grp.rep0, c->d_err, st, form);
+                        grp.lat_stride, c->d_csize + grp.rep0, c->d_err, st, form,
+                        wolff_cs_of(c, grp));
 }
 
 cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int nthreads,
@@ -726,10 +736,79 @@ int tune_small_batch(Ctx* c, Group& grp)
     return J1J2C_OK;
 }
 
+// Wolff growth: 1, 2 or 4 CTAs per lattice (a thread-block cluster) timed on a scratch copy of
+// the group's lattices at the first run of a context with Wolff updates, the fastest kept, cached
+// per (precision, L, H, lattice count, bond dilution).  The coldest lattices' clusters span a
+// third of the lattice or more and are bound by one SM's issue rate; the hot ones are small.
+std::map<std::tuple<bool, int, int, int, bool>, int> g_wolff_cache;
+
+int tune_wolff(Ctx* c, Group& grp)
+{
+    const uint32_t fl = c->P.flags;
+    if (!c->wolff || (fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_WOLFF_CS2 |
+                            J1J2C_FLAG_WOLFF_CS4)))
+        return J1J2C_OK;  // no growth form, or the count is pinned
+    const auto key = std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_wolff_cache.find(key);
+        if (it != g_wolff_cache.end()) {
+            grp.wolff_cs = it->second;
+            return J1J2C_OK;
+        }
+    }
+    if (!c->d_labels) CK(c, dalloc(&c->d_labels, (size_t)c->lab_ints));
+    const int nlat = grp.nlat();
+    uint8_t* tmp = nullptr;
+    const size_t bytes = (size_t)nlat * grp.lat_stride;
+    CK(c, cudaMalloc(&tmp, bytes));
+    cudaError_t e =
+        cudaMemcpyAsync(tmp, c->d_spins + grp.spin_off, bytes, cudaMemcpyDeviceToDevice, c->own);
+    SweepArgs a = group_args(c, grp);
+    a.spins = tmp;
+    int best = 1;
+    float best_ms = 0.0f;
+    for (const int cs : {1, 2, 4}) {
+        if (e != cudaSuccess) break;
+        if (cs > 1 && wolff_grow_clusters(grp.var.fp64, c->masks, cs) <= 0) continue;
+        auto once = [&]() {
+            return launch_wolff(a, grp.var.fp64, c->masks, nlat, c->d_labels + grp.lab_off,
+                                grp.lat_stride, c->d_csize + grp.rep0, c->d_err, c->own,
+                                kWolffGrow, cs);
+        };
+        e = once();  // warm-up
+        float ms = 0.0f;
+        for (int k = 0; k < 3 && e == cudaSuccess; ++k) {  // the fastest of three
+            e = cudaEventRecord(c->ev0, c->own);
+            if (e == cudaSuccess) e = once();
+            if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->own);
+            if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
+            float t = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, c->ev0, c->ev1);
+            if (e == cudaSuccess && (k == 0 || t < ms)) ms = t;
+        }
+        if (e == cudaSuccess && (cs == 1 || ms < best_ms)) {
+            best_ms = ms;
+            best = cs;
+        }
+    }
+    cudaStreamSynchronize(c->own);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the Wolff update");
+    grp.wolff_cs = best;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_wolff_cache[key] = best;
+    return J1J2C_OK;
+}
+
 int autotune(Ctx* c, Group& grp)
 {
     if (grp.tuned) return J1J2C_OK;
     grp.tuned = true;
+    {
+        const int rc = tune_wolff(c, grp);
+        if (rc != J1J2C_OK) return rc;
+    }
     if (c->P.flags & J1J2C_FLAG_CLUSTER) return J1J2C_OK;
     if (grp.var.cluster > 0 && grp.block_threads == 0) return tune_cluster(c, grp);
     if (grp.var.global && grp.var.fixed_nt > 0) return J1J2C_OK;

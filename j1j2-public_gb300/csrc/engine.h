@@ -174,9 +174,11 @@ cudaError_t launch_swap(const SwapArgs& a, cudaStream_t st);
 // Wolff forms: seed-cluster growth (default), slab union-find labelling in shared memory,
 // per-site union-find labelling in global memory; all three flip the same cluster.
 enum WolffForm { kWolffGrow = 0, kWolffSlab = 1, kWolffSite = 2 };
+// grow_cs: CTAs per lattice of the growth form (1, 2 or 4: a thread-block cluster)
 cudaError_t launch_wolff(const SweepArgs& a, bool fp64, bool masks, int nlat, int* labels,
                          long long lab_stride, long long* csize, int* err, cudaStream_t st,
-                         WolffForm form);
+                         WolffForm form, int grow_cs);
+int wolff_grow_clusters(bool fp64, bool masks, int cs);  // resident clusters of cs CTAs
 int wolff_slab_planes(const Geo& g);  // planes per shared-memory slab of the Wolff labelling
 cudaError_t launch_init(const InitArgs& a, cudaStream_t st);
 

@@ -32,7 +32,11 @@
 //   seed site:                     ctr = (replica, cycle, 0xFFFFFFFF, 4), word 0; the site is
 //                                  floor(w * N / 2^32) in reference site order; a vacancy seed
 //                                  means no flip this cycle (a configuration-independent choice)
+#include <cooperative_groups.h>
+
 #include "sweep_common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace j1j2 {
 namespace {
@@ -570,46 +574,71 @@ __global__ void wolff_flip_kernel(SweepArgs a, int* labels, long long lab_stride
 constexpr int kGrowThreads = 1024;
 constexpr int kGrowRing = 8192;  // queue entries kept in shared memory (32 KiB)
 
-template <class Real, bool MASKS>
+// CS > 1: a thread-block cluster of CS CTAs grows one lattice's cluster (levels of thousands of
+// sites in the coldest lattices are bound by one SM's issue rate).  The frontier ring and the
+// counters live in the shared memory of the cluster's first CTA; every CTA takes a share of a
+// level's sites, appends through that CTA's counter (a distributed-shared-memory atomic) and
+// meets the others at a cluster barrier between levels, whose release / acquire ordering makes
+// the level's appends (ring, cluster list) visible to all.
+enum : int { kCtlHead = 0, kCtlEnd = 1, kCtlTail = 2, kCtlRlim = 3, kCtlWlim = 4 };
+
+template <class Real, bool MASKS, int CS>
 __global__ void __launch_bounds__(kGrowThreads, 1)
     wolff_grow_kernel(SweepArgs a, int* list, long long list_stride, long long* csize)
 {
     const Geo g = a.g;
+    int rank = 0;
+    if constexpr (CS > 1) rank = (int)cg::this_cluster().block_rank();
     // coldest slots first: their clusters are the largest, so they start in the first wave
-    const int nconf = (int)gridDim.x / a.nrep;
-    const int slot = (int)blockIdx.x / nconf, conf = (int)blockIdx.x - slot * nconf;
+    const int lb = (int)blockIdx.x / CS;
+    const int nconf = (int)gridDim.x / CS / a.nrep;
+    const int slot = lb / nconf, conf = lb - slot * nconf;
     const int rep = a.rep_at_temp[conf * a.nrep + slot];
     const int lat = conf * a.nrep + rep;
     const int tid = (int)threadIdx.x, NT = (int)blockDim.x;
+    const int gt = rank * NT + tid, GT = CS * NT;  // this thread among the lattice's threads
     uint8_t* S = a.spins + (long long)lat * a.lat_stride;
     uint32_t* S32 = reinterpret_cast<uint32_t*>(S);
     const Real* P = wfield<Real>(a, conf);
     const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
     int* Q = list + (long long)lat * list_stride;
-    __shared__ int ring[kGrowRing];
-    __shared__ int s_head, s_end, s_tail, s_rlim, s_wlim;
+    __shared__ int ring_own[kGrowRing];
+    __shared__ int ctl_own[5];
+    int* ring = ring_own;  // the first CTA's ring and counters
+    int* ctl = ctl_own;
+    if constexpr (CS > 1) {
+        cg::cluster_group cl = cg::this_cluster();
+        ring = cl.map_shared_rank(ring_own, 0);
+        ctl = cl.map_shared_rank(ctl_own, 0);
+    }
+    auto sync_all = []() {
+        if constexpr (CS > 1)
+            cg::this_cluster().sync();
+        else
+            __syncthreads();
+    };
 
     const uint32_t cycle = a.ctl[0];
     const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
-    if (tid == 0) {
+    if (rank == 0 && tid == 0) {
         const uint32_t w =
             philox4x32_10((uint32_t)rep, cycle, 0xFFFFFFFFu, kTagWolffSeed, k0, k1).x;
         const int seed_site = (int)(((unsigned long long)w * (unsigned long long)g.N) >> 32);
         const int cs = compact_of_site(g, seed_site);
-        s_head = s_end = s_tail = 0;
-        s_rlim = s_wlim = kGrowRing;
+        ctl_own[kCtlHead] = ctl_own[kCtlEnd] = ctl_own[kCtlTail] = 0;
+        ctl_own[kCtlRlim] = ctl_own[kCtlWlim] = kGrowRing;
         const int b = S[cs];
         if (b != 1) {  // a vacant seed flips nothing
             S[cs] = (uint8_t)((2 - b) | 4);
             const int x = seed_site % g.L, y = (seed_site / g.L) % g.L, z = seed_site / (g.L * g.L);
             const int cc = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
-            Q[0] = ring[0] = (int)(((uint32_t)cc << 29) | ((uint32_t)(z >> 1) << 20) |
-                                   ((uint32_t)(y >> 1) << 11) | ((uint32_t)(x >> 1) << 2) |
-                                   (uint32_t)b);
-            s_end = s_tail = 1;
+            Q[0] = ring_own[0] = (int)(((uint32_t)cc << 29) | ((uint32_t)(z >> 1) << 20) |
+                                       ((uint32_t)(y >> 1) << 11) | ((uint32_t)(x >> 1) << 2) |
+                                       (uint32_t)b);
+            ctl_own[kCtlEnd] = ctl_own[kCtlTail] = 1;
         }
     }
-    __syncthreads();
+    sync_all();
 
     const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
     Real J2, J3;
@@ -626,9 +655,10 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
     const int s3 = J3 > Real(0) ? 1 : J3 < Real(0) ? -1 : 0;
 
     for (int level = 0; level < g.N; ++level) {  // at most N levels: every site joins once
-        const int head = s_head, end = s_end, rlim = s_rlim, wlim = s_wlim;
+        const int head = ctl[kCtlHead], end = ctl[kCtlEnd], rlim = ctl[kCtlRlim],
+                  wlim = ctl[kCtlWlim];
         if (head == end) break;
-        for (int idx = head + tid; idx < end; idx += NT) {
+        for (int idx = head + gt; idx < end; idx += GT) {
             // entry: compact coordinates and original spin byte of a cluster site
             const uint32_t e = (uint32_t)(idx < rlim ? ring[idx & (kGrowRing - 1)] : Q[idx]);
             const int c = (int)(e >> 29), Z = (int)((e >> 20) & 511), Y = (int)((e >> 11) & 511),
@@ -709,7 +739,7 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
                 const int sh = 8 * (jn[d] & 3);
                 if ((old[d] >> sh) & 4u) continue;  // not active, or joined meanwhile
                 atomicXor(&S32[jn[d] >> 2], 2u << sh);
-                const int pos = atomicAdd(&s_tail, 1);
+                const int pos = atomicAdd(&ctl[kCtlTail], 1);
                 const int entry = (int)(((uint32_t)cof(d) << 29) | ((uint32_t)zof(d) << 20) |
                                         ((uint32_t)yof(d) << 11) | ((uint32_t)xof(d) << 2) |
                                         ((old[d] >> sh) & 3u));
@@ -717,25 +747,82 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
                 if (pos < wlim) ring[pos & (kGrowRing - 1)] = entry;
             }
         }
-        __syncthreads();
-        if (tid == 0) {
-            s_rlim = wlim;
-            s_head = end;
-            s_end = s_tail;
-            s_wlim = end + kGrowRing;
+        sync_all();
+        if (rank == 0 && tid == 0) {
+            ctl_own[kCtlRlim] = wlim;
+            ctl_own[kCtlHead] = end;
+            ctl_own[kCtlEnd] = ctl_own[kCtlTail];
+            ctl_own[kCtlWlim] = end + kGrowRing;
         }
-        __syncthreads();
+        sync_all();
     }
     // clear the join bits of the cluster; atomically, at L2, where the flips were made (a plain
     // read-modify-write could see a line cached before the flip)
-    const int n = s_tail;
-    for (int k = tid; k < n; k += NT) {
+    const int n = ctl[kCtlTail];
+    for (int k = gt; k < n; k += GT) {
         const uint32_t e = (uint32_t)Q[k];
         const int i = cidx(g, (int)(e >> 29), (int)((e >> 20) & 511), (int)((e >> 11) & 511),
                            (int)((e >> 2) & 511));
         atomicAnd(&S32[i >> 2], ~(4u << (8 * (i & 3))));
     }
-    if (tid == 0) csize[lat] += n;
+    if (rank == 0 && tid == 0) csize[lat] += n;
+    if constexpr (CS > 1) cg::this_cluster().sync();  // the first CTA's counters were read above
+}
+
+template <class Real, bool MASKS, int CS>
+cudaError_t grow_launch(const SweepArgs& a, int nlat, int* list, long long list_stride,
+                        long long* csize, cudaStream_t st)
+{
+    auto kern = wolff_grow_kernel<Real, MASKS, CS>;
+    if constexpr (CS == 1) {
+        kern<<<nlat, kGrowThreads, 0, st>>>(a, list, list_stride, csize);
+        return cudaGetLastError();
+    } else {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(nlat * CS));
+        cfg.blockDim = dim3(kGrowThreads);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)CS;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, kern, a, list, list_stride, csize);
+    }
+}
+
+template <class Real, bool MASKS, int CS>
+int grow_fits()
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)CS);
+    cfg.blockDim = dim3(kGrowThreads);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)CS;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, wolff_grow_kernel<Real, MASKS, CS>, &cfg) !=
+        cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+template <class Real, bool MASKS>
+cudaError_t grow_dispatch(const SweepArgs& a, int nlat, int cs, int* list, long long list_stride,
+                          long long* csize, cudaStream_t st)
+{
+    if (cs == 2) return grow_launch<Real, MASKS, 2>(a, nlat, list, list_stride, csize, st);
+    if (cs == 4) return grow_launch<Real, MASKS, 4>(a, nlat, list, list_stride, csize, st);
+    return grow_launch<Real, MASKS, 1>(a, nlat, list, list_stride, csize, st);
 }
 
 template <class Real>
@@ -751,6 +838,18 @@ cudaError_t bonds(const SweepArgs& a, int* labels, long long ls, int* err, int n
 }
 
 }  // namespace
+
+// Clusters of cs CTAs (2 or 4) of the growth kernel that can be resident at once (0: none)
+int wolff_grow_clusters(bool fp64, bool masks, int cs)
+{
+    if (cs == 2)
+        return fp64 ? (masks ? grow_fits<double, true, 2>() : grow_fits<double, false, 2>())
+                    : (masks ? grow_fits<float, true, 2>() : grow_fits<float, false, 2>());
+    if (cs == 4)
+        return fp64 ? (masks ? grow_fits<double, true, 4>() : grow_fits<double, false, 4>())
+                    : (masks ? grow_fits<float, true, 4>() : grow_fits<float, false, 4>());
+    return 0;
+}
 
 // Planes per slab of the shared-memory form: the largest even divisor pz of H whose slab fits
 // kSlabSites2 sites (two CTAs per SM), else kSlabSites1 (one CTA per SM); 0 if none does.
@@ -790,24 +889,21 @@ cudaError_t slab_launch(const SweepArgs& a, int pz, int nlat, int* labels, long 
 // union-find retry overflow.
 cudaError_t launch_wolff(const SweepArgs& a, bool fp64, bool masks, int nlat, int* labels,
                          long long lab_stride, long long* csize, int* err, cudaStream_t st,
-                         WolffForm form)
+                         WolffForm form, int grow_cs)
 {
     const unsigned bx = (unsigned)((a.g.N + 255) / 256);
     const unsigned bxs = bx > 64 ? 64u : bx;
     cudaError_t e;
     if (form == kWolffGrow) {
-        const dim3 grid((unsigned)nlat);
         if (fp64)
-            masks ? wolff_grow_kernel<double, true><<<grid, kGrowThreads, 0, st>>>(
-                        a, labels, lab_stride, csize)
-                  : wolff_grow_kernel<double, false><<<grid, kGrowThreads, 0, st>>>(
-                        a, labels, lab_stride, csize);
-        else
-            masks ? wolff_grow_kernel<float, true><<<grid, kGrowThreads, 0, st>>>(
-                        a, labels, lab_stride, csize)
-                  : wolff_grow_kernel<float, false><<<grid, kGrowThreads, 0, st>>>(
-                        a, labels, lab_stride, csize);
-        return cudaGetLastError();
+            return masks ? grow_dispatch<double, true>(a, nlat, grow_cs, labels, lab_stride,
+                                                       csize, st)
+                         : grow_dispatch<double, false>(a, nlat, grow_cs, labels, lab_stride,
+                                                        csize, st);
+        return masks ? grow_dispatch<float, true>(a, nlat, grow_cs, labels, lab_stride, csize,
+                                                  st)
+                     : grow_dispatch<float, false>(a, nlat, grow_cs, labels, lab_stride, csize,
+                                                   st);
     }
     const int pz = form == kWolffSlab ? wolff_slab_planes(a.g) : 0;
     if (pz > 0) {
