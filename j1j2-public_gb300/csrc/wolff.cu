@@ -28,7 +28,10 @@
 // larger planes and for the per-site test mode.
 //
 // Streams (Philox4x32-10, key = (seed, conf_base + conf)):
-//   bond b of the site in group g: ctr = (replica, cycle, g, 3 + 16*b), word X & 3
+//   in-plane bond b = 0..3 of the site with compact index i: ctr = (replica, cycle, i, 5), word b
+//   +z bond of the site in group g:  ctr = (replica, cycle, g, 3 + 16*4), word X & 3
+//   (one call draws a site's four in-plane words: the growth form, which tests a site's bonds
+//   site by site, needs seven calls per cluster site instead of ten)
 //   seed site:                     ctr = (replica, cycle, 0xFFFFFFFF, 4), word 0; the site is
 //                                  floor(w * N / 2^32) in reference site order; a vacancy seed
 //                                  means no flip this cycle (a configuration-independent choice)
@@ -41,7 +44,8 @@ namespace cg = cooperative_groups;
 namespace j1j2 {
 namespace {
 
-enum : uint32_t { kTagWolffBond = 3u, kTagWolffSeed = 4u };
+enum : uint32_t { kTagWolffBond = 3u, kTagWolffSeed = 4u, kTagWolffSite = 5u };
+constexpr uint32_t kTagWolffZ = kTagWolffBond + 16u * 4u;  // the +z bond's tag
 
 struct SiteCoord {
     int x, y, z;
@@ -183,6 +187,7 @@ __global__ void __launch_bounds__(256) wolff_bond_kernel(SweepArgs a, int* label
                        compact_of_xyz(g, s.x, s.y, zp)};
     const int jh = MASKS ? (BM[ci] & 1) : 1, jv = MASKS ? ((BM[ci] >> 1) & 1) : 1;
     const Real pi = P[ci];
+    const U4 inplane = philox4x32_10((uint32_t)rep, cycle, (uint32_t)ci, kTagWolffSite, k0, k1);
 #pragma unroll
     for (int b = 0; b < 5; ++b) {
         const int cj = nb[b];
@@ -190,8 +195,9 @@ __global__ void __launch_bounds__(256) wolff_bond_kernel(SweepArgs a, int* label
         if (sj == 0) continue;
         Real w;
         if (!bond_weight<Real>(a, b, si, sj, jh, jv, pi, b < 2 ? P[cj] : Real(0), w)) continue;
-        const uint32_t r = u4_word(
-            philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffBond + 16u * b, k0, k1), X & 3);
+        const uint32_t r =
+            b < 4 ? u4_word(inplane, b)
+                  : u4_word(philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffZ, k0, k1), X & 3);
         if (bond_trial<Real>(w, beta, r) && !unite(lab, ci, cj)) atomicExch(err, 1);
     }
 }
@@ -362,6 +368,8 @@ __global__ void __launch_bounds__(512, 2)
 #pragma unroll
         for (int w = 0; w < 4; ++w) si[w] = w < nw ? (int)(ss[row0 + X0 + w] & 3u) - 1 : 0;
         unsigned act = 0;  // bit 5*w + b
+        U4 srr[4];         // each site's in-plane words, drawn when first needed
+        unsigned have = 0;
 #pragma unroll
         for (int b = 0; b < 5; ++b) {
             if (b == 4 && zleave) break;
@@ -389,11 +397,19 @@ __global__ void __launch_bounds__(512, 2)
                 }
             }
             if (!want) continue;
-            const U4 rr = philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffBond + 16u * b, k0, k1);
+            U4 rr{0, 0, 0, 0};
+            if (b == 4) rr = philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffZ, k0, k1);
 #pragma unroll
             for (int w = 0; w < 4; ++w) {
                 if (!((want >> w) & 1u)) continue;
-                const uint32_t word = u4_word(rr, w);
+                // in-plane bonds: word b of the site's own call
+                if (b < 4 && !((have >> w) & 1u)) {
+                    srr[w] = philox4x32_10((uint32_t)rep, cycle,
+                                           (uint32_t)(c * dc + goff + row0 + X0 + w),
+                                           kTagWolffSite, k0, k1);
+                    have |= 1u << w;
+                }
+                const uint32_t word = b == 4 ? u4_word(rr, w) : u4_word(srr[w], b);
                 const bool on = b < 2 ? bond_trial<Real>(wv[w], beta, word)
                                       : uniform_trial<Real>(b < 4 ? thr2 : thr3, word);
                 if (on) act |= 1u << (5 * w + b);
@@ -516,7 +532,7 @@ __global__ void __launch_bounds__(256) wolff_boundary_kernel(SweepArgs a, int pz
     volatile int* lab = labels + (long long)lat * lab_stride;
     const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
     const uint32_t grp = (uint32_t)(((c * g.Hh + Z) * g.Lh + Y) * g.Qr + Xq);
-    const U4 rr = philox4x32_10((uint32_t)rep, a.ctl[0], grp, kTagWolffBond + 16u * 4u, a.seed,
+    const U4 rr = philox4x32_10((uint32_t)rep, a.ctl[0], grp, kTagWolffZ, a.seed,
                                 a.conf_base + (uint32_t)conf);
 #pragma unroll
     for (int w = 0; w < 4; ++w) {
@@ -695,18 +711,33 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
                 m5 = BM[jn[5]];
                 m6 = BM[jn[6]];
             }
-            // the ten bonds' Philox words as independent chains while the loads are in flight
+            // the bonds' Philox words as independent chains while the loads are in flight: the
+            // site's own in-plane call (bonds 0-3), its +z call, each in-plane neighbour's own
+            // call (the word of the bond it owns) and the -z neighbour's +z call
             uint32_t word[10];
+            {
+                const U4 own = philox4x32_10((uint32_t)rep, cycle, (uint32_t)i, kTagWolffSite,
+                                             k0, k1);
+                word[0] = own.x;
+                word[1] = own.y;
+                word[2] = own.z;
+                word[3] = own.w;
+            }
 #pragma unroll
-            for (int d = 0; d < 10; ++d) {
+            for (int d = 4; d < 10; ++d) {
                 const int b = d < 5 ? d : d - 5;
-                const int co = d < 5 ? c : cof(d), Zo = d < 5 ? Z : zof(d);
-                const int Yo = d < 5 ? Y : yof(d), Xo = d < 5 ? X : xof(d);
-                const uint32_t grp =
-                    (uint32_t)(((co * g.Hh + Zo) * g.Lh + Yo) * g.Qr + (Xo >> 2));
-                word[d] = u4_word(
-                    philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffBond + 16u * b, k0, k1),
-                    Xo & 3);
+                if (b < 4) {
+                    word[d] = u4_word(philox4x32_10((uint32_t)rep, cycle, (uint32_t)jn[d],
+                                                    kTagWolffSite, k0, k1),
+                                      b);
+                } else {
+                    const int co = d < 5 ? c : cof(d), Zo = d < 5 ? Z : zof(d);
+                    const int Yo = d < 5 ? Y : yof(d), Xo = d < 5 ? X : xof(d);
+                    const uint32_t grp =
+                        (uint32_t)(((co * g.Hh + Zo) * g.Lh + Yo) * g.Qr + (Xo >> 2));
+                    word[d] = u4_word(
+                        philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffZ, k0, k1), Xo & 3);
+                }
             }
             unsigned act = 0;
 #pragma unroll

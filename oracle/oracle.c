@@ -860,9 +860,10 @@ void or_replay_pt(const or_lat *g, int32_t nrep, const double *beta, int32_t pts
 /* Wolff update of the engine, restated (FP64 form): bonds owned by each site (+x, +y,
  * (+x,+y), (-x,+y), +z = slots m3, m1, m5, m6, m9) with coupling K of Compute_local_field
  * (J:2498-2541); a bond with K s_i s_j > 0 is active when u < 1 - exp(-2 beta K s_i s_j), u from
- * ctr = (rep, cycle, group, 3 + 16*bond); the component of the seed site floor(w*N/2^32),
- * w from ctr = (rep, cycle, 0xFFFFFFFF, 4), is flipped (no flip when the seed is a vacancy).
- * Returns the flipped cluster size. */
+ * word b of ctr = (rep, cycle, compact site index, 5) for the in-plane bonds b = 0..3 and from
+ * word X & 3 of ctr = (rep, cycle, group, 67) for the +z bond; the component of the seed site
+ * floor(w*N/2^32), w from ctr = (rep, cycle, 0xFFFFFFFF, 4), is flipped (no flip when the seed
+ * is a vacancy).  Returns the flipped cluster size. */
 static int32_t uf_find(int32_t *lab, int32_t x)
 {
     while (lab[x] != x) {
@@ -886,6 +887,9 @@ int64_t or_wolff_step(const or_lat *g, int8_t *s, double beta, uint32_t seed, ui
         uint32_t gi;
         int w;
         site_group(L, H, x, y, z, &gi, &w);
+        const int32_t Lh = L / 2, Hh = H / 2;
+        const int32_t cc = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+        const uint32_t ci = (uint32_t)(((cc * Hh + (z >> 1)) * Lh + (y >> 1)) * Lh + (x >> 1));
         for (int b = 0; b < 5; b++) {
             int32_t j = m[slot[b] * N + i];
             if (g->occu[j] != 1) continue;
@@ -900,7 +904,8 @@ int64_t or_wolff_step(const or_lat *g, int8_t *s, double beta, uint32_t seed, ui
                 K = g->J3;
             double wgt = (s[i] * s[j] > 0) ? K : -K;
             if (!(wgt > 0.0)) continue;
-            uint32_t r = philox_word(seed, conf, rep, cycle, gi, 3u + 16u * (uint32_t)b, w);
+            uint32_t r = b < 4 ? philox_word(seed, conf, rep, cycle, ci, 5u, b)
+                               : philox_word(seed, conf, rep, cycle, gi, 3u + 16u * 4u, w);
             double u = (double)((r << 9) | (r >> 23)) * 0x1p-32;
             double pa = 1.0 - or_dexp(-((2.0 * wgt) * beta));
             if (u < pa) {
