@@ -53,7 +53,9 @@ extern "C" {
                                     (testing; with J1J2C_FLAG_GENERIC one site per thread)        */
 #define J1J2C_FLAG_WOLFF 32u     /* one Wolff cluster update at the start of every PT cycle       */
 #define J1J2C_FLAG_WOLFF_CS2 128u /* Wolff growth over 2 CTAs per lattice (testing; else tuned)    */
-#define J1J2C_FLAG_WOLFF_CS4 256u /* Wolff growth over 4 CTAs per lattice (testing; else tuned)    */
+#define J1J2C_FLAG_WOLFF_CS4 256u /* Wolff growth over 4 CTAs per lattice (testing; else tuned);
+                                     both flags: 2 CTAs for the coldest quarter of the slots, one
+                                     for the rest                                                  */
 
 /* Run parameters: the compile-time constants of J:43-96 that the hot path consumes. */
 typedef struct {

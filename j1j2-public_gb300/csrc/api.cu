@@ -42,6 +42,7 @@ struct Group {
     size_t smem = 0;
     bool tuned = false;
     int wolff_cs = 0;  // CTAs per lattice of the Wolff growth kernel (0: not tuned, 1)
+    int wolff_k = 0;   // 0 < k < nrep: only the k coldest slots take wolff_cs CTAs, the rest one
     int nlat() const { return nconf * nrep; }
 };
 
@@ -85,6 +86,9 @@ struct Ctx {
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> join_ev;
     cudaEvent_t fork_ev = nullptr;
+    // per group: the side stream and events of a Wolff update split over two launches
+    std::vector<cudaStream_t> wside;
+    std::vector<cudaEvent_t> wfork, wjoin;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long occ_total = 0;
 
@@ -156,6 +160,12 @@ void release(Ctx* c)
         if (p) cudaFree(p);
     for (auto s : c->side) cudaStreamDestroy(s);
     for (auto e : c->join_ev) cudaEventDestroy(e);
+    for (auto s : c->wside)
+        if (s) cudaStreamDestroy(s);
+    for (auto e : c->wfork)
+        if (e) cudaEventDestroy(e);
+    for (auto e : c->wjoin)
+        if (e) cudaEventDestroy(e);
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -374,12 +384,67 @@ cudaError_t enqueue_locnem(Ctx* c, cudaStream_t st)
     return cudaSuccess;
 }
 
-// CTAs per lattice of the Wolff growth kernel: pinned by a test flag, else the tuned count
+// CTAs per lattice of the Wolff growth kernel: pinned by the test flags (both: 2 CTAs for the
+// coldest quarter of the slots, one for the rest), else the tuned count
+constexpr uint32_t kWolffPinned = J1J2C_FLAG_WOLFF_CS2 | J1J2C_FLAG_WOLFF_CS4;
+
 int wolff_cs_of(const Ctx* c, const Group& grp)
 {
-    if (c->P.flags & J1J2C_FLAG_WOLFF_CS4) return 4;
-    if (c->P.flags & J1J2C_FLAG_WOLFF_CS2) return 2;
+    const uint32_t f = c->P.flags & kWolffPinned;
+    if (f == kWolffPinned || f == J1J2C_FLAG_WOLFF_CS2) return 2;
+    if (f == J1J2C_FLAG_WOLFF_CS4) return 4;
     return grp.wolff_cs > 0 ? grp.wolff_cs : 1;
+}
+
+// Coldest slots that take wolff_cs_of CTAs (0: every slot)
+int wolff_k_of(const Ctx* c, const Group& grp)
+{
+    const uint32_t f = c->P.flags & kWolffPinned;
+    if (f == kWolffPinned) return grp.nrep >= 2 ? (grp.nrep / 4 > 0 ? grp.nrep / 4 : 1) : 0;
+    return f ? 0 : grp.wolff_k;
+}
+
+// The group's Wolff side stream and events (created with the context)
+cudaError_t wolff_side(Ctx* c, const Group& grp)
+{
+    const size_t k = (size_t)(&grp - c->G.data());
+    if (c->wside.size() < c->G.size()) {
+        c->wside.resize(c->G.size(), nullptr);
+        c->wfork.resize(c->G.size(), nullptr);
+        c->wjoin.resize(c->G.size(), nullptr);
+    }
+    cudaError_t e = cudaSuccess;
+    if (!c->wside[k]) e = cudaStreamCreateWithFlags(&c->wside[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess && !c->wfork[k])
+        e = cudaEventCreateWithFlags(&c->wfork[k], cudaEventDisableTiming);
+    if (e == cudaSuccess && !c->wjoin[k])
+        e = cudaEventCreateWithFlags(&c->wjoin[k], cudaEventDisableTiming);
+    return e;
+}
+
+// Growth form over the group's lattices with a (spins of) a: the k coldest slots of every
+// configuration with cs CTAs per lattice and the other slots with one, as two concurrent
+// launches (0 < k < nrep), else every lattice with cs CTAs
+cudaError_t enqueue_wolff_grow(Ctx* c, const Group& grp, const SweepArgs& a, int cs, int k,
+                               cudaStream_t st)
+{
+    int* lab = c->d_labels + grp.lab_off;
+    long long* cz = c->d_csize + grp.rep0;
+    if (k <= 0 || k >= grp.nrep || cs == 1)
+        return launch_wolff_grow(a, grp.var.fp64, c->masks, grp.nconf, 0, grp.nrep, cs, lab,
+                                 grp.lat_stride, cz, st);
+    const size_t gi = (size_t)(&grp - c->G.data());
+    cudaError_t e;
+    if ((e = cudaEventRecord(c->wfork[gi], st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(c->wside[gi], c->wfork[gi], 0)) != cudaSuccess) return e;
+    if ((e = launch_wolff_grow(a, grp.var.fp64, c->masks, grp.nconf, 0, k, cs, lab,
+                               grp.lat_stride, cz, st)) != cudaSuccess)
+        return e;
+    if ((e = launch_wolff_grow(a, grp.var.fp64, c->masks, grp.nconf, k, grp.nrep - k, 1, lab,
+                               grp.lat_stride, cz, c->wside[gi])) != cudaSuccess)
+        return e;
+    if ((e = cudaEventRecord(c->wjoin[gi], c->wside[gi])) != cudaSuccess) return e;
+    return cudaStreamWaitEvent(st, c->wjoin[gi], 0);
 }
 
 // PTSWAPEVER sweeps and the observable reduction of lattices [lat0, lat0 + nlat) of a group
@@ -392,9 +457,10 @@ cudaError_t enqueue_wolff(Ctx* c, const Group& grp, cudaStream_t st)
     const WolffForm form = (c->P.flags & J1J2C_FLAG_GENERIC)    ? kWolffSite
                            : (c->P.flags & J1J2C_FLAG_NO_FIXED) ? kWolffSlab
                                                                 : kWolffGrow;
+    const int cs = wolff_cs_of(c, grp);
+    if (form == kWolffGrow) return enqueue_wolff_grow(c, grp, a, cs, wolff_k_of(c, grp), st);
     return launch_wolff(a, grp.var.fp64, c->masks, grp.nlat(), c->d_labels + grp.lab_off,
-                        grp.lat_stride, c->d_csize + grp.rep0, c->d_err, st, form,
-                        wolff_cs_of(c, grp));
+                        grp.lat_stride, c->d_csize + grp.rep0, c->d_err, st, form, cs);
 }
 
 cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int nthreads,
@@ -736,11 +802,13 @@ int tune_small_batch(Ctx* c, Group& grp)
     return J1J2C_OK;
 }
 
-// Wolff growth: 1, 2 or 4 CTAs per lattice (a thread-block cluster) timed on a scratch copy of
-// the group's lattices at the first run of a context with Wolff updates, the fastest kept, cached
-// per (precision, L, H, lattice count, bond dilution).  The coldest lattices' clusters span a
-// third of the lattice or more and are bound by one SM's issue rate; the hot ones are small.
-std::map<std::tuple<bool, int, int, int, bool>, int> g_wolff_cache;
+// Wolff growth: 1, 2 or 4 CTAs per lattice (a thread-block cluster) for every lattice, or 2 CTAs
+// for the 1/8, 1/4 or 1/2 coldest slots and one for the rest (two concurrent launches), timed on
+// a scratch copy of the group's lattices at the first run of a context with Wolff updates, the
+// fastest kept, cached per (precision, L, H, lattice count, bond dilution).  The coldest
+// lattices' clusters span a third of the lattice or more and are bound by one SM's issue rate;
+// the hot ones are small, and more CTAs per lattice mean more waves.
+std::map<std::tuple<bool, int, int, int, bool>, std::pair<int, int>> g_wolff_cache;
 
 int tune_wolff(Ctx* c, Group& grp)
 {
@@ -753,7 +821,8 @@ int tune_wolff(Ctx* c, Group& grp)
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_wolff_cache.find(key);
         if (it != g_wolff_cache.end()) {
-            grp.wolff_cs = it->second;
+            grp.wolff_cs = it->second.first;
+            grp.wolff_k = it->second.second;
             return J1J2C_OK;
         }
     }
@@ -766,16 +835,20 @@ int tune_wolff(Ctx* c, Group& grp)
         cudaMemcpyAsync(tmp, c->d_spins + grp.spin_off, bytes, cudaMemcpyDeviceToDevice, c->own);
     SweepArgs a = group_args(c, grp);
     a.spins = tmp;
-    int best = 1;
+    // candidates (CTAs per lattice, coldest slots that take them; k = nrep: every slot)
+    struct Cand {
+        int cs, k;
+    };
+    std::vector<Cand> cands{{1, grp.nrep}, {2, grp.nrep}, {4, grp.nrep}};
+    if (grp.nrep >= 8)
+        for (const int k : {grp.nrep / 8, grp.nrep / 4, grp.nrep / 2}) cands.push_back({2, k});
+    int best = 1, best_k = 0;
     float best_ms = 0.0f;
-    for (const int cs : {1, 2, 4}) {
+    for (const Cand cd : cands) {
+        const int cs = cd.cs;
         if (e != cudaSuccess) break;
         if (cs > 1 && wolff_grow_clusters(grp.var.fp64, c->masks, cs) <= 0) continue;
-        auto once = [&]() {
-            return launch_wolff(a, grp.var.fp64, c->masks, nlat, c->d_labels + grp.lab_off,
-                                grp.lat_stride, c->d_csize + grp.rep0, c->d_err, c->own,
-                                kWolffGrow, cs);
-        };
+        auto once = [&]() { return enqueue_wolff_grow(c, grp, a, cs, cd.k, c->own); };
         e = once();  // warm-up
         float ms = 0.0f;
         for (int k = 0; k < 3 && e == cudaSuccess; ++k) {  // the fastest of three
@@ -790,14 +863,16 @@ int tune_wolff(Ctx* c, Group& grp)
         if (e == cudaSuccess && (cs == 1 || ms < best_ms)) {
             best_ms = ms;
             best = cs;
+            best_k = cd.k < grp.nrep ? cd.k : 0;
         }
     }
     cudaStreamSynchronize(c->own);
     cudaFree(tmp);
     if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the Wolff update");
     grp.wolff_cs = best;
+    grp.wolff_k = best_k;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_wolff_cache[key] = best;
+    g_wolff_cache[key] = std::make_pair(best, best_k);
     return J1J2C_OK;
 }
 
@@ -1057,6 +1132,8 @@ int j1j2c_create_multi(void** out, const j1j2c_params* groups, int32_t ngroups)
             c->join_ev.push_back(ev);
         }
     }
+    for (const Group& grp : c->G)
+        if ((e = wolff_side(c, grp)) != cudaSuccess) return cfail(e, "Wolff stream");
     if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess) return cfail(e, "event");
     if ((e = cudaEventCreate(&c->ev1)) != cudaSuccess) return cfail(e, "event");
     if ((e = cudaMemset(c->d_spins, 1, (size_t)spin_bytes)) != cudaSuccess)

@@ -179,6 +179,11 @@ cudaError_t launch_wolff(const SweepArgs& a, bool fp64, bool masks, int nlat, in
                          long long lab_stride, long long* csize, int* err, cudaStream_t st,
                          WolffForm form, int grow_cs);
 int wolff_grow_clusters(bool fp64, bool masks, int cs);  // resident clusters of cs CTAs
+// The growth form for the lattices at temperature slots [slot0, slot0 + nslots) of the group's
+// nconf configurations (a.nrep slots each), cs CTAs per lattice
+cudaError_t launch_wolff_grow(const SweepArgs& a, bool fp64, bool masks, int nconf, int slot0,
+                              int nslots, int cs, int* labels, long long lab_stride,
+                              long long* csize, cudaStream_t st);
 int wolff_slab_planes(const Geo& g);  // planes per shared-memory slab of the Wolff labelling
 cudaError_t launch_init(const InitArgs& a, cudaStream_t st);
 

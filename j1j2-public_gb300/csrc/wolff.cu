@@ -598,17 +598,19 @@ constexpr int kGrowRing = 8192;  // queue entries kept in shared memory (32 KiB)
 // the level's appends (ring, cluster list) visible to all.
 enum : int { kCtlHead = 0, kCtlEnd = 1, kCtlTail = 2, kCtlRlim = 3, kCtlWlim = 4 };
 
+// Grid: the lattices at temperature slots [slot0, slot0 + gridDim.x / (CS nconf)) of the group's
+// nconf configurations, slot-major (coldest slots first: their clusters are the largest, so they
+// start in the first wave), CS CTAs each.
 template <class Real, bool MASKS, int CS>
 __global__ void __launch_bounds__(kGrowThreads, 1)
-    wolff_grow_kernel(SweepArgs a, int* list, long long list_stride, long long* csize)
+    wolff_grow_kernel(SweepArgs a, int* list, long long list_stride, long long* csize, int slot0,
+                      int nconf)
 {
     const Geo g = a.g;
     int rank = 0;
     if constexpr (CS > 1) rank = (int)cg::this_cluster().block_rank();
-    // coldest slots first: their clusters are the largest, so they start in the first wave
     const int lb = (int)blockIdx.x / CS;
-    const int nconf = (int)gridDim.x / CS / a.nrep;
-    const int slot = lb / nconf, conf = lb - slot * nconf;
+    const int slot = slot0 + lb / nconf, conf = lb % nconf;
     const int rep = a.rep_at_temp[conf * a.nrep + slot];
     const int lat = conf * a.nrep + rep;
     const int tid = (int)threadIdx.x, NT = (int)blockDim.x;
@@ -801,12 +803,13 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
 }
 
 template <class Real, bool MASKS, int CS>
-cudaError_t grow_launch(const SweepArgs& a, int nlat, int* list, long long list_stride,
-                        long long* csize, cudaStream_t st)
+cudaError_t grow_launch(const SweepArgs& a, int nconf, int slot0, int nslots, int* list,
+                        long long list_stride, long long* csize, cudaStream_t st)
 {
     auto kern = wolff_grow_kernel<Real, MASKS, CS>;
+    const int nlat = nconf * nslots;
     if constexpr (CS == 1) {
-        kern<<<nlat, kGrowThreads, 0, st>>>(a, list, list_stride, csize);
+        kern<<<nlat, kGrowThreads, 0, st>>>(a, list, list_stride, csize, slot0, nconf);
         return cudaGetLastError();
     } else {
         cudaLaunchConfig_t cfg = {};
@@ -821,7 +824,7 @@ cudaError_t grow_launch(const SweepArgs& a, int nlat, int* list, long long list_
         at[0].val.clusterDim.z = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&cfg, kern, a, list, list_stride, csize);
+        return cudaLaunchKernelEx(&cfg, kern, a, list, list_stride, csize, slot0, nconf);
     }
 }
 
@@ -848,12 +851,14 @@ int grow_fits()
 }
 
 template <class Real, bool MASKS>
-cudaError_t grow_dispatch(const SweepArgs& a, int nlat, int cs, int* list, long long list_stride,
-                          long long* csize, cudaStream_t st)
+cudaError_t grow_dispatch(const SweepArgs& a, int nconf, int slot0, int nslots, int cs, int* list,
+                          long long list_stride, long long* csize, cudaStream_t st)
 {
-    if (cs == 2) return grow_launch<Real, MASKS, 2>(a, nlat, list, list_stride, csize, st);
-    if (cs == 4) return grow_launch<Real, MASKS, 4>(a, nlat, list, list_stride, csize, st);
-    return grow_launch<Real, MASKS, 1>(a, nlat, list, list_stride, csize, st);
+    if (cs == 2)
+        return grow_launch<Real, MASKS, 2>(a, nconf, slot0, nslots, list, list_stride, csize, st);
+    if (cs == 4)
+        return grow_launch<Real, MASKS, 4>(a, nconf, slot0, nslots, list, list_stride, csize, st);
+    return grow_launch<Real, MASKS, 1>(a, nconf, slot0, nslots, list, list_stride, csize, st);
 }
 
 template <class Real>
@@ -869,6 +874,24 @@ cudaError_t bonds(const SweepArgs& a, int* labels, long long ls, int* err, int n
 }
 
 }  // namespace
+
+// The growth form for the lattices at temperature slots [slot0, slot0 + nslots) of the group's
+// nconf configurations, cs CTAs per lattice
+cudaError_t launch_wolff_grow(const SweepArgs& a, bool fp64, bool masks, int nconf, int slot0,
+                              int nslots, int cs, int* labels, long long lab_stride,
+                              long long* csize, cudaStream_t st)
+{
+    if (nslots <= 0) return cudaSuccess;
+    if (fp64)
+        return masks ? grow_dispatch<double, true>(a, nconf, slot0, nslots, cs, labels,
+                                                   lab_stride, csize, st)
+                     : grow_dispatch<double, false>(a, nconf, slot0, nslots, cs, labels,
+                                                    lab_stride, csize, st);
+    return masks ? grow_dispatch<float, true>(a, nconf, slot0, nslots, cs, labels, lab_stride,
+                                              csize, st)
+                 : grow_dispatch<float, false>(a, nconf, slot0, nslots, cs, labels, lab_stride,
+                                               csize, st);
+}
 
 // Clusters of cs CTAs (2 or 4) of the growth kernel that can be resident at once (0: none)
 int wolff_grow_clusters(bool fp64, bool masks, int cs)
@@ -926,15 +949,8 @@ cudaError_t launch_wolff(const SweepArgs& a, bool fp64, bool masks, int nlat, in
     const unsigned bxs = bx > 64 ? 64u : bx;
     cudaError_t e;
     if (form == kWolffGrow) {
-        if (fp64)
-            return masks ? grow_dispatch<double, true>(a, nlat, grow_cs, labels, lab_stride,
-                                                       csize, st)
-                         : grow_dispatch<double, false>(a, nlat, grow_cs, labels, lab_stride,
-                                                        csize, st);
-        return masks ? grow_dispatch<float, true>(a, nlat, grow_cs, labels, lab_stride, csize,
-                                                  st)
-                     : grow_dispatch<float, false>(a, nlat, grow_cs, labels, lab_stride, csize,
-                                                   st);
+        return launch_wolff_grow(a, fp64, masks, nlat / a.nrep, 0, a.nrep, grow_cs, labels,
+                                 lab_stride, csize, st);
     }
     const int pz = form == kWolffSlab ? wolff_slab_planes(a.g) : 0;
     if (pz > 0) {

@@ -34,7 +34,8 @@ def _engine(jc, L, H, nconf, nrep, precision, flags=0, pp=0.0, bonds=0.0, betas=
 
 
 # Forms: flags 0 / 16 the seed-cluster growth (default), 8 the shared-memory slab labelling,
-# 4 the per-site global labelling; 128 / 256 the growth over a cluster of 2 / 4 CTAs per lattice.  Slab shapes: one slab per lattice (8 x 4), several slabs with
+# 4 the per-site global labelling; 128 / 256 the growth over a cluster of 2 / 4 CTAs per lattice,
+# 384 two CTAs for the coldest quarter of the slots and one for the rest (two launches).  Slab shapes: one slab per lattice (8 x 4), several slabs with
 # the +z boundary merge (48^3: 3 slabs of 16 planes; 96 x 8: 2 slabs of 4), one-CTA-per-SM slabs
 # (160 x 4: 2 slabs of 2 planes), no slab fits (200 x 4: the per-site form is used).
 @pytest.mark.parametrize("L,H,pp,bonds,flags", [(8, 4, 0.1, 0.2, 0), (10, 6, 0.0, 0.0, 0),
@@ -45,7 +46,8 @@ def _engine(jc, L, H, nconf, nrep, precision, flags=0, pp=0.0, bonds=0.0, betas=
                                                  (160, 4, 0.0, 0.0, 8), (200, 4, 0.05, 0.0, 8),
                                                  (2, 2, 0.0, 0.0, 0), (8, 4, 0.1, 0.2, 128),
                                                  (48, 48, 0.05, 0.0, 128),
-                                                 (96, 8, 0.1, 0.2, 256), (10, 6, 0.0, 0.0, 256)])
+                                                 (96, 8, 0.1, 0.2, 256), (10, 6, 0.0, 0.0, 256),
+                                                 (48, 48, 0.05, 0.0, 384)])
 def test_wolff_step_bit_identical(engine_mod, oracle, L, H, pp, bonds, flags):
     jc = engine_mod
     eng, dis, betas = _engine(jc, L, H, 2, 3, jc.FP64_PLAIN, flags, pp, bonds)
@@ -67,7 +69,7 @@ def test_wolff_step_bit_identical(engine_mod, oracle, L, H, pp, bonds, flags):
     eng.close()
 
 
-@pytest.mark.parametrize("nconf,flags", [(40, 0), (80, 0), (40, 128), (40, 256)])
+@pytest.mark.parametrize("nconf,flags", [(40, 0), (80, 0), (40, 128), (40, 256), (80, 384)])
 def test_wolff_growth_many_lattices(engine_mod, oracle, nconf, flags):
     """More lattices than SMs (160 and 320 lattices: two and three waves of growth CTAs, coldest
     slots first): the flipped clusters equal the oracle's in the first, middle and last
@@ -101,7 +103,8 @@ def test_wolff_fp32_forms_agree(engine_mod, oracle, L, H, pp, bonds):
     jc = engine_mod
     out = []
     for flags in (jc.FLAG_WOLFF, jc.FLAG_WOLFF | jc.FLAG_NO_FIXED, jc.FLAG_WOLFF | jc.FLAG_GENERIC,
-                  jc.FLAG_WOLFF | jc.FLAG_WOLFF_CS2, jc.FLAG_WOLFF | jc.FLAG_WOLFF_CS4):
+                  jc.FLAG_WOLFF | jc.FLAG_WOLFF_CS2, jc.FLAG_WOLFF | jc.FLAG_WOLFF_CS4,
+                  jc.FLAG_WOLFF | jc.FLAG_WOLFF_CS2 | jc.FLAG_WOLFF_CS4):
         eng, _, _ = _engine(jc, L, H, 2, 3, jc.FP32_BATCHED, flags, pp, bonds)
         sizes = [eng.wolff().copy()]
         eng.run(3, measure=True)
@@ -116,9 +119,12 @@ def test_wolff_fp32_forms_agree(engine_mod, oracle, L, H, pp, bonds):
     assert sum(int(x.sum()) for x in out[0][1]) > 0
 
 
-def test_wolff_inside_pt_cycles(engine_mod, oracle):
+@pytest.mark.parametrize("nrep", [4, 8])
+def test_wolff_inside_pt_cycles(engine_mod, oracle, nrep):
+    """PT cycles with a Wolff update first (the CTAs-per-lattice tuner runs at the first cycle;
+    with 8 replicas it also times the split over two launches) equal the replay."""
     jc = engine_mod
-    L, H, nrep = 8, 4, 4
+    L, H = 8, 4
     eng, dis, betas = _engine(jc, L, H, 2, nrep, jc.FP64_PLAIN, jc.FLAG_WOLFF, 0.05)
     states = [oracle.new_pt_state(np.stack([eng.spins(k, r) for r in range(nrep)]))
               for k in range(2)]
