@@ -52,6 +52,8 @@ extern "C" {
 #define J1J2C_FLAG_CLUSTER 64u   /* force the thread-block-cluster path, largest cluster that fits
                                     (testing; with J1J2C_FLAG_GENERIC one site per thread)        */
 #define J1J2C_FLAG_WOLFF 32u     /* one Wolff cluster update at the start of every PT cycle       */
+#define J1J2C_FLAG_STREAM 512u   /* the streaming form of the shape-specialised kernels: one CTA
+                                    per SM through a range of lattices (testing; else tuned)      */
 #define J1J2C_FLAG_WOLFF_CS2 128u /* Wolff growth over 2 CTAs per lattice (testing; else tuned)    */
 #define J1J2C_FLAG_WOLFF_CS4 256u /* Wolff growth over 4 CTAs per lattice (testing; else tuned);
                                      both flags: 2 CTAs for the coldest quarter of the slots, one

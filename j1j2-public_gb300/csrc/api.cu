@@ -234,25 +234,31 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
     // the shape-specialised kernels do not count flips
     if (!(fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_GLOBAL)) &&
         !c->diag.flip_counts) {
-        int nts[8];
-        bool sp[8];
-        const int n = fixed_candidates(fp64, grp.g.L, grp.g.H, c->masks, c->vac, nts, sp, 8);
-        int pick = n > 0 ? 0 : -1;
-        for (int k = 0; k < n; ++k)
-            if (nts[k] == grp.block_threads) pick = k;
+        FixedChoice fc[16];
+        const int n = fixed_candidates(fp64, grp.g.L, grp.g.H, c->masks, c->vac, fc, 16);
+        // the first per-lattice form (or the block_threads one); the streaming form when the
+        // test flag asks for it
+        const bool stream = (fl & J1J2C_FLAG_STREAM) != 0;
+        int pick = -1;
+        for (int k = n - 1; k >= 0; --k)
+            if (fc[k].stream == stream &&
+                (grp.block_threads == 0 || fc[k].nt == grp.block_threads))
+                pick = k;
         if (pick >= 0) {
-            v.fixed_nt = nts[pick];
+            v.fixed_nt = fc[pick].nt;
             v.quad = true;
-            v.stage_p = sp[pick];
+            v.stage_p = fc[pick].stage_p;
+            v.stream = fc[pick].stream;
             smem = sweep_smem_bytes(grp.g, v);
             if (smem <= budget) {
-                nthreads = nts[pick];
+                nthreads = fc[pick].nt;
                 SweepArgs none{};
                 none.g = grp.g;
-                CK(c, launch_fixed(none, fp64, c->vac, nthreads, 0, smem, nullptr, true));
+                CK(c, launch_fixed(none, fp64, c->vac, fc[pick], 0, smem, nullptr, true));
                 return J1J2C_OK;
             }
             v.fixed_nt = 0;
+            v.stream = false;
         }
     }
     v.quad = quad_ok;
@@ -328,6 +334,7 @@ SweepArgs group_args(Ctx* c, const Group& grp)
     a.lat0 = 0;
     a.use_override = 0;
     a.flips = c->d_flips ? c->d_flips + grp.spin_off : nullptr;
+    a.err = c->d_err;
     return a;
 }
 
@@ -535,11 +542,12 @@ int build_graph(Ctx* c, int measure)
 
 bool valid_conf(Ctx* c, int conf) { return conf >= 0 && conf < c->nconf; }
 
-// Autotuner: times every CTA size of the shape-specialised kernel on a scratch copy of the
-// group's lattices (the live state is not touched) and keeps the fastest.  Choices are cached per
-// (precision, L, H, lattice count) for the life of the process.
+// Autotuner: times every CTA size and form (one CTA per lattice, or streaming) of the
+// shape-specialised kernel on a scratch copy of the group's lattices (the live state is not
+// touched) and keeps the fastest.  Choices are cached per (precision, L, H, lattice count,
+// vacancies) for the life of the process.
 std::mutex g_tune_mu;
-std::map<std::tuple<bool, int, int, int>, int> g_tune_cache;
+std::map<std::tuple<bool, int, int, int, bool>, int> g_tune_cache;
 
 // Device time of 2 PT-cycle sweep launches of a group with kernel variant v (the fastest of three
 // timings), on a scratch copy of its lattices (the live state is not touched; one warm-up launch
@@ -887,23 +895,22 @@ int autotune(Ctx* c, Group& grp)
     if (c->P.flags & J1J2C_FLAG_CLUSTER) return J1J2C_OK;
     if (grp.var.cluster > 0 && grp.block_threads == 0) return tune_cluster(c, grp);
     if (grp.var.global && grp.var.fixed_nt > 0) return J1J2C_OK;
-    if (grp.block_threads > 0) return J1J2C_OK;
+    if (grp.block_threads > 0 || (c->P.flags & J1J2C_FLAG_STREAM)) return J1J2C_OK;
     if (grp.var.fixed_nt == 0) return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
-    int nts[8];
-    bool sp[8];
-    const int n =
-        fixed_candidates(grp.var.fp64, grp.g.L, grp.g.H, c->masks, c->vac, nts, sp, 8);
+    FixedChoice fc[16];
+    const int n = fixed_candidates(grp.var.fp64, grp.g.L, grp.g.H, c->masks, c->vac, fc, 16);
     if (n <= 1) return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
     const int nlat = grp.nlat();
-    const auto key = std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, nlat);
-    int best_nt = 0;
+    const auto key = std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, nlat, c->vac);
+    int best = -1;  // index into fc
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune_cache.find(key);
-        if (it != g_tune_cache.end()) best_nt = it->second;
+        if (it != g_tune_cache.end()) best = it->second;
     }
     const size_t budget = smem_budget(c);
-    if (best_nt == 0) {
+    if (best < 0 || best >= n) {
+        best = 0;
         uint8_t* tmp = nullptr;
         LatObs* tobs = nullptr;
         const size_t bytes = (size_t)nlat * grp.lat_stride;
@@ -923,26 +930,26 @@ int autotune(Ctx* c, Group& grp)
         float best_ms = 1e30f;
         for (int k = 0; k < n && e == cudaSuccess; ++k) {
             SweepVariant v = grp.var;
-            v.fixed_nt = nts[k];
-            v.stage_p = sp[k];
+            v.fixed_nt = fc[k].nt;
+            v.stage_p = fc[k].stage_p;
+            v.stream = fc[k].stream;
             const size_t sm = sweep_smem_bytes(grp.g, v);
             if (sm > budget) continue;
-            if ((e = launch_fixed(a, v.fp64, c->vac, nts[k], 0, sm, nullptr, true)) !=
-                cudaSuccess)
+            if ((e = launch_fixed(a, v.fp64, c->vac, fc[k], 0, sm, nullptr, true)) != cudaSuccess)
                 break;
-            if ((e = launch_fixed(a, v.fp64, c->vac, nts[k], nlat, sm, c->own, false)) !=
+            if ((e = launch_fixed(a, v.fp64, c->vac, fc[k], nlat, sm, c->own, false)) !=
                 cudaSuccess)
                 break;
             cudaEventRecord(c->ev0, c->own);
             for (int r = 0; r < 3 && e == cudaSuccess; ++r)
-                e = launch_fixed(a, v.fp64, c->vac, nts[k], nlat, sm, c->own, false);
+                e = launch_fixed(a, v.fp64, c->vac, fc[k], nlat, sm, c->own, false);
             cudaEventRecord(c->ev1, c->own);
             if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
             float ms = 0.0f;
             if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
             if (e == cudaSuccess && ms < best_ms) {
                 best_ms = ms;
-                best_nt = nts[k];
+                best = k;
             }
         }
         cudaStreamSynchronize(c->own);
@@ -950,19 +957,18 @@ int autotune(Ctx* c, Group& grp)
         cudaFree(tobs);
         if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the sweep kernel");
         std::lock_guard<std::mutex> lk(g_tune_mu);
-        g_tune_cache[key] = best_nt;
+        g_tune_cache[key] = best;
     }
-    for (int k = 0; k < n; ++k)
-        if (nts[k] == best_nt) {
-            grp.var.fixed_nt = nts[k];
-            grp.var.stage_p = sp[k];
-            grp.smem = sweep_smem_bytes(grp.g, grp.var);
-            grp.nthreads = nts[k];
-            SweepArgs none{};
-            none.g = grp.g;
-            CK(c, launch_fixed(none, grp.var.fp64, c->vac, grp.nthreads, 0, grp.smem, nullptr,
-                               true));
-        }
+    grp.var.fixed_nt = fc[best].nt;
+    grp.var.stage_p = fc[best].stage_p;
+    grp.var.stream = fc[best].stream;
+    grp.smem = sweep_smem_bytes(grp.g, grp.var);
+    grp.nthreads = fc[best].nt;
+    {
+        SweepArgs none{};
+        none.g = grp.g;
+        CK(c, launch_fixed(none, grp.var.fp64, c->vac, fc[best], 0, grp.smem, nullptr, true));
+    }
     free_graphs(c);
     return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
 }

@@ -45,6 +45,7 @@ struct SweepArgs {
     uint32_t sweep_override;
     int* flips;              // accepted flips per site, row (conf * nrep + slot) of lat_stride
                              // ints (nullptr: not counted; generic kernels only)
+    int* err;                // set to 1 when a bounded wait of a kernel gave up (or nullptr)
 };
 
 // Replica-indexed arrays are laid out conf by conf: conf c owns entries rbase[c] ..
@@ -126,6 +127,7 @@ struct SweepVariant {
     bool masks;    // bond dilution present
     int mode;      // kModeSweep / kModeAudit
     int fixed_nt;  // > 0: shape-specialised kernel with this many threads per CTA
+    bool stream;   // shape-specialised kernel: the streaming form
     bool global;   // lattice in HBM, one launch per colour phase (too large for shared memory;
                    // with fixed_nt > 0 the shape-specialised form)
     bool vac;      // some conf has vacancies (shape-specialised kernels: vacancy handling on)
@@ -151,9 +153,15 @@ cudaError_t launch_sweep_cluster(const SweepArgs& a, const SweepVariant& v, int 
                                  cudaStream_t st);
 
 // Shape-specialised kernels (sweep_fixed.cu): CTA sizes available for a shape, and the launch.
-int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, int* nts, bool* stage_p,
-                     int cap);
-cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, int nt, int nblocks,
+// A shape-specialised kernel: CTA size, field staged in shared memory, streaming form (one CTA
+// per SM through a range of lattices, spins double-buffered by bulk copies)
+struct FixedChoice {
+    int nt;
+    bool stage_p, stream;
+};
+int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, FixedChoice* out, int cap);
+// nlat lattices from a.lat0 (prepare: only set the kernel's shared-memory limit)
+cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, const FixedChoice& ch, int nlat,
                          size_t smem, cudaStream_t st, bool prepare);
 
 // Shape-specialised kernels for lattices in HBM (one launch per colour phase): CTA size for a

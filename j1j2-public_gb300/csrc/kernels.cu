@@ -853,7 +853,10 @@ cudaError_t dispatch(const SweepArgs& a, const SweepVariant& v, int nb, int nt, 
 
 size_t sweep_smem_bytes(const Geo& g, const SweepVariant& v)
 {
-    size_t b = (size_t)((g.N + 15) & ~15);
+    const size_t spins = (size_t)((g.N + 15) & ~15);
+    const size_t field = ((size_t)g.N * (v.fp64 ? 8 : 4) + 15) & ~(size_t)15;
+    if (v.fixed_nt > 0 && v.stream) return field + 2 * spins;  // two spin buffers
+    size_t b = spins;
     if (v.stage_p) b += (size_t)g.N * (v.fp64 ? 8 : 4);
     return (b + 15) & ~(size_t)15;
 }
@@ -869,7 +872,8 @@ cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks,
                          size_t smem, cudaStream_t st)
 {
     if (v.fixed_nt > 0)
-        return launch_fixed(a, v.fp64, v.vac, v.fixed_nt, nblocks, smem, st, false);
+        return launch_fixed(a, v.fp64, v.vac, FixedChoice{v.fixed_nt, v.stage_p, v.stream},
+                            nblocks, smem, st, false);
     return dispatch(a, v, nblocks, nthreads, smem, st, false);
 }
 

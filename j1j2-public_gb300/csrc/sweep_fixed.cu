@@ -404,12 +404,136 @@ __global__ void __launch_bounds__(NT, MINB) sweep_fixed_kernel(SweepArgs a)
     block_copy16(Sg, S, Sh::NB);
 }
 
+// Streaming form of the same kernel: one resident CTA per SM (MINB per SM) works through a
+// contiguous range of the group's lattices.  The next lattice's spins arrive by a bulk copy of
+// the tensor memory accelerator (completed on an mbarrier) into the second of two shared-memory
+// buffers while the current one is swept, each finished lattice leaves by a bulk store, and the
+// field stays resident while consecutive lattices are replicas of one configuration (a
+// configuration's replicas are contiguous), so a CTA loads it once or twice instead of once per
+// lattice.  Sweeps and results are those of sweep_fixed_kernel, bit for bit.
+template <class Real, int LH, int HH, int NT, int MINB, bool VAC>
+__global__ void __launch_bounds__(NT, MINB) sweep_stream_kernel(SweepArgs a, int nlat)
+{
+    using Sh = Shape<LH, HH>;
+    constexpr int QPT = (Sh::CS + NT - 1) / NT;
+    constexpr uint32_t SB = (uint32_t)Sh::NB;                                  // spin bytes
+    constexpr uint32_t PB = (uint32_t)((Sh::N * sizeof(Real) + 15) & ~(size_t)15);  // field bytes
+    constexpr uint32_t kChunk = 16384;  // bytes per bulk copy instruction
+    extern __shared__ __align__(128) unsigned char smem[];
+    Real* Ps = reinterpret_cast<Real*>(smem);
+    unsigned char* Sbuf = smem + PB;  // two spin buffers of SB bytes
+    __shared__ __align__(8) uint64_t bar[3];  // spin buffer 0, spin buffer 1, field
+    const int tid = (int)threadIdx.x;
+    const int first = (int)(((long long)blockIdx.x * nlat) / gridDim.x);
+    const int last = (int)(((long long)(blockIdx.x + 1) * nlat) / gridDim.x);
+    auto spins_of = [&](int l) { return a.spins + (long long)(a.lat0 + l) * a.lat_stride; };
+    auto field_of = [&](int l) { return field_base<Real>(a, (a.lat0 + l) / a.nrep); };
+    auto copy_in = [&](void* dst, const void* src, uint32_t bytes, uint64_t* b) {
+        mbar_expect_tx(b, bytes);
+        for (uint32_t o = 0; o < bytes; o += kChunk)
+            bulk_load(static_cast<unsigned char*>(dst) + o,
+                      static_cast<const unsigned char*>(src) + o,
+                      bytes - o < kChunk ? bytes - o : kChunk, b);
+    };
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init(&bar[2], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    if (first >= last) return;
+    if (tid == 0) {
+        copy_in(Sbuf, spins_of(first), SB, &bar[0]);
+        copy_in(Ps, field_of(first), PB, &bar[2]);
+    }
+    OffsetCache<QPT> off;
+    if constexpr (OffsetCache<QPT>::kHold) {
+#pragma unroll
+        for (int j = 0; j < QPT; ++j) {
+            const int q = tid + j * NT;
+            off.off[j] = quad_offsets<LH, HH>(q < Sh::CS ? q : 0);
+        }
+    }
+    uint32_t ph0 = 0, ph1 = 0, phf = 0;
+    bool field_pending = true;
+    for (int l = first; l < last; ++l) {
+        const int buf = (l - first) & 1;
+        uint32_t* S32 = reinterpret_cast<uint32_t*>(Sbuf + buf * SB);
+        mbar_wait(&bar[buf], buf ? ph1 : ph0, a.err);
+        if (buf)
+            ph1 ^= 1u;
+        else
+            ph0 ^= 1u;
+        if (field_pending) {
+            mbar_wait(&bar[2], phf, a.err);
+            phf ^= 1u;
+            field_pending = false;
+        }
+        if (tid == 0 && l + 1 < last) {  // next lattice into the other buffer
+            bulk_wait_read();            // its previous lattice has left
+            copy_in(Sbuf + (buf ^ 1) * SB, spins_of(l + 1), SB, &bar[buf ^ 1]);
+        }
+        const int lat = a.lat0 + l;
+        const int conf = lat / a.nrep;
+        const int rep = lat - conf * a.nrep;
+        double beta;
+        uint32_t sweep0;
+        if (a.use_override) {
+            beta = a.beta_override;
+            sweep0 = a.sweep_override;
+        } else {
+            beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+            sweep0 = a.ctl[0] * (uint32_t)a.ptswapever;
+        }
+        const float kb = (float)(-2.0 * beta * 1.4426950408889634);
+        const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+        Acc acc{0, 0, 0, 0, 0};
+#pragma unroll 1
+        for (int t = 0; t < a.nsweeps; ++t)
+            all_colours<Real, LH, HH, NT, QPT, false, VAC>(a, S32, Ps, off, sweep0 + (uint32_t)t,
+                                                           (uint32_t)rep, k0, k1, beta, kb, acc);
+        all_colours<Real, LH, HH, NT, QPT, true, VAC>(a, S32, Ps, off, 0u, 0u, 0u, 0u, beta, kb,
+                                                      acc);
+        const Acc tot = block_reduce(acc);
+        fence_async_shared();  // the sweeps' shared-memory writes, before the bulk copies
+        __syncthreads();
+        if (tid == 0) {
+            store_obs(a.obs + lat, tot);
+            bulk_store(spins_of(l), S32, SB);
+            bulk_commit();
+            if (l + 1 < last && (lat + 1) / a.nrep != conf) {  // next configuration's field
+                copy_in(Ps, field_of(l + 1), PB, &bar[2]);
+            }
+        }
+        if (l + 1 < last && (lat + 1) / a.nrep != conf) field_pending = true;
+    }
+    if (tid == 0) bulk_wait_all();  // every lattice has left before the CTA ends
+}
+
 template <class Real, int LH, int HH, int NT, int MINB, bool STAGE_P, bool VAC>
 cudaError_t run_fixed(const SweepArgs& a, int nblocks, size_t smem, cudaStream_t st, bool prep)
 {
     auto k = sweep_fixed_kernel<Real, LH, HH, NT, MINB, STAGE_P, VAC>;
     if (prep) return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<nblocks, NT, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+// streaming form: MINB CTAs per SM (or one per lattice when there are fewer lattices)
+template <class Real, int LH, int HH, int NT, int MINB, bool STAGE_P, bool VAC>
+cudaError_t run_stream(const SweepArgs& a, int nlat, size_t smem, cudaStream_t st, bool prep)
+{
+    static_assert(STAGE_P, "the streaming form keeps the field in shared memory");
+    auto k = sweep_stream_kernel<Real, LH, HH, NT, MINB, VAC>;
+    if (prep) return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int dev = 0, nsm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int grid = nlat < nsm * MINB ? nlat : nsm * MINB;
+    if (grid <= 0) return cudaSuccess;
+    k<<<grid, NT, smem, st>>>(a, nlat);
     return cudaGetLastError();
 }
 
@@ -421,6 +545,7 @@ struct FixedEntry {
     bool stage_p;
     bool vac;  // handles vacancies (entries without it are only used for vacancy-free contexts)
     FixedFn fn;
+    bool stream = false;  // the streaming form
 };
 
 // Shapes of the reference's configurations (L = 16, 24, 32, 48 with H = L) and the CTA sizes
@@ -439,6 +564,11 @@ const FixedEntry kFixed[] = {
     {false, 48, 48, 576, false, true, run_fixed<float, 24, 24, 576, 1, false, true>},
     {true, 24, 24, 448, true, true, run_fixed<double, 12, 12, 448, 1, true, true>},
     {true, 32, 32, 512, false, true, run_fixed<double, 16, 16, 512, 1, false, true>},
+    // streaming forms (the autotuner times them against the per-lattice CTAs above)
+    {false, 32, 32, 1024, true, false, run_stream<float, 16, 16, 1024, 1, true, false>, true},
+    {false, 32, 32, 1024, true, true, run_stream<float, 16, 16, 1024, 1, true, true>, true},
+    {false, 24, 24, 448, true, true, run_stream<float, 12, 12, 448, 2, true, true>, true},
+    {false, 16, 16, 128, true, true, run_stream<float, 8, 8, 128, 8, true, true>, true},
 };
 
 // Entries usable for a context: vacancy-free entries when it has no vacancy (where they exist),
@@ -608,26 +738,21 @@ const HbmEntry kHbm[] = {
 
 }  // namespace
 
-int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, int* nts, bool* stage_p,
-                     int cap)
+int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, FixedChoice* out, int cap)
 {
     if (masks) return 0;
     int n = 0;
     for (const auto& e : kFixed)
-        if (usable(e, fp64, L, H, vac) && n < cap) {
-            nts[n] = e.nt;
-            stage_p[n] = e.stage_p;
-            ++n;
-        }
+        if (usable(e, fp64, L, H, vac) && n < cap) out[n++] = FixedChoice{e.nt, e.stage_p, e.stream};
     return n;
 }
 
-cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, int nt, int nblocks,
+cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, const FixedChoice& ch, int nlat,
                          size_t smem, cudaStream_t st, bool prepare)
 {
     for (const auto& e : kFixed)
-        if (usable(e, fp64, a.g.L, a.g.H, vac) && e.nt == nt)
-            return e.fn(a, nblocks, smem, st, prepare);
+        if (usable(e, fp64, a.g.L, a.g.H, vac) && e.nt == ch.nt && e.stream == ch.stream)
+            return e.fn(a, nlat, smem, st, prepare);
     return cudaErrorInvalidValue;
 }
 

@@ -358,6 +358,28 @@ def test_hbm_kernel_replicas_per_thread(engine_mod, oracle, precision, nrep):
     np.testing.assert_array_equal(out[0][2], out[1][2])
 
 
+@pytest.mark.parametrize("L,pp", [(32, 0.0), (32, 0.05), (24, 0.05), (16, 0.05)])
+def test_streaming_kernel_equals_per_lattice_kernel(engine_mod, oracle, L, pp):
+    """FP32: the streaming form (one CTA per SM through a range of lattices, spins double-
+    buffered by bulk copies, the field reloaded where the range crosses a configuration) against
+    one CTA per lattice: bitwise equal spins, sums and observables, 320 lattices."""
+    jc = engine_mod
+    nconf, nrep = 10, 32
+    out = []
+    for flags, bt in ((0, {32: 1024, 24: 448, 16: 128}[L]), (jc.FLAG_STREAM, 0)):
+        eng, _, _ = _setup(jc, oracle, L, L, nconf, nrep, jc.FP32_BATCHED, pp=pp, flags=flags,
+                           block_threads=bt)
+        eng.run(2, measure=False)
+        eng.run(2, measure=True)
+        out.append(([eng.spins(k, r) for k in range(nconf) for r in range(nrep)],
+                    eng.slot_sums(-1)[0], eng.observables(-1)))
+        eng.close()
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    np.testing.assert_array_equal(out[0][2], out[1][2])
+
+
 def test_hbm_kernel_L96_fp64_bit_identical_to_replay(engine_mod, oracle):
     """96^3 with 5 % vacancies (the reference's largest configuration) through the shape-
     specialised kernel that keeps lattices in HBM: spins, maps and running sums equal the replay."""
