@@ -410,31 +410,101 @@ __global__ void __launch_bounds__(NT, MINB) sweep_fixed_kernel(SweepArgs a)
 // buffers while the current one is swept, each finished lattice leaves by a bulk store, and the
 // field stays resident while consecutive lattices are replicas of one configuration (a
 // configuration's replicas are contiguous), so a CTA loads it once or twice instead of once per
-// lattice.  Sweeps and results are those of sweep_fixed_kernel, bit for bit.
+// lattice.  Sweeps and results are those of sweep_fixed_kernel, bit for bit.  The two buffers
+// take turns in an unrolled pair of lattice steps, so every shared-memory address of the sweeps
+// stays a register offset plus an immediate.
+template <class Real, int LH, int HH>
+struct StreamLayout {
+    using Sh = Shape<LH, HH>;
+    static constexpr uint32_t SB = (uint32_t)Sh::NB;                                     // spins
+    static constexpr uint32_t PB = (uint32_t)((Sh::N * sizeof(Real) + 15) & ~(size_t)15);  // field
+    static constexpr uint32_t kChunk = 16384;  // bytes per bulk copy instruction
+};
+
+struct StreamState {
+    uint32_t ph[3];      // mbarrier phases: spin buffer 0, spin buffer 1, field
+    bool field_pending;  // the field of the current configuration is still arriving
+};
+
+template <class Real, int LH, int HH>
+__device__ __forceinline__ void stream_copy_in(void* dst, const void* src, uint32_t bytes,
+                                               uint64_t* b)
+{
+    constexpr uint32_t kChunk = StreamLayout<Real, LH, HH>::kChunk;
+    mbar_expect_tx(b, bytes);
+    for (uint32_t o = 0; o < bytes; o += kChunk)
+        bulk_load(static_cast<unsigned char*>(dst) + o, static_cast<const unsigned char*>(src) + o,
+                  bytes - o < kChunk ? bytes - o : kChunk, b);
+}
+
+// One lattice of the range from spin buffer BUF (compile-time: constant shared-memory offsets)
+template <class Real, int LH, int HH, int NT, int QPT, bool VAC, int BUF>
+__device__ __forceinline__ void stream_step(const SweepArgs& a, unsigned char* smem, uint64_t* bar,
+                                            const OffsetCache<QPT>& off, int l, int last,
+                                            StreamState& st)
+{
+    using Lay = StreamLayout<Real, LH, HH>;
+    const int tid = (int)threadIdx.x;
+    Real* Ps = reinterpret_cast<Real*>(smem);
+    uint32_t* S32 = reinterpret_cast<uint32_t*>(smem + Lay::PB + BUF * Lay::SB);
+    mbar_wait(&bar[BUF], st.ph[BUF], a.err);
+    st.ph[BUF] ^= 1u;
+    if (st.field_pending) {
+        mbar_wait(&bar[2], st.ph[2], a.err);
+        st.ph[2] ^= 1u;
+        st.field_pending = false;
+    }
+    const int lat = a.lat0 + l;
+    if (tid == 0 && l + 1 < last) {  // next lattice into the other buffer
+        bulk_wait_read();            // its previous lattice has left
+        stream_copy_in<Real, LH, HH>(smem + Lay::PB + (BUF ^ 1) * Lay::SB,
+                                     a.spins + (long long)(lat + 1) * a.lat_stride, Lay::SB,
+                                     &bar[BUF ^ 1]);
+    }
+    const int conf = lat / a.nrep;
+    const int rep = lat - conf * a.nrep;
+    double beta;
+    uint32_t sweep0;
+    if (a.use_override) {
+        beta = a.beta_override;
+        sweep0 = a.sweep_override;
+    } else {
+        beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+        sweep0 = a.ctl[0] * (uint32_t)a.ptswapever;
+    }
+    const float kb = (float)(-2.0 * beta * 1.4426950408889634);
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    Acc acc{0, 0, 0, 0, 0};
+#pragma unroll 1
+    for (int t = 0; t < a.nsweeps; ++t)
+        all_colours<Real, LH, HH, NT, QPT, false, VAC>(a, S32, Ps, off, sweep0 + (uint32_t)t,
+                                                       (uint32_t)rep, k0, k1, beta, kb, acc);
+    all_colours<Real, LH, HH, NT, QPT, true, VAC>(a, S32, Ps, off, 0u, 0u, 0u, 0u, beta, kb, acc);
+    const Acc tot = block_reduce(acc);
+    fence_async_shared();  // the sweeps' shared-memory accesses, before the bulk copies
+    __syncthreads();
+    const bool next_conf = l + 1 < last && (lat + 1) / a.nrep != conf;
+    if (tid == 0) {
+        store_obs(a.obs + lat, tot);
+        bulk_store(a.spins + (long long)lat * a.lat_stride, S32, Lay::SB);
+        bulk_commit();
+        if (next_conf)  // the next configuration's field
+            stream_copy_in<Real, LH, HH>(Ps, field_base<Real>(a, conf + 1), Lay::PB, &bar[2]);
+    }
+    if (next_conf) st.field_pending = true;
+}
+
 template <class Real, int LH, int HH, int NT, int MINB, bool VAC>
 __global__ void __launch_bounds__(NT, MINB) sweep_stream_kernel(SweepArgs a, int nlat)
 {
     using Sh = Shape<LH, HH>;
+    using Lay = StreamLayout<Real, LH, HH>;
     constexpr int QPT = (Sh::CS + NT - 1) / NT;
-    constexpr uint32_t SB = (uint32_t)Sh::NB;                                  // spin bytes
-    constexpr uint32_t PB = (uint32_t)((Sh::N * sizeof(Real) + 15) & ~(size_t)15);  // field bytes
-    constexpr uint32_t kChunk = 16384;  // bytes per bulk copy instruction
     extern __shared__ __align__(128) unsigned char smem[];
-    Real* Ps = reinterpret_cast<Real*>(smem);
-    unsigned char* Sbuf = smem + PB;  // two spin buffers of SB bytes
     __shared__ __align__(8) uint64_t bar[3];  // spin buffer 0, spin buffer 1, field
     const int tid = (int)threadIdx.x;
     const int first = (int)(((long long)blockIdx.x * nlat) / gridDim.x);
     const int last = (int)(((long long)(blockIdx.x + 1) * nlat) / gridDim.x);
-    auto spins_of = [&](int l) { return a.spins + (long long)(a.lat0 + l) * a.lat_stride; };
-    auto field_of = [&](int l) { return field_base<Real>(a, (a.lat0 + l) / a.nrep); };
-    auto copy_in = [&](void* dst, const void* src, uint32_t bytes, uint64_t* b) {
-        mbar_expect_tx(b, bytes);
-        for (uint32_t o = 0; o < bytes; o += kChunk)
-            bulk_load(static_cast<unsigned char*>(dst) + o,
-                      static_cast<const unsigned char*>(src) + o,
-                      bytes - o < kChunk ? bytes - o : kChunk, b);
-    };
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -444,8 +514,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep_stream_kernel(SweepArgs a, int
     __syncthreads();
     if (first >= last) return;
     if (tid == 0) {
-        copy_in(Sbuf, spins_of(first), SB, &bar[0]);
-        copy_in(Ps, field_of(first), PB, &bar[2]);
+        const int lat = a.lat0 + first;
+        stream_copy_in<Real, LH, HH>(smem + Lay::PB, a.spins + (long long)lat * a.lat_stride,
+                                     Lay::SB, &bar[0]);
+        stream_copy_in<Real, LH, HH>(smem, field_base<Real>(a, lat / a.nrep), Lay::PB, &bar[2]);
     }
     OffsetCache<QPT> off;
     if constexpr (OffsetCache<QPT>::kHold) {
@@ -455,58 +527,11 @@ __global__ void __launch_bounds__(NT, MINB) sweep_stream_kernel(SweepArgs a, int
             off.off[j] = quad_offsets<LH, HH>(q < Sh::CS ? q : 0);
         }
     }
-    uint32_t ph0 = 0, ph1 = 0, phf = 0;
-    bool field_pending = true;
-    for (int l = first; l < last; ++l) {
-        const int buf = (l - first) & 1;
-        uint32_t* S32 = reinterpret_cast<uint32_t*>(Sbuf + buf * SB);
-        mbar_wait(&bar[buf], buf ? ph1 : ph0, a.err);
-        if (buf)
-            ph1 ^= 1u;
-        else
-            ph0 ^= 1u;
-        if (field_pending) {
-            mbar_wait(&bar[2], phf, a.err);
-            phf ^= 1u;
-            field_pending = false;
-        }
-        if (tid == 0 && l + 1 < last) {  // next lattice into the other buffer
-            bulk_wait_read();            // its previous lattice has left
-            copy_in(Sbuf + (buf ^ 1) * SB, spins_of(l + 1), SB, &bar[buf ^ 1]);
-        }
-        const int lat = a.lat0 + l;
-        const int conf = lat / a.nrep;
-        const int rep = lat - conf * a.nrep;
-        double beta;
-        uint32_t sweep0;
-        if (a.use_override) {
-            beta = a.beta_override;
-            sweep0 = a.sweep_override;
-        } else {
-            beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
-            sweep0 = a.ctl[0] * (uint32_t)a.ptswapever;
-        }
-        const float kb = (float)(-2.0 * beta * 1.4426950408889634);
-        const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
-        Acc acc{0, 0, 0, 0, 0};
+    StreamState st{{0u, 0u, 0u}, true};
 #pragma unroll 1
-        for (int t = 0; t < a.nsweeps; ++t)
-            all_colours<Real, LH, HH, NT, QPT, false, VAC>(a, S32, Ps, off, sweep0 + (uint32_t)t,
-                                                           (uint32_t)rep, k0, k1, beta, kb, acc);
-        all_colours<Real, LH, HH, NT, QPT, true, VAC>(a, S32, Ps, off, 0u, 0u, 0u, 0u, beta, kb,
-                                                      acc);
-        const Acc tot = block_reduce(acc);
-        fence_async_shared();  // the sweeps' shared-memory writes, before the bulk copies
-        __syncthreads();
-        if (tid == 0) {
-            store_obs(a.obs + lat, tot);
-            bulk_store(spins_of(l), S32, SB);
-            bulk_commit();
-            if (l + 1 < last && (lat + 1) / a.nrep != conf) {  // next configuration's field
-                copy_in(Ps, field_of(l + 1), PB, &bar[2]);
-            }
-        }
-        if (l + 1 < last && (lat + 1) / a.nrep != conf) field_pending = true;
+    for (int l = first; l < last; l += 2) {
+        stream_step<Real, LH, HH, NT, QPT, VAC, 0>(a, smem, bar, off, l, last, st);
+        if (l + 1 < last) stream_step<Real, LH, HH, NT, QPT, VAC, 1>(a, smem, bar, off, l + 1, last, st);
     }
     if (tid == 0) bulk_wait_all();  // every lattice has left before the CTA ends
 }
