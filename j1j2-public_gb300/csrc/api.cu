@@ -1597,10 +1597,15 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
     }
     CK(c, cudaStreamSynchronize(c->st));
     CK(c, cudaGetLastError());
-    if (c->wolff) {
+    bool bounded = c->wolff;  // kernels whose bounded waits or retries report through d_err
+    for (const Group& grp : c->G) bounded = bounded || grp.var.stream;
+    if (bounded) {
         int herr = 0;
         CK(c, cudaMemcpy(&herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
-        if (herr) return fail(c, J1J2C_ETIMEOUT, "Wolff union-find exceeded its retry budget");
+        if (herr)
+            return fail(c, J1J2C_ETIMEOUT,
+                        "a bounded device wait gave up (Wolff union-find retries or a bulk-copy "
+                        "wait of the streaming sweep kernel)");
     }
     return J1J2C_OK;
 }

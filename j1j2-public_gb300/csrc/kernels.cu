@@ -170,6 +170,13 @@ struct QuadNbr {
     uint32_t own, xp, xm, yp, ym, dpp, dpm, dmp, dmm, zp, zm;
 };
 
+// Flip-count row of the replica's temperature slot (nullptr: flips are not counted)
+__device__ __forceinline__ int* flip_row(const SweepArgs& a, int conf, int rep)
+{
+    if (!a.flips || a.use_override) return nullptr;
+    return a.flips + ((long long)conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]) * a.lat_stride;
+}
+
 // Spin words of a lattice held whole in one array of the compact layout (shared or global memory)
 struct CompactSpins {
     uint32_t* S32;
@@ -470,9 +477,9 @@ __global__ void __launch_bounds__(1024) sweep_kernel(SweepArgs a)
     const float kb = (float)(-2.0 * beta * 1.4426950408889634);
     const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
     Acc acc{0, 0, 0, 0, 0};
-    int* fl = nullptr;  // flip counts of this replica's temperature slot
-    if (a.flips && !a.use_override && MODE == kModeSweep)
-        fl = a.flips + ((long long)conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]) * a.lat_stride;
+    int* fl = (MODE == kModeSweep) ? flip_row(a, conf, rep) : nullptr;
+    const CompactSpins words(reinterpret_cast<uint32_t*>(S), g);
+    const FlatBytes bytes{S};
 
     for (int t = 0; t < a.nsweeps; ++t) {
         const uint32_t sweep = sweep0 + (uint32_t)t;
@@ -481,15 +488,15 @@ __global__ void __launch_bounds__(1024) sweep_kernel(SweepArgs a)
             if constexpr (QUAD) {
                 const int nq = g.Nc >> 2;
                 for (int q = tid; q < nq; q += NT)
-                    quad_step<Real, MASKS, false>(a, g, CompactSpins(reinterpret_cast<uint32_t*>(S), g), P, BM, c,
-                                                  q, sweep, (uint32_t)rep, k0, k1, beta, kb, acc,
-                                                  fl);
+                    quad_step<Real, MASKS, false>(a, g, words, P, BM, c, q, sweep, (uint32_t)rep,
+                                                  k0, k1, beta, kb, acc, fl);
             } else {
                 for (int k = tid; k < g.Nc; k += NT) {
                     const int X = k % g.Lh, r = k / g.Lh;
                     const int Y = r % g.Lh, Z = r / g.Lh;
-                    site_step<Real, MASKS, MODE, false>(a, g, FlatBytes{S}, P, BM, Pf32, c, X, Y, Z, sweep,
-                                                        (uint32_t)rep, k0, k1, beta, kb, acc, fl);
+                    site_step<Real, MASKS, MODE, false>(a, g, bytes, P, BM, Pf32, c, X, Y, Z,
+                                                        sweep, (uint32_t)rep, k0, k1, beta, kb,
+                                                        acc, fl);
                 }
             }
             __syncthreads();
@@ -512,14 +519,14 @@ __global__ void __launch_bounds__(1024) sweep_kernel(SweepArgs a)
         if constexpr (QUAD) {
             const int nq = g.Nc >> 2;
             for (int q = tid; q < nq; q += NT)
-                quad_step<Real, MASKS, true>(a, g, CompactSpins(reinterpret_cast<uint32_t*>(S), g), P, BM, c, q, 0u,
-                                             0u, 0u, 0u, beta, kb, acc);
+                quad_step<Real, MASKS, true>(a, g, words, P, BM, c, q, 0u, 0u, 0u, 0u, beta, kb,
+                                             acc);
         } else {
             for (int k = tid; k < g.Nc; k += NT) {
                 const int X = k % g.Lh, r = k / g.Lh;
                 const int Y = r % g.Lh, Z = r / g.Lh;
-                site_step<Real, MASKS, MODE, true>(a, g, FlatBytes{S}, P, BM, Pf32, c, X, Y, Z, 0u, 0u, 0u,
-                                                   0u, beta, kb, acc);
+                site_step<Real, MASKS, MODE, true>(a, g, bytes, P, BM, Pf32, c, X, Y, Z, 0u, 0u,
+                                                   0u, 0u, beta, kb, acc);
             }
         }
     }
@@ -727,19 +734,18 @@ __global__ void __launch_bounds__(256) sweep_global_kernel(SweepArgs a, int colo
     const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
     const int item = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     Acc acc{0, 0, 0, 0, 0};
-    int* fl = nullptr;  // flip counts of this replica's temperature slot
-    if (a.flips && !a.use_override)
-        fl = a.flips + ((long long)conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]) * a.lat_stride;
+    int* fl = flip_row(a, conf, rep);
     if constexpr (QUAD) {
         if (item < (g.Nc >> 2))
-            quad_step<Real, MASKS, false>(a, g, CompactSpins(reinterpret_cast<uint32_t*>(S), g), P, BM, colour,
-                                          item, sweep, (uint32_t)rep, k0, k1, beta, kb, acc, fl);
+            quad_step<Real, MASKS, false>(a, g, CompactSpins(reinterpret_cast<uint32_t*>(S), g), P,
+                                          BM, colour, item, sweep, (uint32_t)rep, k0, k1, beta,
+                                          kb, acc, fl);
     } else {
         if (item < g.Nc) {
             const int X = item % g.Lh, r = item / g.Lh;
-            site_step<Real, MASKS, kModeSweep, false>(a, g, FlatBytes{S}, P, BM, nullptr, colour, X,
-                                                      r % g.Lh, r / g.Lh, sweep, (uint32_t)rep,
-                                                      k0, k1, beta, kb, acc, fl);
+            site_step<Real, MASKS, kModeSweep, false>(a, g, FlatBytes{S}, P, BM, nullptr, colour,
+                                                      X, r % g.Lh, r / g.Lh, sweep,
+                                                      (uint32_t)rep, k0, k1, beta, kb, acc, fl);
         }
     }
 }
@@ -759,12 +765,13 @@ __global__ void __launch_bounds__(256) measure_global_kernel(SweepArgs a)
     if (item < 8 * per) {
         const int c = item / per, k = item - c * per;
         if constexpr (QUAD) {
-            quad_step<Real, MASKS, true>(a, g, CompactSpins(reinterpret_cast<uint32_t*>(S), g), P, BM, c, k, 0u, 0u,
-                                         0u, 0u, 0.0, 0.0f, acc);
+            quad_step<Real, MASKS, true>(a, g, CompactSpins(reinterpret_cast<uint32_t*>(S), g), P,
+                                         BM, c, k, 0u, 0u, 0u, 0u, 0.0, 0.0f, acc);
         } else {
             const int X = k % g.Lh, r = k / g.Lh;
-            site_step<Real, MASKS, kModeSweep, true>(a, g, FlatBytes{S}, P, BM, nullptr, c, X, r % g.Lh,
-                                                     r / g.Lh, 0u, 0u, 0u, 0u, 0.0, 0.0f, acc);
+            site_step<Real, MASKS, kModeSweep, true>(a, g, FlatBytes{S}, P, BM, nullptr, c, X,
+                                                     r % g.Lh, r / g.Lh, 0u, 0u, 0u, 0u, 0.0,
+                                                     0.0f, acc);
         }
     }
     const Acc tot = block_reduce(acc);
@@ -821,9 +828,9 @@ cudaError_t dispatch_masks(const SweepArgs& a, const SweepVariant& v, int nb, in
 {
     if (v.mode == kModeAudit) {
         if constexpr (sizeof(Real) == 8 && !QUAD && !STAGE_P) {
-            return v.masks ? do_launch<Real, false, false, true, kModeAudit>(a, nb, nt, sm, st, prep)
-                           : do_launch<Real, false, false, false, kModeAudit>(a, nb, nt, sm, st,
-                                                                              prep);
+            return v.masks
+                       ? do_launch<Real, false, false, true, kModeAudit>(a, nb, nt, sm, st, prep)
+                       : do_launch<Real, false, false, false, kModeAudit>(a, nb, nt, sm, st, prep);
         }
         return cudaErrorInvalidValue;
     }
@@ -1021,9 +1028,7 @@ __global__ void __launch_bounds__(kClusterThreads, 2) sweep_cluster_kernel(Sweep
     }
     const float kb = (float)(-2.0 * beta * 1.4426950408889634);
     const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
-    int* fl = nullptr;  // flip counts of this replica's temperature slot
-    if (a.flips && !a.use_override)
-        fl = a.flips + ((long long)conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]) * a.lat_stride;
+    int* fl = flip_row(a, conf, rep);
     Acc acc{0, 0, 0, 0, 0};
     const int q0 = z0 * plane_words;
     for (int t = 0; t < a.nsweeps; ++t) {

@@ -531,7 +531,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep_stream_kernel(SweepArgs a, int
 #pragma unroll 1
     for (int l = first; l < last; l += 2) {
         stream_step<Real, LH, HH, NT, QPT, VAC, 0>(a, smem, bar, off, l, last, st);
-        if (l + 1 < last) stream_step<Real, LH, HH, NT, QPT, VAC, 1>(a, smem, bar, off, l + 1, last, st);
+        if (l + 1 < last)
+            stream_step<Real, LH, HH, NT, QPT, VAC, 1>(a, smem, bar, off, l + 1, last, st);
     }
     if (tid == 0) bulk_wait_all();  // every lattice has left before the CTA ends
 }
@@ -768,7 +769,8 @@ int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, FixedChoice*
     if (masks) return 0;
     int n = 0;
     for (const auto& e : kFixed)
-        if (usable(e, fp64, L, H, vac) && n < cap) out[n++] = FixedChoice{e.nt, e.stage_p, e.stream};
+        if (usable(e, fp64, L, H, vac) && n < cap)
+            out[n++] = FixedChoice{e.nt, e.stage_p, e.stream};
     return n;
 }
 

@@ -14,9 +14,9 @@
 // as cross-checks and selectable by flags.
 //
 // Labelling: components are labelled in a scratch array (one int32 per site, the compact index
-// of a site of the same component) by lock-free union-find: hooking the larger root under the smaller with
-// atomicCAS, path halving in find, so every pointer goes to a smaller compact index and every
-// root is the smallest compact index of its component.  Then the seed's component is flipped.
+// of a site of the same component) by lock-free union-find: hooking the larger root under the
+// smaller with atomicCAS, path halving in find, so every pointer goes to a smaller compact index
+// and every root is the smallest compact index of its component.  Then the seed's component is flipped.
 //
 // Slab form (lattices up to 65536 sites per two planes): one CTA per slab of pz planes
 // (pz even, a divisor of H) stages the slab's spins in shared memory and runs the union-find on
@@ -692,7 +692,9 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
             const int Zm = pz ? Z : (Z == 0 ? g.Hh - 1 : Z - 1);
             // neighbour d: +x, +y, (+x,+y), (-x,+y), +z own the bond (b = d); -x, -y, (-x,-y),
             // (+x,-y), -z are the bonds b = d - 5 owned by the neighbour
-            auto cof = [&](int d) { return c ^ (d % 5 == 0 ? 1 : d % 5 == 1 ? 2 : d % 5 == 4 ? 4 : 3); };
+            auto cof = [&](int d) {
+                return c ^ (d % 5 == 0 ? 1 : d % 5 == 1 ? 2 : d % 5 == 4 ? 4 : 3);
+            };
             auto xof = [&](int d) {
                 return (d == 0 || d == 2 || d == 8) ? Xp : (d == 3 || d == 5 || d == 7) ? Xm : X;
             };
