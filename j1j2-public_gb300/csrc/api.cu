@@ -249,6 +249,7 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
             v.quad = true;
             v.stage_p = fc[pick].stage_p;
             v.stream = fc[pick].stream;
+            v.minb = fc[pick].minb;
             smem = sweep_smem_bytes(grp.g, v);
             if (smem <= budget) {
                 nthreads = fc[pick].nt;
@@ -933,6 +934,7 @@ int autotune(Ctx* c, Group& grp)
             v.fixed_nt = fc[k].nt;
             v.stage_p = fc[k].stage_p;
             v.stream = fc[k].stream;
+            v.minb = fc[k].minb;
             const size_t sm = sweep_smem_bytes(grp.g, v);
             if (sm > budget) continue;
             if ((e = launch_fixed(a, v.fp64, c->vac, fc[k], 0, sm, nullptr, true)) != cudaSuccess)
@@ -962,6 +964,7 @@ int autotune(Ctx* c, Group& grp)
     grp.var.fixed_nt = fc[best].nt;
     grp.var.stage_p = fc[best].stage_p;
     grp.var.stream = fc[best].stream;
+    grp.var.minb = fc[best].minb;
     grp.smem = sweep_smem_bytes(grp.g, grp.var);
     grp.nthreads = fc[best].nt;
     {

@@ -128,6 +128,7 @@ struct SweepVariant {
     int mode;      // kModeSweep / kModeAudit
     int fixed_nt;  // > 0: shape-specialised kernel with this many threads per CTA
     bool stream;   // shape-specialised kernel: the streaming form
+    int minb;      // shape-specialised kernel: resident CTAs per SM it is compiled for
     bool global;   // lattice in HBM, one launch per colour phase (too large for shared memory;
                    // with fixed_nt > 0 the shape-specialised form)
     bool vac;      // some conf has vacancies (shape-specialised kernels: vacancy handling on)
@@ -158,6 +159,7 @@ cudaError_t launch_sweep_cluster(const SweepArgs& a, const SweepVariant& v, int 
 struct FixedChoice {
     int nt;
     bool stage_p, stream;
+    int minb;  // resident CTAs per SM the kernel is compiled for
 };
 int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, FixedChoice* out, int cap);
 // nlat lattices from a.lat0 (prepare: only set the kernel's shared-memory limit)

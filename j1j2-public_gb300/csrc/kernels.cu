@@ -879,8 +879,9 @@ cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks,
                          size_t smem, cudaStream_t st)
 {
     if (v.fixed_nt > 0)
-        return launch_fixed(a, v.fp64, v.vac, FixedChoice{v.fixed_nt, v.stage_p, v.stream},
-                            nblocks, smem, st, false);
+        return launch_fixed(a, v.fp64, v.vac,
+                            FixedChoice{v.fixed_nt, v.stage_p, v.stream, v.minb}, nblocks, smem,
+                            st, false);
     return dispatch(a, v, nblocks, nthreads, smem, st, false);
 }
 

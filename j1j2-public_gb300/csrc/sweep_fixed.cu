@@ -572,16 +572,17 @@ struct FixedEntry {
     bool vac;  // handles vacancies (entries without it are only used for vacancy-free contexts)
     FixedFn fn;
     bool stream = false;  // the streaming form
+    int minb = 1;         // resident CTAs per SM the kernel is compiled for (MINB)
 };
 
 // Shapes of the reference's configurations (L = 16, 24, 32, 48 with H = L) and the CTA sizes
 // the autotuner chooses from; the MINB template argument is the CTAs per SM that shared memory
 // allows (it bounds the registers per thread).
 const FixedEntry kFixed[] = {
-    {false, 16, 16, 128, true, true, run_fixed<float, 8, 8, 128, 8, true, true>},
-    {false, 16, 16, 64, true, true, run_fixed<float, 8, 8, 64, 10, true, true>},
-    {false, 24, 24, 448, true, true, run_fixed<float, 12, 12, 448, 2, true, true>},
-    {false, 24, 24, 224, true, true, run_fixed<float, 12, 12, 224, 2, true, true>},
+    {false, 16, 16, 128, true, true, run_fixed<float, 8, 8, 128, 8, true, true>, false, 8},
+    {false, 16, 16, 64, true, true, run_fixed<float, 8, 8, 64, 10, true, true>, false, 10},
+    {false, 24, 24, 448, true, true, run_fixed<float, 12, 12, 448, 2, true, true>, false, 2},
+    {false, 24, 24, 224, true, true, run_fixed<float, 12, 12, 224, 2, true, true>, false, 2},
     {false, 32, 32, 1024, true, false, run_fixed<float, 16, 16, 1024, 1, true, false>},
     {false, 32, 32, 512, true, false, run_fixed<float, 16, 16, 512, 1, true, false>},
     {false, 32, 32, 1024, true, true, run_fixed<float, 16, 16, 1024, 1, true, true>},
@@ -593,8 +594,8 @@ const FixedEntry kFixed[] = {
     // streaming forms (the autotuner times them against the per-lattice CTAs above)
     {false, 32, 32, 1024, true, false, run_stream<float, 16, 16, 1024, 1, true, false>, true},
     {false, 32, 32, 1024, true, true, run_stream<float, 16, 16, 1024, 1, true, true>, true},
-    {false, 24, 24, 448, true, true, run_stream<float, 12, 12, 448, 2, true, true>, true},
-    {false, 16, 16, 128, true, true, run_stream<float, 8, 8, 128, 8, true, true>, true},
+    {false, 24, 24, 448, true, true, run_stream<float, 12, 12, 448, 2, true, true>, true, 2},
+    {false, 16, 16, 128, true, true, run_stream<float, 8, 8, 128, 8, true, true>, true, 8},
 };
 
 // Entries usable for a context: vacancy-free entries when it has no vacancy (where they exist),
@@ -770,7 +771,7 @@ int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, FixedChoice*
     int n = 0;
     for (const auto& e : kFixed)
         if (usable(e, fp64, L, H, vac) && n < cap)
-            out[n++] = FixedChoice{e.nt, e.stage_p, e.stream};
+            out[n++] = FixedChoice{e.nt, e.stage_p, e.stream, e.minb};
     return n;
 }
 
@@ -778,7 +779,8 @@ cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, const FixedCho
                          size_t smem, cudaStream_t st, bool prepare)
 {
     for (const auto& e : kFixed)
-        if (usable(e, fp64, a.g.L, a.g.H, vac) && e.nt == ch.nt && e.stream == ch.stream)
+        if (usable(e, fp64, a.g.L, a.g.H, vac) && e.nt == ch.nt && e.stream == ch.stream &&
+            e.minb == ch.minb)
             return e.fn(a, nlat, smem, st, prepare);
     return cudaErrorInvalidValue;
 }
