@@ -254,20 +254,30 @@ def test_fp32_decision_mismatch_rate(engine_mod, oracle):
 
 def test_fp32_observables_match_fp64(engine_mod, oracle):
     """Same disorder and streams: per-conf thermal averages of FP32 and FP64 differ only by
-    statistical noise (the two trajectories decorrelate after the first flipped decision)."""
+    statistical noise (the two trajectories decorrelate after the first flipped decision).  Each
+    observable's FP32 - FP64 difference at each temperature slot, in units of its standard error
+    over the configurations, is "within 2 sigma" in the statistical sense: at most 15 % of the
+    48 z-scores beyond 2 (5.7 % expected for 23 degrees of freedom; the observables are
+    correlated) and none beyond 4."""
     jc = engine_mod
-    nconf, nrep, L = 24, 6, 8
+    nconf, nrep, L, nmess = 24, 6, 8, 1500
+    names = ("absmag", "mag2", "en", "en2", "strx_abs", "stry_abs", "nbar", "nbar2")
+    cols = [jc.SUM_FIELDS.index(n) for n in names]
     res = {}
     for prec in (jc.FP64_PLAIN, jc.FP32_BATCHED):
         eng, _, betas = _setup(jc, oracle, L, L, nconf, nrep, prec)
         eng.run(300, measure=False)
         eng.reset_measurements()
-        eng.run(1500, measure=True)
-        res[prec] = np.array([eng.slot_sums(k)[0][:, 4] / 1500 for k in range(nconf)])
+        eng.run(nmess, measure=True)
+        res[prec] = np.array([eng.slot_sums(k)[0][:, cols] / nmess for k in range(nconf)])
         eng.close()
-    d = res[jc.FP32_BATCHED] - res[jc.FP64_PLAIN]
+    d = res[jc.FP32_BATCHED] - res[jc.FP64_PLAIN]  # (nconf, nrep, observable)
     se = d.std(axis=0, ddof=1) / np.sqrt(nconf)
-    assert (np.abs(d.mean(axis=0)) < 5 * se + 1e-12).all(), (d.mean(axis=0), se)
+    z = np.abs(d.mean(axis=0)) / (se + 1e-300)
+    for j, n in enumerate(names):
+        print(f"FP32 - FP64 {n:9s} |z| by slot:", " ".join(f"{v:4.2f}" for v in z[:, j]))
+    assert (z > 2).mean() <= 0.15, z
+    assert z.max() < 4, z
 
 
 def test_invalid_calls_fail_cleanly(engine_mod, oracle):
