@@ -545,10 +545,10 @@ bool valid_conf(Ctx* c, int conf) { return conf >= 0 && conf < c->nconf; }
 
 // Autotuner: times every CTA size and form (one CTA per lattice, or streaming) of the
 // shape-specialised kernel on a scratch copy of the group's lattices (the live state is not
-// touched) and keeps the fastest.  Choices are cached per (precision, L, H, lattice count,
-// vacancies) for the life of the process.
+// touched) and keeps the fastest.  Choices are cached per (device, precision, L, H, lattice
+// count, vacancies) for the life of the process.
 std::mutex g_tune_mu;
-std::map<std::tuple<bool, int, int, int, bool>, int> g_tune_cache;
+std::map<std::tuple<int, bool, int, int, int, bool>, int> g_tune_cache;
 
 // Device time of 2 PT-cycle sweep launches of a group with kernel variant v (the fastest of three
 // timings), on a scratch copy of its lattices (the live state is not touched; one warm-up launch
@@ -612,16 +612,17 @@ int time_variant(Ctx* c, Group& grp, const SweepVariant& v, int nthreads, size_t
 
 // Cluster path or one launch per colour phase for a lattice that does not fit one CTA: the
 // cluster kernel and the HBM kernel (shape-specialised form with 1, 2 or 4 replicas per thread
-// where it exists, else the generic one) are timed and the fastest kept, cached per (precision,
-// L, H, lattice count, bond dilution, HBM kernel).  Choice: 0 cluster, -1 generic HBM kernel,
-// r > 0 shape-specialised HBM kernel with r replicas per thread.
-std::map<std::tuple<bool, int, int, int, bool, int>, int> g_cluster_cache;
+// where it exists, else the generic one) are timed and the fastest kept, cached per (device,
+// precision, L, H, lattice count, bond dilution, HBM kernel).  Choice: 0 cluster, -1 generic HBM
+// kernel, r > 0 shape-specialised HBM kernel with r replicas per thread.
+std::map<std::tuple<int, bool, int, int, int, bool, int>, int> g_cluster_cache;
 
 int tune_cluster(Ctx* c, Group& grp)
 {
     const int hbm_nt = hbm_fixed_threads(c, grp, grp.var.fp64);
     const auto key =
-        std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks, hbm_nt);
+        std::make_tuple(c->P.device, grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks,
+                        hbm_nt);
     int choice = 0;
     bool known = false;
     {
@@ -693,13 +694,13 @@ bool small_batch_ok(Ctx* c, const Group& grp)
 // Small batches (fewer lattices than half the SMs): one CTA per lattice leaves most SMs idle, so
 // the chosen one-CTA kernel is timed against one site per thread in one CTA, every cluster size
 // that divides H/2 (four sites or one site per thread), and one launch per colour phase with one
-// site per thread in CTAs of 32-256 threads; the fastest is kept, cached per (precision, L, H,
-// lattice count, bond dilution, vacancies).
+// site per thread in CTAs of 32-256 threads; the fastest is kept, cached per (device,
+// precision, L, H, lattice count, bond dilution, vacancies).
 enum SmallKind { kKeep = 0, kSiteCta = 1, kClusterQuad = 2, kClusterSite = 3, kGlobalSite = 4 };
 struct SmallChoice {
     int kind, cs, nt;
 };
-std::map<std::tuple<bool, int, int, int, bool, bool>, SmallChoice> g_small_cache;
+std::map<std::tuple<int, bool, int, int, int, bool, bool>, SmallChoice> g_small_cache;
 
 // One site per thread in one CTA per lattice (the generic kernel)
 int site_cta_variant(Ctx* c, Group& grp, SweepVariant& v, size_t& smem, int& nt)
@@ -731,7 +732,8 @@ int tune_small_batch(Ctx* c, Group& grp)
     CK(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->P.device));
     if (2 * grp.nlat() > nsm) return J1J2C_OK;
     const auto key =
-        std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks, c->vac);
+        std::make_tuple(c->P.device, grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks,
+                        c->vac);
     SmallChoice best{kKeep, 0, 0};
     bool known = false;
     {
@@ -814,10 +816,10 @@ int tune_small_batch(Ctx* c, Group& grp)
 // Wolff growth: 1, 2 or 4 CTAs per lattice (a thread-block cluster) for every lattice, or 2 CTAs
 // for the 1/8, 1/4 or 1/2 coldest slots and one for the rest (two concurrent launches), timed on
 // a scratch copy of the group's lattices at the first run of a context with Wolff updates, the
-// fastest kept, cached per (precision, L, H, lattice count, bond dilution).  The coldest
+// fastest kept, cached per (device, precision, L, H, lattice count, bond dilution).  The coldest
 // lattices' clusters span a third of the lattice or more and are bound by one SM's issue rate;
 // the hot ones are small, and more CTAs per lattice mean more waves.
-std::map<std::tuple<bool, int, int, int, bool>, std::pair<int, int>> g_wolff_cache;
+std::map<std::tuple<int, bool, int, int, int, bool>, std::pair<int, int>> g_wolff_cache;
 
 int tune_wolff(Ctx* c, Group& grp)
 {
@@ -825,7 +827,8 @@ int tune_wolff(Ctx* c, Group& grp)
     if (!c->wolff || (fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_WOLFF_CS2 |
                             J1J2C_FLAG_WOLFF_CS4)))
         return J1J2C_OK;  // no growth form, or the count is pinned
-    const auto key = std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks);
+    const auto key =
+        std::make_tuple(c->P.device, grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks);
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_wolff_cache.find(key);
@@ -902,7 +905,7 @@ int autotune(Ctx* c, Group& grp)
     const int n = fixed_candidates(grp.var.fp64, grp.g.L, grp.g.H, c->masks, c->vac, fc, 16);
     if (n <= 1) return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
     const int nlat = grp.nlat();
-    const auto key = std::make_tuple(grp.var.fp64, grp.g.L, grp.g.H, nlat, c->vac);
+    const auto key = std::make_tuple(c->P.device, grp.var.fp64, grp.g.L, grp.g.H, nlat, c->vac);
     int best = -1;  // index into fc
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
