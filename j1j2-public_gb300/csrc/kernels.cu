@@ -1212,7 +1212,7 @@ cudaError_t launch_sweep_global(const SweepArgs& a, const SweepVariant& v, int c
 cudaError_t launch_measure_global(const SweepArgs& a, const SweepVariant& v, int nlat,
                                   cudaStream_t st)
 {
-    if (v.fixed_nt > 0) return launch_fixed_hbm(a, v.fp64, -1, 0, nlat, 1, st);
+    if (v.fixed_nt > 0) return launch_fixed_hbm(a, v.fp64, -1, 0, nlat, v.rpt, st);
     return v.fp64 ? global_dispatch<double>(a, v, 0, 0, nlat, st, true)
                   : global_dispatch<float>(a, v, 0, 0, nlat, st, true);
 }

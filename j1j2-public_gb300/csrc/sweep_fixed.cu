@@ -680,26 +680,38 @@ __global__ void __launch_bounds__(NT, sizeof(Real) == 8 ? 1 : RPT == 4 ? 768 / N
     }
 }
 
-// Observables: one thread per quad, grid.z = colour; per-CTA sums are added into the lattice's
+// Observables: one thread per quad in RPT replicas of one configuration (field operands loaded
+// once), grid (quads / NT, lattices / RPT, colour); per-CTA sums are added into the lattices'
 // (zeroed) observables with atomics (integer sums: order-independent).
-template <class Real, int LH, int HH, int NT, bool VAC>
+template <class Real, int LH, int HH, int NT, int RPT, bool VAC>
 __global__ void __launch_bounds__(NT) measure_fixed_hbm_kernel(SweepArgs a)
 {
     using Sh = Shape<LH, HH>;
     const int q = (int)(blockIdx.x * NT + threadIdx.x);
-    const int lat = a.lat0 + (int)blockIdx.y;
+    const int lat = a.lat0 + (int)blockIdx.y * RPT;
     const int conf = lat / a.nrep;
-    uint32_t* S32 = reinterpret_cast<uint32_t*>(a.spins + (long long)lat * a.lat_stride);
     const Real* P = field_base<Real>(a, conf);
-    Acc acc{0, 0, 0, 0, 0};
+    Acc acc[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) acc[r] = Acc{0, 0, 0, 0, 0};
     if (q < Sh::CS) {
         const QuadOff o = quad_offsets<LH, HH>(q);
         switch (blockIdx.z) {
-#define J1J2_HBM_MEASURE(C)                                                                    \
-    case C: {                                                                                  \
-        const QuadData<Real> d = load_quad<Real, LH, HH, C>(S32, P, o);                        \
-        compute_quad<Real, LH, HH, C, true, VAC>(a, S32, d, 0u, 0u, 0u, 0u, 0.0, 0.0f, acc);   \
-        break;                                                                                 \
+#define J1J2_HBM_MEASURE(C)                                                                     \
+    case C: {                                                                                   \
+        QuadData<Real> d[RPT];                                                                  \
+        load_quad_field<Real, LH, HH, C>(P, o, d[0]);                                           \
+        _Pragma("unroll") for (int r = 0; r < RPT; ++r)                                         \
+        {                                                                                       \
+            if (r > 0) d[r] = d[0];                                                             \
+            load_quad_spins<Real, LH, HH, C>(                                                   \
+                reinterpret_cast<const uint32_t*>(a.spins + (long long)(lat + r) * a.lat_stride), \
+                o, d[r]);                                                                       \
+        }                                                                                       \
+        _Pragma("unroll") for (int r = 0; r < RPT; ++r)                                         \
+            compute_quad<Real, LH, HH, C, true, VAC>(a, nullptr, d[r], 0u, 0u, 0u, 0u, 0.0,     \
+                                                     0.0f, acc[r]);                             \
+        break;                                                                                  \
     }
             J1J2_HBM_MEASURE(0)
             J1J2_HBM_MEASURE(1)
@@ -714,14 +726,18 @@ __global__ void __launch_bounds__(NT) measure_fixed_hbm_kernel(SweepArgs a)
                 break;
         }
     }
-    const Acc tot = block_reduce(acc);
-    if (threadIdx.x == 0) {
-        LatObs* ob = a.obs + lat;
-        atomicAdd(reinterpret_cast<unsigned long long*>(&ob->eacc), (unsigned long long)tot.e);
-        atomicAdd(&ob->M, tot.M);
-        atomicAdd(&ob->SX, tot.SX);
-        atomicAdd(&ob->SY, tot.SY);
-        atomicAdd(&ob->NB, tot.NB);
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+        const Acc tot = block_reduce(acc[r]);
+        if (threadIdx.x == 0) {
+            LatObs* ob = a.obs + lat + r;
+            atomicAdd(reinterpret_cast<unsigned long long*>(&ob->eacc), (unsigned long long)tot.e);
+            atomicAdd(&ob->M, tot.M);
+            atomicAdd(&ob->SX, tot.SX);
+            atomicAdd(&ob->SY, tot.SY);
+            atomicAdd(&ob->NB, tot.NB);
+        }
+        __syncthreads();  // block_reduce's scratch is reused by the next replica
     }
 }
 
@@ -730,8 +746,14 @@ cudaError_t run_hbm(const SweepArgs& a, int colour, int t, int nlat, int rpt, cu
 {
     constexpr int CS = Shape<LH, HH>::CS;
     const unsigned gx = (unsigned)((CS + NT - 1) / NT);
-    if (colour < 0) {
-        measure_fixed_hbm_kernel<Real, LH, HH, NT, true>
+    if (colour < 0 && rpt == 4) {
+        measure_fixed_hbm_kernel<Real, LH, HH, NT, 4, true>
+            <<<dim3(gx, (unsigned)(nlat / 4), 8u), NT, 0, st>>>(a);
+    } else if (colour < 0 && rpt == 2) {
+        measure_fixed_hbm_kernel<Real, LH, HH, NT, 2, true>
+            <<<dim3(gx, (unsigned)(nlat / 2), 8u), NT, 0, st>>>(a);
+    } else if (colour < 0) {
+        measure_fixed_hbm_kernel<Real, LH, HH, NT, 1, true>
             <<<dim3(gx, (unsigned)nlat, 8u), NT, 0, st>>>(a);
     } else if (rpt == 4) {
         sweep_fixed_hbm_kernel<Real, LH, HH, NT, 4, true>
