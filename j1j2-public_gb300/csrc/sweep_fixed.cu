@@ -147,18 +147,20 @@ __device__ __forceinline__ QuadData<Real> load_quad(const uint32_t* S32, const R
 
 // Update (or measure) one quad from its loaded operands.  VAC: vacancies may be present (the
 // FP32 acceptance threshold is then scaled by s^2 so that a vacancy never flips).
+// qshift: words between S32 and the lattice's first word (the quad's Philox group is its
+// position in the lattice)
 template <class Real, int LH, int HH, int C, bool MEASURE, bool VAC>
 __device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
                                              const QuadData<Real>& d, uint32_t sweep,
                                              uint32_t rep, uint32_t k0, uint32_t k1, double beta,
-                                             float kb, Acc& acc)
+                                             float kb, Acc& acc, int qshift = 0)
 {
     using Sh = Shape<LH, HH>;
     constexpr int px = C & 1, py = (C >> 1) & 1;
     constexpr int B0 = C * Sh::CS;
     U4 rnd{0, 0, 0, 0};
     if constexpr (!MEASURE)
-        rnd = philox4x32_10(rep, sweep, (uint32_t)(B0 + d.self), kTagSweep, k0, k1);
+        rnd = philox4x32_10(rep, sweep, (uint32_t)(B0 + d.self + qshift), kTagSweep, k0, k1);
     uint32_t flipmask = 0;
     if constexpr (sizeof(Real) == 4) {
         // Sites in pairs (0,1), (2,3) with packed FP32x2 arithmetic: every element follows
@@ -285,7 +287,37 @@ template <int QPT>
 struct OffsetCache {
     static constexpr bool kHold = QPT <= 2;
     QuadOff off[kHold ? QPT : 1];
+    QuadOff base;  // plane-strided threads: the first quad's offsets
+    int zp_last;   // and the +z plane offset of the last quad (the only one that can wrap)
 };
+
+// A thread's quads lie NT / RS planes apart in the same row and column when NT is a whole
+// number of planes and the quads exactly fill the colour: their offsets are the first quad's
+// shifted by a constant, apart from the -z plane of the first and the +z plane of the last
+// (periodic wrap), so nothing is recomputed per colour phase.
+template <int LH, int HH, int NT, int QPT>
+struct Strided {
+    static constexpr int RS = Shape<LH, HH>::RS;
+    static constexpr int ZS = NT / RS;  // planes between a thread's quads
+    static constexpr bool value =
+        QPT > 2 && NT % RS == 0 && QPT * NT == Shape<LH, HH>::CS && QPT * ZS == HH;
+};
+
+template <int LH, int HH, int NT, int QPT>
+__device__ __forceinline__ void fill_offsets(OffsetCache<QPT>& off, int tid)
+{
+    using Sh = Shape<LH, HH>;
+    if constexpr (OffsetCache<QPT>::kHold) {
+#pragma unroll
+        for (int j = 0; j < QPT; ++j) {
+            const int q = tid + j * NT;
+            off.off[j] = quad_offsets<LH, HH>(q < Sh::CS ? q : 0);
+        }
+    } else if constexpr (Strided<LH, HH, NT, QPT>::value) {
+        off.base = quad_offsets<LH, HH>(tid);
+        off.zp_last = quad_offsets<LH, HH>(tid + (QPT - 1) * NT).zp;
+    }
+}
 
 template <int LH, int HH, int NT, int QPT>
 __device__ __forceinline__ QuadOff offsets_for(const OffsetCache<QPT>& oc, int j)
@@ -318,6 +350,19 @@ __device__ __forceinline__ void colour_phase(const SweepArgs& a, uint32_t* S32, 
         if (has1)
             compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32, d1, sweep, rep, k0, k1, beta,
                                                         kb, acc);
+    } else if constexpr (Strided<LH, HH, NT, QPT>::value) {
+        constexpr int RS = Strided<LH, HH, NT, QPT>::RS;
+        constexpr int SH = Strided<LH, HH, NT, QPT>::ZS * RS;  // words between the quads
+#pragma unroll 2
+        for (int j = 0; j < QPT; ++j) {
+            const int shift = j * SH;
+            QuadOff o = oc.base;
+            o.zm = j == 0 ? oc.base.zm : oc.base.self - RS;
+            o.zp = j == QPT - 1 ? oc.zp_last - shift : oc.base.self + RS;
+            const QuadData<Real> dj = load_quad<Real, LH, HH, C>(S32 + shift, P + 4 * shift, o);
+            compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32 + shift, dj, sweep, rep, k0, k1,
+                                                        beta, kb, acc, shift);
+        }
     } else {
 #pragma unroll 2
         for (int j = 0; j < QPT; ++j)
@@ -371,13 +416,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_fixed_kernel(SweepArgs a)
     if constexpr (STAGE_P)
         block_copy16_ldg(Ps, Pg, (int)((Sh::N * sizeof(Real) + 15) & ~(size_t)15));
     OffsetCache<QPT> off;
-    if constexpr (OffsetCache<QPT>::kHold) {
-#pragma unroll
-        for (int j = 0; j < QPT; ++j) {
-            const int q = (int)threadIdx.x + j * NT;
-            off.off[j] = quad_offsets<LH, HH>(q < Sh::CS ? q : 0);
-        }
-    }
+    fill_offsets<LH, HH, NT, QPT>(off, (int)threadIdx.x);
     __syncthreads();
     const Real* P = STAGE_P ? Ps : Pg;
     uint32_t* S32 = reinterpret_cast<uint32_t*>(S);
@@ -520,13 +559,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_stream_kernel(SweepArgs a, int
         stream_copy_in<Real, LH, HH>(smem, field_base<Real>(a, lat / a.nrep), Lay::PB, &bar[2]);
     }
     OffsetCache<QPT> off;
-    if constexpr (OffsetCache<QPT>::kHold) {
-#pragma unroll
-        for (int j = 0; j < QPT; ++j) {
-            const int q = tid + j * NT;
-            off.off[j] = quad_offsets<LH, HH>(q < Sh::CS ? q : 0);
-        }
-    }
+    fill_offsets<LH, HH, NT, QPT>(off, tid);
     StreamState st{{0u, 0u, 0u}, true};
 #pragma unroll 1
     for (int l = first; l < last; l += 2) {

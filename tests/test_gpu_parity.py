@@ -137,12 +137,13 @@ def test_quad_and_per_site_paths_agree_bitwise(engine_mod, oracle, precision):
         np.testing.assert_array_equal(a, b)
 
 
-@pytest.mark.parametrize("precision,L", [(1, 16), (1, 24), (1, 32), (0, 24), (0, 32)])
+@pytest.mark.parametrize("precision,L", [(1, 16), (1, 24), (1, 32), (1, 48), (0, 24), (0, 32)])
 def test_specialised_kernels_agree_bitwise(engine_mod, oracle, precision, L):
     """Shape-specialised kernel (every CTA size the autotuner may pick), generic quad kernel
     and per-site kernel give the same spins, observables and running sums."""
     jc = engine_mod
-    nts = {16: [128, 64], 24: [448, 224], 32: [1024, 512]}[L] if precision == 1 else \
+    nts = {16: [128, 64], 24: [448, 224], 32: [1024, 512], 48: [864, 576]}[L] \
+        if precision == 1 else \
         {24: [448], 32: [512]}[L]
     runs = []
     for flags, bt in [(jc.FLAG_NO_FIXED, 0), (jc.FLAG_GENERIC, 0), (jc.FLAG_GLOBAL, 0),
