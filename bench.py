@@ -196,10 +196,16 @@ def time_steps(torch, eng, steps, warmup, flush, cycles=1):
 
 
 def time_workload(torch, jc, w, device, flush, steps):
-    """Device throughput of one workload (CUDA events per PT cycle, L2 flushed between)."""
-    eng, _ = make_engine(jc, w, device, flags=jc.FLAG_PROFILE)
+    """Device throughput of one workload (CUDA events per step, L2 flushed between).  The value
+    comes from an engine without profiling events (graph event nodes cost microseconds per
+    cycle, a sizeable share of a small lattice's cycle); the sweep-kernel split from a second,
+    profiled engine over the same steps."""
     cycles = w.get("cycles_per_step", 1)
-    ms, prof_ms = time_steps(torch, eng, steps, 3, flush, cycles)
+    eng, _ = make_engine(jc, w, device)
+    ms, _ = time_steps(torch, eng, steps, 3, flush, cycles)
+    eng.close()
+    eng, _ = make_engine(jc, w, device, flags=jc.FLAG_PROFILE)
+    _, prof_ms = time_steps(torch, eng, steps, 3, flush, cycles)
     att = attempts_per_cycle(eng) * cycles
     out = {"value": round(att * steps / (ms * 1e6), 4), "unit": UNIT,
            "ms_per_step": round(ms / steps, 4), "steps": steps, "attempts_per_step": att,
@@ -246,8 +252,13 @@ def run_ours(args):
     if args.nconf:  # a smaller case of the same kernels (profiling captures)
         w = dict(w, groups=[(L, args.nconf, r) for L, _, r in w["groups"]])
     nconf = sum(n for _, n, _ in w["groups"])
-    eng, betas = make_engine(jc, w, local, conf_base=conf_base_of(rank, w),
-                             flags=jc.FLAG_PROFILE | args.flags)
+    # `value` and e2e: the engine as a user runs it (no profiling event nodes in its cycle
+    # graph); the roofline: the sweep kernel's CUDA-event duration over the timed steps of a
+    # second engine of the same workload whose graph brackets the sweep launch with events
+    # (those nodes cost ~1 % of a cycle, so its steps are not used for `value`)
+    eng, betas = make_engine(jc, w, local, conf_base=conf_base_of(rank, w), flags=args.flags)
+    peng, _ = make_engine(jc, w, local, conf_base=conf_base_of(rank, w),
+                          flags=jc.FLAG_PROFILE | args.flags)
     cfg = eng.config()
     cycles = w.get("cycles_per_step", 1)
     attempts_per_step = attempts_per_cycle(eng) * cycles
@@ -256,8 +267,11 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     with Clocks(local) as clk:
-        total_ms, prof_ms = time_steps(torch, eng, args.steps, args.warmup, flush, cycles)
+        total_ms, _ = time_steps(torch, eng, args.steps, args.warmup, flush, cycles)
+        torch.cuda.synchronize()
+        _, prof_ms = time_steps(torch, peng, args.steps, args.warmup, flush, cycles)
     torch.cuda.synchronize()
+    peng.close()
     if ws > 1:
         total_ms = max_over_ranks(dist, total_ms, "cuda")
         dist.barrier()

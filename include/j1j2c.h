@@ -313,8 +313,10 @@ int j1j2c_results_write(void *res, const char *dir);
 
 void j1j2c_results_destroy(void *res);
 
-/* Sweep-kernel timing accumulated under J1J2C_FLAG_PROFILE/* Sweep-kernel timing accumulated under J1J2C_FLAG_PROFILE: milliseconds, launches, and the
- * attempts those launches made (occupied sites x sweeps). */
+/* Sweep-kernel timing accumulated under J1J2C_FLAG_PROFILE: milliseconds, launches, and the
+ * attempts those launches made (occupied sites x sweeps).  Every PT cycle brackets its sweep
+ * launches with its own pair of CUDA events; j1j2c_run reads them after its final
+ * synchronisation, so profiling adds no host wait between the cycles of a run. */
 int j1j2c_get_profile(void *ctx, double *sweep_ms, int64_t *sweep_launches, int64_t *attempts);
 
 /* Kernel configuration the context chose: threads per CTA, sites per thread per colour phase

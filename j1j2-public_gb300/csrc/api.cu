@@ -46,6 +46,8 @@ struct Group {
     int nlat() const { return nconf * nrep; }
 };
 
+constexpr int kProfPool = 64;  // profiling event pairs in flight before the host reads them
+
 struct Ctx {
     j1j2c_params P{};
     std::vector<Group> G;
@@ -90,10 +92,17 @@ struct Ctx {
     std::vector<cudaStream_t> wside;
     std::vector<cudaEvent_t> wfork, wjoin;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraph_t graph_src[2] = {nullptr, nullptr};  // kept: its event-record nodes are retargeted
+    cudaGraphNode_t graph_ev[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     long long occ_total = 0;
 
+    // J1J2C_FLAG_PROFILE: every cycle brackets its sweep launches with its own pair of a pool of
+    // event pairs (the graph's event-record nodes retargeted before each launch); the pairs are
+    // read after the run's final synchronisation, so profiling adds no host wait between cycles
     bool profile = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> pev0, pev1;
+    int prof_pending = 0;
     double prof_ms = 0.0;
     long long prof_launches = 0, prof_attempts = 0;
 
@@ -140,11 +149,13 @@ cudaError_t dalloc(T** p, size_t n)
 
 void free_graphs(Ctx* c)
 {
-    for (auto& gx : c->graph)
-        if (gx) {
-            cudaGraphExecDestroy(gx);
-            gx = nullptr;
-        }
+    for (int m = 0; m < 2; ++m) {
+        if (c->graph[m]) cudaGraphExecDestroy(c->graph[m]);
+        if (c->graph_src[m]) cudaGraphDestroy(c->graph_src[m]);
+        c->graph[m] = nullptr;
+        c->graph_src[m] = nullptr;
+        c->graph_ev[m][0] = c->graph_ev[m][1] = nullptr;
+    }
 }
 
 void release(Ctx* c)
@@ -169,6 +180,8 @@ void release(Ctx* c)
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    for (auto e : c->pev0) cudaEventDestroy(e);
+    for (auto e : c->pev1) cudaEventDestroy(e);
     if (c->own) cudaStreamDestroy(c->own);
 }
 
@@ -482,22 +495,33 @@ cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int n
         return launch_sweep_cluster(a, v, nlat, st);
     }
     if (!v.global) return launch_sweep(a, v, nlat, nthreads, smem, st);
-    for (int t = 0; t < a.nsweeps; ++t)
-        for (int col = 0; col < 8; ++col)
-            if ((e = launch_sweep_global(a, v, col, t, nlat, st)) != cudaSuccess) return e;
+    // one launch per colour phase: the observables are zeroed first (no sweep reads them), so
+    // every launch after the first follows a kernel of the same chain and may overlap its tail
+    // (programmatic dependent launch: each kernel waits for its predecessor before any access)
     if ((e = cudaMemsetAsync(a.obs + a.lat0, 0, sizeof(LatObs) * nlat, st)) != cudaSuccess)
         return e;
+    for (int t = 0; t < a.nsweeps; ++t)
+        for (int col = 0; col < 8; ++col) {
+            a.pdl = (t > 0 || col > 0) ? 1 : 0;
+            if ((e = launch_sweep_global(a, v, col, t, nlat, st)) != cudaSuccess) return e;
+        }
+    a.pdl = 1;
     (void)grp;
     (void)c;
     return launch_measure_global(a, v, nlat, st);
 }
 
-// one PT cycle: every group's sweeps + observables (parallel branches), then swap / accumulate
-cudaError_t enqueue_cycle(Ctx* c, int measure, cudaStream_t st)
+// one PT cycle: every group's sweeps + observables (parallel branches), then swap / accumulate;
+// with profiling, events e0 / e1 bracket the sweep launches
+cudaError_t enqueue_cycle(Ctx* c, int measure, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1)
 {
     cudaError_t e;
-    if (c->profile &&
-        (e = cudaEventRecordWithFlags(c->ev0, st, cudaEventRecordExternal)) != cudaSuccess)
+    // Several groups: the pair is recorded with or without profiling, so that one event node
+    // heads the cycle's graph and one closes its branches before the swap (measured on the mixed
+    // L = 16/24/32/48 batch: 403 attempts/ns with the two nodes, 382-396 with four root kernels
+    // and a four-way join into the swap kernel)
+    const bool rec = c->profile || c->G.size() > 1;
+    if (rec && (e = cudaEventRecordWithFlags(e0, st, cudaEventRecordExternal)) != cudaSuccess)
         return e;
     if (c->G.size() == 1) {
         const Group& grp = c->G[0];
@@ -516,10 +540,11 @@ cudaError_t enqueue_cycle(Ctx* c, int measure, cudaStream_t st)
             if ((e = cudaStreamWaitEvent(st, c->join_ev[k], 0)) != cudaSuccess) return e;
         }
     }
-    if (c->profile &&
-        (e = cudaEventRecordWithFlags(c->ev1, st, cudaEventRecordExternal)) != cudaSuccess)
+    if (rec && (e = cudaEventRecordWithFlags(e1, st, cudaEventRecordExternal)) != cudaSuccess)
         return e;
-    if ((e = launch_swap(swap_args(c, measure), st)) != cudaSuccess) return e;
+    // one group without profiling events: the swap follows that group's last kernel directly
+    const bool pdl = c->G.size() == 1 && !c->profile;
+    if ((e = launch_swap(swap_args(c, measure), st, pdl)) != cudaSuccess) return e;
     if (measure && c->d_loc_s) return enqueue_locnem(c, st);
     return cudaSuccess;
 }
@@ -528,7 +553,7 @@ int build_graph(Ctx* c, int measure)
 {
     cudaGraph_t graph = nullptr;
     CK(c, cudaStreamBeginCapture(c->own, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = enqueue_cycle(c, measure, c->own);
+    cudaError_t e = enqueue_cycle(c, measure, c->own, c->ev0, c->ev1);
     cudaError_t e2 = cudaStreamEndCapture(c->own, &graph);
     if (e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
@@ -536,8 +561,28 @@ int build_graph(Ctx* c, int measure)
     }
     if (e2 != cudaSuccess) return cuda_fail(c, e2, "cudaStreamEndCapture");
     e = cudaGraphInstantiate(&c->graph[measure], graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return cuda_fail(c, e, "cudaGraphInstantiate");
+    }
+    c->graph_src[measure] = graph;
+    if (c->profile) {  // the two event-record nodes, retargeted to a pool pair per launch
+        size_t n = 0;
+        CK(c, cudaGraphGetNodes(graph, nullptr, &n));
+        std::vector<cudaGraphNode_t> nodes(n);
+        CK(c, cudaGraphGetNodes(graph, nodes.data(), &n));
+        for (cudaGraphNode_t nd : nodes) {
+            cudaGraphNodeType t;
+            CK(c, cudaGraphNodeGetType(nd, &t));
+            if (t != cudaGraphNodeTypeEventRecord) continue;
+            cudaEvent_t ev = nullptr;
+            CK(c, cudaGraphEventRecordNodeGetEvent(nd, &ev));
+            if (ev == c->ev0) c->graph_ev[measure][0] = nd;
+            if (ev == c->ev1) c->graph_ev[measure][1] = nd;
+        }
+        if (!c->graph_ev[measure][0] || !c->graph_ev[measure][1])
+            return fail(c, J1J2C_ECUDA, "profiling events missing from the PT-cycle graph");
+    }
     return J1J2C_OK;
 }
 
@@ -1148,6 +1193,13 @@ int j1j2c_create_multi(void** out, const j1j2c_params* groups, int32_t ngroups)
         if ((e = wolff_side(c, grp)) != cudaSuccess) return cfail(e, "Wolff stream");
     if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess) return cfail(e, "event");
     if ((e = cudaEventCreate(&c->ev1)) != cudaSuccess) return cfail(e, "event");
+    for (int k = 0; c->profile && k < kProfPool; ++k) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        if ((e = cudaEventCreate(&a)) != cudaSuccess) return cfail(e, "event");
+        c->pev0.push_back(a);
+        if ((e = cudaEventCreate(&b)) != cudaSuccess) return cfail(e, "event");
+        c->pev1.push_back(b);
+    }
     if ((e = cudaMemset(c->d_spins, 1, (size_t)spin_bytes)) != cudaSuccess)
         return cfail(e, "memset");
     if ((e = cudaMemset(c->d_bm, 3, (size_t)mask_bytes)) != cudaSuccess) return cfail(e, "memset");
@@ -1563,6 +1615,21 @@ int j1j2c_get_flip_counts(void* ctx, int32_t conf, int32_t* counts)
     return J1J2C_OK;
 }
 
+// Adds the sweep time of every cycle whose profiling pair is pending (waits for the last pair).
+int drain_profile(Ctx* c)
+{
+    for (int k = 0; k < c->prof_pending; ++k) {
+        CK(c, cudaEventSynchronize(c->pev1[k]));
+        float ms = 0.0f;
+        CK(c, cudaEventElapsedTime(&ms, c->pev0[k], c->pev1[k]));
+        c->prof_ms += ms;
+        c->prof_launches += 1;
+        c->prof_attempts += c->occ_total * c->P.ptswapever;
+    }
+    c->prof_pending = 0;
+    return J1J2C_OK;
+}
+
 int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_phase)
 {
     if (!ctx) return J1J2C_EINVAL;
@@ -1588,20 +1655,31 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
         if (rc != J1J2C_OK) return rc;
     }
     for (int k = 0; k < ncycles; ++k) {
-        if (direct)
-            CK(c, enqueue_cycle(c, m, c->st));
-        else
-            CK(c, cudaGraphLaunch(c->graph[m], c->st));
-        if (c->profile) {  // the events bracket the sweep launches (graph event-record nodes)
-            CK(c, cudaEventSynchronize(c->ev1));
-            float ms = 0.0f;
-            CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-            c->prof_ms += ms;
-            c->prof_launches += 1;
-            c->prof_attempts += c->occ_total * c->P.ptswapever;
+        cudaEvent_t e0 = c->ev0, e1 = c->ev1;
+        if (c->profile) {
+            if (c->prof_pending == kProfPool) {
+                const int rc = drain_profile(c);
+                if (rc != J1J2C_OK) return rc;
+            }
+            e0 = c->pev0[c->prof_pending];
+            e1 = c->pev1[c->prof_pending];
+            ++c->prof_pending;
         }
+        if (direct) {
+            CK(c, enqueue_cycle(c, m, c->st, e0, e1));
+            continue;
+        }
+        if (c->profile) {
+            CK(c, cudaGraphExecEventRecordNodeSetEvent(c->graph[m], c->graph_ev[m][0], e0));
+            CK(c, cudaGraphExecEventRecordNodeSetEvent(c->graph[m], c->graph_ev[m][1], e1));
+        }
+        CK(c, cudaGraphLaunch(c->graph[m], c->st));
     }
     CK(c, cudaStreamSynchronize(c->st));
+    if (c->profile) {
+        const int rc = drain_profile(c);
+        if (rc != J1J2C_OK) return rc;
+    }
     CK(c, cudaGetLastError());
     bool bounded = c->wolff;  // kernels whose bounded waits or retries report through d_err
     for (const Group& grp : c->G) bounded = bounded || grp.var.stream;

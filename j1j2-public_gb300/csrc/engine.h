@@ -46,6 +46,8 @@ struct SweepArgs {
     int* flips;              // accepted flips per site, row (conf * nrep + slot) of lat_stride
                              // ints (nullptr: not counted; generic kernels only)
     int* err;                // set to 1 when a bounded wait of a kernel gave up (or nullptr)
+    int pdl;                 // host side: the launch may overlap the stream's previous kernel
+                             // (programmatic dependent launch; global-memory kernels only)
 };
 
 // Replica-indexed arrays are laid out conf by conf: conf c owns entries rbase[c] ..
@@ -180,7 +182,7 @@ size_t sweep_smem_bytes(const Geo& g, const SweepVariant& v);
 cudaError_t prepare_sweep_variant(const SweepVariant& v, size_t smem);
 cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks, int nthreads,
                          size_t smem, cudaStream_t st);
-cudaError_t launch_swap(const SwapArgs& a, cudaStream_t st);
+cudaError_t launch_swap(const SwapArgs& a, cudaStream_t st, bool pdl = false);
 // Wolff forms: seed-cluster growth (default), slab union-find labelling in shared memory,
 // per-site union-find labelling in global memory; all three flip the same cluster.
 enum WolffForm { kWolffGrow = 0, kWolffSlab = 1, kWolffSite = 2 };

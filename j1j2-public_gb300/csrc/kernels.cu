@@ -556,6 +556,8 @@ constexpr int kSwapWarps = 4;
 
 __global__ void __launch_bounds__(32 * kSwapWarps) swap_kernel(SwapArgs a)
 {
+    pdl_wait();
+    pdl_release();
     const uint32_t cycle = a.ctl[0];
     const int phase = (int)a.ctl[1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -714,6 +716,8 @@ __global__ void __launch_bounds__(256) locnem_kernel(LocnemArgs a)
 template <class Real, bool QUAD, bool MASKS>
 __global__ void __launch_bounds__(256) sweep_global_kernel(SweepArgs a, int colour, int t)
 {
+    pdl_wait();
+    pdl_release();
     const Geo g = a.g;
     const int lat = a.lat0 + (int)blockIdx.y;
     const int conf = lat / a.nrep;
@@ -753,6 +757,8 @@ __global__ void __launch_bounds__(256) sweep_global_kernel(SweepArgs a, int colo
 template <class Real, bool QUAD, bool MASKS>
 __global__ void __launch_bounds__(256) measure_global_kernel(SweepArgs a)
 {
+    pdl_wait();
+    pdl_release();
     const Geo g = a.g;
     const int lat = a.lat0 + (int)blockIdx.y;
     const int conf = lat / a.nrep;
@@ -893,12 +899,12 @@ cudaError_t global_pass(const SweepArgs& a, int colour, int t, int nlat, int nt,
     const int per = QUAD ? (a.g.Nc >> 2) : a.g.Nc;
     if (measure) {
         dim3 grid((unsigned)((8 * per + nt - 1) / nt), (unsigned)nlat);
-        measure_global_kernel<Real, QUAD, MASKS><<<grid, nt, 0, st>>>(a);
-    } else {
-        dim3 grid((unsigned)((per + nt - 1) / nt), (unsigned)nlat);
-        sweep_global_kernel<Real, QUAD, MASKS><<<grid, nt, 0, st>>>(a, colour, t);
+        return launch_k(a.pdl != 0, grid, dim3((unsigned)nt), 0, st,
+                        measure_global_kernel<Real, QUAD, MASKS>, a);
     }
-    return cudaGetLastError();
+    dim3 grid((unsigned)((per + nt - 1) / nt), (unsigned)nlat);
+    return launch_k(a.pdl != 0, grid, dim3((unsigned)nt), 0, st,
+                    sweep_global_kernel<Real, QUAD, MASKS>, a, colour, t);
 }
 
 template <class Real>
@@ -1217,11 +1223,10 @@ cudaError_t launch_measure_global(const SweepArgs& a, const SweepVariant& v, int
                   : global_dispatch<float>(a, v, 0, 0, nlat, st, true);
 }
 
-cudaError_t launch_swap(const SwapArgs& a, cudaStream_t st)
+cudaError_t launch_swap(const SwapArgs& a, cudaStream_t st, bool pdl)
 {
     const int nb = (a.nconf + kSwapWarps - 1) / kSwapWarps;
-    swap_kernel<<<nb, 32 * kSwapWarps, 0, st>>>(a);
-    return cudaGetLastError();
+    return launch_k(pdl, dim3((unsigned)nb), dim3(32u * kSwapWarps), 0, st, swap_kernel, a);
 }
 
 cudaError_t launch_locnem(const LocnemArgs& a, int nconf, cudaStream_t st)

@@ -292,4 +292,34 @@ __device__ __forceinline__ void fence_async_shared()
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// Programmatic dependent launch.  A kernel launched with the programmatic-serialisation attribute
+// may be scheduled while the previous kernel of its stream still runs; pdl_wait() returns once
+// that kernel has completed and its memory operations are visible (in a kernel launched without
+// the attribute it returns at once).  Every kernel launched through launch_k with pdl set calls
+// pdl_wait() before its first global-memory access.  pdl_release() lets the next such kernel be
+// scheduled as soon as every CTA of this one has started.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+__device__ __forceinline__ void pdl_release()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <class... P, class... A>
+cudaError_t launch_k(bool pdl, dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                     void (*kernel)(P...), A&&... args)
+{
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1u : 0u;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<A&&>(args)...);
+}
+
 }  // namespace j1j2

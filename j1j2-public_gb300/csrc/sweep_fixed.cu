@@ -683,6 +683,8 @@ template <class Real, int LH, int HH, int NT, int RPT, bool VAC>
 __global__ void __launch_bounds__(NT, sizeof(Real) == 8 ? 1 : RPT == 4 ? 768 / NT : 1024 / NT)
     sweep_fixed_hbm_kernel(SweepArgs a, int colour, int t)
 {
+    pdl_wait();
+    pdl_release();
     using Sh = Shape<LH, HH>;
     const int q = (int)(blockIdx.x * NT + threadIdx.x);
     if (q >= Sh::CS) return;
@@ -719,6 +721,8 @@ __global__ void __launch_bounds__(NT, sizeof(Real) == 8 ? 1 : RPT == 4 ? 768 / N
 template <class Real, int LH, int HH, int NT, int RPT, bool VAC>
 __global__ void __launch_bounds__(NT) measure_fixed_hbm_kernel(SweepArgs a)
 {
+    pdl_wait();
+    pdl_release();
     using Sh = Shape<LH, HH>;
     const int q = (int)(blockIdx.x * NT + threadIdx.x);
     const int lat = a.lat0 + (int)blockIdx.y * RPT;
@@ -779,26 +783,25 @@ cudaError_t run_hbm(const SweepArgs& a, int colour, int t, int nlat, int rpt, cu
 {
     constexpr int CS = Shape<LH, HH>::CS;
     const unsigned gx = (unsigned)((CS + NT - 1) / NT);
-    if (colour < 0 && rpt == 4) {
-        measure_fixed_hbm_kernel<Real, LH, HH, NT, 4, true>
-            <<<dim3(gx, (unsigned)(nlat / 4), 8u), NT, 0, st>>>(a);
-    } else if (colour < 0 && rpt == 2) {
-        measure_fixed_hbm_kernel<Real, LH, HH, NT, 2, true>
-            <<<dim3(gx, (unsigned)(nlat / 2), 8u), NT, 0, st>>>(a);
-    } else if (colour < 0) {
-        measure_fixed_hbm_kernel<Real, LH, HH, NT, 1, true>
-            <<<dim3(gx, (unsigned)nlat, 8u), NT, 0, st>>>(a);
-    } else if (rpt == 4) {
-        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 4, true>
-            <<<dim3(gx, (unsigned)(nlat / 4)), NT, 0, st>>>(a, colour, t);
-    } else if (rpt == 2) {
-        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 2, true>
-            <<<dim3(gx, (unsigned)(nlat / 2)), NT, 0, st>>>(a, colour, t);
-    } else {
-        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 1, true>
-            <<<dim3(gx, (unsigned)nlat), NT, 0, st>>>(a, colour, t);
-    }
-    return cudaGetLastError();
+    const bool pdl = a.pdl != 0;
+    const dim3 b((unsigned)NT);
+    if (colour < 0 && rpt == 4)
+        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 4), 8u), b, 0, st,
+                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 4, true>, a);
+    if (colour < 0 && rpt == 2)
+        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 2), 8u), b, 0, st,
+                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 2, true>, a);
+    if (colour < 0)
+        return launch_k(pdl, dim3(gx, (unsigned)nlat, 8u), b, 0, st,
+                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 1, true>, a);
+    if (rpt == 4)
+        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 4)), b, 0, st,
+                        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 4, true>, a, colour, t);
+    if (rpt == 2)
+        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 2)), b, 0, st,
+                        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 2, true>, a, colour, t);
+    return launch_k(pdl, dim3(gx, (unsigned)nlat), b, 0, st,
+                    sweep_fixed_hbm_kernel<Real, LH, HH, NT, 1, true>, a, colour, t);
 }
 
 using HbmFn = cudaError_t (*)(const SweepArgs&, int, int, int, int, cudaStream_t);
