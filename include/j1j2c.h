@@ -52,6 +52,10 @@ extern "C" {
 #define J1J2C_FLAG_CLUSTER 64u   /* force the thread-block-cluster path, largest cluster that fits
                                     (testing; with J1J2C_FLAG_GENERIC one site per thread)        */
 #define J1J2C_FLAG_WOLFF 32u     /* one Wolff cluster update at the start of every PT cycle       */
+#define J1J2C_FLAG_WOLFF_SPLIT 1024u /* with J1J2C_FLAG_WOLFF and lattices in HBM (one launch per
+                                        colour): the Wolff update and sweeps of the coldest quarter
+                                        of the slots on one stream, those of the other slots on a
+                                        second one (testing; else tuned)                          */
 #define J1J2C_FLAG_STREAM 512u   /* the streaming form of the shape-specialised kernels: one CTA
                                     per SM through a range of lattices (testing; else tuned)      */
 #define J1J2C_FLAG_WOLFF_CS2 128u /* Wolff growth over 2 CTAs per lattice (testing; else tuned)    */

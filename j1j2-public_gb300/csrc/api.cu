@@ -8,6 +8,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -43,6 +44,10 @@ struct Group {
     bool tuned = false;
     int wolff_cs = 0;  // CTAs per lattice of the Wolff growth kernel (0: not tuned, 1)
     int wolff_k = 0;   // 0 < k < nrep: only the k coldest slots take wolff_cs CTAs, the rest one
+    // HBM sweep form with Wolff: 0 < split_k < nrep runs the Wolff update and sweeps of the
+    // split_k coldest slots of every configuration (split_cs CTAs per growing cluster) on the
+    // main stream and those of the other slots on the Wolff side stream
+    int split_k = 0, split_cs = 1;
     int nlat() const { return nconf * nrep; }
 };
 
@@ -91,6 +96,7 @@ struct Ctx {
     // per group: the side stream and events of a Wolff update split over two launches
     std::vector<cudaStream_t> wside;
     std::vector<cudaEvent_t> wfork, wjoin;
+    int prio_hi = 0;  // the device's highest launch priority (the split form's cold slots)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaGraph_t graph_src[2] = {nullptr, nullptr};  // kept: its event-record nodes are retargeted
     cudaGraphNode_t graph_ev[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
@@ -468,6 +474,65 @@ cudaError_t enqueue_wolff_grow(Ctx* c, const Group& grp, const SweepArgs& a, int
     return cudaStreamWaitEvent(st, c->wjoin[gi], 0);
 }
 
+// Coldest slots of the split Wolff + sweep form (0: not split)
+int split_k_of(const Ctx* c, const Group& grp)
+{
+    if (!c->wolff || !grp.var.global || grp.var.fixed_nt <= 0) return 0;
+    if (c->P.flags & J1J2C_FLAG_WOLFF_SPLIT) return grp.nrep >= 2 ? (grp.nrep + 3) / 4 : 0;
+    return grp.split_k;
+}
+
+// CTAs per growing cluster of the split form's cold slots
+int split_cs_of(const Ctx* c, const Group& grp)
+{
+    if (c->P.flags & J1J2C_FLAG_WOLFF_SPLIT) return wolff_cs_of(c, grp);
+    return grp.split_cs;
+}
+
+// The Wolff update, PTSWAPEVER sweeps and the observables of a group in the HBM sweep form (a:
+// its arguments, whole configurations), split by temperature slot: the k coldest slots of every
+// configuration on stream st, the others on the group's Wolff side stream.  The hot lattices'
+// sweeps run while the cold lattices' clusters still grow; every lattice keeps its own order
+// (its Wolff update, then its sweeps), and the observables follow both halves.
+cudaError_t enqueue_split(Ctx* c, const Group& grp, const SweepVariant& v, SweepArgs a, int k,
+                          int cs, cudaStream_t st)
+{
+    const size_t gi = (size_t)(&grp - c->G.data());
+    const int nlat = grp.nlat();
+    int* lab = c->d_labels + grp.lab_off;
+    long long* cz = c->d_csize + grp.rep0;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(cz, 0, sizeof(long long) * nlat, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(a.obs + a.lat0, 0, sizeof(LatObs) * nlat, st)) != cudaSuccess)
+        return e;
+    if ((e = cudaEventRecord(c->wfork[gi], st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(c->wside[gi], c->wfork[gi], 0)) != cudaSuccess) return e;
+    const cudaStream_t ss[2] = {st, c->wside[gi]};
+    const int s0[2] = {0, k}, ns[2] = {k, grp.nrep - k}, ncs[2] = {cs, 1};
+    for (int h = 0; h < 2; ++h) {
+        // the cold slots' kernels first wherever both halves have CTAs waiting (graph node
+        // priorities): their clusters grow longest, and their sweeps end the cycle
+        SweepArgs b = a;
+        b.prio = h == 0 ? c->prio_hi : 0;
+        if ((e = launch_wolff_grow(b, v.fp64, c->masks, grp.nconf, s0[h], ns[h], ncs[h], lab,
+                                   grp.lat_stride, cz, ss[h])) != cudaSuccess)
+            return e;
+        b.slot0 = s0[h];
+        b.nslots = ns[h];
+        for (int t = 0; t < a.nsweeps; ++t)
+            for (int col = 0; col < 8; ++col) {
+                b.pdl = (t > 0 || col > 0) ? 1 : 0;
+                if ((e = launch_sweep_global(b, v, col, t, nlat, ss[h])) != cudaSuccess) return e;
+            }
+    }
+    if ((e = cudaEventRecord(c->wjoin[gi], c->wside[gi])) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st, c->wjoin[gi], 0)) != cudaSuccess) return e;
+    a.pdl = 0;
+    a.nslots = 0;
+    a.prio = 0;
+    return launch_measure_global(a, v, nlat, st);
+}
+
 // PTSWAPEVER sweeps and the observable reduction of lattices [lat0, lat0 + nlat) of a group
 cudaError_t enqueue_wolff(Ctx* c, const Group& grp, cudaStream_t st)
 {
@@ -488,6 +553,10 @@ cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int n
                           size_t smem, SweepArgs a, int nlat, cudaStream_t st, bool cycle)
 {
     cudaError_t e;
+    if (cycle && c->wolff && nlat == grp.nlat() && v.global && v.fixed_nt > 0) {
+        const int k = split_k_of(c, grp);
+        if (k > 0) return enqueue_split(c, grp, v, a, k, split_cs_of(c, grp), st);
+    }
     if (cycle && c->wolff && (e = enqueue_wolff(c, grp, st)) != cudaSuccess) return e;
     if (v.cluster > 0) {
         if ((e = cudaMemsetAsync(a.obs + a.lat0, 0, sizeof(LatObs) * nlat, st)) != cudaSuccess)
@@ -560,7 +629,7 @@ int build_graph(Ctx* c, int measure)
         return cuda_fail(c, e, "capturing the PT-cycle graph");
     }
     if (e2 != cudaSuccess) return cuda_fail(c, e2, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&c->graph[measure], graph, 0);
+    e = cudaGraphInstantiate(&c->graph[measure], graph, cudaGraphInstantiateFlagUseNodePriority);
     if (e != cudaSuccess) {
         cudaGraphDestroy(graph);
         return cuda_fail(c, e, "cudaGraphInstantiate");
@@ -933,6 +1002,116 @@ int tune_wolff(Ctx* c, Group& grp)
     return J1J2C_OK;
 }
 
+// J1J2C_TUNE_LOG=1 in the environment: the autotuners print every candidate's time to stderr
+bool tune_log()
+{
+    const char* v = std::getenv("J1J2C_TUNE_LOG");
+    return v && v[0] == '1';
+}
+
+// Split Wolff + sweep form (lattices in HBM with Wolff): the whole cycle's Wolff update, sweeps
+// and observables timed on a scratch copy of the group's lattices (the live state is not
+// touched) unsplit and split at the 1/4, 1/2 and 3/4 coldest slots, one CTA per cluster; the
+// fastest is kept, cached per (device, precision, L, H, lattice count, dilution).  Two CTAs per
+// cold cluster are not candidates: on a fresh HOT start (small clusters) they time fastest, on
+// equilibrated lattices they are the slowest choice (L = 96, 8 x 48: 11.0-12.4 vs 9.6 ms).
+std::map<std::tuple<int, bool, int, int, int, bool>, std::pair<int, int>> g_split_cache;
+
+int tune_split(Ctx* c, Group& grp)
+{
+    const uint32_t fl = c->P.flags;
+    if (!c->wolff || !grp.var.global || grp.var.fixed_nt <= 0 || grp.nrep < 8 ||
+        (fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_WOLFF_CS2 |
+               J1J2C_FLAG_WOLFF_CS4 | J1J2C_FLAG_WOLFF_SPLIT | J1J2C_FLAG_NO_GRAPH)))
+        return J1J2C_OK;
+    const auto key =
+        std::make_tuple(c->P.device, grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_split_cache.find(key);
+        if (it != g_split_cache.end()) {
+            grp.split_k = it->second.first;
+            grp.split_cs = it->second.second;
+            return J1J2C_OK;
+        }
+    }
+    if (!c->d_labels) CK(c, dalloc(&c->d_labels, (size_t)c->lab_ints));
+    const int nlat = grp.nlat();
+    uint8_t* tmp = nullptr;
+    LatObs* tobs = nullptr;
+    const size_t bytes = (size_t)nlat * grp.lat_stride;
+    CK(c, cudaMalloc(&tmp, bytes));
+    if (cudaMalloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess) {
+        cudaFree(tmp);
+        return fail(c, J1J2C_ENOMEM, "autotuner scratch");
+    }
+    cudaError_t e =
+        cudaMemcpyAsync(tmp, c->d_spins + grp.spin_off, bytes, cudaMemcpyDeviceToDevice, c->own);
+    SweepArgs a = group_args(c, grp);
+    a.spins = tmp;
+    a.obs = tobs;
+    a.flips = nullptr;
+    struct Cand {
+        int k, cs;
+    };
+    std::vector<Cand> cands{{0, 1}};
+    for (const int k : {grp.nrep / 4, grp.nrep / 2, 3 * grp.nrep / 4}) cands.push_back({k, 1});
+    int best_k = 0, best_cs = 1;
+    float best_ms = 0.0f;
+    for (const Cand cd : cands) {
+        if (e != cudaSuccess) break;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        e = cudaStreamBeginCapture(c->own, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t e1;
+            if (cd.k > 0) {
+                e1 = enqueue_split(c, grp, grp.var, a, cd.k, cd.cs, c->own);
+            } else {
+                e1 = enqueue_wolff_grow(c, grp, a, wolff_cs_of(c, grp), wolff_k_of(c, grp),
+                                        c->own);
+                if (e1 == cudaSuccess)
+                    e1 = enqueue_group(c, grp, grp.var, grp.nthreads, grp.smem, a, nlat, c->own,
+                                       false);
+            }
+            e = cudaStreamEndCapture(c->own, &graph);
+            if (e1 != cudaSuccess) e = e1;
+        }
+        if (e == cudaSuccess)
+            e = cudaGraphInstantiate(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+        if (graph) cudaGraphDestroy(graph);
+        if (e == cudaSuccess) e = cudaGraphLaunch(exec, c->own);  // warm-up
+        float ms = 0.0f;
+        for (int r = 0; r < 3 && e == cudaSuccess; ++r) {  // the fastest of three
+            e = cudaEventRecord(c->ev0, c->own);
+            if (e == cudaSuccess) e = cudaGraphLaunch(exec, c->own);
+            if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->own);
+            if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
+            float t = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, c->ev0, c->ev1);
+            if (e == cudaSuccess && (r == 0 || t < ms)) ms = t;
+        }
+        if (exec) cudaGraphExecDestroy(exec);
+        if (e == cudaSuccess && tune_log())
+            std::fprintf(stderr, "j1j2c tune split L=%d H=%d lattices=%d: k=%d cs=%d %.3f ms\n",
+                         grp.g.L, grp.g.H, nlat, cd.k, cd.cs, ms);
+        if (e == cudaSuccess && (cd.k == 0 || ms < best_ms)) {
+            best_ms = ms;
+            best_k = cd.k;
+            best_cs = cd.cs;
+        }
+    }
+    cudaStreamSynchronize(c->own);
+    cudaFree(tmp);
+    cudaFree(tobs);
+    if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the split Wolff + sweep form");
+    grp.split_k = best_k;
+    grp.split_cs = best_cs;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_split_cache[key] = std::make_pair(best_k, best_cs);
+    return J1J2C_OK;
+}
+
 int autotune(Ctx* c, Group& grp)
 {
     if (grp.tuned) return J1J2C_OK;
@@ -942,7 +1121,10 @@ int autotune(Ctx* c, Group& grp)
         if (rc != J1J2C_OK) return rc;
     }
     if (c->P.flags & J1J2C_FLAG_CLUSTER) return J1J2C_OK;
-    if (grp.var.cluster > 0 && grp.block_threads == 0) return tune_cluster(c, grp);
+    if (grp.var.cluster > 0 && grp.block_threads == 0) {
+        const int rc = tune_cluster(c, grp);
+        return rc != J1J2C_OK ? rc : tune_split(c, grp);
+    }
     if (grp.var.global && grp.var.fixed_nt > 0) return J1J2C_OK;
     if (grp.block_threads > 0 || (c->P.flags & J1J2C_FLAG_STREAM)) return J1J2C_OK;
     if (grp.var.fixed_nt == 0) return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
@@ -1191,6 +1373,11 @@ int j1j2c_create_multi(void** out, const j1j2c_params* groups, int32_t ngroups)
     }
     for (const Group& grp : c->G)
         if ((e = wolff_side(c, grp)) != cudaSuccess) return cfail(e, "Wolff stream");
+    {
+        int least = 0;
+        if ((e = cudaDeviceGetStreamPriorityRange(&least, &c->prio_hi)) != cudaSuccess)
+            return cfail(e, "stream priorities");
+    }
     if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess) return cfail(e, "event");
     if ((e = cudaEventCreate(&c->ev1)) != cudaSuccess) return cfail(e, "event");
     for (int k = 0; c->profile && k < kProfPool; ++k) {

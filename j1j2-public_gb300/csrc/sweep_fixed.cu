@@ -652,7 +652,7 @@ bool usable(const FixedEntry& e, bool fp64, int L, int H, bool vac)
 // once and shared, the spin operands of every replica are loaded before any is updated.
 template <class Real, int LH, int HH, int C, int RPT, bool VAC>
 __device__ __forceinline__ void hbm_phase(const SweepArgs& a, const Real* P, const QuadOff& o,
-                                          int lat, int conf, int rep, uint32_t sweep,
+                                          int conf, const int* rep, uint32_t sweep,
                                           uint32_t k0, uint32_t k1)
 {
     QuadData<Real> d[RPT];
@@ -661,25 +661,30 @@ __device__ __forceinline__ void hbm_phase(const SweepArgs& a, const Real* P, con
     for (int r = 0; r < RPT; ++r) {
         if (r > 0) d[r] = d[0];
         load_quad_spins<Real, LH, HH, C>(
-            reinterpret_cast<const uint32_t*>(a.spins + (long long)(lat + r) * a.lat_stride), o,
-            d[r]);
+            reinterpret_cast<const uint32_t*>(
+                a.spins + (long long)(conf * a.nrep + rep[r]) * a.lat_stride),
+            o, d[r]);
     }
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
         const double beta = a.use_override
                                 ? a.beta_override
-                                : a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep + r]];
+                                : a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep[r]]];
         const float kb = (float)(-2.0 * beta * 1.4426950408889634);
         Acc none{0, 0, 0, 0, 0};
         compute_quad<Real, LH, HH, C, false, VAC>(
-            a, reinterpret_cast<uint32_t*>(a.spins + (long long)(lat + r) * a.lat_stride), d[r],
-            sweep, (uint32_t)(rep + r), k0, k1, beta, kb, none);
+            a,
+            reinterpret_cast<uint32_t*>(a.spins +
+                                        (long long)(conf * a.nrep + rep[r]) * a.lat_stride),
+            d[r], sweep, (uint32_t)rep[r], k0, k1, beta, kb, none);
     }
 }
 
 // Grid: (quads of a colour / NT, lattices / RPT); with RPT > 1 the launcher guarantees that the
-// RPT lattices of a block row are replicas of one configuration.
-template <class Real, int LH, int HH, int NT, int RPT, bool VAC>
+// RPT lattices of a block row are replicas of one configuration.  SLOTS: block row y covers
+// temperature slots slot0 + RPT * (y % (nslots / RPT)) .. + RPT - 1 of configuration
+// lat0 / nrep + y / (nslots / RPT), the lattices that hold them now (rep_at_temp).
+template <class Real, int LH, int HH, int NT, int RPT, bool VAC, bool SLOTS>
 __global__ void __launch_bounds__(NT, sizeof(Real) == 8 ? 1 : RPT == 4 ? 768 / NT : 1024 / NT)
     sweep_fixed_hbm_kernel(SweepArgs a, int colour, int t)
 {
@@ -688,9 +693,19 @@ __global__ void __launch_bounds__(NT, sizeof(Real) == 8 ? 1 : RPT == 4 ? 768 / N
     using Sh = Shape<LH, HH>;
     const int q = (int)(blockIdx.x * NT + threadIdx.x);
     if (q >= Sh::CS) return;
-    const int lat = a.lat0 + (int)blockIdx.y * RPT;
-    const int conf = lat / a.nrep;
-    const int rep = lat - conf * a.nrep;
+    int conf, rep[RPT];
+    if (SLOTS) {
+        const int per = a.nslots / RPT;
+        conf = a.lat0 / a.nrep + (int)blockIdx.y / per;
+        const int s0 = a.slot0 + ((int)blockIdx.y % per) * RPT;
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) rep[r] = a.rep_at_temp[conf * a.nrep + s0 + r];
+    } else {
+        const int lat = a.lat0 + (int)blockIdx.y * RPT;
+        conf = lat / a.nrep;
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) rep[r] = lat - conf * a.nrep + r;
+    }
     const Real* P = field_base<Real>(a, conf);
     const uint32_t sweep = (a.use_override ? a.sweep_override
                                            : a.ctl[0] * (uint32_t)a.ptswapever) + (uint32_t)t;
@@ -699,7 +714,7 @@ __global__ void __launch_bounds__(NT, sizeof(Real) == 8 ? 1 : RPT == 4 ? 768 / N
     switch (colour) {
 #define J1J2_HBM_PHASE(C)                                                                     \
     case C:                                                                                   \
-        hbm_phase<Real, LH, HH, C, RPT, VAC>(a, P, o, lat, conf, rep, sweep, k0, k1);         \
+        hbm_phase<Real, LH, HH, C, RPT, VAC>(a, P, o, conf, rep, sweep, k0, k1);              \
         break;
         J1J2_HBM_PHASE(0)
         J1J2_HBM_PHASE(1)
@@ -784,24 +799,38 @@ cudaError_t run_hbm(const SweepArgs& a, int colour, int t, int nlat, int rpt, cu
     constexpr int CS = Shape<LH, HH>::CS;
     const unsigned gx = (unsigned)((CS + NT - 1) / NT);
     const bool pdl = a.pdl != 0;
+    const int pr = a.prio;
     const dim3 b((unsigned)NT);
     if (colour < 0 && rpt == 4)
-        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 4), 8u), b, 0, st,
+        return launch_k(pdl, pr, dim3(gx, (unsigned)(nlat / 4), 8u), b, 0, st,
                         measure_fixed_hbm_kernel<Real, LH, HH, NT, 4, true>, a);
     if (colour < 0 && rpt == 2)
-        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 2), 8u), b, 0, st,
+        return launch_k(pdl, pr, dim3(gx, (unsigned)(nlat / 2), 8u), b, 0, st,
                         measure_fixed_hbm_kernel<Real, LH, HH, NT, 2, true>, a);
     if (colour < 0)
-        return launch_k(pdl, dim3(gx, (unsigned)nlat, 8u), b, 0, st,
+        return launch_k(pdl, pr, dim3(gx, (unsigned)nlat, 8u), b, 0, st,
                         measure_fixed_hbm_kernel<Real, LH, HH, NT, 1, true>, a);
+    if (a.nslots > 0) {  // a slot range of every configuration (nlat: whole configurations)
+        const unsigned gy = (unsigned)(nlat / a.nrep * (a.nslots / rpt));
+        if (rpt == 4)
+            return launch_k(pdl, pr, dim3(gx, gy), b, 0, st,
+                            sweep_fixed_hbm_kernel<Real, LH, HH, NT, 4, true, true>, a, colour,
+                            t);
+        if (rpt == 2)
+            return launch_k(pdl, pr, dim3(gx, gy), b, 0, st,
+                            sweep_fixed_hbm_kernel<Real, LH, HH, NT, 2, true, true>, a, colour,
+                            t);
+        return launch_k(pdl, pr, dim3(gx, gy), b, 0, st,
+                        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 1, true, true>, a, colour, t);
+    }
     if (rpt == 4)
-        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 4)), b, 0, st,
-                        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 4, true>, a, colour, t);
+        return launch_k(pdl, pr, dim3(gx, (unsigned)(nlat / 4)), b, 0, st,
+                        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 4, true, false>, a, colour, t);
     if (rpt == 2)
-        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 2)), b, 0, st,
-                        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 2, true>, a, colour, t);
-    return launch_k(pdl, dim3(gx, (unsigned)nlat), b, 0, st,
-                    sweep_fixed_hbm_kernel<Real, LH, HH, NT, 1, true>, a, colour, t);
+        return launch_k(pdl, pr, dim3(gx, (unsigned)(nlat / 2)), b, 0, st,
+                        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 2, true, false>, a, colour, t);
+    return launch_k(pdl, pr, dim3(gx, (unsigned)nlat), b, 0, st,
+                    sweep_fixed_hbm_kernel<Real, LH, HH, NT, 1, true, false>, a, colour, t);
 }
 
 using HbmFn = cudaError_t (*)(const SweepArgs&, int, int, int, int, cudaStream_t);
@@ -858,6 +887,12 @@ cudaError_t launch_fixed_hbm(const SweepArgs& a, bool fp64, int colour, int t, i
     // their configuration's field)
     if (rpt > 1 && (a.nrep % rpt != 0 || a.lat0 % a.nrep != 0 || nlat % a.nrep != 0)) rpt = 1;
     if (rpt != 2 && rpt != 4) rpt = 1;
+    if (a.nslots > 0) {  // slot ranges: whole configurations, RPT dividing the range
+        if (colour < 0 || a.lat0 % a.nrep != 0 || nlat % a.nrep != 0 || a.slot0 < 0 ||
+            a.slot0 + a.nslots > a.nrep)
+            return cudaErrorInvalidValue;
+        while (rpt > 1 && a.nslots % rpt != 0) rpt /= 2;
+    }
     for (const auto& e : kHbm)
         if (e.fp64 == fp64 && e.L == a.g.L && e.H == a.g.H)
             return e.fn(a, colour, t, nlat, rpt, st);

@@ -810,24 +810,26 @@ cudaError_t grow_launch(const SweepArgs& a, int nconf, int slot0, int nslots, in
 {
     auto kern = wolff_grow_kernel<Real, MASKS, CS>;
     const int nlat = nconf * nslots;
-    if constexpr (CS == 1) {
-        kern<<<nlat, kGrowThreads, 0, st>>>(a, list, list_stride, csize, slot0, nconf);
-        return cudaGetLastError();
-    } else {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((unsigned)(nlat * CS));
-        cfg.blockDim = dim3(kGrowThreads);
-        cfg.dynamicSmemBytes = 0;
-        cfg.stream = st;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = (unsigned)CS;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&cfg, kern, a, list, list_stride, csize, slot0, nconf);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nlat * CS));
+    cfg.blockDim = dim3(kGrowThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[2];
+    unsigned n = 0;
+    if (CS > 1) {
+        at[n].id = cudaLaunchAttributeClusterDimension;
+        at[n].val.clusterDim.x = (unsigned)CS;
+        at[n].val.clusterDim.y = 1;
+        at[n++].val.clusterDim.z = 1;
     }
+    if (a.prio != 0) {  // launch priority (the split Wolff + sweep form's cold slots)
+        at[n].id = cudaLaunchAttributePriority;
+        at[n++].val.priority = a.prio;
+    }
+    cfg.attrs = at;
+    cfg.numAttrs = n;
+    return cudaLaunchKernelEx(&cfg, kern, a, list, list_stride, csize, slot0, nconf);
 }
 
 template <class Real, bool MASKS, int CS>

@@ -146,6 +146,57 @@ def test_wolff_inside_pt_cycles(engine_mod, oracle, nrep):
     eng.close()
 
 
+@pytest.mark.parametrize("extra", ["split", "tuned"])
+def test_split_wolff_sweeps_bit_identical(engine_mod, oracle, extra):
+    """Lattices in HBM (the one-launch-per-colour kernel; L = 32 is its cross-check shape) with a
+    Wolff update per cycle: the Wolff update and sweeps of the coldest slots and of the others
+    on two streams, each sweep launch finding its lattices through the temperature map (flag
+    1024 pins the split at a quarter of the slots; unpinned the tuner times it against the
+    unsplit cycle), equal the replay bit for bit over cycles with replica exchanges."""
+    jc = engine_mod
+    L, H, nconf, nrep, ncyc = 32, 32, 2, 8, 3
+    flags = jc.FLAG_WOLFF | jc.FLAG_GLOBAL | (jc.FLAG_WOLFF_SPLIT if extra == "split" else 0)
+    eng, dis, betas = _engine(jc, L, H, nconf, nrep, jc.FP64_PLAIN, flags, 0.05)
+    states = [oracle.new_pt_state(np.stack([eng.spins(k, r) for r in range(nrep)]))
+              for k in range(nconf)]
+    eng.run(ncyc, measure=True, restart_swap_phase=True)
+    assert eng.config()["smem_bytes"] == 0
+    for k in range(nconf):
+        p, occu, _, _ = dis[k]
+        M = oracle.Model(L, H, p, occu)
+        st = states[k]
+        for cyc in range(ncyc):
+            for r in range(nrep):
+                s = st["spins"][r].copy()
+                M.wolff_step(s, betas[st["temp_of_rep"][r]], SEED, k, r, cyc)
+                st["spins"][r] = s
+            M.replay_pt(st, betas, 5, 1, cyc, SEED, k, True, 1 if cyc % 2 == 0 else 2)
+        for r in range(nrep):
+            np.testing.assert_array_equal(eng.spins(k, r), st["spins"][r])
+        np.testing.assert_array_equal(eng.slot_sums(k)[0], st["sums"])
+        np.testing.assert_array_equal(eng.maps(k)[0], st["rep_at_temp"])
+    eng.close()
+
+
+def test_split_wolff_sweeps_fp32_equals_unsplit(engine_mod, oracle):
+    """FP32, L = 96 with vacancies and 8 replicas: the split cycle (flag 1024) and the unsplit one
+    (growth pinned to two CTAs per lattice, which also pins the cycle unsplit) give bitwise equal
+    spins, running sums, maps and cluster sizes."""
+    jc = engine_mod
+    out = []
+    base = jc.FLAG_WOLFF | jc.FLAG_GLOBAL
+    for flags in (base | jc.FLAG_WOLFF_SPLIT, base | jc.FLAG_WOLFF_CS2):
+        eng, _, _ = _engine(jc, 96, 96, 1, 8, jc.FP32_BATCHED, flags, 0.05)
+        eng.run(2, measure=True, restart_swap_phase=True)
+        out.append(([eng.spins(0, r) for r in range(8)], eng.slot_sums(0)[0], eng.maps(0)[0],
+                    eng.cluster_sizes()))
+        eng.close()
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    for i in (1, 2, 3):
+        np.testing.assert_array_equal(out[0][i], out[1][i])
+
+
 def _cpu_exact(oracle, L, H, p, betas):
     M = oracle.Model(L, H, p)
     N = L * L * H
