@@ -96,7 +96,6 @@ struct Ctx {
     // per group: the side stream and events of a Wolff update split over two launches
     std::vector<cudaStream_t> wside;
     std::vector<cudaEvent_t> wfork, wjoin;
-    int prio_hi = 0;  // the device's highest launch priority (the split form's cold slots)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaGraph_t graph_src[2] = {nullptr, nullptr};  // kept: its event-record nodes are retargeted
     cudaGraphNode_t graph_ev[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
@@ -510,10 +509,7 @@ cudaError_t enqueue_split(Ctx* c, const Group& grp, const SweepVariant& v, Sweep
     const cudaStream_t ss[2] = {st, c->wside[gi]};
     const int s0[2] = {0, k}, ns[2] = {k, grp.nrep - k}, ncs[2] = {cs, 1};
     for (int h = 0; h < 2; ++h) {
-        // the cold slots' kernels first wherever both halves have CTAs waiting (graph node
-        // priorities): their clusters grow longest, and their sweeps end the cycle
         SweepArgs b = a;
-        b.prio = h == 0 ? c->prio_hi : 0;
         if ((e = launch_wolff_grow(b, v.fp64, c->masks, grp.nconf, s0[h], ns[h], ncs[h], lab,
                                    grp.lat_stride, cz, ss[h])) != cudaSuccess)
             return e;
@@ -529,7 +525,6 @@ cudaError_t enqueue_split(Ctx* c, const Group& grp, const SweepVariant& v, Sweep
     if ((e = cudaStreamWaitEvent(st, c->wjoin[gi], 0)) != cudaSuccess) return e;
     a.pdl = 0;
     a.nslots = 0;
-    a.prio = 0;
     return launch_measure_global(a, v, nlat, st);
 }
 
@@ -629,7 +624,7 @@ int build_graph(Ctx* c, int measure)
         return cuda_fail(c, e, "capturing the PT-cycle graph");
     }
     if (e2 != cudaSuccess) return cuda_fail(c, e2, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&c->graph[measure], graph, cudaGraphInstantiateFlagUseNodePriority);
+    e = cudaGraphInstantiate(&c->graph[measure], graph, 0);
     if (e != cudaSuccess) {
         cudaGraphDestroy(graph);
         return cuda_fail(c, e, "cudaGraphInstantiate");
@@ -1077,8 +1072,7 @@ int tune_split(Ctx* c, Group& grp)
             e = cudaStreamEndCapture(c->own, &graph);
             if (e1 != cudaSuccess) e = e1;
         }
-        if (e == cudaSuccess)
-            e = cudaGraphInstantiate(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
         if (graph) cudaGraphDestroy(graph);
         if (e == cudaSuccess) e = cudaGraphLaunch(exec, c->own);  // warm-up
         float ms = 0.0f;
@@ -1373,11 +1367,6 @@ int j1j2c_create_multi(void** out, const j1j2c_params* groups, int32_t ngroups)
     }
     for (const Group& grp : c->G)
         if ((e = wolff_side(c, grp)) != cudaSuccess) return cfail(e, "Wolff stream");
-    {
-        int least = 0;
-        if ((e = cudaDeviceGetStreamPriorityRange(&least, &c->prio_hi)) != cudaSuccess)
-            return cfail(e, "stream priorities");
-    }
     if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess) return cfail(e, "event");
     if ((e = cudaEventCreate(&c->ev1)) != cudaSuccess) return cfail(e, "event");
     for (int k = 0; c->profile && k < kProfPool; ++k) {

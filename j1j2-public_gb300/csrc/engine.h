@@ -48,7 +48,6 @@ struct SweepArgs {
     int* err;                // set to 1 when a bounded wait of a kernel gave up (or nullptr)
     int pdl;                 // host side: the launch may overlap the stream's previous kernel
                              // (programmatic dependent launch; global-memory kernels only)
-    int prio;                // host side: launch priority (0: the stream's; graphs honour it)
     int slot0, nslots;       // HBM sweep kernel: temperature slots [slot0, slot0 + nslots) of
                              // every configuration of the launch, each slot's lattice found
                              // through rep_at_temp (nslots = 0: lattices lat0 .. in order)

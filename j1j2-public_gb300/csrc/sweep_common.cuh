@@ -309,31 +309,16 @@ template <class... P, class... A>
 cudaError_t launch_k(bool pdl, dim3 grid, dim3 block, size_t smem, cudaStream_t st,
                      void (*kernel)(P...), A&&... args)
 {
-    return launch_k(pdl, 0, grid, block, smem, st, kernel, static_cast<A&&>(args)...);
-}
-
-// the same with a launch priority (0: the stream's own)
-template <class... P, class... A>
-cudaError_t launch_k(bool pdl, int prio, dim3 grid, dim3 block, size_t smem, cudaStream_t st,
-                     void (*kernel)(P...), A&&... args)
-{
-    cudaLaunchAttribute at[2];
-    unsigned n = 0;
-    if (pdl) {
-        at[n].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        at[n++].val.programmaticStreamSerializationAllowed = 1;
-    }
-    if (prio != 0) {
-        at[n].id = cudaLaunchAttributePriority;
-        at[n++].val.priority = prio;
-    }
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = grid;
     cfg.blockDim = block;
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cfg.attrs = at;
-    cfg.numAttrs = n;
+    cfg.numAttrs = pdl ? 1u : 0u;
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<A&&>(args)...);
 }
 

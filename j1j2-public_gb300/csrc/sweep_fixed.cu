@@ -799,37 +799,36 @@ cudaError_t run_hbm(const SweepArgs& a, int colour, int t, int nlat, int rpt, cu
     constexpr int CS = Shape<LH, HH>::CS;
     const unsigned gx = (unsigned)((CS + NT - 1) / NT);
     const bool pdl = a.pdl != 0;
-    const int pr = a.prio;
     const dim3 b((unsigned)NT);
     if (colour < 0 && rpt == 4)
-        return launch_k(pdl, pr, dim3(gx, (unsigned)(nlat / 4), 8u), b, 0, st,
+        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 4), 8u), b, 0, st,
                         measure_fixed_hbm_kernel<Real, LH, HH, NT, 4, true>, a);
     if (colour < 0 && rpt == 2)
-        return launch_k(pdl, pr, dim3(gx, (unsigned)(nlat / 2), 8u), b, 0, st,
+        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 2), 8u), b, 0, st,
                         measure_fixed_hbm_kernel<Real, LH, HH, NT, 2, true>, a);
     if (colour < 0)
-        return launch_k(pdl, pr, dim3(gx, (unsigned)nlat, 8u), b, 0, st,
+        return launch_k(pdl, dim3(gx, (unsigned)nlat, 8u), b, 0, st,
                         measure_fixed_hbm_kernel<Real, LH, HH, NT, 1, true>, a);
     if (a.nslots > 0) {  // a slot range of every configuration (nlat: whole configurations)
         const unsigned gy = (unsigned)(nlat / a.nrep * (a.nslots / rpt));
         if (rpt == 4)
-            return launch_k(pdl, pr, dim3(gx, gy), b, 0, st,
+            return launch_k(pdl, dim3(gx, gy), b, 0, st,
                             sweep_fixed_hbm_kernel<Real, LH, HH, NT, 4, true, true>, a, colour,
                             t);
         if (rpt == 2)
-            return launch_k(pdl, pr, dim3(gx, gy), b, 0, st,
+            return launch_k(pdl, dim3(gx, gy), b, 0, st,
                             sweep_fixed_hbm_kernel<Real, LH, HH, NT, 2, true, true>, a, colour,
                             t);
-        return launch_k(pdl, pr, dim3(gx, gy), b, 0, st,
+        return launch_k(pdl, dim3(gx, gy), b, 0, st,
                         sweep_fixed_hbm_kernel<Real, LH, HH, NT, 1, true, true>, a, colour, t);
     }
     if (rpt == 4)
-        return launch_k(pdl, pr, dim3(gx, (unsigned)(nlat / 4)), b, 0, st,
+        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 4)), b, 0, st,
                         sweep_fixed_hbm_kernel<Real, LH, HH, NT, 4, true, false>, a, colour, t);
     if (rpt == 2)
-        return launch_k(pdl, pr, dim3(gx, (unsigned)(nlat / 2)), b, 0, st,
+        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 2)), b, 0, st,
                         sweep_fixed_hbm_kernel<Real, LH, HH, NT, 2, true, false>, a, colour, t);
-    return launch_k(pdl, pr, dim3(gx, (unsigned)nlat), b, 0, st,
+    return launch_k(pdl, dim3(gx, (unsigned)nlat), b, 0, st,
                     sweep_fixed_hbm_kernel<Real, LH, HH, NT, 1, true, false>, a, colour, t);
 }
 

@@ -815,20 +815,13 @@ cudaError_t grow_launch(const SweepArgs& a, int nconf, int slot0, int nslots, in
     cfg.blockDim = dim3(kGrowThreads);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
-    cudaLaunchAttribute at[2];
-    unsigned n = 0;
-    if (CS > 1) {
-        at[n].id = cudaLaunchAttributeClusterDimension;
-        at[n].val.clusterDim.x = (unsigned)CS;
-        at[n].val.clusterDim.y = 1;
-        at[n++].val.clusterDim.z = 1;
-    }
-    if (a.prio != 0) {  // launch priority (the split Wolff + sweep form's cold slots)
-        at[n].id = cudaLaunchAttributePriority;
-        at[n++].val.priority = a.prio;
-    }
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)CS;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
-    cfg.numAttrs = n;
+    cfg.numAttrs = CS > 1 ? 1u : 0u;
     return cudaLaunchKernelEx(&cfg, kern, a, list, list_stride, csize, slot0, nconf);
 }
 
