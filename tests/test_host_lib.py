@@ -28,6 +28,17 @@ def test_library_exports_every_declared_symbol(engine_mod):
 
 
 
+def test_header_constants_match_python_mirror(engine_mod):
+    """Every J1J2C_FLAG_ / START_ / AXIS_ / precision constant of the header has the same value in
+    the ctypes host mirror (a flag added on one side only would silently pin the wrong path)."""
+    text = open(HEADER).read()
+    defs = dict(re.findall(r"#define J1J2C_((?:FLAG|START|AXIS|FP64|FP32)_[A-Z0-9_]+)\s+(-?\d+)u?",
+                           text))
+    assert len(defs) >= 15
+    for name, value in defs.items():
+        assert getattr(engine_mod, name) == int(value), name
+
+
 def test_corr_rand_3d_matches_ooura_golden(engine_mod):
     g = np.load(os.path.join(ROOT, "tests", "golden", "corr3d_golden.npz"))
     n = 0
