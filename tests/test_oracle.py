@@ -1,5 +1,6 @@
 """CPU tests of the oracle: pinned against the committed golden vectors (Ooura-FFT reference build,
 Random123 known answers) and against identities of the reference arithmetic."""
+import itertools
 import json
 import math
 import os
@@ -202,6 +203,56 @@ def test_wolff_restatement_limits(oracle):
     s = np.ones(L * L * H, np.int8)
     assert F.wolff_step(s, 50.0, 1, 0, 0, 7) == L * L * H
     assert (s == -1).all()
+
+
+def _exact_averages(M, occ, beta):
+    """<e>, <|m|>, <m^2> over every spin state of the occupied sites (vacancies 0)."""
+    idx = np.flatnonzero(occ)
+    rows = []
+    for bits in itertools.product((-1, 1), repeat=idx.size):
+        s = np.zeros(occ.size, np.int8)
+        s[idx] = bits
+        m, e, _, _ = M.measurement(s)
+        rows.append((e, abs(m), m * m))
+    a = np.array(rows)
+    E = a[:, 0] * idx.size
+    w = np.exp(-beta * (E - E.min()))
+    return (a * w[:, None]).sum(0) / w.sum()
+
+
+@pytest.mark.parametrize("L,H,T,vac,metro", [(2, 2, 3.0, False, False), (2, 4, 4.0, False, False),
+                                             (2, 4, 4.0, True, False), (2, 4, 2.5, False, True)])
+def test_wolff_restatement_samples_boltzmann(oracle, L, H, T, vac, metro):
+    """The Wolff update as the engine defines it (restated in the oracle) leaves the Boltzmann
+    distribution of the reference Hamiltonian invariant: on lattices small enough to enumerate
+    every state (L = 2 and H = 2 double the x, y, diagonal and z couplings as in the reference's
+    neighbour table), a chain of Wolff updates alone, or alternating with the engine's colour-
+    order Metropolis sweep, reproduces the exact <e>, <|m|> and <m^2> within 4.5 standard errors
+    (batch means over 40 batches).  With a vacancy the vacant site never flips and is excluded."""
+    rng = np.random.default_rng(11)
+    N = L * L * H
+    p = rng.uniform(-2.0, 2.0, N)
+    occ = np.ones(N, np.int8)
+    if vac:
+        occ[5] = 0
+    M = oracle.Model(L, H, p, occ)
+    beta = 1.0 / T
+    exact = _exact_averages(M, occ, beta)
+    s = occ.astype(np.int8).copy()
+    nstep, nburn, nb = 120000, 2000, 40
+    rec = np.empty((nstep, 3))
+    for c in range(nburn + nstep):
+        M.wolff_step(s, beta, 7, 0, 0, c)
+        if metro:
+            M.replay_sweeps(s, beta, 7, 0, 0, c, 1)
+        if c >= nburn:
+            m, e, _, _ = M.measurement(s)
+            rec[c - nburn] = (e, abs(m), m * m)
+    assert (s[occ == 0] == 0).all()
+    bm = rec.reshape(nb, -1, 3).mean(1)
+    se = bm.std(0, ddof=1) / np.sqrt(nb)
+    z = np.abs(bm.mean(0) - exact) / se
+    assert (z < 4.5).all(), (bm.mean(0), exact, z)
 
 
 def test_ladder(oracle):
