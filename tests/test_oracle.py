@@ -220,15 +220,19 @@ def _exact_averages(M, occ, beta):
     return (a * w[:, None]).sum(0) / w.sum()
 
 
-@pytest.mark.parametrize("L,H,T,vac,metro", [(2, 2, 3.0, False, False), (2, 4, 4.0, False, False),
-                                             (2, 4, 4.0, True, False), (2, 4, 2.5, False, True)])
-def test_wolff_restatement_samples_boltzmann(oracle, L, H, T, vac, metro):
+@pytest.mark.parametrize("L,H,T,vac,wolff,metro", [(2, 2, 3.0, False, True, False),
+                                                   (2, 4, 4.0, False, True, False),
+                                                   (2, 4, 4.0, True, True, False),
+                                                   (2, 4, 2.5, False, True, True),
+                                                   (2, 4, 2.5, True, False, True)])
+def test_wolff_restatement_samples_boltzmann(oracle, L, H, T, vac, wolff, metro):
     """The Wolff update as the engine defines it (restated in the oracle) leaves the Boltzmann
     distribution of the reference Hamiltonian invariant: on lattices small enough to enumerate
     every state (L = 2 and H = 2 double the x, y, diagonal and z couplings as in the reference's
-    neighbour table), a chain of Wolff updates alone, or alternating with the engine's colour-
-    order Metropolis sweep, reproduces the exact <e>, <|m|> and <m^2> within 4.5 standard errors
-    (batch means over 40 batches).  With a vacancy the vacant site never flips and is excluded."""
+    neighbour table), a chain of Wolff updates alone, of the engine's colour-order Metropolis
+    sweeps alone, or of both alternating, reproduces the exact <e>, <|m|> and <m^2> within 4.5
+    standard errors (batch means over 40 batches).  With a vacancy the vacant site never flips
+    and is excluded."""
     rng = np.random.default_rng(11)
     N = L * L * H
     p = rng.uniform(-2.0, 2.0, N)
@@ -242,7 +246,8 @@ def test_wolff_restatement_samples_boltzmann(oracle, L, H, T, vac, metro):
     nstep, nburn, nb = 120000, 2000, 40
     rec = np.empty((nstep, 3))
     for c in range(nburn + nstep):
-        M.wolff_step(s, beta, 7, 0, 0, c)
+        if wolff:
+            M.wolff_step(s, beta, 7, 0, 0, c)
         if metro:
             M.replay_sweeps(s, beta, 7, 0, 0, c, 1)
         if c >= nburn:
