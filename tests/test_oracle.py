@@ -289,6 +289,32 @@ def test_replay_pt_slot_averages_match_exact(oracle):
         assert (z < 4.5).all(), (k, means[:, k].mean(0), exact, z)
 
 
+def test_reference_restatement_samples_exact(oracle):
+    """The oracle's restatement of the reference algorithm itself (one KISS05 stream, sequential
+    site order, Metropolis with exp, the PT SERIAL driver and the LOCAL sampler) reproduces the
+    exact averages on 2 x 2 x 4: PT per slot over 40 independent seeds, LOCAL over 40 batches of
+    one long chain, both within 4.5 standard errors."""
+    L, H, nrep = 2, 4, 4
+    N = L * L * H
+    rng = np.random.default_rng(17)
+    M = oracle.Model(L, H, rng.uniform(-2.0, 2.0, N))
+    occ = np.ones(N, np.int8)
+    betas = 1.0 / oracle.ladder(nrep, 2.0, 4.0)
+    nmess, runs, cols = 400, 40, [4, 1, 2]
+    per = np.array([M.pt_serial(betas, 5, 100, nmess, irinit, 1, 0, 0)["sums"][:, cols] / nmess
+                    for irinit in range(1, runs + 1)])
+    se = per.std(0, ddof=1) / np.sqrt(runs)
+    for k in range(nrep):
+        z = np.abs(per[:, k].mean(0) - _exact_averages(M, occ, betas[k])) / se[k]
+        assert (z < 4.5).all(), (k, z)
+    beta = betas[1]
+    lists, _ = M.local(np.ones(N, np.int8), beta, 200, 80000, oracle.kiss_state(5))
+    m, e = lists[0], lists[1]
+    rec = np.stack([e, np.abs(m), m * m], 1).reshape(40, -1, 3).mean(1)
+    z = np.abs(rec.mean(0) - _exact_averages(M, occ, beta)) / (rec.std(0, ddof=1) / np.sqrt(40))
+    assert (z < 4.5).all(), z
+
+
 def test_ladder(oracle):
     t = oracle.ladder(16, 8.0, 11.5)
     np.testing.assert_allclose(t, 8.0 + 3.5 * np.arange(16) / 15, rtol=0, atol=1e-15)
