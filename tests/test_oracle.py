@@ -232,14 +232,18 @@ def test_wolff_restatement_samples_boltzmann(oracle, L, H, T, vac, wolff, metro)
     neighbour table), a chain of Wolff updates alone, of the engine's colour-order Metropolis
     sweeps alone, or of both alternating, reproduces the exact <e>, <|m|> and <m^2> within 4.5
     standard errors (batch means over 40 batches).  With a vacancy the vacant site never flips
-    and is excluded."""
+    and is excluded; diluted J1 bonds carry only the random-field part of their coupling."""
     rng = np.random.default_rng(11)
     N = L * L * H
     p = rng.uniform(-2.0, 2.0, N)
     occ = np.ones(N, np.int8)
-    if vac:
+    jh = np.ones(N, np.int8)
+    jv = np.ones(N, np.int8)
+    if vac:  # a vacancy and diluted J1 bonds
         occ[5] = 0
-    M = oracle.Model(L, H, p, occ)
+        jh[[1, 9]] = 0
+        jv[[4, 14]] = 0
+    M = oracle.Model(L, H, p, occ, jh, jv)
     beta = 1.0 / T
     exact = _exact_averages(M, occ, beta)
     s = occ.astype(np.int8).copy()
@@ -289,16 +293,24 @@ def test_replay_pt_slot_averages_match_exact(oracle):
         assert (z < 4.5).all(), (k, means[:, k].mean(0), exact, z)
 
 
-def test_reference_restatement_samples_exact(oracle):
+@pytest.mark.parametrize("dilute", [False, True])
+def test_reference_restatement_samples_exact(oracle, dilute):
     """The oracle's restatement of the reference algorithm itself (one KISS05 stream, sequential
     site order, Metropolis with exp, the PT SERIAL driver and the LOCAL sampler) reproduces the
-    exact averages on 2 x 2 x 4: PT per slot over 40 independent seeds, LOCAL over 40 batches of
-    one long chain, both within 4.5 standard errors."""
+    exact averages on 2 x 2 x 4, also with a vacancy and diluted J1 bonds: PT per slot over 40
+    independent seeds, LOCAL over 40 batches of one long chain, both within 4.5 standard
+    errors."""
     L, H, nrep = 2, 4, 4
     N = L * L * H
     rng = np.random.default_rng(17)
-    M = oracle.Model(L, H, rng.uniform(-2.0, 2.0, N))
     occ = np.ones(N, np.int8)
+    jh = np.ones(N, np.int8)
+    jv = np.ones(N, np.int8)
+    if dilute:
+        occ[6] = 0
+        jh[[1, 9]] = 0
+        jv[[4, 14]] = 0
+    M = oracle.Model(L, H, rng.uniform(-2.0, 2.0, N), occ, jh, jv)
     betas = 1.0 / oracle.ladder(nrep, 2.0, 4.0)
     nmess, runs, cols = 400, 40, [4, 1, 2]
     per = np.array([M.pt_serial(betas, 5, 100, nmess, irinit, 1, 0, 0)["sums"][:, cols] / nmess
@@ -308,7 +320,7 @@ def test_reference_restatement_samples_exact(oracle):
         z = np.abs(per[:, k].mean(0) - _exact_averages(M, occ, betas[k])) / se[k]
         assert (z < 4.5).all(), (k, z)
     beta = betas[1]
-    lists, _ = M.local(np.ones(N, np.int8), beta, 200, 80000, oracle.kiss_state(5))
+    lists, _ = M.local(occ.copy(), beta, 200, 80000, oracle.kiss_state(5))
     m, e = lists[0], lists[1]
     rec = np.stack([e, np.abs(m), m * m], 1).reshape(40, -1, 3).mean(1)
     z = np.abs(rec.mean(0) - _exact_averages(M, occ, beta)) / (rec.std(0, ddof=1) / np.sqrt(40))
