@@ -6,7 +6,12 @@ T=8.0-11.5, HOT starts; J1=1, J2=-1, Jperp=1, no dilution.  2048 lattices reside
 One step = one PT cycle: PTSWAPEVER=5 fused FP32 sweeps of all lattices, the observable
 reduction, the replica exchange and the FP64 running sums.  Synthetic inputs of the reference's
 shapes (no dataset is involved).  The FP64 plain form is timed beside it on the L=24, 16-replica
-PT configuration.
+PT configuration (START=STR, STRAXIS=X).
+
+`value`, the sweep kernel's CUDA-event time behind the roofline and e2e all come from one engine
+and the same timed steps (its cycle graph brackets the sweep launch with event nodes).  The
+reference arm times the reference's CPU path, restated in the oracle (the Fortran program has no
+toolchain here), on the same workload: every step is one whole PT cycle of every ladder.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -36,13 +41,18 @@ L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one sweep-kernel launch (5 sweeps
 # + measure of every lattice), from an ncu capture of the same workload
 TRAFFIC = {"batched_fp32_L32_64x32": 75578112 + 10685696}
+# issue-slot utilisation and thread instructions per attempt of the same capture (the kernel is
+# bound by instruction issue inside shared memory, not by DRAM)
+NCU_ISSUE = {"batched_fp32_L32_64x32": {"issue_active": 0.582, "inst_per_attempt": 53.4,
+                                        "source": "profiles/sweep_fixed_fp32_L32_2048lat.md"}}
 
 # name -> lattice-shape groups (L, nconf, nreplica), precision and options
 WORKLOADS = {
     # L=32, 64 disorder configurations x 32-replica ladders (2048 lattices), FP32 sweep
     "batched_fp32_L32_64x32": dict(groups=[(32, 64, 32)], precision=1),
-    # L=24, one disorder configuration, 16-replica PT ladder, FP64 sweep (plain form)
-    "plain_fp64_L24_1x16": dict(groups=[(24, 1, 16)], precision=0),
+    # L=24, one disorder configuration, 16-replica PT ladder, FP64 sweep (plain form), stripe
+    # start along x (START=STR, STRAXIS=X)
+    "plain_fp64_L24_1x16": dict(groups=[(24, 1, 16)], precision=0, start="STR_X"),
     # the batched workload in the FP64 form (same seeds)
     "batched_fp64_L32_64x32": dict(groups=[(32, 64, 32)], precision=0),
     # uneven batch: L=16/24/32/48 with 128/64/32/8 configurations and 16/24/32/48 replicas
@@ -138,10 +148,28 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(mhz)}
 
 
+def workload_config(wname, w, ws=1):
+    """The workload as both arms name it in their JSON line."""
+    g0 = w["groups"][0]
+    cfg = {"workload": wname, "L": g0[0], "H": g0[0],
+           "nconf_per_gpu": sum(n for _, n, _ in w["groups"]), "nreplica": g0[2],
+           "ptswapever": w.get("ptswapever", 5), "T": [w["T"]] if "T" in w else [8.0, 11.5],
+           "phi": 2.0, "xi": 3.0, "start": w.get("start", "HOT"),
+           "lattices_per_gpu": sum(n * r for _, n, r in w["groups"]),
+           "attempts_per_step": None, "parallelism": f"confs x{ws}"}
+    if len(w["groups"]) > 1:
+        cfg["groups_L_nconf_nreplica"] = [list(g) for g in w["groups"]]
+    if w.get("vacancies"):
+        cfg["vacancies"] = w["vacancies"]
+    if w.get("wolff"):
+        cfg["wolff_per_cycle"] = 1
+    return cfg
+
+
 def make_engine(jc, w, device, conf_base=0, flags=0, irinit=1):
     """Engine of one workload: disorder of conf k from seed irinit + conf_base + k (PHI=2,
     XI=3), optional Bernoulli site vacancies from the same seed, linear ladders over
-    T = 8.0-11.5 (or one temperature), HOT starts."""
+    T = 8.0-11.5 (or one temperature), HOT starts (or the workload's stripe start)."""
     ptswapever = w.get("ptswapever", 5)
     if w.get("wolff"):
         flags |= jc.FLAG_WOLFF
@@ -161,8 +189,9 @@ def make_engine(jc, w, device, conf_base=0, flags=0, irinit=1):
             k += 1
     betas = np.concatenate(betas)
     eng.set_ladder(-1, betas)
+    start, axis = (jc.START_STR, jc.AXIS_X) if w.get("start") == "STR_X" else (jc.START_HOT, 0)
     for k in range(eng.nconf):
-        eng.init_spins(k, jc.START_HOT)
+        eng.init_spins(k, start, axis)
     eng.reset_measurements()
     return eng, betas
 
@@ -198,19 +227,22 @@ def time_steps(torch, eng, steps, warmup, flush, cycles=1):
 def time_workload(torch, jc, w, device, flush, steps):
     """Device throughput of one workload (CUDA events per step, L2 flushed between).  The value
     comes from an engine without profiling events (graph event nodes cost microseconds per
-    cycle, a sizeable share of a small lattice's cycle); the sweep-kernel split from a second,
-    profiled engine over the same steps."""
+    cycle, a sizeable share of a small lattice's cycle); a second engine with them gives its own
+    step time and the sweep launches' share of it, over the same number of steps."""
     cycles = w.get("cycles_per_step", 1)
     eng, _ = make_engine(jc, w, device)
     ms, _ = time_steps(torch, eng, steps, 3, flush, cycles)
     eng.close()
     eng, _ = make_engine(jc, w, device, flags=jc.FLAG_PROFILE)
-    _, prof_ms = time_steps(torch, eng, steps, 3, flush, cycles)
+    pms, prof_ms = time_steps(torch, eng, steps, 3, flush, cycles)
     att = attempts_per_cycle(eng) * cycles
     out = {"value": round(att * steps / (ms * 1e6), 4), "unit": UNIT,
            "ms_per_step": round(ms / steps, 4), "steps": steps, "attempts_per_step": att,
-           "sweep_ms_per_step": round(prof_ms / steps, 4),
+           "profiled_engine": {"ms_per_step": round(pms / steps, 4),
+                               "sweep_ms_per_step": round(prof_ms / steps, 4)},
            "groups_L_nconf_nreplica": [list(g) for g in w["groups"]]}
+    if w.get("start"):
+        out["start"] = w["start"]
     if cycles > 1:
         out["cycles_per_step"] = cycles
     cfg = eng.config()
@@ -235,6 +267,34 @@ def secondary_workloads(torch, jc, device, flush, steps):
     return res
 
 
+def precision_report(jc, eng, w, device, equil, measured):
+    """The FP32 form against the FP64 form on the headline workload's seeds: (1) the flip-decision
+    mismatch rate in deterministic replay (one FP64 sweep of every lattice from the FP32 run's
+    current state, the FP32 decision evaluated on the same configuration and uniform); (2) per
+    temperature slot and observable, the FP32 - FP64 difference of the configuration-averaged
+    thermal average in units of its standard error over the configurations (both forms from the
+    same starts, equil + measured PT cycles)."""
+    att, mis = eng.audit_fp32(1)
+    names = ("absmag", "mag2", "en", "en2", "strx_abs", "stry_abs", "nbar", "nbar2")
+    cols = [jc.SUM_FIELDS.index(n) for n in names]
+    avg = {}
+    for prec in (0, 1):
+        e, _ = make_engine(jc, dict(w, precision=prec), device)
+        e.run(equil, measure=False)
+        e.reset_measurements()
+        e.run(measured, measure=True)
+        s, nm = e.slot_sums(-1)
+        avg[prec] = (s[:, cols] / nm[:, None]).reshape(e.nconf, -1, len(cols))
+        e.close()
+    d = avg[1] - avg[0]  # (conf, slot, observable)
+    se = d.std(axis=0, ddof=1) / np.sqrt(d.shape[0])
+    z = np.abs(d.mean(axis=0)) / np.where(se > 0, se, np.inf)
+    return {"fp32_flip_mismatch_rate": mis / att, "attempts_audited": int(att),
+            "observable_z_max": {n: round(float(z[:, j].max()), 3) for j, n in enumerate(names)},
+            "z_above_2_fraction": round(float((z > 2).mean()), 4),
+            "cycles": [equil, measured], "nconf": int(d.shape[0])}
+
+
 def run_ours(args):
     import torch
 
@@ -251,14 +311,10 @@ def run_ours(args):
     w = WORKLOADS[wname]
     if args.nconf:  # a smaller case of the same kernels (profiling captures)
         w = dict(w, groups=[(L, args.nconf, r) for L, _, r in w["groups"]])
-    nconf = sum(n for _, n, _ in w["groups"])
-    # `value` and e2e: the engine as a user runs it (no profiling event nodes in its cycle
-    # graph); the roofline: the sweep kernel's CUDA-event duration over the timed steps of a
-    # second engine of the same workload whose graph brackets the sweep launch with events
-    # (those nodes cost ~1 % of a cycle, so its steps are not used for `value`)
-    eng, betas = make_engine(jc, w, local, conf_base=conf_base_of(rank, w), flags=args.flags)
-    peng, _ = make_engine(jc, w, local, conf_base=conf_base_of(rank, w),
-                          flags=jc.FLAG_PROFILE | args.flags)
+    # One engine for `value`, the roofline and e2e: its cycle graph brackets the sweep launch
+    # with CUDA events, so the sweep kernel's duration comes from the very steps that are timed
+    eng, betas = make_engine(jc, w, local, conf_base=conf_base_of(rank, w),
+                             flags=jc.FLAG_PROFILE | args.flags)
     cycles = w.get("cycles_per_step", 1)
     attempts_per_step = attempts_per_cycle(eng) * cycles
 
@@ -266,11 +322,8 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     with Clocks(local) as clk:
-        total_ms, _ = time_steps(torch, eng, args.steps, args.warmup, flush, cycles)
-        torch.cuda.synchronize()
-        _, prof_ms = time_steps(torch, peng, args.steps, args.warmup, flush, cycles)
+        total_ms, prof_ms = time_steps(torch, eng, args.steps, args.warmup, flush, cycles)
     torch.cuda.synchronize()
-    peng.close()
     cfg = eng.config()  # the kernel the first run's tuners kept
     if ws > 1:
         total_ms = max_over_ranks(dist, total_ms, "cuda")
@@ -306,6 +359,10 @@ def run_ours(args):
     bpa = B_PER_ATTEMPT_FP32 if w["precision"] == 1 else B_PER_ATTEMPT_FP64
     achieved = attempts_per_step * bpa / (sweep_ms_avg * 1e-3) / 1e9 if sweep_ms_avg > 0 else 0.0
 
+    prec = None
+    if w["precision"] == 1 and not args.headline_only and not args.nconf:
+        prec = precision_report(jc, eng, w, local, 100, 300)
+
     # FP64 plain form on the L=24, 16-replica PT configuration (the 10x target's denominator)
     fp64 = time_workload(torch, jc, WORKLOADS["plain_fp64_L24_1x16"], local, flush,
                          max(4, args.steps // 4))
@@ -313,27 +370,26 @@ def run_ours(args):
     if not args.headline_only:
         extra = secondary_workloads(torch, jc, local, flush, max(5, args.steps // 10))
 
-    cpu = cpu_baseline() if (rank == 0 and not args.no_cpu) else None
+    cpu = cpu_baseline(w) if (rank == 0 and not args.no_cpu) else None
     clocks = clk.summary()
-    g0 = w["groups"][0]
+    config = workload_config(wname, w, ws)
+    config["attempts_per_step"] = attempts_per_step * ws
+    config["l2"] = "flushed before each step"
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if w["precision"] == 1 else "f64",
         "data": "synthetic (corr_rand_3d disorder from seeds IRINIT+k, HOT starts)",
-        "config": {"workload": wname, "L": g0[0], "H": g0[0], "nconf_per_gpu": nconf,
-                   "nreplica": g0[2], "ptswapever": eng.ptswapever, "T": [8.0, 11.5],
-                   "phi": 2.0, "xi": 3.0,
-                   "lattices_per_gpu": sum(n * r for _, n, r in w["groups"]),
-                   "attempts_per_step": attempts_per_step * ws, "l2": "flushed before each step",
-                   "block_threads": cfg["block_threads"], "sites_per_thread": cfg["sites_per_thread"],
-                   "smem_bytes": cfg["smem_bytes"], "parallelism": f"confs x{ws}"},
+        "config": config,
+        "kernel": {"block_threads": cfg["block_threads"],
+                   "sites_per_thread": cfg["sites_per_thread"], "smem_bytes": cfg["smem_bytes"]},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
                      "unit": "GB/s", "frac": round(achieved / hbm, 4),
                      "traffic": None if args.nconf else TRAFFIC.get(wname),
                      "peak_source": peak_src, "bytes_per_attempt": bpa,
-                     "sweep_kernel_ms": round(sweep_ms_avg, 4)},
+                     "sweep_kernel_ms": round(sweep_ms_avg, 4),
+                     "binding_limit": "instruction issue (shared-memory resident lattices)"},
         "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "fp64_plain": dict(fp64, workload="plain_fp64_L24_1x16",
@@ -341,6 +397,10 @@ def run_ours(args):
         "gpu_launches": 2 * args.steps,
         "clocks": clocks,
     }
+    if not args.nconf and wname in NCU_ISSUE:
+        line["roofline"].update(NCU_ISSUE[wname])
+    if prec is not None:
+        line["precision"] = prec
     if extra is not None:
         line["workloads"] = extra
     if cpu is not None:
@@ -352,53 +412,83 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def cpu_baseline(nthreads=None, ncycles=1):
-    """The oracle's restatement of the reference PT cycle (sequential site order, KISS, FP64,
-    neighbour tables), one ladder per host thread, on a bounded sample of the workload."""
+def reference_models(w, irinit=1):
+    """One oracle Model per configuration of the workload, its disorder from the oracle's numpy
+    restatement of corr_rand_3d (seed irinit + k, PHI=2, XI=3) and its vacancies from the
+    oracle's Setup_vacancies: nothing of the engine's library is loaded."""
+    from oracle import corr3d
     from oracle import oracle as O
-    import j1j2cuda as jc
 
-    nthreads = nthreads or os.cpu_count() or 1
-    L, nrep = 32, 32
-    M = O.Model(L, L, jc.disorder(L, L, 1))
-    betas = 1.0 / O.ladder(nrep, 8.0, 11.5)
-    secs = M.bench_pt(nthreads, betas, 5, ncycles)
-    attempts = nthreads * nrep * 5 * ncycles * L ** 3
-    return {"value": round(attempts / secs / 1e9, 5), "unit": UNIT, "cores": nthreads,
+    models, k = [], 0
+    for L, n, _ in w["groups"]:
+        for _ in range(n):
+            seed = irinit + k
+            p = corr3d.make_corr_rand_3d(L, L, L, 3.0, seed, True, 2.0).reshape(-1)
+            occu = O.setup_vacancies(seed, L, L, w["vacancies"])[0] if w.get("vacancies") else None
+            models.append(O.Model(L, L, p, occu))
+            k += 1
+    return models
+
+
+def reference_steps(w, nthreads, steps, warmup=0):
+    """Seconds of each of `steps` steps (after `warmup` untimed ones) of the reference CPU path on
+    the workload (one PT cycle of every ladder per step; ladders round-robin over nthreads
+    threads) and the attempts per step."""
+    from oracle import oracle as O
+
+    if len(w["groups"]) != 1:
+        raise ValueError("the CPU path is timed on single-shape workloads")
+    L, n, nrep = w["groups"][0]
+    models = reference_models(w)
+    betas = 1.0 / O.ladder(nrep, 8.0, 11.5) if "T" not in w else np.full(nrep, 1.0 / w["T"])
+    ptswapever = w.get("ptswapever", 5)
+    cycles = w.get("cycles_per_step", 1)
+    for _ in range(warmup):
+        O.bench_pt_multi(models, nthreads, betas, ptswapever, cycles)
+    secs = [O.bench_pt_multi(models, nthreads, betas, ptswapever, cycles) for _ in range(steps)]
+    attempts = sum(int(m.N - m.nimp) for m in models) * nrep * ptswapever * cycles
+    return secs, attempts
+
+
+def cpu_baseline(w):
+    """The oracle's restatement of the reference PT cycle (sequential site order, KISS, FP64,
+    neighbour tables) on all host threads: two whole PT cycles of the workload (every ladder),
+    the faster one reported."""
+    nthreads = os.cpu_count() or 1
+    secs, attempts = reference_steps(w, nthreads, 2)
+    best = min(secs)
+    return {"value": round(attempts / best / 1e9, 5), "unit": UNIT, "cores": nthreads,
             "kind": "port",
-            "sample": f"{nthreads} independent L=32 ladders x 32 replicas x {ncycles} PT cycle(s) "
-                      f"of 5 sweeps, one ladder per thread ({attempts} attempts, {secs:.2f} s)"}
+            "sample": f"the whole workload, one PT cycle of all {sum(n for _, n, _ in w['groups'])}"
+                      f" ladders ({attempts} attempts) in {best:.2f} s, ladders round-robin over "
+                      f"{nthreads} threads; Fortran toolchain absent"}
 
 
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    from oracle import oracle as O  # the reference's CPU path (restated; Fortran not buildable)
-    import j1j2cuda as jc
-
+    w = WORKLOADS[args.workload]
     nthreads = os.cpu_count() or 1
-    L, nrep = 32, 32
-    M = O.Model(L, L, jc.disorder(L, L, 1))
-    betas = 1.0 / O.ladder(nrep, 8.0, 11.5)
-    for _ in range(args.warmup):
-        M.bench_pt(nthreads, betas, 5, 1)
-    secs = 0.0
-    for _ in range(args.steps):
-        secs += M.bench_pt(nthreads, betas, 5, 1)
-    attempts = nthreads * nrep * 5 * L ** 3 * args.steps
-    value = attempts / secs / 1e9
+    secs, attempts = reference_steps(w, nthreads, args.steps, args.warmup)
+    total = sum(secs)
+    value = attempts * args.steps / total / 1e9
+    config = workload_config(args.workload, w, ws)
+    config["attempts_per_step"] = attempts
+    config["l2"] = "flushed before each step"
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": UNIT,
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(secs * 1e3 / args.steps, 2), "higher_is_better": True,
+            "ms_per_step": round(total * 1e3 / args.steps, 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (corr_rand_3d disorder seed 1, HOT starts)",
-            "config": {"workload": args.workload, "L": L, "nreplica": nrep, "ptswapever": 5,
-                       "ladders_per_step": nthreads, "threads": nthreads},
+            "data": "synthetic (corr_rand_3d disorder from seeds IRINIT+k, HOT starts)",
+            "config": config,
             "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": nthreads,
                              "kind": "port",
-                             "sample": f"{nthreads} L=32 ladders x 32 replicas, 1 PT cycle per "
-                                       "step, one ladder per thread (Fortran toolchain absent)"},
+                             "sample": f"every step one whole PT cycle of the workload (all "
+                                       f"ladders, {attempts} attempts), ladders round-robin over "
+                                       f"{nthreads} threads; the reference's sequential site "
+                                       "order, KISS stream and FP64 arithmetic restated in C "
+                                       "(Fortran toolchain absent)"},
             "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

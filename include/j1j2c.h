@@ -213,6 +213,14 @@ int j1j2c_metro_sweep_fp64(void *ctx, int32_t conf, int32_t rep, double beta,
  * Replaces the Wolff update named in the reference's header (J:7), which it never implements. */
 int j1j2c_wolff(void *ctx, int64_t *cluster_sizes);
 
+/* Attempts per bond that the union-find labelling forms of the Wolff update (J1J2C_FLAG_NO_FIXED,
+ * J1J2C_FLAG_GENERIC) make to merge two clusters before giving up (default 2^20, tries >= 0).
+ * A labelling that gives up flips a cluster that may be incomplete, and the call that ran it
+ * (j1j2c_wolff, or j1j2c_run with J1J2C_FLAG_WOLFF) returns J1J2C_ETIMEOUT; the error is then
+ * cleared and the context stays usable.  For tests of that path (0 makes every activated bond
+ * give up); no reference counterpart (the reference stops on errors, J:443-444). */
+int j1j2c_set_retry_budget(void *ctx, int32_t tries);
+
 /* Flipped-cluster sizes of the last Wolff update of one conf (NREPLICA; conf < 0: all). */
 int j1j2c_get_cluster_sizes(void *ctx, int32_t conf, int64_t *out);
 
@@ -376,12 +384,21 @@ int j1j2c_enumerate_exact(int32_t L, int32_t H, double J1h, double J1v, double J
  * held by every GPU that loads the library until exit), enough for any lattice of <= 32 sites.
  * Larger requests (more than 32 sites or 4 betas) return J1J2C_EINVAL.  The first call on a
  * device looks the array's device address up (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  Calls share the array: calls that overlap on
- * the GPU race.  Arguments and output as j1j2c_enumerate_exact.  No counterpart in the reference. */
+ * make that first call before any stream capture.  The address is kept for the life of the
+ * process, so a cudaDeviceReset between calls is not supported.  Calls share the array: calls
+ * that overlap on the GPU race.  Arguments and output as j1j2c_enumerate_exact.  No counterpart
+ * in the reference. */
 int j1j2c_enumerate_exact_noalloc(int32_t L, int32_t H, double J1h, double J1v, double J2,
                                   double J3, const double *p, const int8_t *occu,
                                   const int8_t *jh, const int8_t *jv, int32_t nbeta,
                                   const double *beta, double *out);
+
+/* Failure injection for tests of the error paths (process-wide, one shot): kind 1 fails the next
+ * device allocation of an engine context as out of memory (J1J2C_ENOMEM from the call that made
+ * it), kind 2 the next PT-cycle launch of j1j2c_run (J1J2C_ECUDA); 0 clears.  The failure is
+ * reported without calling CUDA, so the device and every context stay usable.  No reference
+ * counterpart (the reference stops on errors: MPI_ABORT / stop, J:443-444, J:841-925). */
+int j1j2c_inject_fault(int32_t kind);
 
 /* Library version string. */
 const char *j1j2c_version(void);

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <limits>
 #include <map>
 #include <mutex>
@@ -82,6 +83,7 @@ struct Ctx {
     int* d_labels = nullptr;        // Wolff union-find labels / cluster list, one int per site
     long long* d_csize = nullptr;   // Wolff cluster size of the last update, per replica
     int* d_err = nullptr;           // device error word (union-find retry overflow)
+    int uf_tries = 1 << 20;         // union-find attempts per bond (j1j2c_set_retry_budget)
     long long lab_ints = 0;
     bool wolff = false;
 
@@ -146,10 +148,34 @@ int cuda_fail(Ctx* c, cudaError_t e, const char* what)
         if (e_ != cudaSuccess) return cuda_fail((c), e_, #call); \
     } while (0)
 
+// j1j2c_inject_fault: a one-shot failure of the next device allocation (1) or the next PT-cycle
+// launch (2) that any context of the process makes; the failure is reported as CUDA would report
+// it, without calling CUDA, so the device and its context are untouched
+std::atomic<int> g_inject{0};
+
+bool take_injected(int kind)
+{
+    int k = kind;
+    return g_inject.load() == kind && g_inject.compare_exchange_strong(k, 0);
+}
+
+// every device allocation of the engine comes through here
+cudaError_t dev_malloc(void** p, size_t bytes)
+{
+    if (take_injected(1)) return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, bytes);
+}
+
+template <class T>
+cudaError_t dev_malloc(T** p, size_t bytes)
+{
+    return dev_malloc(reinterpret_cast<void**>(p), bytes);
+}
+
 template <class T>
 cudaError_t dalloc(T** p, size_t n)
 {
-    return cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T) + 16);
+    return dev_malloc(reinterpret_cast<void**>(p), n * sizeof(T) + 16);
 }
 
 void free_graphs(Ctx* c)
@@ -209,6 +235,15 @@ int cluster_site_threads(const Group& grp, int cs)
     return nt > 512 ? 512 : nt;
 }
 
+// J2 and J3 are integers with |J| <= 8 in FP32, as the FP32 shape-specialised kernels need (their
+// first two field terms are then formed exactly in integer arithmetic)
+bool int_couplings(const Ctx* c)
+{
+    const float j2 = (float)c->P.J2, j3 = (float)c->P.J3;
+    return std::fabs(j2) <= 8.0f && std::fabs(j3) <= 8.0f && j2 == std::nearbyint(j2) &&
+           j3 == std::nearbyint(j3);
+}
+
 // CTA size of the shape-specialised kernel for a group whose lattices stay in HBM (0: the
 // generic global-memory kernel).  Like the shared-memory ones it counts no flips and handles no
 // bond dilution; the test flags GENERIC and NO_FIXED pin the generic kernel.
@@ -216,7 +251,7 @@ int hbm_fixed_threads(const Ctx* c, const Group& grp, bool fp64)
 {
     if ((c->P.flags & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED)) || c->diag.flip_counts)
         return 0;
-    return fixed_hbm_threads(fp64, grp.g.L, grp.g.H, c->masks);
+    return fixed_hbm_threads(fp64, grp.g.L, grp.g.H, c->masks, int_couplings(c));
 }
 
 // Kernel shape for a group: the shape-specialised kernel when one exists for (precision, L, H)
@@ -253,7 +288,8 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
     if (!(fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_GLOBAL)) &&
         !c->diag.flip_counts) {
         FixedChoice fc[16];
-        const int n = fixed_candidates(fp64, grp.g.L, grp.g.H, c->masks, c->vac, fc, 16);
+        const int n =
+            fixed_candidates(fp64, grp.g.L, grp.g.H, c->masks, c->vac, int_couplings(c), fc, 16);
         // the first per-lattice form (or the block_threads one); the streaming form when the
         // test flag asks for it
         const bool stream = (fl & J1J2C_FLAG_STREAM) != 0;
@@ -345,15 +381,27 @@ SweepArgs group_args(Ctx* c, const Group& grp)
     a.J1vf = (float)c->P.J1v;
     a.J2f = (float)c->P.J2;
     a.J3f = (float)c->P.J3;
+    if (int_couplings(c)) {
+        a.J2i = (int)a.J2f;
+        a.J3i = (int)a.J3f;
+        const int bias = 4 * std::abs(a.J3i) + 8 * std::abs(a.J2i);
+        a.ij_bias = 0x01010101u * (uint32_t)bias;
+        a.ij_off = 8388608.0f + (float)(bias + 2 * a.J3i + 4 * a.J2i);
+    }
     a.nrep = grp.nrep;
     a.nsweeps = c->P.ptswapever;
     a.ptswapever = c->P.ptswapever;
     a.seed = c->P.seed;
     a.conf_base = c->P.conf_base + (uint32_t)grp.conf0;
+    for (int r = 0; r < 10; ++r) {
+        a.rk0[r] = a.seed + (uint32_t)r * 0x9E3779B9u;
+        a.rk1[r] = a.conf_base + (uint32_t)r * 0xBB67AE85u;
+    }
     a.lat0 = 0;
     a.use_override = 0;
     a.flips = c->d_flips ? c->d_flips + grp.spin_off : nullptr;
     a.err = c->d_err;
+    a.uf_tries = c->uf_tries;
     return a;
 }
 
@@ -669,8 +717,8 @@ int time_variant(Ctx* c, Group& grp, const SweepVariant& v, int nthreads, size_t
     uint8_t* tmp = nullptr;
     LatObs* tobs = nullptr;
     const size_t bytes = (size_t)nlat * grp.lat_stride;
-    CK(c, cudaMalloc(&tmp, bytes));
-    if (cudaMalloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess) {
+    CK(c, dev_malloc(&tmp, bytes));
+    if (dev_malloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess) {
         cudaFree(tmp);
         return fail(c, J1J2C_ENOMEM, "autotuner scratch");
     }
@@ -951,7 +999,7 @@ int tune_wolff(Ctx* c, Group& grp)
     const int nlat = grp.nlat();
     uint8_t* tmp = nullptr;
     const size_t bytes = (size_t)nlat * grp.lat_stride;
-    CK(c, cudaMalloc(&tmp, bytes));
+    CK(c, dev_malloc(&tmp, bytes));
     cudaError_t e =
         cudaMemcpyAsync(tmp, c->d_spins + grp.spin_off, bytes, cudaMemcpyDeviceToDevice, c->own);
     SweepArgs a = group_args(c, grp);
@@ -1035,8 +1083,8 @@ int tune_split(Ctx* c, Group& grp)
     uint8_t* tmp = nullptr;
     LatObs* tobs = nullptr;
     const size_t bytes = (size_t)nlat * grp.lat_stride;
-    CK(c, cudaMalloc(&tmp, bytes));
-    if (cudaMalloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess) {
+    CK(c, dev_malloc(&tmp, bytes));
+    if (dev_malloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess) {
         cudaFree(tmp);
         return fail(c, J1J2C_ENOMEM, "autotuner scratch");
     }
@@ -1123,7 +1171,8 @@ int autotune(Ctx* c, Group& grp)
     if (grp.block_threads > 0 || (c->P.flags & J1J2C_FLAG_STREAM)) return J1J2C_OK;
     if (grp.var.fixed_nt == 0) return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
     FixedChoice fc[16];
-    const int n = fixed_candidates(grp.var.fp64, grp.g.L, grp.g.H, c->masks, c->vac, fc, 16);
+    const int n = fixed_candidates(grp.var.fp64, grp.g.L, grp.g.H, c->masks, c->vac,
+                                   int_couplings(c), fc, 16);
     if (n <= 1) return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
     const int nlat = grp.nlat();
     const auto key = std::make_tuple(c->P.device, grp.var.fp64, grp.g.L, grp.g.H, nlat, c->vac);
@@ -1139,8 +1188,8 @@ int autotune(Ctx* c, Group& grp)
         uint8_t* tmp = nullptr;
         LatObs* tobs = nullptr;
         const size_t bytes = (size_t)nlat * grp.lat_stride;
-        CK(c, cudaMalloc(&tmp, bytes));
-        if (cudaMalloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess) {
+        CK(c, dev_malloc(&tmp, bytes));
+        if (dev_malloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess) {
             cudaFree(tmp);
             return fail(c, J1J2C_ENOMEM, "autotuner scratch");
         }
@@ -1806,6 +1855,16 @@ int drain_profile(Ctx* c)
     return J1J2C_OK;
 }
 
+// Reads the device error word and clears it (each give-up is reported once; the context stays
+// usable).  Called after the stream has drained.
+int take_device_error(Ctx* c, int& herr)
+{
+    herr = 0;
+    CK(c, cudaMemcpy(&herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
+    if (herr) CK(c, cudaMemset(c->d_err, 0, sizeof(int)));
+    return J1J2C_OK;
+}
+
 int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_phase)
 {
     if (!ctx) return J1J2C_EINVAL;
@@ -1831,6 +1890,8 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
         if (rc != J1J2C_OK) return rc;
     }
     for (int k = 0; k < ncycles; ++k) {
+        if (take_injected(2))
+            return cuda_fail(c, cudaErrorLaunchFailure, "PT-cycle launch (injected failure)");
         cudaEvent_t e0 = c->ev0, e1 = c->ev1;
         if (c->profile) {
             if (c->prof_pending == kProfPool) {
@@ -1861,7 +1922,8 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
     for (const Group& grp : c->G) bounded = bounded || grp.var.stream;
     if (bounded) {
         int herr = 0;
-        CK(c, cudaMemcpy(&herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
+        const int rc = take_device_error(c, herr);
+        if (rc != J1J2C_OK) return rc;
         if (herr)
             return fail(c, J1J2C_ETIMEOUT,
                         "a bounded device wait gave up (Wolff union-find retries or a bulk-copy "
@@ -1884,8 +1946,26 @@ int j1j2c_wolff(void* ctx, int64_t* cluster_sizes)
                               cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaStreamSynchronize(c->st));
     int herr = 0;
-    CK(c, cudaMemcpy(&herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
+    const int rc = take_device_error(c, herr);
+    if (rc != J1J2C_OK) return rc;
     if (herr) return fail(c, J1J2C_ETIMEOUT, "Wolff union-find exceeded its retry budget");
+    return J1J2C_OK;
+}
+
+int j1j2c_inject_fault(int32_t kind)
+{
+    if (kind < 0 || kind > 2) return J1J2C_EINVAL;
+    g_inject.store(kind);
+    return J1J2C_OK;
+}
+
+int j1j2c_set_retry_budget(void* ctx, int32_t tries)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (tries < 0) return fail(c, J1J2C_EINVAL, "the retry budget must be >= 0");
+    c->uf_tries = tries;
+    free_graphs(c);  // captured graphs hold the old budget in their kernel arguments
     return J1J2C_OK;
 }
 
@@ -2121,7 +2201,7 @@ int j1j2c_enumerate_exact(int32_t L, int32_t H, double J1h, double J1v, double J
     const int nb = enum_blocks(a);
     const size_t np = (size_t)nb * kEnumBeta * kEnumSums;
     double* d_part = nullptr;  // scratch: one partial-sum record per block
-    cudaError_t e = cudaMalloc(&d_part, np * sizeof(double));
+    cudaError_t e = dev_malloc(&d_part, np * sizeof(double));
     if (e != cudaSuccess) {
         g_create_error = std::string("enumeration scratch: ") + cudaGetErrorString(e);
         return J1J2C_ENOMEM;

@@ -56,6 +56,28 @@ __host__ __device__ __forceinline__ U4 philox4x32_10(uint32_t c0, uint32_t c1, u
     return U4{c0, c1, c2, c3};
 }
 
+// The same generator with its key schedule given: round r uses k0s[r] and k1s[r] + k1add, which
+// equal k0 + r * 0x9E3779B9 and k1 + r * 0xBB67AE85 of philox4x32_10 for k0s[r] = k0 + r *
+// 0x9E3779B9 and k1s[r] + k1add = k1 + r * 0xBB67AE85.  A kernel passes the launch-uniform part of
+// the schedule among its parameters, so the rounds XOR a parameter instead of forming the key.
+__device__ __forceinline__ U4 philox4x32_10_rk(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                               const uint32_t (&k0s)[10],
+                                               const uint32_t (&k1s)[10], uint32_t k1add)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+        const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+        const uint32_t n0 = hi1 ^ c1 ^ k0s[r];
+        const uint32_t n2 = hi0 ^ c3 ^ (k1s[r] + k1add);
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+    }
+    return U4{c0, c1, c2, c3};
+}
+
 __host__ __device__ __forceinline__ uint32_t u4_word(const U4& v, int w)
 {
     return w == 0 ? v.x : (w == 1 ? v.y : (w == 2 ? v.z : v.w));

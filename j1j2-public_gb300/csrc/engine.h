@@ -35,10 +35,19 @@ struct SweepArgs {
     unsigned long long* audit;  // [2]: attempts, mismatches (audit mode)
     double J1h, J1v, J2, J3;
     float J1hf, J1vf, J2f, J3f;
+    // integer J2, J3 (|J| <= 8; the FP32 shape-specialised kernels need them): per byte lane,
+    // J3*z + J2*d + ij_bias (z, d the biased byte sums of the inter-layer and diagonal spins) is
+    // J3*Zs + J2*D + ij_off - 2^23, each lane within 0..255
+    int J2i, J3i;
+    uint32_t ij_bias;  // 0x01010101 * (4|J3| + 8|J2|)
+    float ij_off;      // 2^23 + 4|J3| + 8|J2| + 2 J3 + 4 J2
     int nrep;
     int nsweeps;             // sweeps per launch
     int ptswapever;          // sweep counter = cycle*ptswapever (+ sweep within the cycle)
     uint32_t seed, conf_base;
+    // Philox key schedule of the sweep stream: round r of configuration conf uses key words
+    // rk0[r] = seed + r * 0x9E3779B9 and rk1[r] + conf = conf_base + conf + r * 0xBB67AE85
+    uint32_t rk0[10], rk1[10];
     int lat0;                // lattice handled by blockIdx.x == 0
     int use_override;        // 1: beta_override / sweep_override instead of ladder / cycle
     double beta_override;
@@ -46,6 +55,7 @@ struct SweepArgs {
     int* flips;              // accepted flips per site, row (conf * nrep + slot) of lat_stride
                              // ints (nullptr: not counted; generic kernels only)
     int* err;                // set to 1 when a bounded wait of a kernel gave up (or nullptr)
+    int uf_tries;            // union-find attempts per bond before the labelling gives up
     int pdl;                 // host side: the launch may overlap the stream's previous kernel
                              // (programmatic dependent launch; global-memory kernels only)
     int slot0, nslots;       // HBM sweep kernel: temperature slots [slot0, slot0 + nslots) of
@@ -166,7 +176,9 @@ struct FixedChoice {
     bool stage_p, stream;
     int minb;  // resident CTAs per SM the kernel is compiled for
 };
-int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, FixedChoice* out, int cap);
+// int_cpl: J2 and J3 are integers with |J| <= 8 (SweepArgs::J2i, J3i); the FP32 kernels need it
+int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, bool int_cpl, FixedChoice* out,
+                     int cap);
 // nlat lattices from a.lat0 (prepare: only set the kernel's shared-memory limit)
 cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, const FixedChoice& ch, int nlat,
                          size_t smem, cudaStream_t st, bool prepare);
@@ -177,7 +189,7 @@ cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, const FixedCho
 // With rpt = 2 or 4 each thread updates its quad in that many replicas of one configuration
 // (sharing the field loads); the launch falls back to 1 when the range is not whole
 // configurations or rpt does not divide the replica count.
-int fixed_hbm_threads(bool fp64, int L, int H, bool masks);
+int fixed_hbm_threads(bool fp64, int L, int H, bool masks, bool int_cpl);
 cudaError_t launch_fixed_hbm(const SweepArgs& a, bool fp64, int colour, int t, int nlat, int rpt,
                              cudaStream_t st);
 

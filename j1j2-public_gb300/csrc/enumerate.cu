@@ -182,7 +182,9 @@ std::mutex g_scratch_mu;
 double* g_scratch_ptr[kMaxDevices] = {};
 
 // Device address of g_enum_scratch on the current device, looked up once per device.  In host
-// code the symbol is only a host-side stand-in, so the kernel must receive this address.
+// code the symbol is only a host-side stand-in, so the kernel must receive this address.  The
+// address is kept for the life of the process: a cudaDeviceReset between calls (which unloads
+// the module and with it the array) is not supported.
 cudaError_t scratch_address(double** out)
 {
     int dev = 0;
@@ -211,6 +213,7 @@ extern "C" int j1j2c_enumerate_exact_noalloc(int32_t L, int32_t H, double J1h, d
                                              double* out)
 {
     using namespace j1j2;
+    set_global_error("");  // j1j2c_last_error(NULL) reports this call's outcome only
     const int N = L * L * H;
     if (L < 2 || H < 2 || (L & 1) || (H & 1) || N > 32 || !p || !beta || !out || nbeta < 1 ||
         nbeta > kEnumBeta) {

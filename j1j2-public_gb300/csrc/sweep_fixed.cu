@@ -145,34 +145,66 @@ __device__ __forceinline__ QuadData<Real> load_quad(const uint32_t* S32, const R
     return d;
 }
 
+// Byte k of the result is 0xFF when element k of the site pairs (d01: sites 0, 1; d23: sites 2, 3)
+// has its sign bit set, else 0 (prmt with sign replication of each source word's top byte).
+__device__ __forceinline__ uint32_t sign_bytes(f2 d01, f2 d23)
+{
+    uint32_t r;
+    asm("{\n\t.reg .b32 a0, a1, b0, b1, m0, m1;\n\t"
+        "mov.b64 {a0, a1}, %1;\n\t"
+        "mov.b64 {b0, b1}, %2;\n\t"
+        "prmt.b32 m0, a0, a1, 0x00FB;\n\t"
+        "prmt.b32 m1, b0, b1, 0xFB00;\n\t"
+        "lop3.b32 %0, m0, m1, 0x0000FFFF, 0xE4;\n\t}"
+        : "=r"(r)
+        : "l"(d01), "l"(d23));
+    return r;
+}
+
 // Update (or measure) one quad from its loaded operands.  VAC: vacancies may be present (the
 // FP32 acceptance threshold is then scaled by s^2 so that a vacancy never flips).
 // qshift: words between S32 and the lattice's first word (the quad's Philox group is its
-// position in the lattice)
-template <class Real, int LH, int HH, int C, bool MEASURE, bool VAC>
+// position in the lattice); conf: the lattice's configuration within the launch (Philox key word
+// 1 is conf_base + conf).  GSTORE: S32 is in global memory, where the quad's word is written
+// only when a site flips; in shared memory it is always written (cheaper than the test).
+template <class Real, int LH, int HH, int C, bool MEASURE, bool VAC, bool GSTORE = false>
 __device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
                                              const QuadData<Real>& d, uint32_t sweep,
-                                             uint32_t rep, uint32_t k0, uint32_t k1, double beta,
-                                             float kb, Acc& acc, int qshift = 0)
+                                             uint32_t rep, uint32_t conf, double beta, float kb,
+                                             Acc& acc, int qshift = 0)
 {
     using Sh = Shape<LH, HH>;
     constexpr int px = C & 1, py = (C >> 1) & 1;
     constexpr int B0 = C * Sh::CS;
     U4 rnd{0, 0, 0, 0};
-    if constexpr (!MEASURE)
-        rnd = philox4x32_10(rep, sweep, (uint32_t)(B0 + d.self + qshift), kTagSweep, k0, k1);
+    if constexpr (!MEASURE) {
+        const uint32_t grp = (uint32_t)(B0 + d.self + qshift);
+        // shared-memory kernels: round keys from the parameters (fewer integer instructions);
+        // the HBM kernels keep the plain form, which their register budget holds without spills
+        if constexpr (GSTORE)
+            rnd = philox4x32_10(rep, sweep, grp, kTagSweep, a.seed, a.conf_base + conf);
+        else
+            rnd = philox4x32_10_rk(rep, sweep, grp, kTagSweep, a.rk0, a.rk1, conf);
+    }
     uint32_t flipmask = 0;
     if constexpr (sizeof(Real) == 4) {
         // Sites in pairs (0,1), (2,3) with packed FP32x2 arithmetic: every element follows
         // field_fp32's operations and rounding (the -y terms enter as products with the negated
-        // spins, the J1v term as (pi - J1v) * (-sy): the same products, exactly).
+        // spins, the J1v term as (pi - J1v) * (-sy): the same products, exactly).  The FP32
+        // kernels here run only with integer J2, J3 (|J| <= 8; the host checks): the first two
+        // terms, J3*Zs rounded and then fma(J2, D, .), are then an exact small integer, formed
+        // for all four sites at once in integer arithmetic on the byte sums (each byte lane
+        // J3*z + J2*d + bias stays in 0..255, so the word is exact modulo 2^32 lane by lane) and
+        // read out of the bytes like the spins.  (A zero may differ in sign from the
+        // floating-point form's, which no later sum, product or test can see.)
         const uint32_t dsum = d.wdpp + d.wdpm + d.wdmp + d.wdmm;  // bytewise, <= 8
         const uint32_t zsum = d.wzp + d.wzm;                      // bytewise, <= 4
-        const f2 c1 = f2_splat(8388609.0f), c2 = f2_splat(8388610.0f), c4 = f2_splat(8388612.0f);
-        const f2 j3 = f2_splat(a.J3f), j2 = f2_splat(a.J2f), j1h = f2_splat(a.J1hf),
-                 j1v = f2_splat(a.J1vf);
+        const uint32_t cpl = zsum * (uint32_t)a.J3i + dsum * (uint32_t)a.J2i + a.ij_bias;
+        const f2 c1 = f2_splat(8388609.0f), coff = f2_splat(a.ij_off);
+        const f2 j1h = f2_splat(a.J1hf), j1v = f2_splat(a.J1vf);
         int ehi = 0, elo = 0;  // fixed-point energy of the quad, split as in efix32_split
         float nbf = 0.0f;      // nematic sum of the quad (exact small integers)
+        f2 dlt[2];             // u - threshold per site pair: its sign bit is the decision
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int k = 2 * h;
@@ -180,8 +212,6 @@ __device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
             const f2 sxm = f2_sub(byte_pair(d.wxm, k), c1);
             const f2 nsyp = f2_sub(c1, byte_pair(d.wyp, k));   // -s at +y
             const f2 nsym = f2_sub(c1, byte_pair(d.wym, k));   // -s at -y
-            const f2 D = f2_sub(byte_pair(dsum, k), c4);
-            const f2 Zs = f2_sub(byte_pair(zsum, k), c2);
             const f2 si = f2_sub(byte_pair(d.own, k), c1);
             const f2 pi = f2_pack(d.pown[k], d.pown[k + 1]);
             const f2 pxp = px ? f2_pack(d.pxa[k + 1], k + 1 < 3 ? d.pxa[k + 2] : d.pextra)
@@ -191,8 +221,7 @@ __device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
             const f2 pyp = f2_pack(d.pyp[k], d.pyp[k + 1]);
             const f2 pym = f2_pack(d.pym[k], d.pym[k + 1]);
             const f2 sx = f2_add(sxp, sxm), nsy = f2_add(nsyp, nsym);
-            f2 f = f2_mul(j3, Zs);
-            f = f2_fma(j2, D, f);
+            f2 f = f2_sub(byte_pair(cpl, k), coff);  // J3*Zs + J2*D, exact
             f = f2_fma(f2_add(j1h, pi), sx, f);
             f = f2_fma(f2_sub(pi, j1v), nsy, f);
             f = f2_fma(pxp, sxp, f);
@@ -213,7 +242,10 @@ __device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
                 nbf = __fadd_rn(__fadd_rn(nbf, f2_get(nb, 0)), f2_get(nb, 1));
             } else {
                 // Metropolis test u < exp(-beta dE) as 2^(kb s f); with vacancies the threshold
-                // is scaled by s^2, so a vacancy (s = 0) never flips
+                // is scaled by s^2, so a vacancy (s = 0) never flips.  u < thr exactly when
+                // u - thr is negative: the difference of two floats is zero only when they are
+                // equal (+0 then), and u (0 or >= 2^-23) and thr (0 or normal: ex2.approx.ftz)
+                // leave no room for an underflow
                 const f2 arg = f2_mul(f2_splat(kb), sf);
                 f2 thr = f2_pack(ex2_approx(f2_get(arg, 0)), ex2_approx(f2_get(arg, 1)));
                 if constexpr (VAC) thr = f2_mul(thr, f2_mul(si, si));
@@ -221,10 +253,10 @@ __device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
                     f2_pack(__uint_as_float(0x3F800000u | (u4_word(rnd, k) & 0x007FFFFFu)),
                             __uint_as_float(0x3F800000u | (u4_word(rnd, k + 1) & 0x007FFFFFu))),
                     f2_splat(1.0f));
-                if (f2_get(u, 0) < f2_get(thr, 0)) flipmask |= 2u << (8 * k);
-                if (f2_get(u, 1) < f2_get(thr, 1)) flipmask |= 2u << (8 * k + 8);
+                dlt[h] = f2_sub(u, thr);
             }
         }
+        if constexpr (!MEASURE) flipmask = sign_bytes(dlt[0], dlt[1]) & 0x02020202u;
         if constexpr (MEASURE) {
             // magnetisation and stripe sums from the byte sum of the own word (s = b - 1)
             const int mq = (int)((d.own * 0x01010101u) >> 24) - 4;
@@ -276,7 +308,11 @@ __device__ __forceinline__ void compute_quad(const SweepArgs& a, uint32_t* S32,
         }
     }
     if constexpr (!MEASURE) {
-        if (flipmask) S32[B0 + d.self] = d.own ^ flipmask;
+        if constexpr (GSTORE) {
+            if (flipmask) S32[B0 + d.self] = d.own ^ flipmask;
+        } else {
+            S32[B0 + d.self] = d.own ^ flipmask;
+        }
     }
 }
 
@@ -335,8 +371,8 @@ __device__ __forceinline__ QuadOff offsets_for(const OffsetCache<QPT>& oc, int j
 template <class Real, int LH, int HH, int NT, int QPT, int C, bool MEASURE, bool VAC>
 __device__ __forceinline__ void colour_phase(const SweepArgs& a, uint32_t* S32, const Real* P,
                                              const OffsetCache<QPT>& oc, uint32_t sweep,
-                                             uint32_t rep, uint32_t k0, uint32_t k1,
-                                             double beta, float kb, Acc& acc)
+                                             uint32_t rep, uint32_t kconf, double beta,
+                                             float kb, Acc& acc)
 {
     constexpr int NQ = Shape<LH, HH>::CS;
     if constexpr (QPT == 2) {
@@ -345,10 +381,10 @@ __device__ __forceinline__ void colour_phase(const SweepArgs& a, uint32_t* S32, 
         const QuadData<Real> d0 = load_quad<Real, LH, HH, C>(S32, P, oc.off[0]);
         QuadData<Real> d1 = d0;
         if (has1) d1 = load_quad<Real, LH, HH, C>(S32, P, oc.off[1]);
-        compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32, d0, sweep, rep, k0, k1, beta, kb,
+        compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32, d0, sweep, rep, kconf, beta, kb,
                                                     acc);
         if (has1)
-            compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32, d1, sweep, rep, k0, k1, beta,
+            compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32, d1, sweep, rep, kconf, beta,
                                                         kb, acc);
     } else if constexpr (Strided<LH, HH, NT, QPT>::value) {
         constexpr int RS = Strided<LH, HH, NT, QPT>::RS;
@@ -360,7 +396,7 @@ __device__ __forceinline__ void colour_phase(const SweepArgs& a, uint32_t* S32, 
             o.zm = j == 0 ? oc.base.zm : oc.base.self - RS;
             o.zp = j == QPT - 1 ? oc.zp_last - shift : oc.base.self + RS;
             const QuadData<Real> dj = load_quad<Real, LH, HH, C>(S32 + shift, P + 4 * shift, o);
-            compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32 + shift, dj, sweep, rep, k0, k1,
+            compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32 + shift, dj, sweep, rep, kconf,
                                                         beta, kb, acc, shift);
         }
     } else {
@@ -369,7 +405,7 @@ __device__ __forceinline__ void colour_phase(const SweepArgs& a, uint32_t* S32, 
             if (QPT * NT == NQ || (int)threadIdx.x + j * NT < NQ) {
                 const QuadData<Real> dj =
                     load_quad<Real, LH, HH, C>(S32, P, offsets_for<LH, HH, NT, QPT>(oc, j));
-                compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32, dj, sweep, rep, k0, k1,
+                compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32, dj, sweep, rep, kconf,
                                                             beta, kb, acc);
             }
     }
@@ -378,13 +414,13 @@ __device__ __forceinline__ void colour_phase(const SweepArgs& a, uint32_t* S32, 
 template <class Real, int LH, int HH, int NT, int QPT, bool MEASURE, bool VAC>
 __device__ __forceinline__ void all_colours(const SweepArgs& a, uint32_t* S32, const Real* P,
                                             const OffsetCache<QPT>& oc, uint32_t sweep,
-                                            uint32_t rep, uint32_t k0, uint32_t k1, double beta,
+                                            uint32_t rep, uint32_t kconf, double beta,
                                             float kb, Acc& acc)
 {
     // One barrier per colour.  The measurement only reads, but without the barrier the
     // instruction scheduler interleaves all eight read-only phases and runs out of registers.
 #define J1J2_PHASE(C)                                                                        \
-    colour_phase<Real, LH, HH, NT, QPT, C, MEASURE, VAC>(a, S32, P, oc, sweep, rep, k0, k1,  \
+    colour_phase<Real, LH, HH, NT, QPT, C, MEASURE, VAC>(a, S32, P, oc, sweep, rep, kconf,  \
                                                          beta, kb, acc);                     \
     __syncthreads();
     J1J2_PHASE(0)
@@ -431,13 +467,13 @@ __global__ void __launch_bounds__(NT, MINB) sweep_fixed_kernel(SweepArgs a)
         sweep0 = a.ctl[0] * (uint32_t)a.ptswapever;
     }
     const float kb = (float)(-2.0 * beta * 1.4426950408889634);
-    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    const uint32_t kconf = (uint32_t)conf;
     Acc acc{0, 0, 0, 0, 0};
 #pragma unroll 1
     for (int t = 0; t < a.nsweeps; ++t)
         all_colours<Real, LH, HH, NT, QPT, false, VAC>(a, S32, P, off, sweep0 + (uint32_t)t,
-                                                       (uint32_t)rep, k0, k1, beta, kb, acc);
-    all_colours<Real, LH, HH, NT, QPT, true, VAC>(a, S32, P, off, 0u, 0u, 0u, 0u, beta, kb, acc);
+                                                       (uint32_t)rep, kconf, beta, kb, acc);
+    all_colours<Real, LH, HH, NT, QPT, true, VAC>(a, S32, P, off, 0u, 0u, 0u, beta, kb, acc);
     const Acc tot = block_reduce(acc);
     if (threadIdx.x == 0) store_obs(a.obs + lat, tot);
     block_copy16(Sg, S, Sh::NB);
@@ -460,9 +496,13 @@ struct StreamLayout {
     static constexpr uint32_t kChunk = 16384;  // bytes per bulk copy instruction
 };
 
+// Bookkeeping of the bulk loads, kept in shared memory and touched by thread 0 only (the other
+// threads carry no copy of it in registers, where the sweeps need every one)
 struct StreamState {
-    uint32_t ph[3];      // mbarrier phases: spin buffer 0, spin buffer 1, field
-    bool field_pending;  // the field of the current configuration is still arriving
+    uint32_t ph;    // bit b: parity of the phase of barrier b (spin buffer 0, 1, field) to wait for
+    uint32_t pend;  // bit b: a load completing on barrier b was issued and not yet seen complete
+    int field_pending;  // the field of the current configuration is still arriving
+    int fail;           // a bounded wait gave up: the CTA sweeps, stores and loads nothing more
 };
 
 template <class Real, int LH, int HH>
@@ -476,30 +516,50 @@ __device__ __forceinline__ void stream_copy_in(void* dst, const void* src, uint3
                   bytes - o < kChunk ? bytes - o : kChunk, b);
 }
 
-// One lattice of the range from spin buffer BUF (compile-time: constant shared-memory offsets)
+// One lattice of the range from spin buffer BUF (compile-time: constant shared-memory offsets).
+// Thread 0 waits (bounded) for the lattice's spins and, at a configuration change, its field;
+// the barrier after the wait passes the completed copies, or the failure, to every thread.  On a
+// failure the CTA stops before touching the buffer: no sweep, no store and no further load.
+// Returns false once stopped (the same value in every thread: read after a barrier, and written
+// again only by thread 0 before the next step's barrier).
 template <class Real, int LH, int HH, int NT, int QPT, bool VAC, int BUF>
-__device__ __forceinline__ void stream_step(const SweepArgs& a, unsigned char* smem, uint64_t* bar,
-                                            const OffsetCache<QPT>& off, int l, int last,
-                                            StreamState& st)
+__device__ __forceinline__ bool stream_step(const SweepArgs& a, unsigned char* smem, uint64_t* bar,
+                                            StreamState* st, const OffsetCache<QPT>& off, int l,
+                                            int last)
 {
     using Lay = StreamLayout<Real, LH, HH>;
     const int tid = (int)threadIdx.x;
     Real* Ps = reinterpret_cast<Real*>(smem);
     uint32_t* S32 = reinterpret_cast<uint32_t*>(smem + Lay::PB + BUF * Lay::SB);
-    mbar_wait(&bar[BUF], st.ph[BUF], a.err);
-    st.ph[BUF] ^= 1u;
-    if (st.field_pending) {
-        mbar_wait(&bar[2], st.ph[2], a.err);
-        st.ph[2] ^= 1u;
-        st.field_pending = false;
-    }
     const int lat = a.lat0 + l;
-    if (tid == 0 && l + 1 < last) {  // next lattice into the other buffer
-        bulk_wait_read();            // its previous lattice has left
-        stream_copy_in<Real, LH, HH>(smem + Lay::PB + (BUF ^ 1) * Lay::SB,
-                                     a.spins + (long long)(lat + 1) * a.lat_stride, Lay::SB,
-                                     &bar[BUF ^ 1]);
+    if (tid == 0) {
+        uint32_t ph = st->ph, pend = st->pend;
+        bool ok = mbar_wait(&bar[BUF], (ph >> BUF) & 1u, a.err);
+        if (ok) {
+            ph ^= 1u << BUF;
+            pend &= ~(1u << BUF);
+            if (st->field_pending) {
+                ok = mbar_wait(&bar[2], (ph >> 2) & 1u, a.err);
+                if (ok) {
+                    ph ^= 4u;
+                    pend &= ~4u;
+                    st->field_pending = 0;
+                }
+            }
+        }
+        if (ok && l + 1 < last) {  // next lattice into the other buffer
+            bulk_wait_read();      // its previous lattice has left
+            stream_copy_in<Real, LH, HH>(smem + Lay::PB + (BUF ^ 1) * Lay::SB,
+                                         a.spins + (long long)(lat + 1) * a.lat_stride, Lay::SB,
+                                         &bar[BUF ^ 1]);
+            pend |= 1u << (BUF ^ 1);
+        }
+        st->ph = ph;
+        st->pend = pend;
+        if (!ok) st->fail = 1;
     }
+    __syncthreads();
+    if (st->fail) return false;
     const int conf = lat / a.nrep;
     const int rep = lat - conf * a.nrep;
     double beta;
@@ -512,25 +572,27 @@ __device__ __forceinline__ void stream_step(const SweepArgs& a, unsigned char* s
         sweep0 = a.ctl[0] * (uint32_t)a.ptswapever;
     }
     const float kb = (float)(-2.0 * beta * 1.4426950408889634);
-    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    const uint32_t kconf = (uint32_t)conf;
     Acc acc{0, 0, 0, 0, 0};
 #pragma unroll 1
     for (int t = 0; t < a.nsweeps; ++t)
         all_colours<Real, LH, HH, NT, QPT, false, VAC>(a, S32, Ps, off, sweep0 + (uint32_t)t,
-                                                       (uint32_t)rep, k0, k1, beta, kb, acc);
-    all_colours<Real, LH, HH, NT, QPT, true, VAC>(a, S32, Ps, off, 0u, 0u, 0u, 0u, beta, kb, acc);
+                                                       (uint32_t)rep, kconf, beta, kb, acc);
+    all_colours<Real, LH, HH, NT, QPT, true, VAC>(a, S32, Ps, off, 0u, 0u, 0u, beta, kb, acc);
     const Acc tot = block_reduce(acc);
     fence_async_shared();  // the sweeps' shared-memory accesses, before the bulk copies
     __syncthreads();
-    const bool next_conf = l + 1 < last && (lat + 1) / a.nrep != conf;
     if (tid == 0) {
         store_obs(a.obs + lat, tot);
         bulk_store(a.spins + (long long)lat * a.lat_stride, S32, Lay::SB);
         bulk_commit();
-        if (next_conf)  // the next configuration's field
+        if (l + 1 < last && (lat + 1) / a.nrep != conf) {  // the next configuration's field
             stream_copy_in<Real, LH, HH>(Ps, field_base<Real>(a, conf + 1), Lay::PB, &bar[2]);
+            st->field_pending = 1;
+            st->pend |= 4u;
+        }
     }
-    if (next_conf) st.field_pending = true;
+    return true;
 }
 
 template <class Real, int LH, int HH, int NT, int MINB, bool VAC>
@@ -541,33 +603,42 @@ __global__ void __launch_bounds__(NT, MINB) sweep_stream_kernel(SweepArgs a, int
     constexpr int QPT = (Sh::CS + NT - 1) / NT;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar[3];  // spin buffer 0, spin buffer 1, field
+    __shared__ StreamState st;
     const int tid = (int)threadIdx.x;
     const int first = (int)(((long long)blockIdx.x * nlat) / gridDim.x);
     const int last = (int)(((long long)(blockIdx.x + 1) * nlat) / gridDim.x);
+    if (first >= last) return;  // uniform over the CTA: no thread waits at a barrier below
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         mbar_init(&bar[2], 1);
         mbar_init_fence();
-    }
-    __syncthreads();
-    if (first >= last) return;
-    if (tid == 0) {
         const int lat = a.lat0 + first;
         stream_copy_in<Real, LH, HH>(smem + Lay::PB, a.spins + (long long)lat * a.lat_stride,
                                      Lay::SB, &bar[0]);
         stream_copy_in<Real, LH, HH>(smem, field_base<Real>(a, lat / a.nrep), Lay::PB, &bar[2]);
+        st = StreamState{0u, 1u | 4u, 1, 0};
     }
     OffsetCache<QPT> off;
     fill_offsets<LH, HH, NT, QPT>(off, tid);
-    StreamState st{{0u, 0u, 0u}, true};
+    // (the first step's barrier publishes thread 0's initialisation)
 #pragma unroll 1
     for (int l = first; l < last; l += 2) {
-        stream_step<Real, LH, HH, NT, QPT, VAC, 0>(a, smem, bar, off, l, last, st);
-        if (l + 1 < last)
-            stream_step<Real, LH, HH, NT, QPT, VAC, 1>(a, smem, bar, off, l + 1, last, st);
+        if (!stream_step<Real, LH, HH, NT, QPT, VAC, 0>(a, smem, bar, &st, off, l, last)) break;
+        if (l + 1 < last &&
+            !stream_step<Real, LH, HH, NT, QPT, VAC, 1>(a, smem, bar, &st, off, l + 1, last))
+            break;
     }
-    if (tid == 0) bulk_wait_all();  // every lattice has left before the CTA ends
+    if (tid == 0) {
+        // A wait gave up (err is set; the rest of the range was not swept): before the CTA's
+        // shared memory is released, wait once more, again bounded, for every load that thread 0
+        // issued and has not seen complete.  Outside the lattice loop, so it adds no register
+        // pressure there.
+        if (st.fail)
+            for (int b = 0; b < 3; ++b)
+                if (st.pend & (1u << b)) mbar_wait(&bar[b], (st.ph >> b) & 1u, a.err);
+        bulk_wait_all();  // every stored lattice has left before the CTA ends
+    }
 }
 
 template <class Real, int LH, int HH, int NT, int MINB, bool STAGE_P, bool VAC>
@@ -652,8 +723,7 @@ bool usable(const FixedEntry& e, bool fp64, int L, int H, bool vac)
 // once and shared, the spin operands of every replica are loaded before any is updated.
 template <class Real, int LH, int HH, int C, int RPT, bool VAC>
 __device__ __forceinline__ void hbm_phase(const SweepArgs& a, const Real* P, const QuadOff& o,
-                                          int conf, const int* rep, uint32_t sweep,
-                                          uint32_t k0, uint32_t k1)
+                                          int conf, const int* rep, uint32_t sweep)
 {
     QuadData<Real> d[RPT];
     load_quad_field<Real, LH, HH, C>(P, o, d[0]);
@@ -672,11 +742,11 @@ __device__ __forceinline__ void hbm_phase(const SweepArgs& a, const Real* P, con
                                 : a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep[r]]];
         const float kb = (float)(-2.0 * beta * 1.4426950408889634);
         Acc none{0, 0, 0, 0, 0};
-        compute_quad<Real, LH, HH, C, false, VAC>(
+        compute_quad<Real, LH, HH, C, false, VAC, true>(
             a,
             reinterpret_cast<uint32_t*>(a.spins +
                                         (long long)(conf * a.nrep + rep[r]) * a.lat_stride),
-            d[r], sweep, (uint32_t)rep[r], k0, k1, beta, kb, none);
+            d[r], sweep, (uint32_t)rep[r], (uint32_t)conf, beta, kb, none);
     }
 }
 
@@ -709,12 +779,11 @@ __global__ void __launch_bounds__(NT, sizeof(Real) == 8 ? 1 : RPT == 4 ? 768 / N
     const Real* P = field_base<Real>(a, conf);
     const uint32_t sweep = (a.use_override ? a.sweep_override
                                            : a.ctl[0] * (uint32_t)a.ptswapever) + (uint32_t)t;
-    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
     const QuadOff o = quad_offsets<LH, HH>(q);
     switch (colour) {
 #define J1J2_HBM_PHASE(C)                                                                     \
     case C:                                                                                   \
-        hbm_phase<Real, LH, HH, C, RPT, VAC>(a, P, o, conf, rep, sweep, k0, k1);              \
+        hbm_phase<Real, LH, HH, C, RPT, VAC>(a, P, o, conf, rep, sweep);                      \
         break;
         J1J2_HBM_PHASE(0)
         J1J2_HBM_PHASE(1)
@@ -761,8 +830,8 @@ __global__ void __launch_bounds__(NT) measure_fixed_hbm_kernel(SweepArgs a)
                 o, d[r]);                                                                       \
         }                                                                                       \
         _Pragma("unroll") for (int r = 0; r < RPT; ++r)                                         \
-            compute_quad<Real, LH, HH, C, true, VAC>(a, nullptr, d[r], 0u, 0u, 0u, 0u, 0.0,     \
-                                                     0.0f, acc[r]);                             \
+            compute_quad<Real, LH, HH, C, true, VAC>(a, nullptr, d[r], 0u, 0u, 0u, 0.0, 0.0f,      \
+                                                     acc[r]);                                   \
         break;                                                                                  \
     }
             J1J2_HBM_MEASURE(0)
@@ -851,9 +920,10 @@ const HbmEntry kHbm[] = {
 
 }  // namespace
 
-int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, FixedChoice* out, int cap)
+int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, bool int_cpl, FixedChoice* out,
+                     int cap)
 {
-    if (masks) return 0;
+    if (masks || (!fp64 && !int_cpl)) return 0;
     int n = 0;
     for (const auto& e : kFixed)
         if (usable(e, fp64, L, H, vac) && n < cap)
@@ -871,9 +941,9 @@ cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, const FixedCho
     return cudaErrorInvalidValue;
 }
 
-int fixed_hbm_threads(bool fp64, int L, int H, bool masks)
+int fixed_hbm_threads(bool fp64, int L, int H, bool masks, bool int_cpl)
 {
-    if (masks) return 0;
+    if (masks || (!fp64 && !int_cpl)) return 0;
     for (const auto& e : kHbm)
         if (e.fp64 == fp64 && e.L == L && e.H == H) return e.nt;
     return 0;

@@ -78,10 +78,11 @@ __device__ __forceinline__ int find_root(volatile int* lab, int x)
     return x;
 }
 
-// Union of the components of a and b; false if the retry budget ran out (set as an error).
-__device__ __forceinline__ bool unite(volatile int* lab, int a, int b)
+// Union of the components of a and b; false if the retry budget (tries attempts, SweepArgs::
+// uf_tries) ran out (the caller sets the error word).
+__device__ __forceinline__ bool unite(volatile int* lab, int a, int b, int tries)
 {
-    for (int it = 0; it < (1 << 20); ++it) {
+    for (int it = 0; it < tries; ++it) {
         a = find_root(lab, a);
         b = find_root(lab, b);
         if (a == b) return true;
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(256) wolff_bond_kernel(SweepArgs a, int* label
         const uint32_t r =
             b < 4 ? u4_word(inplane, b)
                   : u4_word(philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffZ, k0, k1), X & 3);
-        if (bond_trial<Real>(w, beta, r) && !unite(lab, ci, cj)) atomicExch(err, 1);
+        if (bond_trial<Real>(w, beta, r) && !unite(lab, ci, cj, a.uf_tries)) atomicExch(err, 1);
     }
 }
 
@@ -213,24 +214,6 @@ __device__ __forceinline__ int sfind(volatile uint16_t* lab, int x)
         p = gp;
     }
     return x;
-}
-
-__device__ __forceinline__ bool sunite(volatile uint16_t* lab, int a, int b)
-{
-    for (int it = 0; it < (1 << 20); ++it) {
-        a = sfind(lab, a);
-        b = sfind(lab, b);
-        if (a == b) return true;
-        if (a < b) {
-            const int t = a;
-            a = b;
-            b = t;
-        }
-        if (atomicCAS(const_cast<unsigned short*>(reinterpret_cast<volatile unsigned short*>(lab)) + a,
-                      (unsigned short)a, (unsigned short)b) == (unsigned short)a)
-            return true;
-    }
-    return false;
 }
 
 // Slab geometry: pz planes starting at plane z0 = slab * pz (pz even); the slab holds Zh = pz/2
@@ -484,7 +467,7 @@ __global__ void __launch_bounds__(512, 2)
                         (unsigned short)hi, (unsigned short)lo);
                     if (old == (unsigned short)hi) {
                         st = kFetch;
-                    } else if (++tries >= (1 << 20)) {  // retry budget spent: give up this bond
+                    } else if (++tries >= a.uf_tries) {  // retry budget spent: give up this bond
                         ok = false;
                         st = kFetch;
                     } else {  // hi stopped being a root: find both roots again
@@ -543,7 +526,8 @@ __global__ void __launch_bounds__(256) wolff_boundary_kernel(SweepArgs a, int pz
         if (si == 0 || sj == 0) continue;
         Real wv;
         if (!bond_weight<Real>(a, 4, si, sj, 1, 1, Real(0), Real(0), wv)) continue;
-        if (bond_trial<Real>(wv, beta, u4_word(rr, w)) && !unite(lab, ci, cj)) atomicExch(err, 1);
+        if (bond_trial<Real>(wv, beta, u4_word(rr, w)) && !unite(lab, ci, cj, a.uf_tries))
+            atomicExch(err, 1);
     }
 }
 

@@ -43,7 +43,8 @@ EXPORTS = ("j1j2c_create", "j1j2c_create_multi", "j1j2c_conf_shape", "j1j2c_dest
            "j1j2c_get_flip_counts", "j1j2c_state_size", "j1j2c_save_state", "j1j2c_load_state",
            "j1j2c_get_diagnostics", "j1j2c_get_occupied", "j1j2c_corr_rand_3d_gpu",
            "j1j2c_results_create", "j1j2c_results_add_conf", "j1j2c_results_write",
-           "j1j2c_results_destroy")
+           "j1j2c_results_destroy", "j1j2c_set_retry_budget", "j1j2c_inject_fault",
+           "j1j2c_enumerate_exact_noalloc")
 
 ENUM_FIELDS = ("lnZ", "e", "e2", "absm", "m2", "m4", "abssx", "sx2", "abssy", "sy2", "nbar",
                "nbar2")
@@ -178,6 +179,15 @@ def enumerate_exact(L, H, p, betas, occu=None, jh=None, jv=None, J1h=1.0, J1v=1.
     return out
 
 
+INJECT_NONE, INJECT_ALLOC, INJECT_LAUNCH = 0, 1, 2
+
+
+def inject_fault(kind):
+    """One-shot failure of the next device allocation (INJECT_ALLOC) or PT-cycle launch
+    (INJECT_LAUNCH) of any engine context, reported without touching the device (tests)."""
+    _check(None, lib().j1j2c_inject_fault(C.c_int32(kind)))
+
+
 def disorder(L, H, seed, phi=2.0, xi=3.0, map_uniform=True, gpu=False) -> np.ndarray:
     """Setup_phi_table (J:590-633): p(site) for disorder seed IRINIT + iconf - 1."""
     return corr_rand_3d(L, L, H, xi, seed, map_uniform, phi, gpu).reshape(-1)
@@ -295,6 +305,11 @@ class Engine:
                                               C.c_double(beta), C.c_uint32(sweep_index),
                                               C.c_int32(nsweeps), *[C.byref(o) for o in out]))
         return tuple(o.value for o in out)
+
+    def set_retry_budget(self, tries):
+        """Union-find attempts per bond before the labelling forms of the Wolff update give up
+        (default 2^20; the call then raises ETIMEOUT and the context stays usable)."""
+        self._ck(lib().j1j2c_set_retry_budget(self._ctx, C.c_int32(tries)))
 
     def wolff(self):
         """One Wolff update of every lattice; returns the flipped-cluster sizes per replica."""

@@ -548,60 +548,87 @@ static double now_s(void)
     return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
 }
 
+/* One ladder of the benchmark: spins from KISS HOT starts (seed + replica), observables, the
+ * swap stream after seed + 100000, running sums by slot */
+typedef struct {
+    pt_state P;
+    double *sums;
+    int32_t phase;
+} bench_ladder;
+
+static void bench_ladder_init(bench_ladder *b, const or_lat *g, int32_t nrep, int32_t ptswapever,
+                              const double *beta, int32_t seed)
+{
+    const int32_t N = g->N;
+    pt_state *P = &b->P;
+    P->g = g;
+    P->nrep = nrep;
+    P->ptswapever = ptswapever;
+    P->beta = beta;
+    P->s = (int8_t *)malloc((size_t)N * nrep);
+    P->rat = (int32_t *)malloc(sizeof(int32_t) * nrep);
+    P->tor = (int32_t *)malloc(sizeof(int32_t) * nrep);
+    P->mag = (double *)malloc(sizeof(double) * nrep * 5);
+    P->en = P->mag + nrep;
+    P->sx = P->en + nrep;
+    P->sy = P->sx + nrep;
+    P->nb = P->sy + nrep;
+    P->att = (int64_t *)calloc(nrep, sizeof(int64_t));
+    P->acc = (int64_t *)calloc(nrep, sizeof(int64_t));
+    b->sums = (double *)calloc((size_t)OR_NSUM * nrep, sizeof(double));
+    for (int32_t rep = 0; rep < nrep; rep++) {
+        P->rat[rep] = P->tor[rep] = rep;
+        or_kiss_init(P->kiss, seed + rep);
+        init_spin_array(P->kiss, g->L, g->H, 0, 0, P->s + (size_t)rep * N);
+        double o[4];
+        or_measurement_ref(g, P->s + (size_t)rep * N, o);
+        P->mag[rep] = o[0];
+        P->en[rep] = o[1];
+        P->sx[rep] = o[2];
+        P->sy[rep] = o[3];
+    }
+    or_kiss_init(P->kiss, seed + 100000);
+    b->phase = 1;
+}
+
+/* ncycles measurement-loop cycles (sweeps, swaps, nbar, slot sums: J:1428-1524) */
+static void bench_ladder_cycles(bench_ladder *b, int32_t ncycles)
+{
+    pt_state *P = &b->P;
+    const int32_t N = P->g->N, nrep = P->nrep;
+    for (int32_t c = 0; c < ncycles; c++) {
+        pt_cycle_ref(P, b->phase);
+        for (int32_t rep = 0; rep < nrep; rep++)
+            P->nb[rep] = or_nbar_ref(P->g, P->s + (size_t)rep * N);
+        for (int32_t sl = 0; sl < nrep; sl++) {
+            int32_t rep = P->rat[sl];
+            slot_accumulate(b->sums + sl * OR_NSUM, P->mag[rep], P->en[rep], P->sx[rep],
+                            P->sy[rep], P->nb[rep]);
+        }
+        b->phase = (b->phase == 1) ? 2 : 1;
+    }
+}
+
+static void bench_ladder_free(bench_ladder *b)
+{
+    free(b->sums);
+    free(b->P.att);
+    free(b->P.acc);
+    free(b->P.s);
+    free(b->P.rat);
+    free(b->P.tor);
+    free(b->P.mag);
+}
+
 static void *bench_worker(void *vp)
 {
     bench_arg *a = (bench_arg *)vp;
-    const or_lat *g = a->g;
-    const int32_t N = g->N, nrep = a->nrep;
-    pt_state P;
-    P.g = g;
-    P.nrep = nrep;
-    P.ptswapever = a->ptswapever;
-    P.beta = a->beta;
-    P.s = (int8_t *)malloc((size_t)N * nrep);
-    P.rat = (int32_t *)malloc(sizeof(int32_t) * nrep);
-    P.tor = (int32_t *)malloc(sizeof(int32_t) * nrep);
-    P.mag = (double *)malloc(sizeof(double) * nrep * 5);
-    P.en = P.mag + nrep;
-    P.sx = P.en + nrep;
-    P.sy = P.sx + nrep;
-    P.nb = P.sy + nrep;
-    P.att = (int64_t *)calloc(nrep, sizeof(int64_t));
-    P.acc = (int64_t *)calloc(nrep, sizeof(int64_t));
-    double *sums = (double *)calloc((size_t)OR_NSUM * nrep, sizeof(double));
-    for (int32_t rep = 0; rep < nrep; rep++) {
-        P.rat[rep] = P.tor[rep] = rep;
-        or_kiss_init(P.kiss, a->seed + rep);
-        init_spin_array(P.kiss, g->L, g->H, 0, 0, P.s + (size_t)rep * N);
-        double o[4];
-        or_measurement_ref(g, P.s + (size_t)rep * N, o);
-        P.mag[rep] = o[0];
-        P.en[rep] = o[1];
-        P.sx[rep] = o[2];
-        P.sy[rep] = o[3];
-    }
-    or_kiss_init(P.kiss, a->seed + 100000);
-    int32_t phase = 1;
+    bench_ladder b;
+    bench_ladder_init(&b, a->g, a->nrep, a->ptswapever, a->beta, a->seed);
     double t0 = now_s();
-    for (int32_t c = 0; c < a->ncycles; c++) {
-        pt_cycle_ref(&P, phase);
-        for (int32_t rep = 0; rep < nrep; rep++)
-            P.nb[rep] = or_nbar_ref(g, P.s + (size_t)rep * N);
-        for (int32_t sl = 0; sl < nrep; sl++) {
-            int32_t rep = P.rat[sl];
-            slot_accumulate(sums + sl * OR_NSUM, P.mag[rep], P.en[rep], P.sx[rep], P.sy[rep],
-                            P.nb[rep]);
-        }
-        phase = (phase == 1) ? 2 : 1;
-    }
+    bench_ladder_cycles(&b, a->ncycles);
     a->seconds = now_s() - t0;
-    free(sums);
-    free(P.att);
-    free(P.acc);
-    free(P.s);
-    free(P.rat);
-    free(P.tor);
-    free(P.mag);
+    bench_ladder_free(&b);
     return NULL;
 }
 
@@ -628,6 +655,61 @@ double or_bench_pt_ref(const or_lat *g, int32_t nthreads, int32_t nrep, const do
     free(th);
     free(args);
     return worst;
+}
+
+/* The same over nlad ladders, one disorder configuration each (gs[k]), on nthreads threads:
+ * ladder k belongs to thread k % nthreads (the reference's configurations round-robin over
+ * ranks, J:287-301).  Every thread first initialises its ladders; after a barrier the wall time
+ * of ncycles cycles of every ladder is measured (until the last thread finishes) and returned in
+ * seconds. */
+typedef struct {
+    const or_lat *const *gs;
+    int32_t nlad, nthreads, t, nrep, ptswapever, ncycles, irinit;
+    const double *beta;
+    pthread_barrier_t *start;
+    double done;
+} bench_multi_arg;
+
+static void *bench_multi_worker(void *vp)
+{
+    bench_multi_arg *a = (bench_multi_arg *)vp;
+    int32_t mine = 0;
+    for (int32_t k = a->t; k < a->nlad; k += a->nthreads) mine++;
+    bench_ladder *b = (bench_ladder *)malloc(sizeof(bench_ladder) * (mine > 0 ? mine : 1));
+    int32_t j = 0;
+    for (int32_t k = a->t; k < a->nlad; k += a->nthreads, j++)
+        bench_ladder_init(&b[j], a->gs[k], a->nrep, a->ptswapever, a->beta, a->irinit + 1000 * k);
+    pthread_barrier_wait(a->start);
+    for (j = 0; j < mine; j++) bench_ladder_cycles(&b[j], a->ncycles);
+    a->done = now_s();
+    for (j = 0; j < mine; j++) bench_ladder_free(&b[j]);
+    free(b);
+    return NULL;
+}
+
+double or_bench_pt_multi(const or_lat *const *gs, int32_t nlad, int32_t nthreads, int32_t nrep,
+                         const double *beta, int32_t ptswapever, int32_t ncycles, int32_t irinit)
+{
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    bench_multi_arg *args = (bench_multi_arg *)malloc(sizeof(bench_multi_arg) * nthreads);
+    pthread_barrier_t start;
+    pthread_barrier_init(&start, NULL, (unsigned)nthreads + 1u);
+    for (int32_t t = 0; t < nthreads; t++) {
+        args[t] = (bench_multi_arg){gs, nlad, nthreads, t, nrep, ptswapever, ncycles, irinit,
+                                    beta, &start, 0.0};
+        pthread_create(&th[t], NULL, bench_multi_worker, &args[t]);
+    }
+    pthread_barrier_wait(&start);
+    const double t0 = now_s();
+    double last = t0;
+    for (int32_t t = 0; t < nthreads; t++) {
+        pthread_join(th[t], NULL);
+        if (args[t].done > last) last = args[t].done;
+    }
+    pthread_barrier_destroy(&start);
+    free(th);
+    free(args);
+    return last - t0;
 }
 
 /* ------------------------------------------------------------------------------------------ */

@@ -64,6 +64,8 @@ void or_local_ref(const or_lat *g, const int8_t *s0, double beta, int32_t neq, i
                   double *strylist, double *nbarlist, int8_t *s_out);
 double or_bench_pt_ref(const or_lat *g, int32_t nthreads, int32_t nrep, const double *beta,
                        int32_t ptswapever, int32_t ncycles, int32_t irinit);
+double or_bench_pt_multi(const or_lat *const *gs, int32_t nlad, int32_t nthreads, int32_t nrep,
+                         const double *beta, int32_t ptswapever, int32_t ncycles, int32_t irinit);
 
 /* device-engine replay */
 void or_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

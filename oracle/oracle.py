@@ -25,11 +25,13 @@ _lib = None
 _ref = None
 
 
-def build(ref: bool = False) -> None:
-    """Compile the oracle (and, with ref=True, the Ooura-linked reference) with make."""
+def build(ref: bool = False, reference: str | None = None) -> None:
+    """Compile the oracle (and, with ref=True, the Ooura-linked reference from the reference tree
+    `reference`, default: beside the repository) with make."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        extra = [f"REFERENCE={reference}"] if reference else []
+        subprocess.run(["make", "-s", "-C", HERE, "ref"] + extra, check=True)
 
 
 def _p(a, ct):
@@ -62,6 +64,7 @@ def lib():
         L.or_replay_sweeps.restype = C.c_int64
         L.or_setup_vacancies.restype = C.c_int32
         L.or_bench_pt_ref.restype = C.c_double
+        L.or_bench_pt_multi.restype = C.c_double
         L.or_wolff_step.restype = C.c_int64
     return _lib
 
@@ -220,6 +223,17 @@ class Model:
                            _p(state["accepts"], C.c_int64), _p(state["visited"], C.c_uint8),
                            _p(obs, C.c_double), None if flips is None else _p(flips, C.c_int32))
         return obs
+
+
+def bench_pt_multi(models, nthreads, betas, ptswapever, ncycles, irinit=1) -> float:
+    """Wall seconds of ncycles PT cycles of one ladder per model (the reference restatement:
+    sequential site order, KISS, FP64), the ladders spread round-robin over nthreads threads;
+    initialisation is not timed."""
+    b = np.ascontiguousarray(betas, np.float64)
+    arr = (C.POINTER(Lat) * len(models))(*[C.pointer(m.lat) for m in models])
+    return lib().or_bench_pt_multi(arr, C.c_int32(len(models)), C.c_int32(nthreads),
+                                   C.c_int32(len(b)), _p(b, C.c_double), C.c_int32(ptswapever),
+                                   C.c_int32(ncycles), C.c_int32(irinit))
 
 
 def new_pt_state(spins):

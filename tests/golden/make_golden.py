@@ -1,6 +1,6 @@
 """Generate the committed golden fixtures in this folder.
 
-Run here, where the reference tree exists (REFERENCE, default /root/reference); the GPU tests
+Run where the reference tree exists (REFERENCE, default: beside this repository); the GPU tests
 only read the committed outputs:
 
 * ``corr3d_golden.npz`` — make_corr_rand_3d (sim/corr_rand_3d.f90:191-386) evaluated by the
@@ -24,7 +24,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-REFERENCE = os.environ.get("REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 
 from oracle import oracle as O  # noqa: E402
 

@@ -512,3 +512,46 @@ def test_small_batch_cluster_path_fp32_bitwise(engine_mod, oracle):
         np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(out[0][1], out[1][1])
     np.testing.assert_array_equal(out[0][2], out[1][2])
+
+
+def test_non_integer_couplings(engine_mod, oracle):
+    """J2 = -0.7, J3 = 1.3: the shape-specialised FP32 kernels form J3*Zs + J2*D in integer
+    arithmetic and so take integer J2, J3 only; here the FP32 form runs the generic kernels,
+    whose variants agree bit for bit, and the FP64 form (shape-specialised kernel, any
+    couplings) equals the oracle's replay bit for bit."""
+    jc = engine_mod
+    L, nrep, J2, J3 = 32, 3, -0.7, 1.3
+    betas = _betas(nrep)
+    out = []
+    for flags in (0, jc.FLAG_GENERIC, jc.FLAG_GLOBAL):
+        eng = jc.Engine(L, L, nconf=2, nreplica=nrep, precision=jc.FP32_BATCHED, seed=SEED,
+                        flags=flags, J2=J2, J3=J3)
+        for k in range(2):
+            eng.set_disorder(k, jc.disorder(L, L, SEED + k))
+            eng.set_ladder(k, betas)
+            eng.init_spins(k, jc.START_HOT)
+        eng.reset_measurements()
+        eng.run(3, measure=True)
+        out.append(([eng.spins(k, r) for k in range(2) for r in range(nrep)],
+                    eng.slot_sums(-1)[0], eng.observables(-1)))
+        eng.close()
+    for other in out[1:]:
+        for a, b in zip(out[0][0], other[0]):
+            np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(out[0][1], other[1])
+        np.testing.assert_array_equal(out[0][2], other[2])
+    p = jc.disorder(L, L, SEED)
+    eng = jc.Engine(L, L, nconf=1, nreplica=nrep, precision=jc.FP64_PLAIN, seed=SEED, J2=J2, J3=J3)
+    eng.set_disorder(0, p)
+    eng.set_ladder(0, betas)
+    eng.init_spins(0, jc.START_HOT)
+    eng.reset_measurements()
+    st = oracle.new_pt_state(np.stack([eng.spins(0, r) for r in range(nrep)]))
+    eng.run(4, measure=True)
+    M = oracle.Model(L, L, p, J2=J2, J3=J3)
+    obs = M.replay_pt(st, betas, 5, 4, 0, SEED, 0, True, 1)
+    for r in range(nrep):
+        np.testing.assert_array_equal(eng.spins(0, r), st["spins"][r])
+    np.testing.assert_array_equal(eng.slot_sums(0)[0], st["sums"])
+    np.testing.assert_array_equal(eng.observables(0), obs)
+    eng.close()
