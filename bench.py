@@ -40,10 +40,10 @@ B_PER_ATTEMPT_FP64 = 21.4
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one sweep-kernel launch (5 sweeps
 # + measure of every lattice), from an ncu capture of the same workload
-TRAFFIC = {"batched_fp32_L32_64x32": 75578112 + 10685696}
+TRAFFIC = {"batched_fp32_L32_64x32": 75584000 + 8890368}
 # issue-slot utilisation and thread instructions per attempt of the same capture (the kernel is
 # bound by instruction issue inside shared memory, not by DRAM)
-NCU_ISSUE = {"batched_fp32_L32_64x32": {"issue_active": 0.582, "inst_per_attempt": 53.4,
+NCU_ISSUE = {"batched_fp32_L32_64x32": {"issue_active": 0.602, "inst_per_attempt": 48.1,
                                         "source": "profiles/sweep_fixed_fp32_L32_2048lat.md"}}
 
 # name -> lattice-shape groups (L, nconf, nreplica), precision and options
@@ -251,11 +251,45 @@ def time_workload(torch, jc, w, device, flush, steps):
     return out
 
 
+B_PER_WOLFF_SITE = 18  # spin 1 + J_eff 8 + label write/read 8 + flip 1, per cluster site
+
+
+def wolff_report(torch, jc, w, device, warm=30, n=10):
+    """The Wolff update alone (j1j2c_wolff, every lattice at its slot's temperature) on lattices
+    equilibrated for `warm` PT cycles: device time per update (CUDA events on the engine's
+    stream), flipped-cluster sites per update, sites per ns, and the streaming model of 18 bytes
+    per cluster site against the measured copy bandwidth."""
+    eng, _ = make_engine(jc, w, device)
+    stream = torch.cuda.current_stream()
+    eng.set_stream(stream.cuda_stream)
+    eng.run(warm, measure=False)
+    eng.wolff()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sites = 0
+    a.record(stream)
+    for _ in range(n):
+        sites += int(eng.wolff().sum())
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / n
+    eng.close()
+    per = sites / n
+    gbs = B_PER_WOLFF_SITE * per / (ms * 1e-3) / 1e9
+    hbm = peaks().get("hbm_gbs") or 6800.0
+    return {"ms_per_update": round(ms, 4), "cluster_sites_per_update": int(per),
+            "sites_per_ns": round(per / (ms * 1e6), 3), "bytes_per_site": B_PER_WOLFF_SITE,
+            "model_gbs": round(gbs, 1), "frac_of_hbm": round(gbs / hbm, 4),
+            "equilibration_cycles": warm}
+
+
 def secondary_workloads(torch, jc, device, flush, steps):
     """The other configurations of the same path, each timed alone on this GPU."""
     res = {}
     for name in ("batched_fp64_L32_64x32", "mixed_L16_24_32_48", "large_L96_vac5_wolff_8x48"):
         res[name] = time_workload(torch, jc, WORKLOADS[name], device, flush, steps)
+    res["large_L96_vac5_wolff_8x48"]["wolff"] = wolff_report(
+        torch, jc, WORKLOADS["large_L96_vac5_wolff_8x48"], device)
     # per-L throughput of the uneven batch: each lattice-shape group alone
     per_l = {}
     for L, n, r in WORKLOADS["mixed_L16_24_32_48"]["groups"]:

@@ -49,6 +49,9 @@ struct Group {
     // split_k coldest slots of every configuration (split_cs CTAs per growing cluster) on the
     // main stream and those of the other slots on the Wolff side stream
     int split_k = 0, split_cs = 1;
+    // the Wolff update of the cold slots (split form: slots [0, split_k); unsplit: every slot)
+    // reads bond activations decided beforehand on every SM (wolff_bits_kernel)
+    bool split_bits = false;
     int nlat() const { return nconf * nrep; }
 };
 
@@ -81,6 +84,7 @@ struct Ctx {
     int* d_nreps = nullptr;
     unsigned long long* d_audit = nullptr;
     int* d_labels = nullptr;        // Wolff union-find labels / cluster list, one int per site
+    uint8_t* d_act = nullptr;       // Wolff bond activation bits, one byte per site (first use)
     long long* d_csize = nullptr;   // Wolff cluster size of the last update, per replica
     int* d_err = nullptr;           // device error word (union-find retry overflow)
     int uf_tries = 1 << 20;         // union-find attempts per bond (j1j2c_set_retry_budget)
@@ -195,7 +199,7 @@ void release(Ctx* c)
     void* ptrs[] = {c->d_spins, c->d_pf,    c->d_pd,   c->d_bm,    c->d_occ,   c->d_beta,
                     c->d_rat,   c->d_tor,   c->d_obs,  c->d_sums,  c->d_nmeas, c->d_att,
                     c->d_acc,   c->d_vis,   c->d_last, c->d_ctl,   c->d_nocc,  c->d_rbase,
-                    c->d_nreps, c->d_audit, c->d_labels, c->d_csize, c->d_err,
+                    c->d_nreps, c->d_audit, c->d_labels, c->d_act, c->d_csize, c->d_err,
                     c->d_loc_s, c->d_loc_n, c->d_loc_samples, c->d_hist, c->d_hist_lo,
                     c->d_hist_bs, c->d_trace, c->d_trace_tor, c->d_flips};
     for (void* p : ptrs)
@@ -496,14 +500,36 @@ cudaError_t wolff_side(Ctx* c, const Group& grp)
     return e;
 }
 
+// The growth reads bond activations decided beforehand (test flag, or the split tuner's choice)
+bool bits_of(const Ctx* c, const Group& grp)
+{
+    return (c->P.flags & J1J2C_FLAG_WOLFF_BITS) != 0 || grp.split_bits;
+}
+
+// Device buffer of the activation bits (the spins' layout, one byte per site), on first use
+int ensure_act(Ctx* c)
+{
+    if (!c->d_act) CK(c, dalloc(&c->d_act, (size_t)c->spin_bytes));
+    return J1J2C_OK;
+}
+
 // Growth form over the group's lattices with a (spins of) a: the k coldest slots of every
 // configuration with cs CTAs per lattice and the other slots with one, as two concurrent
-// launches (0 < k < nrep), else every lattice with cs CTAs
+// launches (0 < k < nrep), else every lattice with cs CTAs.  With bond activations decided
+// beforehand (bits_of; c->d_act allocated): every lattice, one CTA each, reading them.
 cudaError_t enqueue_wolff_grow(Ctx* c, const Group& grp, const SweepArgs& a, int cs, int k,
                                cudaStream_t st)
 {
     int* lab = c->d_labels + grp.lab_off;
     long long* cz = c->d_csize + grp.rep0;
+    if (bits_of(c, grp) && c->d_act) {
+        uint8_t* act = c->d_act + grp.spin_off;
+        cudaError_t e = launch_wolff_bits(a, grp.var.fp64, c->masks, grp.nconf, 0, grp.nrep, act,
+                                          grp.lat_stride, st);
+        if (e != cudaSuccess) return e;
+        return launch_wolff_grow(a, grp.var.fp64, c->masks, grp.nconf, 0, grp.nrep, 1, lab,
+                                 grp.lat_stride, cz, st, act, grp.lat_stride);
+    }
     if (k <= 0 || k >= grp.nrep || cs == 1)
         return launch_wolff_grow(a, grp.var.fp64, c->masks, grp.nconf, 0, grp.nrep, cs, lab,
                                  grp.lat_stride, cz, st);
@@ -542,7 +568,7 @@ int split_cs_of(const Ctx* c, const Group& grp)
 // sweeps run while the cold lattices' clusters still grow; every lattice keeps its own order
 // (its Wolff update, then its sweeps), and the observables follow both halves.
 cudaError_t enqueue_split(Ctx* c, const Group& grp, const SweepVariant& v, SweepArgs a, int k,
-                          int cs, cudaStream_t st)
+                          int cs, cudaStream_t st, bool bits)
 {
     const size_t gi = (size_t)(&grp - c->G.data());
     const int nlat = grp.nlat();
@@ -558,9 +584,18 @@ cudaError_t enqueue_split(Ctx* c, const Group& grp, const SweepVariant& v, Sweep
     const int s0[2] = {0, k}, ns[2] = {k, grp.nrep - k}, ncs[2] = {cs, 1};
     for (int h = 0; h < 2; ++h) {
         SweepArgs b = a;
-        if ((e = launch_wolff_grow(b, v.fp64, c->masks, grp.nconf, s0[h], ns[h], ncs[h], lab,
-                                   grp.lat_stride, cz, ss[h])) != cudaSuccess)
-            return e;
+        if (h == 0 && bits && c->d_act) {  // the cold slots: activations first, on every SM
+            uint8_t* act = c->d_act + grp.spin_off;
+            if ((e = launch_wolff_bits(b, v.fp64, c->masks, grp.nconf, 0, k, act, grp.lat_stride,
+                                       st)) != cudaSuccess)
+                return e;
+            e = launch_wolff_grow(b, v.fp64, c->masks, grp.nconf, 0, k, 1, lab, grp.lat_stride,
+                                  cz, st, act, grp.lat_stride);
+        } else {
+            e = launch_wolff_grow(b, v.fp64, c->masks, grp.nconf, s0[h], ns[h], ncs[h], lab,
+                                  grp.lat_stride, cz, ss[h]);
+        }
+        if (e != cudaSuccess) return e;
         b.slot0 = s0[h];
         b.nslots = ns[h];
         for (int t = 0; t < a.nsweeps; ++t)
@@ -598,7 +633,8 @@ cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int n
     cudaError_t e;
     if (cycle && c->wolff && nlat == grp.nlat() && v.global && v.fixed_nt > 0) {
         const int k = split_k_of(c, grp);
-        if (k > 0) return enqueue_split(c, grp, v, a, k, split_cs_of(c, grp), st);
+        if (k > 0)
+            return enqueue_split(c, grp, v, a, k, split_cs_of(c, grp), st, bits_of(c, grp));
     }
     if (cycle && c->wolff && (e = enqueue_wolff(c, grp, st)) != cudaSuccess) return e;
     if (v.cluster > 0) {
@@ -1058,14 +1094,22 @@ bool tune_log()
 // fastest is kept, cached per (device, precision, L, H, lattice count, dilution).  Two CTAs per
 // cold cluster are not candidates: on a fresh HOT start (small clusters) they time fastest, on
 // equilibrated lattices they are the slowest choice (L = 96, 8 x 48: 11.0-12.4 vs 9.6 ms).
-std::map<std::tuple<int, bool, int, int, int, bool>, std::pair<int, int>> g_split_cache;
+// A split choice: k coldest slots on the main stream (0: unsplit), cs CTAs per cold cluster, the
+// cold slots' (unsplit: every slot's) bond activations decided beforehand
+struct SplitChoice {
+    int k, cs;
+    bool bits;
+};
+constexpr int kSplitWarm = 40;  // cycles run on the tuner's scratch lattices before timing
+std::map<std::tuple<int, bool, int, int, int, bool>, SplitChoice> g_split_cache;
 
 int tune_split(Ctx* c, Group& grp)
 {
     const uint32_t fl = c->P.flags;
     if (!c->wolff || !grp.var.global || grp.var.fixed_nt <= 0 || grp.nrep < 8 ||
         (fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_WOLFF_CS2 |
-               J1J2C_FLAG_WOLFF_CS4 | J1J2C_FLAG_WOLFF_SPLIT | J1J2C_FLAG_NO_GRAPH)))
+               J1J2C_FLAG_WOLFF_CS4 | J1J2C_FLAG_WOLFF_SPLIT | J1J2C_FLAG_WOLFF_BITS |
+               J1J2C_FLAG_NO_GRAPH)))
         return J1J2C_OK;
     const auto key =
         std::make_tuple(c->P.device, grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks);
@@ -1073,12 +1117,17 @@ int tune_split(Ctx* c, Group& grp)
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_split_cache.find(key);
         if (it != g_split_cache.end()) {
-            grp.split_k = it->second.first;
-            grp.split_cs = it->second.second;
+            grp.split_k = it->second.k;
+            grp.split_cs = it->second.cs;
+            grp.split_bits = it->second.bits;
             return J1J2C_OK;
         }
     }
     if (!c->d_labels) CK(c, dalloc(&c->d_labels, (size_t)c->lab_ints));
+    {
+        const int rc = ensure_act(c);
+        if (rc != J1J2C_OK) return rc;
+    }
     const int nlat = grp.nlat();
     uint8_t* tmp = nullptr;
     LatObs* tobs = nullptr;
@@ -1094,34 +1143,60 @@ int tune_split(Ctx* c, Group& grp)
     a.spins = tmp;
     a.obs = tobs;
     a.flips = nullptr;
-    struct Cand {
-        int k, cs;
+    // the cycle of one candidate, captured as a graph (as in a run)
+    // one cycle of a candidate (the Wolff update, PTSWAPEVER sweeps, the observables) with
+    // arguments b, enqueued on the context's stream
+    auto enqueue = [&](const SplitChoice& cd, const SweepArgs& b) {
+        if (cd.k > 0) return enqueue_split(c, grp, grp.var, b, cd.k, cd.cs, c->own, cd.bits);
+        grp.split_bits = cd.bits;  // read by enqueue_wolff_grow
+        cudaError_t e1 = enqueue_wolff_grow(c, grp, b, wolff_cs_of(c, grp), wolff_k_of(c, grp),
+                                            c->own);
+        grp.split_bits = false;
+        if (e1 == cudaSuccess)
+            e1 = enqueue_group(c, grp, grp.var, grp.nthreads, grp.smem, b, nlat, c->own, false);
+        return e1;
     };
-    std::vector<Cand> cands{{0, 1}};
-    for (const int k : {grp.nrep / 4, grp.nrep / 2, 3 * grp.nrep / 4}) cands.push_back({k, 1});
-    int best_k = 0, best_cs = 1;
-    float best_ms = 0.0f;
-    for (const Cand cd : cands) {
-        if (e != cudaSuccess) break;
+    auto capture = [&](const SplitChoice& cd, cudaGraphExec_t& exec) {
         cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        e = cudaStreamBeginCapture(c->own, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            cudaError_t e1;
-            if (cd.k > 0) {
-                e1 = enqueue_split(c, grp, grp.var, a, cd.k, cd.cs, c->own);
-            } else {
-                e1 = enqueue_wolff_grow(c, grp, a, wolff_cs_of(c, grp), wolff_k_of(c, grp),
-                                        c->own);
-                if (e1 == cudaSuccess)
-                    e1 = enqueue_group(c, grp, grp.var, grp.nthreads, grp.smem, a, nlat, c->own,
-                                       false);
-            }
-            e = cudaStreamEndCapture(c->own, &graph);
-            if (e1 != cudaSuccess) e = e1;
+        exec = nullptr;
+        cudaError_t r = cudaStreamBeginCapture(c->own, cudaStreamCaptureModeThreadLocal);
+        if (r == cudaSuccess) {
+            const cudaError_t e1 = enqueue(cd, a);
+            r = cudaStreamEndCapture(c->own, &graph);
+            if (e1 != cudaSuccess) r = e1;
         }
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (r == cudaSuccess) r = cudaGraphInstantiate(&exec, graph, 0);
         if (graph) cudaGraphDestroy(graph);
+        return r;
+    };
+    std::vector<SplitChoice> cands{{0, 1, false}, {0, 1, true}};
+    for (const int k : {grp.nrep / 4, grp.nrep / 2, 3 * grp.nrep / 4})
+        for (const bool bits : {false, true}) cands.push_back({k, 1, bits});
+    // The scratch lattices first run kSplitWarm cycles of the unsplit form at their slots'
+    // temperatures (the clusters of a freshly started lattice are far smaller than those of an
+    // equilibrated cold one, which decide the choice); each of these cycles reads its own cycle
+    // counter, so the random stream moves on as in a run
+    uint32_t* wctl = nullptr;
+    if (e == cudaSuccess) e = dev_malloc(&wctl, sizeof(uint32_t) * 4 * kSplitWarm);
+    if (e == cudaSuccess) {
+        std::vector<uint32_t> h(4 * kSplitWarm, 0u);
+        for (int r = 0; r < kSplitWarm; ++r) h[4 * r] = 0x7A000000u + (uint32_t)r;
+        e = cudaMemcpy(wctl, h.data(), h.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    }
+    for (int r = 0; r < kSplitWarm && e == cudaSuccess; ++r) {
+        SweepArgs b = a;
+        b.ctl = wctl + 4 * r;
+        e = enqueue(cands[0], b);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->own);
+    if (wctl) cudaFree(wctl);
+    SplitChoice best = cands[0];
+    float best_ms = 0.0f;
+    for (size_t ci = 0; ci < cands.size(); ++ci) {
+        const SplitChoice cd = cands[ci];
+        if (e != cudaSuccess) break;
+        cudaGraphExec_t exec = nullptr;
+        e = capture(cd, exec);
         if (e == cudaSuccess) e = cudaGraphLaunch(exec, c->own);  // warm-up
         float ms = 0.0f;
         for (int r = 0; r < 3 && e == cudaSuccess; ++r) {  // the fastest of three
@@ -1135,22 +1210,23 @@ int tune_split(Ctx* c, Group& grp)
         }
         if (exec) cudaGraphExecDestroy(exec);
         if (e == cudaSuccess && tune_log())
-            std::fprintf(stderr, "j1j2c tune split L=%d H=%d lattices=%d: k=%d cs=%d %.3f ms\n",
-                         grp.g.L, grp.g.H, nlat, cd.k, cd.cs, ms);
-        if (e == cudaSuccess && (cd.k == 0 || ms < best_ms)) {
+            std::fprintf(stderr,
+                         "j1j2c tune split L=%d H=%d lattices=%d: k=%d cs=%d bits=%d %.3f ms\n",
+                         grp.g.L, grp.g.H, nlat, cd.k, cd.cs, (int)cd.bits, ms);
+        if (e == cudaSuccess && (ci == 0 || ms < best_ms)) {
             best_ms = ms;
-            best_k = cd.k;
-            best_cs = cd.cs;
+            best = cd;
         }
     }
     cudaStreamSynchronize(c->own);
     cudaFree(tmp);
     cudaFree(tobs);
     if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the split Wolff + sweep form");
-    grp.split_k = best_k;
-    grp.split_cs = best_cs;
+    grp.split_k = best.k;
+    grp.split_cs = best.cs;
+    grp.split_bits = best.bits;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_split_cache[key] = std::make_pair(best_k, best_cs);
+    g_split_cache[key] = best;
     return J1J2C_OK;
 }
 
@@ -1882,6 +1958,7 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
     }
     for (auto& grp : c->G) {
         int rct = autotune(c, grp);
+        if (rct == J1J2C_OK && c->wolff && bits_of(c, grp)) rct = ensure_act(c);
         if (rct != J1J2C_OK) return rct;
     }
     const bool direct = (c->P.flags & J1J2C_FLAG_NO_GRAPH) != 0;
@@ -1940,6 +2017,11 @@ int j1j2c_wolff(void* ctx, int64_t* cluster_sizes)
         if (!c->have_dis[k] || !c->have_ladder[k] || !c->have_spins[k])
             return fail(c, J1J2C_ESTATE, "every conf needs disorder, ladder and spins");
     if (!c->d_labels) CK(c, dalloc(&c->d_labels, (size_t)c->lab_ints));
+    for (auto& grp : c->G)
+        if (bits_of(c, grp)) {
+            const int rc = ensure_act(c);
+            if (rc != J1J2C_OK) return rc;
+        }
     for (auto& grp : c->G) CK(c, enqueue_wolff(c, grp, c->st));
     if (cluster_sizes)
         CK(c, cudaMemcpyAsync(cluster_sizes, c->d_csize, sizeof(long long) * c->nentries,

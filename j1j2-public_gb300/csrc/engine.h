@@ -207,10 +207,17 @@ cudaError_t launch_wolff(const SweepArgs& a, bool fp64, bool masks, int nlat, in
                          WolffForm form, int grow_cs);
 int wolff_grow_clusters(bool fp64, bool masks, int cs);  // resident clusters of cs CTAs
 // The growth form for the lattices at temperature slots [slot0, slot0 + nslots) of the group's
-// nconf configurations (a.nrep slots each), cs CTAs per lattice
+// nconf configurations (a.nrep slots each), cs CTAs per lattice; with act (one byte per site,
+// lattice l at act + l * act_stride, filled by launch_wolff_bits for the same lattices and cycle)
+// the bonds' activation is read from it (one CTA per lattice)
 cudaError_t launch_wolff_grow(const SweepArgs& a, bool fp64, bool masks, int nconf, int slot0,
                               int nslots, int cs, int* labels, long long lab_stride,
-                              long long* csize, cudaStream_t st);
+                              long long* csize, cudaStream_t st, const uint8_t* act = nullptr,
+                              long long act_stride = 0);
+// The activation of every owned bond of the lattices at slots [slot0, slot0 + nslots) for the
+// next growth of the same cycle, exactly as the growth form would decide it
+cudaError_t launch_wolff_bits(const SweepArgs& a, bool fp64, bool masks, int nconf, int slot0,
+                              int nslots, uint8_t* act, long long act_stride, cudaStream_t st);
 int wolff_slab_planes(const Geo& g);  // planes per shared-memory slab of the Wolff labelling
 cudaError_t launch_init(const InitArgs& a, cudaStream_t st);
 

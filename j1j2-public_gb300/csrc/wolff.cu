@@ -584,11 +584,13 @@ enum : int { kCtlHead = 0, kCtlEnd = 1, kCtlTail = 2, kCtlRlim = 3, kCtlWlim = 4
 
 // Grid: the lattices at temperature slots [slot0, slot0 + gridDim.x / (CS nconf)) of the group's
 // nconf configurations, slot-major (coldest slots first: their clusters are the largest, so they
-// start in the first wave), CS CTAs each.
-template <class Real, bool MASKS, int CS>
+// start in the first wave), CS CTAs each.  BITS: every bond's activation was decided beforehand
+// by wolff_bits_kernel (act, one byte per site: bit b for the site's owned bond b), so a
+// frontier site reads bits instead of drawing Philox words and evaluating weights.
+template <class Real, bool MASKS, int CS, bool BITS>
 __global__ void __launch_bounds__(kGrowThreads, 1)
     wolff_grow_kernel(SweepArgs a, int* list, long long list_stride, long long* csize, int slot0,
-                      int nconf)
+                      int nconf, const uint8_t* act, long long act_stride)
 {
     const Geo g = a.g;
     int rank = 0;
@@ -692,67 +694,85 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
             // every load first (independent, in flight together)
 #pragma unroll
             for (int d = 0; d < 10; ++d) bn[d] = S[jn[d]];
-            const Real p_i = P[i], p0 = P[jn[0]], p1 = P[jn[1]], p5 = P[jn[5]], p6 = P[jn[6]];
-            int m_i = 3, m5 = 3, m6 = 3;
-            if (MASKS) {
-                m_i = BM[i];
-                m5 = BM[jn[5]];
-                m6 = BM[jn[6]];
-            }
-            // the bonds' Philox words as independent chains while the loads are in flight: the
-            // site's own in-plane call (bonds 0-3), its +z call, each in-plane neighbour's own
-            // call (the word of the bond it owns) and the -z neighbour's +z call
-            uint32_t word[10];
-            {
-                const U4 own = philox4x32_10((uint32_t)rep, cycle, (uint32_t)i, kTagWolffSite,
-                                             k0, k1);
-                word[0] = own.x;
-                word[1] = own.y;
-                word[2] = own.z;
-                word[3] = own.w;
-            }
+            unsigned act_bits = 0;
+            if constexpr (BITS) {
+                // own bonds from the site's byte, the others from their owners' bytes
+                const uint8_t* A = act + (long long)lat * act_stride;
+                unsigned ab = A[i] & 31u;
 #pragma unroll
-            for (int d = 4; d < 10; ++d) {
-                const int b = d < 5 ? d : d - 5;
-                if (b < 4) {
-                    word[d] = u4_word(philox4x32_10((uint32_t)rep, cycle, (uint32_t)jn[d],
-                                                    kTagWolffSite, k0, k1),
-                                      b);
-                } else {
-                    const int co = d < 5 ? c : cof(d), Zo = d < 5 ? Z : zof(d);
-                    const int Yo = d < 5 ? Y : yof(d), Xo = d < 5 ? X : xof(d);
-                    const uint32_t grp =
-                        (uint32_t)(((co * g.Hh + Zo) * g.Lh + Yo) * g.Qr + (Xo >> 2));
-                    word[d] = u4_word(
-                        philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffZ, k0, k1), Xo & 3);
-                }
-            }
-            unsigned act = 0;
+                for (int d = 5; d < 10; ++d) ab |= (((unsigned)A[jn[d]] >> (d - 5)) & 1u) << d;
 #pragma unroll
-            for (int d = 0; d < 10; ++d) {
-                const int sj = (bn[d] & 3) - 1;
-                if (sj == 0 || (bn[d] & 4)) continue;  // vacancy, or joined already
-                const int b = d < 5 ? d : d - 5;
-                bool on;
-                if (b < 2) {
-                    const int mo = d < 5 ? m_i : (d == 5 ? m5 : m6);
-                    const Real po = d < 5 ? p_i : (d == 5 ? p5 : p6);
-                    const Real pt = d == 0 ? p0 : d == 1 ? p1 : p_i;
-                    Real wv;
-                    on = bond_weight<Real>(a, b, si, sj, mo & 1, (mo >> 1) & 1, po, pt, wv) &&
-                         bond_trial<Real>(wv, beta, word[d]);
-                } else {
-                    on = si * sj == (b < 4 ? s2 : s3) &&
-                         uniform_trial<Real>(b < 4 ? thr2 : thr3, word[d]);
+                for (int d = 0; d < 10; ++d) {
+                    const int sj = (bn[d] & 3) - 1;
+                    if (sj == 0 || (bn[d] & 4)) continue;  // vacancy, or joined already
+                    if ((ab >> d) & 1u) act_bits |= 1u << d;
                 }
-                if (on) act |= 1u << d;
+            } else {
+                const Real p_i = P[i], p0 = P[jn[0]], p1 = P[jn[1]], p5 = P[jn[5]],
+                           p6 = P[jn[6]];
+                int m_i = 3, m5 = 3, m6 = 3;
+                if (MASKS) {
+                    m_i = BM[i];
+                    m5 = BM[jn[5]];
+                    m6 = BM[jn[6]];
+                }
+                // the bonds' Philox words as independent chains while the loads are in flight:
+                // the site's own in-plane call (bonds 0-3), its +z call, each in-plane
+                // neighbour's own call (the word of the bond it owns) and the -z neighbour's +z
+                // call
+                uint32_t word[10];
+                {
+                    const U4 own = philox4x32_10((uint32_t)rep, cycle, (uint32_t)i,
+                                                 kTagWolffSite, k0, k1);
+                    word[0] = own.x;
+                    word[1] = own.y;
+                    word[2] = own.z;
+                    word[3] = own.w;
+                }
+#pragma unroll
+                for (int d = 4; d < 10; ++d) {
+                    const int b = d < 5 ? d : d - 5;
+                    if (b < 4) {
+                        word[d] = u4_word(philox4x32_10((uint32_t)rep, cycle, (uint32_t)jn[d],
+                                                        kTagWolffSite, k0, k1),
+                                          b);
+                    } else {
+                        const int co = d < 5 ? c : cof(d), Zo = d < 5 ? Z : zof(d);
+                        const int Yo = d < 5 ? Y : yof(d), Xo = d < 5 ? X : xof(d);
+                        const uint32_t grp =
+                            (uint32_t)(((co * g.Hh + Zo) * g.Lh + Yo) * g.Qr + (Xo >> 2));
+                        word[d] = u4_word(
+                            philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffZ, k0, k1), Xo & 3);
+                    }
+                }
+#pragma unroll
+                for (int d = 0; d < 10; ++d) {
+                    const int sj = (bn[d] & 3) - 1;
+                    if (sj == 0 || (bn[d] & 4)) continue;  // vacancy, or joined already
+                    const int b = d < 5 ? d : d - 5;
+                    bool on;
+                    if (b < 2) {
+                        const int mo = d < 5 ? m_i : (d == 5 ? m5 : m6);
+                        const Real po = d < 5 ? p_i : (d == 5 ? p5 : p6);
+                        const Real pt = d == 0 ? p0 : d == 1 ? p1 : p_i;
+                        Real wv;
+                        on = bond_weight<Real>(a, b, si, sj, mo & 1, (mo >> 1) & 1, po, pt,
+                                               wv) &&
+                             bond_trial<Real>(wv, beta, word[d]);
+                    } else {
+                        on = si * sj == (b < 4 ? s2 : s3) &&
+                             uniform_trial<Real>(b < 4 ? thr2 : thr3, word[d]);
+                    }
+                    if (on) act_bits |= 1u << d;
+                }
             }
             // claims: every atomic issued before any result is used
             uint32_t old[10];
 #pragma unroll
             for (int d = 0; d < 10; ++d)
-                old[d] = ((act >> d) & 1u) ? atomicOr(&S32[jn[d] >> 2], 4u << (8 * (jn[d] & 3)))
-                                           : 4u << (8 * (jn[d] & 3));
+                old[d] = ((act_bits >> d) & 1u)
+                             ? atomicOr(&S32[jn[d] >> 2], 4u << (8 * (jn[d] & 3)))
+                             : 4u << (8 * (jn[d] & 3));
 #pragma unroll
             for (int d = 0; d < 10; ++d) {
                 const int sh = 8 * (jn[d] & 3);
@@ -788,11 +808,12 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
     if constexpr (CS > 1) cg::this_cluster().sync();  // the first CTA's counters were read above
 }
 
-template <class Real, bool MASKS, int CS>
+template <class Real, bool MASKS, int CS, bool BITS>
 cudaError_t grow_launch(const SweepArgs& a, int nconf, int slot0, int nslots, int* list,
-                        long long list_stride, long long* csize, cudaStream_t st)
+                        long long list_stride, long long* csize, const uint8_t* act,
+                        long long act_stride, cudaStream_t st)
 {
-    auto kern = wolff_grow_kernel<Real, MASKS, CS>;
+    auto kern = wolff_grow_kernel<Real, MASKS, CS, BITS>;
     const int nlat = nconf * nslots;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(nlat * CS));
@@ -806,7 +827,8 @@ cudaError_t grow_launch(const SweepArgs& a, int nconf, int slot0, int nslots, in
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = CS > 1 ? 1u : 0u;
-    return cudaLaunchKernelEx(&cfg, kern, a, list, list_stride, csize, slot0, nconf);
+    return cudaLaunchKernelEx(&cfg, kern, a, list, list_stride, csize, slot0, nconf, act,
+                              act_stride);
 }
 
 template <class Real, bool MASKS, int CS>
@@ -823,7 +845,7 @@ int grow_fits()
     cfg.attrs = at;
     cfg.numAttrs = 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, wolff_grow_kernel<Real, MASKS, CS>, &cfg) !=
+    if (cudaOccupancyMaxActiveClusters(&n, wolff_grow_kernel<Real, MASKS, CS, false>, &cfg) !=
         cudaSuccess) {
         (void)cudaGetLastError();
         return 0;
@@ -831,15 +853,122 @@ int grow_fits()
     return n;
 }
 
+// act: the activation bits of wolff_bits_kernel (one CTA per lattice), or nullptr
 template <class Real, bool MASKS>
 cudaError_t grow_dispatch(const SweepArgs& a, int nconf, int slot0, int nslots, int cs, int* list,
-                          long long list_stride, long long* csize, cudaStream_t st)
+                          long long list_stride, long long* csize, const uint8_t* act,
+                          long long act_stride, cudaStream_t st)
 {
+    if (act)
+        return grow_launch<Real, MASKS, 1, true>(a, nconf, slot0, nslots, list, list_stride,
+                                                 csize, act, act_stride, st);
     if (cs == 2)
-        return grow_launch<Real, MASKS, 2>(a, nconf, slot0, nslots, list, list_stride, csize, st);
+        return grow_launch<Real, MASKS, 2, false>(a, nconf, slot0, nslots, list, list_stride,
+                                                  csize, nullptr, 0, st);
     if (cs == 4)
-        return grow_launch<Real, MASKS, 4>(a, nconf, slot0, nslots, list, list_stride, csize, st);
-    return grow_launch<Real, MASKS, 1>(a, nconf, slot0, nslots, list, list_stride, csize, st);
+        return grow_launch<Real, MASKS, 4, false>(a, nconf, slot0, nslots, list, list_stride,
+                                                  csize, nullptr, 0, st);
+    return grow_launch<Real, MASKS, 1, false>(a, nconf, slot0, nslots, list, list_stride, csize,
+                                              nullptr, 0, st);
+}
+
+// Activation of every site's five owned bonds (+x, +y, (+x,+y), (-x,+y), +z) for the next Wolff
+// update, decided exactly as the growth kernel decides them when it reaches the bond (the
+// owner's Philox word, K s_i s_j > 0 from the configuration before the flip, the same
+// arithmetic): bit b of act[i].  One thread per Philox quad group of four sites; grid (quad
+// groups / 256, lattices at temperature slots [slot0, ...) of the nconf configurations,
+// slot-major like the growth grid).  Every site is evaluated whether or not the cluster reaches
+// it, so this pays where the cluster spans most of the lattice (the cold slots), and it runs on
+// every SM instead of the one that grows the cluster.
+template <class Real, bool MASKS>
+__global__ void __launch_bounds__(256) wolff_bits_kernel(SweepArgs a, uint8_t* act,
+                                                         long long act_stride, int slot0, int nconf)
+{
+    const Geo g = a.g;
+    const int lb = (int)blockIdx.y;
+    const int slot = slot0 + lb / nconf, conf = lb % nconf;
+    const int rep = a.rep_at_temp[conf * a.nrep + slot];
+    const int lat = conf * a.nrep + rep;
+    const int q = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (q >= 8 * g.Hh * g.Lh * g.Qr) return;
+    int r = q;
+    const int Xq = r % g.Qr;
+    r /= g.Qr;
+    const int Y = r % g.Lh;
+    r /= g.Lh;
+    const int Z = r % g.Hh, c = r / g.Hh;
+    const int X0 = 4 * Xq, nw = g.Lh - X0 < 4 ? g.Lh - X0 : 4;
+    const int px = c & 1, py = (c >> 1) & 1, pz = c >> 2;
+    const uint8_t* S = a.spins + (long long)lat * a.lat_stride;
+    const Real* P = wfield<Real>(a, conf);
+    const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
+    uint8_t* A = act + (long long)lat * act_stride;
+    const uint32_t cycle = a.ctl[0];
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+    Real J2, J3;
+    if constexpr (sizeof(Real) == 8) {
+        J2 = a.J2;
+        J3 = a.J3;
+    } else {
+        J2 = a.J2f;
+        J3 = a.J3f;
+    }
+    const unsigned long long thr2 = uniform_threshold<Real>(J2 < Real(0) ? -J2 : J2, beta);
+    const unsigned long long thr3 = uniform_threshold<Real>(J3 < Real(0) ? -J3 : J3, beta);
+    const int s2 = J2 > Real(0) ? 1 : J2 < Real(0) ? -1 : 0;  // s_i s_j of a satisfied bond
+    const int s3 = J3 > Real(0) ? 1 : J3 < Real(0) ? -1 : 0;
+    const int Yp = py ? (Y + 1 == g.Lh ? 0 : Y + 1) : Y;
+    const int Zp = pz ? (Z + 1 == g.Hh ? 0 : Z + 1) : Z;
+    // the +z bonds' words: one call for the quad group (word X & 3)
+    const U4 zw = philox4x32_10((uint32_t)rep, cycle, (uint32_t)q, kTagWolffZ, k0, k1);
+    uint32_t out = 0;
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        if (w >= nw) break;
+        const int X = X0 + w;
+        const int i = cidx(g, c, Z, Y, X);
+        const int si = (S[i] & 3) - 1;
+        if (si == 0) continue;  // a vacancy owns no bond
+        const int Xp = px ? (X + 1 == g.Lh ? 0 : X + 1) : X;
+        const int Xm = px ? X : (X == 0 ? g.Lh - 1 : X - 1);
+        int jn[5];
+        jn[0] = cidx(g, c ^ 1, Z, Y, Xp);
+        jn[1] = cidx(g, c ^ 2, Z, Yp, X);
+        jn[2] = cidx(g, c ^ 3, Z, Yp, Xp);
+        jn[3] = cidx(g, c ^ 3, Z, Yp, Xm);
+        jn[4] = cidx(g, c ^ 4, Zp, Y, X);
+        int sj[5];
+#pragma unroll
+        for (int b = 0; b < 5; ++b) sj[b] = (S[jn[b]] & 3) - 1;
+        const U4 own = philox4x32_10((uint32_t)rep, cycle, (uint32_t)i, kTagWolffSite, k0, k1);
+        int m = 3;
+        if (MASKS) m = BM[i];
+        unsigned bits = 0;
+#pragma unroll
+        for (int b = 0; b < 5; ++b) {
+            if (sj[b] == 0) continue;
+            bool on;
+            if (b < 2) {
+                Real wv;
+                on = bond_weight<Real>(a, b, si, sj[b], m & 1, (m >> 1) & 1, P[i], P[jn[b]],
+                                       wv) &&
+                     bond_trial<Real>(wv, beta, u4_word(own, b));
+            } else {
+                on = si * sj[b] == (b < 4 ? s2 : s3) &&
+                     uniform_trial<Real>(b < 4 ? thr2 : thr3, b < 4 ? u4_word(own, b)
+                                                                    : u4_word(zw, X & 3));
+            }
+            if (on) bits |= 1u << b;
+        }
+        out |= bits << (8 * w);
+    }
+    const int i0 = cidx(g, c, Z, Y, X0);
+    if (nw == 4 && (i0 & 3) == 0) {
+        *reinterpret_cast<uint32_t*>(A + i0) = out;
+    } else {
+        for (int w = 0; w < nw; ++w) A[i0 + w] = (uint8_t)(out >> (8 * w));
+    }
 }
 
 template <class Real>
@@ -860,18 +989,41 @@ cudaError_t bonds(const SweepArgs& a, int* labels, long long ls, int* err, int n
 // nconf configurations, cs CTAs per lattice
 cudaError_t launch_wolff_grow(const SweepArgs& a, bool fp64, bool masks, int nconf, int slot0,
                               int nslots, int cs, int* labels, long long lab_stride,
-                              long long* csize, cudaStream_t st)
+                              long long* csize, cudaStream_t st, const uint8_t* act,
+                              long long act_stride)
 {
     if (nslots <= 0) return cudaSuccess;
     if (fp64)
         return masks ? grow_dispatch<double, true>(a, nconf, slot0, nslots, cs, labels,
-                                                   lab_stride, csize, st)
+                                                   lab_stride, csize, act, act_stride, st)
                      : grow_dispatch<double, false>(a, nconf, slot0, nslots, cs, labels,
-                                                    lab_stride, csize, st);
+                                                    lab_stride, csize, act, act_stride, st);
     return masks ? grow_dispatch<float, true>(a, nconf, slot0, nslots, cs, labels, lab_stride,
-                                              csize, st)
+                                              csize, act, act_stride, st)
                  : grow_dispatch<float, false>(a, nconf, slot0, nslots, cs, labels, lab_stride,
-                                               csize, st);
+                                               csize, act, act_stride, st);
+}
+
+cudaError_t launch_wolff_bits(const SweepArgs& a, bool fp64, bool masks, int nconf, int slot0,
+                              int nslots, uint8_t* act, long long act_stride, cudaStream_t st)
+{
+    if (nslots <= 0) return cudaSuccess;
+    const int nq = 8 * a.g.Hh * a.g.Lh * a.g.Qr;
+    const dim3 grid((unsigned)((nq + 255) / 256), (unsigned)(nconf * nslots));
+    if (fp64) {
+        if (masks)
+            wolff_bits_kernel<double, true><<<grid, 256, 0, st>>>(a, act, act_stride, slot0, nconf);
+        else
+            wolff_bits_kernel<double, false><<<grid, 256, 0, st>>>(a, act, act_stride, slot0,
+                                                                   nconf);
+    } else {
+        if (masks)
+            wolff_bits_kernel<float, true><<<grid, 256, 0, st>>>(a, act, act_stride, slot0, nconf);
+        else
+            wolff_bits_kernel<float, false><<<grid, 256, 0, st>>>(a, act, act_stride, slot0,
+                                                                  nconf);
+    }
+    return cudaGetLastError();
 }
 
 // Clusters of cs CTAs (2 or 4) of the growth kernel that can be resident at once (0: none)
