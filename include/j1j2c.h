@@ -61,6 +61,9 @@ extern "C" {
 #define J1J2C_FLAG_WOLFF_BITS 2048u /* the Wolff growth reads bond activations decided beforehand
                                         for every lattice on every SM (testing; else tuned for the
                                         coldest slots of the split form)                          */
+#define J1J2C_FLAG_PAIRS 4096u   /* the shape-specialised kernels with two replicas of one
+                                    configuration per CTA, sharing the field copy (testing; else
+                                    tuned)                                                        */
 #define J1J2C_FLAG_WOLFF_CS2 128u /* Wolff growth over 2 CTAs per lattice (testing; else tuned)    */
 #define J1J2C_FLAG_WOLFF_CS4 256u /* Wolff growth over 4 CTAs per lattice (testing; else tuned);
                                      both flags: 2 CTAs for the coldest quarter of the slots, one

@@ -292,14 +292,15 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
     if (!(fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_GLOBAL)) &&
         !c->diag.flip_counts) {
         FixedChoice fc[16];
-        const int n =
-            fixed_candidates(fp64, grp.g.L, grp.g.H, c->masks, c->vac, int_couplings(c), fc, 16);
-        // the first per-lattice form (or the block_threads one); the streaming form when the
-        // test flag asks for it
+        const int n = fixed_candidates(fp64, grp.g.L, grp.g.H, c->masks, c->vac,
+                                       int_couplings(c), grp.nrep, fc, 16);
+        // the first one-replica-per-CTA form (or the block_threads one); the streaming form or
+        // two replicas per CTA when a test flag asks for it
         const bool stream = (fl & J1J2C_FLAG_STREAM) != 0;
+        const int rpc = (fl & J1J2C_FLAG_PAIRS) ? 2 : 1;
         int pick = -1;
         for (int k = n - 1; k >= 0; --k)
-            if (fc[k].stream == stream &&
+            if (fc[k].stream == stream && fc[k].rpc == rpc &&
                 (grp.block_threads == 0 || fc[k].nt == grp.block_threads))
                 pick = k;
         if (pick >= 0) {
@@ -308,6 +309,7 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
             v.stage_p = fc[pick].stage_p;
             v.stream = fc[pick].stream;
             v.minb = fc[pick].minb;
+            v.rpc = fc[pick].rpc;
             smem = sweep_smem_bytes(grp.g, v);
             if (smem <= budget) {
                 nthreads = fc[pick].nt;
@@ -1169,9 +1171,10 @@ int tune_split(Ctx* c, Group& grp)
         if (graph) cudaGraphDestroy(graph);
         return r;
     };
-    std::vector<SplitChoice> cands{{0, 1, false}, {0, 1, true}};
-    for (const int k : {grp.nrep / 4, grp.nrep / 2, 3 * grp.nrep / 4})
-        for (const bool bits : {false, true}) cands.push_back({k, 1, bits});
+    // (the cold slots' growth from bond activations decided beforehand, bits = true, measured
+    // slower on equilibrated L = 96 lattices at every split and is left to its test flag)
+    std::vector<SplitChoice> cands{{0, 1, false}};
+    for (const int k : {grp.nrep / 4, grp.nrep / 2, 3 * grp.nrep / 4}) cands.push_back({k, 1, false});
     // The scratch lattices first run kSplitWarm cycles of the unsplit form at their slots'
     // temperatures (the clusters of a freshly started lattice are far smaller than those of an
     // equilibrated cold one, which decide the choice); each of these cycles reads its own cycle
@@ -1244,11 +1247,12 @@ int autotune(Ctx* c, Group& grp)
         return rc != J1J2C_OK ? rc : tune_split(c, grp);
     }
     if (grp.var.global && grp.var.fixed_nt > 0) return J1J2C_OK;
-    if (grp.block_threads > 0 || (c->P.flags & J1J2C_FLAG_STREAM)) return J1J2C_OK;
+    if (grp.block_threads > 0 || (c->P.flags & (J1J2C_FLAG_STREAM | J1J2C_FLAG_PAIRS)))
+        return J1J2C_OK;
     if (grp.var.fixed_nt == 0) return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
     FixedChoice fc[16];
     const int n = fixed_candidates(grp.var.fp64, grp.g.L, grp.g.H, c->masks, c->vac,
-                                   int_couplings(c), fc, 16);
+                                   int_couplings(c), grp.nrep, fc, 16);
     if (n <= 1) return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;
     const int nlat = grp.nlat();
     const auto key = std::make_tuple(c->P.device, grp.var.fp64, grp.g.L, grp.g.H, nlat, c->vac);
@@ -1284,6 +1288,7 @@ int autotune(Ctx* c, Group& grp)
             v.stage_p = fc[k].stage_p;
             v.stream = fc[k].stream;
             v.minb = fc[k].minb;
+            v.rpc = fc[k].rpc;
             const size_t sm = sweep_smem_bytes(grp.g, v);
             if (sm > budget) continue;
             if ((e = launch_fixed(a, v.fp64, c->vac, fc[k], 0, sm, nullptr, true)) != cudaSuccess)
@@ -1314,6 +1319,7 @@ int autotune(Ctx* c, Group& grp)
     grp.var.stage_p = fc[best].stage_p;
     grp.var.stream = fc[best].stream;
     grp.var.minb = fc[best].minb;
+    grp.var.rpc = fc[best].rpc;
     grp.smem = sweep_smem_bytes(grp.g, grp.var);
     grp.nthreads = fc[best].nt;
     {

@@ -150,6 +150,7 @@ struct SweepVariant {
     int cluster;   // > 0: thread-block cluster of this many CTAs per lattice (distributed smem;
                    // quad: four sites per thread, else one)
     int rpt;       // shape-specialised HBM kernel: replicas per thread (1, 2 or 4)
+    int rpc;       // shape-specialised shared-memory kernel: replicas per CTA (0 or 1: one)
     int threads;   // threads per CTA of the generic global-memory kernels (0: 256) and of the
                    // cluster kernel (0: 512)
 };
@@ -174,11 +175,13 @@ cudaError_t launch_sweep_cluster(const SweepArgs& a, const SweepVariant& v, int 
 struct FixedChoice {
     int nt;
     bool stage_p, stream;
-    int minb;  // resident CTAs per SM the kernel is compiled for
+    int minb;     // resident CTAs per SM the kernel is compiled for
+    int rpc = 1;  // replicas of one configuration per CTA (their lattices share the field copy)
 };
-// int_cpl: J2 and J3 are integers with |J| <= 8 (SweepArgs::J2i, J3i); the FP32 kernels need it
-int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, bool int_cpl, FixedChoice* out,
-                     int cap);
+// int_cpl: J2 and J3 are integers with |J| <= 8 (SweepArgs::J2i, J3i); the FP32 kernels need it;
+// nrep: ladder length (forms with several replicas per CTA need it to divide)
+int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, bool int_cpl, int nrep,
+                     FixedChoice* out, int cap);
 // nlat lattices from a.lat0 (prepare: only set the kernel's shared-memory limit)
 cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, const FixedChoice& ch, int nlat,
                          size_t smem, cudaStream_t st, bool prepare);

@@ -869,6 +869,7 @@ size_t sweep_smem_bytes(const Geo& g, const SweepVariant& v)
     const size_t spins = (size_t)((g.N + 15) & ~15);
     const size_t field = ((size_t)g.N * (v.fp64 ? 8 : 4) + 15) & ~(size_t)15;
     if (v.fixed_nt > 0 && v.stream) return field + 2 * spins;  // two spin buffers
+    if (v.fixed_nt > 0 && v.rpc > 1) return field + (size_t)v.rpc * spins;  // replicas per CTA
     size_t b = spins;
     if (v.stage_p) b += (size_t)g.N * (v.fp64 ? 8 : 4);
     return (b + 15) & ~(size_t)15;
@@ -886,7 +887,9 @@ cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks,
 {
     if (v.fixed_nt > 0)
         return launch_fixed(a, v.fp64, v.vac,
-                            FixedChoice{v.fixed_nt, v.stage_p, v.stream, v.minb}, nblocks, smem,
+                            FixedChoice{v.fixed_nt, v.stage_p, v.stream, v.minb,
+                                        v.rpc > 1 ? v.rpc : 1},
+                            nblocks, smem,
                             st, false);
     return dispatch(a, v, nblocks, nthreads, smem, st, false);
 }

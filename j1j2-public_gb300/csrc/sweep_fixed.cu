@@ -479,6 +479,113 @@ __global__ void __launch_bounds__(NT, MINB) sweep_fixed_kernel(SweepArgs a)
     block_copy16(Sg, S, Sh::NB);
 }
 
+// The same kernel over R replicas of one configuration per CTA: their lattices side by side in
+// shared memory behind one staged copy of their configuration's field.  A thread takes the same
+// quad positions in all R lattices: the field operands of a position (and the arithmetic on
+// them alone) are loaded once for the R quads, every replica's spin words are loaded before any
+// is updated, and the lattices of a CTA share its barriers and set-up.  Results are those of
+// sweep_fixed_kernel bit for bit (same operations per quad, same Philox words).
+template <class Real, int LH, int HH, int NT, int QPT, int R, int C, bool MEASURE, bool VAC>
+__device__ __forceinline__ void colour_phase_r(const SweepArgs& a, uint32_t* const (&S32)[R],
+                                               const Real* P, const OffsetCache<QPT>& oc,
+                                               uint32_t sweep, const int (&rep)[R],
+                                               uint32_t kconf, const double (&beta)[R],
+                                               const float (&kb)[R], Acc (&acc)[R])
+{
+    constexpr int NQ = Shape<LH, HH>::CS;
+#pragma unroll
+    for (int j = 0; j < QPT; ++j) {
+        if (!(QPT * NT == NQ || (int)threadIdx.x + j * NT < NQ)) continue;
+        const QuadOff o = offsets_for<LH, HH, NT, QPT>(oc, j);
+        QuadData<Real> d[R];
+        load_quad_field<Real, LH, HH, C>(P, o, d[0]);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (r > 0) d[r] = d[0];
+            load_quad_spins<Real, LH, HH, C>(S32[r], o, d[r]);
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            compute_quad<Real, LH, HH, C, MEASURE, VAC>(a, S32[r], d[r], sweep, (uint32_t)rep[r],
+                                                        kconf, beta[r], kb[r], acc[r]);
+    }
+}
+
+template <class Real, int LH, int HH, int NT, int QPT, int R, bool MEASURE, bool VAC>
+__device__ __forceinline__ void all_colours_r(const SweepArgs& a, uint32_t* const (&S32)[R],
+                                              const Real* P, const OffsetCache<QPT>& oc,
+                                              uint32_t sweep, const int (&rep)[R], uint32_t kconf,
+                                              const double (&beta)[R], const float (&kb)[R],
+                                              Acc (&acc)[R])
+{
+#define J1J2_PHASE_R(C)                                                                       \
+    colour_phase_r<Real, LH, HH, NT, QPT, R, C, MEASURE, VAC>(a, S32, P, oc, sweep, rep, kconf, \
+                                                              beta, kb, acc);                  \
+    __syncthreads();
+    J1J2_PHASE_R(0)
+    J1J2_PHASE_R(1)
+    J1J2_PHASE_R(2)
+    J1J2_PHASE_R(3)
+    J1J2_PHASE_R(4)
+    J1J2_PHASE_R(5)
+    J1J2_PHASE_R(6)
+    J1J2_PHASE_R(7)
+#undef J1J2_PHASE_R
+}
+
+// Grid: one CTA per R consecutive lattices from a.lat0 (the launcher guarantees that they are
+// replicas of one configuration)
+template <class Real, int LH, int HH, int NT, int MINB, bool VAC, int R>
+__global__ void __launch_bounds__(NT, MINB) sweep_fixed_r_kernel(SweepArgs a)
+{
+    using Sh = Shape<LH, HH>;
+    constexpr int QPT = (Sh::CS + NT - 1) / NT;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lat0 = a.lat0 + (int)blockIdx.x * R;
+    const int conf = lat0 / a.nrep;
+    Real* Ps = reinterpret_cast<Real*>(smem + R * Sh::NB);
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        block_copy16(smem + r * Sh::NB, a.spins + (long long)(lat0 + r) * a.lat_stride, Sh::NB);
+    block_copy16_ldg(Ps, field_base<Real>(a, conf),
+                     (int)((Sh::N * sizeof(Real) + 15) & ~(size_t)15));
+    OffsetCache<QPT> off;
+    fill_offsets<LH, HH, NT, QPT>(off, (int)threadIdx.x);
+    __syncthreads();
+    uint32_t* S32[R];
+    int rep[R];
+    double beta[R];
+    float kb[R];
+    Acc acc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        S32[r] = reinterpret_cast<uint32_t*>(smem + r * Sh::NB);
+        rep[r] = lat0 + r - conf * a.nrep;
+        beta[r] = a.use_override ? a.beta_override
+                                 : a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep[r]]];
+        kb[r] = (float)(-2.0 * beta[r] * 1.4426950408889634);
+        acc[r] = Acc{0, 0, 0, 0, 0};
+    }
+    const uint32_t sweep0 =
+        a.use_override ? a.sweep_override : a.ctl[0] * (uint32_t)a.ptswapever;
+    const uint32_t kconf = (uint32_t)conf;
+#pragma unroll 1
+    for (int t = 0; t < a.nsweeps; ++t)
+        all_colours_r<Real, LH, HH, NT, QPT, R, false, VAC>(a, S32, Ps, off, sweep0 + (uint32_t)t,
+                                                             rep, kconf, beta, kb, acc);
+    all_colours_r<Real, LH, HH, NT, QPT, R, true, VAC>(a, S32, Ps, off, 0u, rep, kconf, beta, kb,
+                                                        acc);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const Acc tot = block_reduce(acc[r]);
+        if (threadIdx.x == 0) store_obs(a.obs + lat0 + r, tot);
+        __syncthreads();  // block_reduce's scratch is reused by the next replica
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        block_copy16(a.spins + (long long)(lat0 + r) * a.lat_stride, smem + r * Sh::NB, Sh::NB);
+}
+
 // Streaming form of the same kernel: one resident CTA per SM (MINB per SM) works through a
 // contiguous range of the group's lattices.  The next lattice's spins arrive by a bulk copy of
 // the tensor memory accelerator (completed on an mbarrier) into the second of two shared-memory
@@ -667,6 +774,18 @@ cudaError_t run_stream(const SweepArgs& a, int nlat, size_t smem, cudaStream_t s
     return cudaGetLastError();
 }
 
+// R replicas per CTA: nlat / R CTAs (whole configurations, R dividing the ladder)
+template <class Real, int LH, int HH, int NT, int MINB, bool VAC, int R>
+cudaError_t run_fixed_r(const SweepArgs& a, int nlat, size_t smem, cudaStream_t st, bool prep)
+{
+    auto k = sweep_fixed_r_kernel<Real, LH, HH, NT, MINB, VAC, R>;
+    if (prep) return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (a.nrep % R != 0 || a.lat0 % R != 0 || nlat % R != 0) return cudaErrorInvalidValue;
+    if (nlat == 0) return cudaSuccess;
+    k<<<nlat / R, NT, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
 using FixedFn = cudaError_t (*)(const SweepArgs&, int, size_t, cudaStream_t, bool);
 
 struct FixedEntry {
@@ -677,6 +796,7 @@ struct FixedEntry {
     FixedFn fn;
     bool stream = false;  // the streaming form
     int minb = 1;         // resident CTAs per SM the kernel is compiled for (MINB)
+    int rpc = 1;          // replicas of one configuration per CTA
 };
 
 // Shapes of the reference's configurations (L = 16, 24, 32, 48 with H = L) and the CTA sizes
@@ -700,6 +820,11 @@ const FixedEntry kFixed[] = {
     {false, 32, 32, 1024, true, true, run_stream<float, 16, 16, 1024, 1, true, true>, true},
     {false, 24, 24, 448, true, true, run_stream<float, 12, 12, 448, 2, true, true>, true, 2},
     {false, 16, 16, 128, true, true, run_stream<float, 8, 8, 128, 8, true, true>, true, 8},
+    // two replicas of one configuration per CTA (the autotuner times them against the above)
+    {false, 32, 32, 512, true, false, run_fixed_r<float, 16, 16, 512, 1, false, 2>, false, 1, 2},
+    {false, 32, 32, 512, true, true, run_fixed_r<float, 16, 16, 512, 1, true, 2>, false, 1, 2},
+    {false, 24, 24, 448, true, true, run_fixed_r<float, 12, 12, 448, 2, true, 2>, false, 2, 2},
+    {false, 16, 16, 128, true, true, run_fixed_r<float, 8, 8, 128, 4, true, 2>, false, 4, 2},
 };
 
 // Entries usable for a context: vacancy-free entries when it has no vacancy (where they exist),
@@ -920,14 +1045,14 @@ const HbmEntry kHbm[] = {
 
 }  // namespace
 
-int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, bool int_cpl, FixedChoice* out,
-                     int cap)
+int fixed_candidates(bool fp64, int L, int H, bool masks, bool vac, bool int_cpl, int nrep,
+                     FixedChoice* out, int cap)
 {
     if (masks || (!fp64 && !int_cpl)) return 0;
     int n = 0;
     for (const auto& e : kFixed)
-        if (usable(e, fp64, L, H, vac) && n < cap)
-            out[n++] = FixedChoice{e.nt, e.stage_p, e.stream, e.minb};
+        if (usable(e, fp64, L, H, vac) && nrep % e.rpc == 0 && n < cap)
+            out[n++] = FixedChoice{e.nt, e.stage_p, e.stream, e.minb, e.rpc};
     return n;
 }
 
@@ -936,7 +1061,7 @@ cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, const FixedCho
 {
     for (const auto& e : kFixed)
         if (usable(e, fp64, a.g.L, a.g.H, vac) && e.nt == ch.nt && e.stream == ch.stream &&
-            e.minb == ch.minb)
+            e.minb == ch.minb && e.rpc == ch.rpc)
             return e.fn(a, nlat, smem, st, prepare);
     return cudaErrorInvalidValue;
 }

@@ -28,6 +28,7 @@ FLAG_WOLFF_CS2, FLAG_WOLFF_CS4 = 128, 256  # Wolff growth over 2 / 4 CTAs per la
 FLAG_STREAM = 512  # streaming form of the shape-specialised kernels (testing)
 FLAG_WOLFF_SPLIT = 1024  # Wolff + sweeps of cold and hot slots on two streams (HBM form; testing)
 FLAG_WOLFF_BITS = 2048  # Wolff growth from bond activations decided beforehand (testing)
+FLAG_PAIRS = 4096  # two replicas of one configuration per CTA in the shape-specialised kernels
 
 SUM_FIELDS = ("mag", "absmag", "mag2", "mag4", "en", "en2", "strx_abs", "stry_abs", "strx2",
               "strx4", "stry2", "stry4", "str2", "str4", "absstr", "nem", "nbar", "nbarabs",

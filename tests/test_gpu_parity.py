@@ -555,3 +555,29 @@ def test_non_integer_couplings(engine_mod, oracle):
     np.testing.assert_array_equal(eng.slot_sums(0)[0], st["sums"])
     np.testing.assert_array_equal(eng.observables(0), obs)
     eng.close()
+
+
+@pytest.mark.parametrize("L,pp,nrep", [(32, 0.0, 32), (32, 0.05, 8), (24, 0.05, 24),
+                                        (16, 0.05, 16)])
+def test_pair_kernel_equals_per_lattice_kernel(engine_mod, oracle, L, pp, nrep):
+    """FP32: two replicas of one configuration per CTA (their lattices behind one shared copy of
+    the field, each quad position's field operands loaded once for both) against one CTA per
+    lattice: bitwise equal spins, sums and observables, over cycles with replica exchanges."""
+    jc = engine_mod
+    nconf = 3
+    out = []
+    for flags, bt in ((0, {32: 512, 24: 448, 16: 128}[L]), (jc.FLAG_PAIRS, 0)):
+        eng, _, _ = _setup(jc, oracle, L, L, nconf, nrep, jc.FP32_BATCHED, pp=pp, flags=flags,
+                           block_threads=bt)
+        eng.run(2, measure=False)
+        eng.run(3, measure=True)
+        cfg = eng.config()
+        out.append(([eng.spins(k, r) for k in range(nconf) for r in range(nrep)],
+                    eng.slot_sums(-1)[0], eng.observables(-1), cfg))
+        eng.close()
+    n = L ** 3
+    assert out[1][3]["smem_bytes"] == 2 * n + 4 * n, out[1][3]
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    np.testing.assert_array_equal(out[0][2], out[1][2])
