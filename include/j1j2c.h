@@ -64,6 +64,9 @@ extern "C" {
 #define J1J2C_FLAG_PAIRS 4096u   /* the shape-specialised kernels with two replicas of one
                                     configuration per CTA, sharing the field copy (testing; else
                                     tuned)                                                        */
+#define J1J2C_FLAG_MULTI 8192u   /* several lattice-shape groups (L = H = 16, 24, 32, 48): every
+                                    group's sweeps in one persistent launch (testing; else tuned
+                                    against one graph branch per group)                          */
 #define J1J2C_FLAG_WOLFF_CS2 128u /* Wolff growth over 2 CTAs per lattice (testing; else tuned)    */
 #define J1J2C_FLAG_WOLFF_CS4 256u /* Wolff growth over 4 CTAs per lattice (testing; else tuned);
                                      both flags: 2 CTAs for the coldest quarter of the slots, one
@@ -338,7 +341,8 @@ void j1j2c_results_destroy(void *res);
 int j1j2c_get_profile(void *ctx, double *sweep_ms, int64_t *sweep_launches, int64_t *attempts);
 
 /* Kernel configuration the context chose: threads per CTA, sites per thread per colour phase
- * (4 = quad path, 1 = per-site path), dynamic shared memory bytes per CTA. */
+ * (4 = quad path, 1 = per-site path), dynamic shared memory bytes per CTA (of the first group's
+ * kernel, or of the persistent launch over every group when the context uses it). */
 int j1j2c_get_config(void *ctx, int32_t *block_threads, int32_t *sites_per_thread,
                      int32_t *smem_bytes);
 

@@ -29,10 +29,11 @@ def _nvcc() -> str:
 
 def _sources():
     cu = [os.path.join(CSRC, f)
-          for f in ("sweep_fixed.cu", "kernels.cu", "wolff.cu", "enumerate.cu", "disorder.cu",
-                    "api.cu")]
+          for f in ("sweep_fixed.cu", "sweep_multi.cu", "kernels.cu", "wolff.cu", "enumerate.cu",
+                    "disorder.cu", "api.cu")]
     cpp = [os.path.join(CSRC, f) for f in ("host_model.cpp", "results.cpp")]
-    hdr = [os.path.join(CSRC, f) for f in ("device_common.cuh", "engine.h", "sweep_common.cuh")]
+    hdr = [os.path.join(CSRC, f) for f in ("device_common.cuh", "engine.h", "sweep_common.cuh",
+                                           "quad_sweep.cuh")]
     hdr.append(os.path.join(ROOT, "include", "j1j2c.h"))
     return cu, cpp, hdr
 

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <atomic>
 #include <limits>
 #include <map>
@@ -111,6 +112,13 @@ struct Ctx {
     // event pairs (the graph's event-record nodes retargeted before each launch); the pairs are
     // read after the run's final synchronisation, so profiling adds no host wait between cycles
     bool profile = false;
+    // several lattice-shape groups swept by one persistent launch (sweep_multi.cu) instead of one
+    // graph branch per group: chosen at the first run (multi_tuned), its device tables on first use
+    bool multi = false, multi_tuned = false;
+    GroupDesc* d_gdesc = nullptr;
+    int2* d_tasks = nullptr;
+    unsigned* d_queue = nullptr;
+    int ntasks = 0, multi_grid = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> pev0, pev1;
     int prof_pending = 0;
@@ -201,7 +209,8 @@ void release(Ctx* c)
                     c->d_acc,   c->d_vis,   c->d_last, c->d_ctl,   c->d_nocc,  c->d_rbase,
                     c->d_nreps, c->d_audit, c->d_labels, c->d_act, c->d_csize, c->d_err,
                     c->d_loc_s, c->d_loc_n, c->d_loc_samples, c->d_hist, c->d_hist_lo,
-                    c->d_hist_bs, c->d_trace, c->d_trace_tor, c->d_flips};
+                    c->d_hist_bs, c->d_trace, c->d_trace_tor, c->d_flips, c->d_gdesc,
+                    c->d_tasks, c->d_queue};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto s : c->side) cudaStreamDestroy(s);
@@ -661,8 +670,62 @@ cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int n
     return launch_measure_global(a, v, nlat, st);
 }
 
-// one PT cycle: every group's sweeps + observables (parallel branches), then swap / accumulate;
-// with profiling, events e0 / e1 bracket the sweep launches
+// Every group of the context has a tile of the persistent multi-shape kernel: FP32 with integer
+// J2, J3, no diluted bond, no flip counting, no test flag pinning another kernel, each shape one of
+// L = H = 16, 24, 32, 48 with a ladder that the tile's replica count divides
+bool multi_possible(Ctx* c)
+{
+    const uint32_t f = c->P.flags;
+    if (c->G.size() < 2 || c->P.precision != J1J2C_FP32_BATCHED || c->masks ||
+        !int_couplings(c) || c->diag.flip_counts ||
+        (f & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_GLOBAL | J1J2C_FLAG_CLUSTER |
+              J1J2C_FLAG_STREAM | J1J2C_FLAG_PAIRS)))
+        return false;
+    for (const Group& grp : c->G) {
+        const int kind = multi_tile_kind(grp.g.L, grp.g.H);
+        if (kind < 0 || grp.nrep % multi_tile_lattices(kind) != 0) return false;
+    }
+    return multi_smem_bytes() <= smem_budget(c);
+}
+
+// Every group's Wolff update (with J1J2C_FLAG_WOLFF), sweeps and observables of one PT cycle:
+// one group on st; several as parallel graph branches on the side streams, joined on st; or
+// (multi) the groups' Wolff updates on st, then one persistent launch over all of them.
+cudaError_t enqueue_sweeps(Ctx* c, cudaStream_t st, bool multi)
+{
+    cudaError_t e;
+    if (multi) {
+        for (const Group& grp : c->G)
+            if (c->wolff && (e = enqueue_wolff(c, grp, st)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(c->d_queue, 0, sizeof(unsigned), st)) != cudaSuccess) return e;
+        MultiArgs m{};
+        m.a = group_args(c, c->G[0]);  // group 0 starts at configuration 0: conf_base as is
+        m.groups = c->d_gdesc;
+        m.tasks = c->d_tasks;
+        m.ntasks = c->ntasks;
+        m.queue = c->d_queue;
+        return launch_multi(m, c->vac, c->multi_grid, st, false);
+    }
+    if (c->G.size() == 1) {
+        const Group& grp = c->G[0];
+        return enqueue_group(c, grp, grp.var, grp.nthreads, grp.smem, group_args(c, grp),
+                             grp.nlat(), st, true);
+    }
+    if ((e = cudaEventRecord(c->fork_ev, st)) != cudaSuccess) return e;
+    for (size_t k = 0; k < c->G.size(); ++k) {
+        const Group& grp = c->G[k];
+        if ((e = cudaStreamWaitEvent(c->side[k], c->fork_ev, 0)) != cudaSuccess) return e;
+        e = enqueue_group(c, grp, grp.var, grp.nthreads, grp.smem, group_args(c, grp),
+                          grp.nlat(), c->side[k], true);
+        if (e != cudaSuccess) return e;
+        if ((e = cudaEventRecord(c->join_ev[k], c->side[k])) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(st, c->join_ev[k], 0)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// one PT cycle: every group's sweeps + observables, then swap / accumulate; with profiling,
+// events e0 / e1 bracket the sweep launches
 cudaError_t enqueue_cycle(Ctx* c, int measure, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1)
 {
     cudaError_t e;
@@ -673,23 +736,7 @@ cudaError_t enqueue_cycle(Ctx* c, int measure, cudaStream_t st, cudaEvent_t e0, 
     const bool rec = c->profile || c->G.size() > 1;
     if (rec && (e = cudaEventRecordWithFlags(e0, st, cudaEventRecordExternal)) != cudaSuccess)
         return e;
-    if (c->G.size() == 1) {
-        const Group& grp = c->G[0];
-        e = enqueue_group(c, grp, grp.var, grp.nthreads, grp.smem, group_args(c, grp), grp.nlat(),
-                          st, true);
-        if (e != cudaSuccess) return e;
-    } else {
-        if ((e = cudaEventRecord(c->fork_ev, st)) != cudaSuccess) return e;
-        for (size_t k = 0; k < c->G.size(); ++k) {
-            const Group& grp = c->G[k];
-            if ((e = cudaStreamWaitEvent(c->side[k], c->fork_ev, 0)) != cudaSuccess) return e;
-            e = enqueue_group(c, grp, grp.var, grp.nthreads, grp.smem, group_args(c, grp),
-                              grp.nlat(), c->side[k], true);
-            if (e != cudaSuccess) return e;
-            if ((e = cudaEventRecord(c->join_ev[k], c->side[k])) != cudaSuccess) return e;
-            if ((e = cudaStreamWaitEvent(st, c->join_ev[k], 0)) != cudaSuccess) return e;
-        }
-    }
+    if ((e = enqueue_sweeps(c, st, c->multi && multi_possible(c))) != cudaSuccess) return e;
     if (rec && (e = cudaEventRecordWithFlags(e1, st, cudaEventRecordExternal)) != cudaSuccess)
         return e;
     // one group without profiling events: the swap follows that group's last kernel directly
@@ -1230,6 +1277,137 @@ int tune_split(Ctx* c, Group& grp)
     grp.split_bits = best.bits;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_split_cache[key] = best;
+    return J1J2C_OK;
+}
+
+// Device tables of the persistent multi-shape launch: one descriptor per group and the tile
+// queue, groups with the largest tiles first (a longest-first order, so the last tiles to start
+// are the shortest ones)
+int setup_multi(Ctx* c)
+{
+    if (c->d_gdesc) return J1J2C_OK;
+    const size_t ng = c->G.size();
+    std::vector<GroupDesc> gd(ng);
+    std::vector<int> order(ng);
+    std::vector<long long> work(ng);
+    for (size_t k = 0; k < ng; ++k) {
+        const Group& grp = c->G[k];
+        GroupDesc& d = gd[k];
+        d.spins = c->d_spins + grp.spin_off;
+        d.pf = c->d_pf + grp.p_off;
+        d.lat_stride = grp.lat_stride;
+        d.p_stride = grp.p_stride;
+        d.beta = c->d_beta + grp.rep0;
+        d.tor = c->d_tor + grp.rep0;
+        d.obs = c->d_obs + grp.rep0;
+        d.nrep = grp.nrep;
+        d.conf0 = grp.conf0;
+        d.kind = multi_tile_kind(grp.g.L, grp.g.H);
+        order[k] = (int)k;
+        work[k] = (long long)multi_tile_lattices(d.kind) * grp.g.N;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+    std::vector<int2> tasks;
+    for (const int k : order) {
+        const int r = multi_tile_lattices(gd[k].kind);
+        for (int l = 0; l < c->G[k].nlat(); l += r) tasks.push_back(make_int2(k, l));
+    }
+    int dev = 0, nsm = 0;
+    CK(c, cudaGetDevice(&dev));
+    CK(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    CK(c, dalloc(&c->d_gdesc, ng));
+    CK(c, dalloc(&c->d_tasks, tasks.size()));
+    CK(c, dalloc(&c->d_queue, 1));
+    CK(c, cudaMemcpy(c->d_gdesc, gd.data(), ng * sizeof(GroupDesc), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(c->d_tasks, tasks.data(), tasks.size() * sizeof(int2),
+                     cudaMemcpyHostToDevice));
+    c->ntasks = (int)tasks.size();
+    c->multi_grid = nsm < c->ntasks ? nsm : c->ntasks;
+    MultiArgs none{};
+    CK(c, launch_multi(none, c->vac, 0, nullptr, true));
+    return J1J2C_OK;
+}
+
+// One persistent launch over every group, or one graph branch per group: at the first run the
+// sweeps of one cycle in both forms are timed as graph replays on the live lattices (the fastest
+// of three), whose spins, observables and cluster sizes are then put back; the faster form is
+// kept for the life of the context.  Both give the same results bit for bit.
+int tune_multi(Ctx* c)
+{
+    if (c->multi_tuned) return J1J2C_OK;
+    c->multi_tuned = true;
+    c->multi = false;
+    if (!multi_possible(c)) return J1J2C_OK;
+    {
+        const int rc = setup_multi(c);
+        if (rc != J1J2C_OK) return rc;
+    }
+    if (c->P.flags & J1J2C_FLAG_MULTI) {
+        c->multi = true;
+        free_graphs(c);
+        return J1J2C_OK;
+    }
+    if (c->P.flags & J1J2C_FLAG_NO_GRAPH) return J1J2C_OK;
+    if (c->wolff && !c->d_labels) CK(c, dalloc(&c->d_labels, (size_t)c->lab_ints));
+    const size_t ne = (size_t)c->nentries;
+    uint8_t* keep_s = nullptr;
+    LatObs* keep_o = nullptr;
+    long long* keep_c = nullptr;
+    cudaError_t e = dev_malloc(&keep_s, (size_t)c->spin_bytes);
+    if (e == cudaSuccess) e = dev_malloc(&keep_o, ne * sizeof(LatObs));
+    if (e == cudaSuccess) e = dev_malloc(&keep_c, ne * sizeof(long long));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(keep_s, c->d_spins, (size_t)c->spin_bytes, cudaMemcpyDeviceToDevice,
+                            c->own);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(keep_o, c->d_obs, ne * sizeof(LatObs), cudaMemcpyDeviceToDevice,
+                            c->own);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(keep_c, c->d_csize, ne * sizeof(long long),
+                            cudaMemcpyDeviceToDevice, c->own);
+    float ms[2] = {0.0f, 0.0f};
+    for (int form = 0; form < 2 && e == cudaSuccess; ++form) {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        e = cudaStreamBeginCapture(c->own, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const cudaError_t e1 = enqueue_sweeps(c, c->own, form == 1);
+            e = cudaStreamEndCapture(c->own, &graph);
+            if (e1 != cudaSuccess) e = e1;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e == cudaSuccess) e = cudaGraphLaunch(exec, c->own);  // warm-up
+        for (int r = 0; r < 3 && e == cudaSuccess; ++r) {
+            e = cudaEventRecord(c->ev0, c->own);
+            if (e == cudaSuccess) e = cudaGraphLaunch(exec, c->own);
+            if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->own);
+            if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
+            float t = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, c->ev0, c->ev1);
+            if (e == cudaSuccess && (r == 0 || t < ms[form])) ms[form] = t;
+        }
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->d_spins, keep_s, (size_t)c->spin_bytes, cudaMemcpyDeviceToDevice,
+                            c->own);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->d_obs, keep_o, ne * sizeof(LatObs), cudaMemcpyDeviceToDevice,
+                            c->own);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->d_csize, keep_c, ne * sizeof(long long),
+                            cudaMemcpyDeviceToDevice, c->own);
+    cudaStreamSynchronize(c->own);
+    cudaFree(keep_s);
+    cudaFree(keep_o);
+    cudaFree(keep_c);
+    if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the multi-shape launch");
+    if (tune_log())
+        std::fprintf(stderr, "j1j2c tune multi-shape sweeps: branches %.3f ms, one launch %.3f ms\n",
+                     ms[0], ms[1]);
+    c->multi = ms[1] < ms[0];
+    free_graphs(c);
     return J1J2C_OK;
 }
 
@@ -1967,6 +2145,10 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
         if (rct == J1J2C_OK && c->wolff && bits_of(c, grp)) rct = ensure_act(c);
         if (rct != J1J2C_OK) return rct;
     }
+    {
+        const int rct = tune_multi(c);
+        if (rct != J1J2C_OK) return rct;
+    }
     const bool direct = (c->P.flags & J1J2C_FLAG_NO_GRAPH) != 0;
     if (!direct && !c->graph[m]) {
         int rc = build_graph(c, m);
@@ -2330,6 +2512,12 @@ int j1j2c_get_config(void* ctx, int32_t* block_threads, int32_t* sites_per_threa
 {
     if (!ctx) return J1J2C_EINVAL;
     Ctx* c = static_cast<Ctx*>(ctx);
+    if (c->multi && multi_possible(c)) {  // the persistent launch over every group
+        if (block_threads) *block_threads = multi_threads();
+        if (sites_per_thread) *sites_per_thread = 4;
+        if (smem_bytes) *smem_bytes = (int32_t)multi_smem_bytes();
+        return J1J2C_OK;
+    }
     const Group& grp = c->G[0];
     if (block_threads) *block_threads = grp.nthreads;
     if (sites_per_thread) *sites_per_thread = grp.var.quad ? 4 : 1;

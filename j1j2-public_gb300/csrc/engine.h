@@ -196,6 +196,34 @@ int fixed_hbm_threads(bool fp64, int L, int H, bool masks, bool int_cpl);
 cudaError_t launch_fixed_hbm(const SweepArgs& a, bool fp64, int colour, int t, int nlat, int rpt,
                              cudaStream_t st);
 
+// One persistent launch over several lattice-shape groups (sweep_multi.cu).  A tile is R
+// replicas of one configuration of a group; tile kinds exist for L = H = 16, 24, 32, 48.
+struct GroupDesc {
+    uint8_t* spins;           // the group's first lattice
+    const float* pf;          // the group's first configuration's FP32 field
+    long long lat_stride;     // bytes between lattices
+    long long p_stride;       // elements between configurations' fields
+    const double* beta;       // the group's first replica-indexed entry (by slot)
+    const int* tor;           // temp_of_rep, same indexing
+    LatObs* obs;              // observables of the group's first lattice
+    int nrep, conf0;          // ladder length; the group's first configuration in the context
+    int kind;                 // tile kind (multi_tile_kind)
+};
+struct MultiArgs {
+    SweepArgs a;              // couplings, cycle counter, sweeps, key schedule of the context's
+                              // conf_base (a tile passes conf0 + its configuration)
+    const GroupDesc* groups;  // device array
+    const int2* tasks;        // (group, first lattice of the tile), largest tiles first
+    int ntasks;
+    unsigned* queue;          // [0]: next task, zero at each launch
+};
+int multi_tile_kind(int L, int H);   // -1: the shape has no tile
+int multi_tile_lattices(int kind);   // replicas of one configuration per tile
+size_t multi_smem_bytes();           // dynamic shared memory of the launch (its largest tile)
+int multi_threads();                 // threads per CTA
+// grid: CTAs (at most one per SM); prepare: only raise the shared-memory limit
+cudaError_t launch_multi(const MultiArgs& m, bool vac, int grid, cudaStream_t st, bool prepare);
+
 size_t sweep_smem_bytes(const Geo& g, const SweepVariant& v);
 cudaError_t prepare_sweep_variant(const SweepVariant& v, size_t smem);
 cudaError_t launch_sweep(const SweepArgs& a, const SweepVariant& v, int nblocks, int nthreads,

@@ -29,6 +29,7 @@ FLAG_STREAM = 512  # streaming form of the shape-specialised kernels (testing)
 FLAG_WOLFF_SPLIT = 1024  # Wolff + sweeps of cold and hot slots on two streams (HBM form; testing)
 FLAG_WOLFF_BITS = 2048  # Wolff growth from bond activations decided beforehand (testing)
 FLAG_PAIRS = 4096  # two replicas of one configuration per CTA in the shape-specialised kernels
+FLAG_MULTI = 8192  # every lattice-shape group in one persistent launch (testing)
 
 SUM_FIELDS = ("mag", "absmag", "mag2", "mag4", "en", "en2", "strx_abs", "stry_abs", "strx2",
               "strx4", "stry2", "stry4", "str2", "str4", "absstr", "nem", "nbar", "nbarabs",

@@ -49,9 +49,9 @@ def test_batched_fp32_kernel_decisions_match_fp64_replay(engine_mod, oracle):
     eng, betas = _batched_engine(jc, jc.FP32_BATCHED)
     eng.run(50, measure=False)  # equilibrate (the tuner has picked the kernel by now)
     cfg = eng.config()
-    # the shape-specialised kernel, lattice (32 KiB) and FP32 field (128 KiB) in shared memory,
-    # a spin word (four sites) per thread and colour phase
-    assert cfg["smem_bytes"] == L3 ** 3 + 4 * L3 ** 3, cfg
+    # the shape-specialised kernel: one or two lattices (32 KiB each) and their FP32 field
+    # (128 KiB) in shared memory, a spin word (four sites) per thread and colour phase
+    assert cfg["smem_bytes"] in (L3 ** 3 + 4 * L3 ** 3, 2 * L3 ** 3 + 4 * L3 ** 3), cfg
     assert cfg["sites_per_thread"] == 4 and cfg["block_threads"] in (512, 1024), cfg
     confs = (0, 21, 42, 63)
     before = {(k, r): eng.spins(k, r).copy() for k in confs for r in range(NREP3)}

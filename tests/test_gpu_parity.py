@@ -581,3 +581,48 @@ def test_pair_kernel_equals_per_lattice_kernel(engine_mod, oracle, L, pp, nrep):
         np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(out[0][1], out[1][1])
     np.testing.assert_array_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("pp,wolff", [(0.0, False), (0.05, False), (0.05, True)])
+def test_multi_shape_launch_equals_single_shape_contexts(engine_mod, oracle, pp, wolff):
+    """Lattice shapes L = 16, 24, 32, 48 in one context swept by one persistent launch (flag
+    8192: a CTA per SM takes tiles of R replicas of one configuration from one queue) equal
+    single-shape contexts with the same Philox keys bit for bit: spins, running sums, maps and
+    observables over cycles with replica exchanges (and Wolff updates)."""
+    jc = engine_mod
+    groups = [(16, 16, 2, 16), (24, 24, 1, 24), (32, 32, 2, 32), (48, 48, 1, 48)]
+    flags = jc.FLAG_MULTI | (jc.FLAG_WOLFF if wolff else 0)
+    eng = jc.Engine(groups=groups, precision=jc.FP32_BATCHED, seed=SEED, flags=flags)
+    confs, conf = [], 0
+    for L, H, n, r in groups:
+        for _ in range(n):
+            p = jc.disorder(L, H, SEED + conf)
+            occu = jc.setup_vacancies(SEED + conf, L, H, pp)[0] if pp > 0 else None
+            eng.set_disorder(conf, p, occu)
+            eng.set_ladder(conf, _betas(r))
+            eng.init_spins(conf, jc.START_HOT)
+            confs.append((L, H, r, p, occu))
+            conf += 1
+    eng.reset_measurements()
+    eng.run(2, measure=False)
+    eng.reset_measurements()
+    eng.run(3, measure=True)
+    cfg = eng.config()
+    assert cfg["block_threads"] == 512 and cfg["smem_bytes"] == 2 * 32 ** 3 + 4 * 32 ** 3, cfg
+    for k, (L, H, r, p, occu) in enumerate(confs):
+        single = jc.Engine(L, H, nconf=1, nreplica=r, precision=jc.FP32_BATCHED, seed=SEED,
+                           conf_base=k, flags=jc.FLAG_WOLFF if wolff else 0)
+        single.set_disorder(0, p, occu)
+        single.set_ladder(0, _betas(r))
+        single.init_spins(0, jc.START_HOT)
+        single.reset_measurements()
+        single.run(2, measure=False)
+        single.reset_measurements()
+        single.run(3, measure=True)
+        for rep in range(r):
+            np.testing.assert_array_equal(eng.spins(k, rep), single.spins(0, rep))
+        np.testing.assert_array_equal(eng.slot_sums(k)[0], single.slot_sums(0)[0])
+        np.testing.assert_array_equal(eng.maps(k)[0], single.maps(0)[0])
+        np.testing.assert_array_equal(eng.observables(k), single.observables(0))
+        single.close()
+    eng.close()
