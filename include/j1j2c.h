@@ -67,6 +67,10 @@ extern "C" {
 #define J1J2C_FLAG_MULTI 8192u   /* several lattice-shape groups (L = H = 16, 24, 32, 48): every
                                     group's sweeps in one persistent launch (testing; else tuned
                                     against one graph branch per group)                          */
+#define J1J2C_FLAG_COOP 16384u   /* small batches: every colour phase, sweep and the observables of
+                                    a cycle in one cooperative launch with grid barriers between
+                                    the phases (testing; slower than one launch per phase,
+                                    never chosen by the tuner)                                   */
 #define J1J2C_FLAG_WOLFF_CS2 128u /* Wolff growth over 2 CTAs per lattice (testing; else tuned)    */
 #define J1J2C_FLAG_WOLFF_CS4 256u /* Wolff growth over 4 CTAs per lattice (testing; else tuned);
                                      both flags: 2 CTAs for the coldest quarter of the slots, one

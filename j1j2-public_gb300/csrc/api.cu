@@ -88,6 +88,7 @@ struct Ctx {
     uint8_t* d_act = nullptr;       // Wolff bond activation bits, one byte per site (first use)
     long long* d_csize = nullptr;   // Wolff cluster size of the last update, per replica
     int* d_err = nullptr;           // device error word (union-find retry overflow)
+    unsigned* d_gbar = nullptr;     // grid-barrier words of the cooperative form, two per group
     int uf_tries = 1 << 20;         // union-find attempts per bond (j1j2c_set_retry_budget)
     long long lab_ints = 0;
     bool wolff = false;
@@ -210,7 +211,7 @@ void release(Ctx* c)
                     c->d_nreps, c->d_audit, c->d_labels, c->d_act, c->d_csize, c->d_err,
                     c->d_loc_s, c->d_loc_n, c->d_loc_samples, c->d_hist, c->d_hist_lo,
                     c->d_hist_bs, c->d_trace, c->d_trace_tor, c->d_flips, c->d_gdesc,
-                    c->d_tasks, c->d_queue};
+                    c->d_tasks, c->d_queue, c->d_gbar};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto s : c->side) cudaStreamDestroy(s);
@@ -654,6 +655,14 @@ cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int n
         return launch_sweep_cluster(a, v, nlat, st);
     }
     if (!v.global) return launch_sweep(a, v, nlat, nthreads, smem, st);
+    if (v.coop && c->d_gbar) {  // every phase in one cooperative launch
+        const size_t gi = (size_t)(&grp - c->G.data());
+        unsigned* bar = c->d_gbar + 2 * (gi < c->G.size() ? gi : 0);
+        if ((e = cudaMemsetAsync(a.obs + a.lat0, 0, sizeof(LatObs) * nlat, st)) != cudaSuccess)
+            return e;
+        if ((e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st)) != cudaSuccess) return e;
+        return launch_sweep_coop(a, v, nlat, bar, st, false);
+    }
     // one launch per colour phase: the observables are zeroed first (no sweep reads them), so
     // every launch after the first follows a kernel of the same chain and may overlap its tail
     // (programmatic dependent launch: each kernel waits for its predecessor before any access)
@@ -832,16 +841,30 @@ int time_variant(Ctx* c, Group& grp, const SweepVariant& v, int nthreads, size_t
         return exec ? cudaGraphLaunch(exec, c->own)
                     : enqueue_group(c, grp, v, nthreads, smem, a, nlat, c->own, false);
     };
+    // one untimed cycle, then one timed to size the timings: each covers at least about 1 ms of
+    // cycles (a single small-batch cycle of tens of microseconds ranks candidates by launch
+    // jitter)
     if (e == cudaSuccess) e = once();
-    // the fastest of three timings of two cycles each (close candidates, noisy neighbours)
+    int reps = 2;
+    {
+        float t0 = 0.0f;
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev0, c->own);
+        if (e == cudaSuccess) e = once();
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->own);
+        if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t0, c->ev0, c->ev1);
+        if (e == cudaSuccess && t0 > 0.0f && t0 < 0.5f) reps = std::min(64, (int)(1.0f / t0) + 1);
+    }
+    // the fastest of three timings (close candidates, noisy neighbours)
     ms = 0.0f;
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
         e = cudaEventRecord(c->ev0, c->own);
-        for (int r = 0; r < 2 && e == cudaSuccess; ++r) e = once();
+        for (int r = 0; r < reps && e == cudaSuccess; ++r) e = once();
         if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->own);
         if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
         float t = 0.0f;
         if (e == cudaSuccess) e = cudaEventElapsedTime(&t, c->ev0, c->ev1);
+        t /= (float)reps;  // per cycle: candidates are timed over different cycle counts
         if (e == cudaSuccess && (k == 0 || t < ms)) ms = t;
     }
     cudaStreamSynchronize(c->own);
@@ -938,7 +961,14 @@ bool small_batch_ok(Ctx* c, const Group& grp)
 // that divides H/2 (four sites or one site per thread), and one launch per colour phase with one
 // site per thread in CTAs of 32-256 threads; the fastest is kept, cached per (device,
 // precision, L, H, lattice count, bond dilution, vacancies).
-enum SmallKind { kKeep = 0, kSiteCta = 1, kClusterQuad = 2, kClusterSite = 3, kGlobalSite = 4 };
+enum SmallKind {
+    kKeep = 0,
+    kSiteCta = 1,
+    kClusterQuad = 2,
+    kClusterSite = 3,
+    kGlobalSite = 4,
+    kGlobalCoop = 5  // kGlobalSite's phases in one cooperative launch
+};
 struct SmallChoice {
     int kind, cs, nt;
 };
@@ -978,7 +1008,15 @@ int tune_small_batch(Ctx* c, Group& grp)
                         c->vac);
     SmallChoice best{kKeep, 0, 0};
     bool known = false;
-    {
+    if (c->P.flags & J1J2C_FLAG_COOP) {  // pinned: the cooperative form, 64 threads per CTA
+        SweepVariant vc = global_site_variant(c, grp.var.fp64, 64);
+        vc.coop = true;
+        SweepArgs probe = group_args(c, grp);
+        if (launch_sweep_coop(probe, vc, grp.nlat(), nullptr, nullptr, true) != cudaSuccess)
+            return fail(c, J1J2C_EINVAL, "the cooperative form does not fit this batch");
+        best = SmallChoice{kGlobalCoop, 0, 64};
+        known = true;
+    } else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_small_cache.find(key);
         if (it != g_small_cache.end()) {
@@ -1028,6 +1066,10 @@ int tune_small_batch(Ctx* c, Group& grp)
                           SmallChoice{kGlobalSite, 0, nt});
             if (rc != J1J2C_OK) return rc;
         }
+        // (the same phases in one cooperative launch per cycle, grid barriers instead of kernel
+        // boundaries, is slower on both the L = 16 single lattice and 16 lattices of 24^3: a
+        // barrier through L2 costs more than a programmatic dependent launch; J1J2C_FLAG_COOP
+        // pins it)
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_small_cache[key] = best;
     }
@@ -1039,7 +1081,11 @@ int tune_small_batch(Ctx* c, Group& grp)
             grp.nthreads = best.nt;
             break;
         case kGlobalSite:
+        case kGlobalCoop:
+            if (best.kind == kGlobalCoop && !c->d_gbar)
+                CK(c, dalloc(&c->d_gbar, 2 * c->G.size()));
             grp.var = global_site_variant(c, grp.var.fp64, best.nt);
+            grp.var.coop = best.kind == kGlobalCoop;
             grp.smem = 0;
             grp.nthreads = best.nt;
             break;
@@ -2184,15 +2230,16 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
     }
     CK(c, cudaGetLastError());
     bool bounded = c->wolff;  // kernels whose bounded waits or retries report through d_err
-    for (const Group& grp : c->G) bounded = bounded || grp.var.stream;
+    for (const Group& grp : c->G) bounded = bounded || grp.var.stream || grp.var.coop;
     if (bounded) {
         int herr = 0;
         const int rc = take_device_error(c, herr);
         if (rc != J1J2C_OK) return rc;
         if (herr)
             return fail(c, J1J2C_ETIMEOUT,
-                        "a bounded device wait gave up (Wolff union-find retries or a bulk-copy "
-                        "wait of the streaming sweep kernel)");
+                        "a bounded device wait gave up (Wolff union-find retries, a bulk-copy "
+                        "wait of the streaming sweep kernel or a grid barrier of the cooperative "
+                        "form)");
     }
     return J1J2C_OK;
 }

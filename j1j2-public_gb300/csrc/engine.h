@@ -151,6 +151,8 @@ struct SweepVariant {
                    // quad: four sites per thread, else one)
     int rpt;       // shape-specialised HBM kernel: replicas per thread (1, 2 or 4)
     int rpc;       // shape-specialised shared-memory kernel: replicas per CTA (0 or 1: one)
+    bool coop;     // global-memory form: every colour phase, sweep and the observables in one
+                   // cooperative launch with grid barriers between the phases
     int threads;   // threads per CTA of the generic global-memory kernels (0: 256) and of the
                    // cluster kernel (0: 512)
 };
@@ -161,6 +163,10 @@ cudaError_t launch_sweep_global(const SweepArgs& a, const SweepVariant& v, int c
                                 int nlat, cudaStream_t st);
 cudaError_t launch_measure_global(const SweepArgs& a, const SweepVariant& v, int nlat,
                                   cudaStream_t st);
+// The cooperative form (v.coop): bar two zeroed words, a.obs of the lattices zeroed; with check,
+// nothing is launched and the result says whether every CTA can be resident at once
+cudaError_t launch_sweep_coop(const SweepArgs& a, const SweepVariant& v, int nlat, unsigned* bar,
+                              cudaStream_t st, bool check);
 
 // Cluster path: CTAs per lattice for a shape (0: not available), and the launch (PTSWAPEVER
 // sweeps and the observables, added into a.obs, which the caller zeroes first).

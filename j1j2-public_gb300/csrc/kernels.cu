@@ -791,6 +791,122 @@ __global__ void __launch_bounds__(256) measure_global_kernel(SweepArgs a)
     }
 }
 
+// ------------------------------------------------------------------------------------------------
+// Small batches in one cooperative launch: the colour phases of the global-memory form, every
+// sweep of the cycle and the observable reduction in one kernel whose CTAs are all resident (a
+// cooperative launch), a grid-wide barrier between colour phases instead of a kernel boundary.
+// Same per-site / per-quad arithmetic, Philox words and integer sums as the one-launch-per-colour
+// form, so the results are bit for bit those of every other kernel.
+// ------------------------------------------------------------------------------------------------
+constexpr int kGridWait = 1 << 22;  // polls of one grid barrier before it gives up
+
+// Grid-wide barrier: bar[0] counts arrivals, bar[1] the barriers passed (both zero at the
+// launch).  Thread 0 of each CTA arrives after the CTA's barrier and a device-scope fence (which
+// publishes the CTA's writes); the last arrival resets the count and releases the others, who
+// wait at most kGridWait polls (a wait that gives up sets err and goes on: nothing hangs, and the
+// host reports J1J2C_ETIMEOUT).
+__device__ __forceinline__ void grid_barrier(unsigned* bar, unsigned nblocks, unsigned& passed,
+                                             int* err)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned want = passed + 1u;
+        __threadfence();
+        if (atomicAdd(&bar[0], 1u) == nblocks - 1u) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            atomicExch(&bar[1], want);
+        } else {
+            int it = 0;
+            while (*reinterpret_cast<volatile unsigned*>(&bar[1]) != want) {
+                if (++it >= kGridWait) {
+                    if (err) atomicExch(err, 1);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        passed = want;
+    }
+    __syncthreads();
+}
+
+// Grid (work items / CTA, lattices), every CTA resident; bar: two zeroed words; a.obs of the
+// launch's lattices zeroed before it
+template <class Real, bool QUAD, bool MASKS>
+__global__ void __launch_bounds__(256) sweep_coop_kernel(SweepArgs a, unsigned* bar)
+{
+    const Geo g = a.g;
+    const int lat = a.lat0 + (int)blockIdx.y;
+    const int conf = lat / a.nrep;
+    const int rep = lat - conf * a.nrep;
+    uint8_t* S = a.spins + (long long)lat * a.lat_stride;
+    const Real* P = field_base<Real>(a, conf);
+    const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
+    double beta;
+    uint32_t sweep0;
+    if (a.use_override) {
+        beta = a.beta_override;
+        sweep0 = a.sweep_override;
+    } else {
+        beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+        sweep0 = a.ctl[0] * (uint32_t)a.ptswapever;
+    }
+    const float kb = (float)(-2.0 * beta * 1.4426950408889634);
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    const int item = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int per = QUAD ? (g.Nc >> 2) : g.Nc;
+    const unsigned nblocks = gridDim.x * gridDim.y;
+    unsigned passed = 0;
+    int* fl = flip_row(a, conf, rep);
+    Acc acc{0, 0, 0, 0, 0};
+#pragma unroll 1
+    for (int t = 0; t < a.nsweeps; ++t)
+#pragma unroll 1
+        for (int colour = 0; colour < 8; ++colour) {
+            if (item < per) {
+                const uint32_t sweep = sweep0 + (uint32_t)t;
+                if constexpr (QUAD) {
+                    quad_step<Real, MASKS, false>(a, g,
+                                                  CompactSpins(reinterpret_cast<uint32_t*>(S), g),
+                                                  P, BM, colour, item, sweep, (uint32_t)rep, k0,
+                                                  k1, beta, kb, acc, fl);
+                } else {
+                    const int X = item % g.Lh, r = item / g.Lh;
+                    site_step<Real, MASKS, kModeSweep, false>(a, g, FlatBytes{S}, P, BM, nullptr,
+                                                              colour, X, r % g.Lh, r / g.Lh,
+                                                              sweep, (uint32_t)rep, k0, k1, beta,
+                                                              kb, acc, fl);
+                }
+            }
+            grid_barrier(bar, nblocks, passed, a.err);
+        }
+    // observables: this thread's item in every colour (integer sums: any order gives the same)
+    if (item < per)
+#pragma unroll 1
+        for (int c = 0; c < 8; ++c) {
+            if constexpr (QUAD) {
+                quad_step<Real, MASKS, true>(a, g,
+                                             CompactSpins(reinterpret_cast<uint32_t*>(S), g), P,
+                                             BM, c, item, 0u, 0u, 0u, 0u, 0.0, 0.0f, acc);
+            } else {
+                const int X = item % g.Lh, r = item / g.Lh;
+                site_step<Real, MASKS, kModeSweep, true>(a, g, FlatBytes{S}, P, BM, nullptr, c,
+                                                         X, r % g.Lh, r / g.Lh, 0u, 0u, 0u, 0u,
+                                                         0.0, 0.0f, acc);
+            }
+        }
+    const Acc tot = block_reduce(acc);
+    if (threadIdx.x == 0) {
+        LatObs* o = a.obs + lat;
+        atomicAdd(reinterpret_cast<unsigned long long*>(&o->eacc), (unsigned long long)tot.e);
+        atomicAdd(&o->M, tot.M);
+        atomicAdd(&o->SX, tot.SX);
+        atomicAdd(&o->SY, tot.SY);
+        atomicAdd(&o->NB, tot.NB);
+    }
+}
+
 // HOT (device Philox), FER, STR starts for every replica of one conf; vacancies stored as 0
 __global__ void init_kernel(InitArgs a)
 {
@@ -923,6 +1039,55 @@ cudaError_t global_dispatch(const SweepArgs& a, const SweepVariant& v, int colou
                    : global_pass<Real, false, false>(a, colour, t, nlat, nt, st, measure);
 }
 }  // namespace
+
+namespace {
+template <class Real, bool QUAD, bool MASKS>
+cudaError_t coop_launch(const SweepArgs& a, int nlat, int nt, unsigned* bar, cudaStream_t st,
+                        bool check)
+{
+    auto k = sweep_coop_kernel<Real, QUAD, MASKS>;
+    const int per = QUAD ? (a.g.Nc >> 2) : a.g.Nc;
+    const int gx = (per + nt - 1) / nt;
+    if (check) {  // every CTA must be resident at once
+        int dev = 0, nsm = 0, per_sm = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, nt, 0);
+        if (e != cudaSuccess) return e;
+        return (long long)gx * nlat <= (long long)per_sm * nsm ? cudaSuccess
+                                                                : cudaErrorCooperativeLaunchTooLarge;
+    }
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)gx, (unsigned)nlat);
+    cfg.blockDim = dim3((unsigned)nt);
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, a, bar);
+}
+}  // namespace
+
+cudaError_t launch_sweep_coop(const SweepArgs& a, const SweepVariant& v, int nlat, unsigned* bar,
+                              cudaStream_t st, bool check)
+{
+    const int nt = v.threads > 0 ? v.threads : 64;
+    if (nt > 256 || nt % 32) return cudaErrorInvalidValue;
+    if (v.fp64) {
+        if (v.quad)
+            return v.masks ? coop_launch<double, true, true>(a, nlat, nt, bar, st, check)
+                           : coop_launch<double, true, false>(a, nlat, nt, bar, st, check);
+        return v.masks ? coop_launch<double, false, true>(a, nlat, nt, bar, st, check)
+                       : coop_launch<double, false, false>(a, nlat, nt, bar, st, check);
+    }
+    if (v.quad)
+        return v.masks ? coop_launch<float, true, true>(a, nlat, nt, bar, st, check)
+                       : coop_launch<float, true, false>(a, nlat, nt, bar, st, check);
+    return v.masks ? coop_launch<float, false, true>(a, nlat, nt, bar, st, check)
+                   : coop_launch<float, false, false>(a, nlat, nt, bar, st, check);
+}
 
 // ------------------------------------------------------------------------------------------------
 // Lattices too large for one CTA's shared memory but not for a thread-block cluster's (L = 96:

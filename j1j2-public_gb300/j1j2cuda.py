@@ -30,6 +30,7 @@ FLAG_WOLFF_SPLIT = 1024  # Wolff + sweeps of cold and hot slots on two streams (
 FLAG_WOLFF_BITS = 2048  # Wolff growth from bond activations decided beforehand (testing)
 FLAG_PAIRS = 4096  # two replicas of one configuration per CTA in the shape-specialised kernels
 FLAG_MULTI = 8192  # every lattice-shape group in one persistent launch (testing)
+FLAG_COOP = 16384  # small batches: a cycle's colour phases in one cooperative launch (testing)
 
 SUM_FIELDS = ("mag", "absmag", "mag2", "mag4", "en", "en2", "strx_abs", "stry_abs", "strx2",
               "strx4", "stry2", "stry4", "str2", "str4", "absstr", "nem", "nbar", "nbarabs",

@@ -626,3 +626,48 @@ def test_multi_shape_launch_equals_single_shape_contexts(engine_mod, oracle, pp,
         np.testing.assert_array_equal(eng.observables(k), single.observables(0))
         single.close()
     eng.close()
+
+
+@pytest.mark.parametrize("L,H,nconf,nrep,pp,ptswapever", [(16, 16, 1, 1, 0.05, 1),
+                                                           (24, 24, 1, 16, 0.0, 5),
+                                                           (32, 8, 2, 2, 0.1, 5)])
+def test_cooperative_small_batch_fp64_bit_identical(engine_mod, oracle, L, H, nconf, nrep, pp,
+                                                    ptswapever):
+    """Small batches with every colour phase, sweep and the observables of a cycle in one
+    cooperative launch (flag 16384; grid barriers between the phases): FP64 equals the replay
+    bit for bit, the LOCAL shape (one lattice, one sweep per cycle) and the PT configuration's
+    shape included."""
+    jc = engine_mod
+    betas = _betas(nrep) if nrep > 1 else np.array([1.0 / 9.5])
+    eng, models, _ = _setup(jc, oracle, L, H, nconf, nrep, jc.FP64_PLAIN, pp=pp,
+                            flags=jc.FLAG_COOP, ptswapever=ptswapever, betas=betas)
+    eng.run(3, measure=False)
+    eng.reset_measurements()
+    eng.run(4, measure=True)
+    assert eng.config()["smem_bytes"] == 0 and eng.config()["block_threads"] == 64
+    for k in range(nconf):
+        st = oracle.new_pt_state(np.stack([oracle.hot_spins_philox(L, H, SEED, k, q) *
+                                           models[k].occu for q in range(nrep)]))
+        models[k].replay_pt(st, betas, ptswapever, 3, 0, SEED, k, False, 1)
+        obs = models[k].replay_pt(st, betas, ptswapever, 4, 3, SEED, k, True, 1)
+        for r in range(nrep):
+            np.testing.assert_array_equal(eng.spins(k, r), st["spins"][r])
+        np.testing.assert_array_equal(eng.slot_sums(k)[0], st["sums"])
+        np.testing.assert_array_equal(eng.observables(k), obs)
+    eng.close()
+
+
+def test_cooperative_small_batch_fp32_bitwise(engine_mod, oracle):
+    """FP32: the cooperative form equals the generic shared-memory kernels bit for bit."""
+    jc = engine_mod
+    out = []
+    for flags in (jc.FLAG_NO_FIXED, jc.FLAG_COOP):
+        eng, _, _ = _setup(jc, oracle, 32, 16, 2, 3, jc.FP32_BATCHED, pp=0.05, flags=flags)
+        eng.run(4, measure=True)
+        out.append(([eng.spins(k, r) for k in range(2) for r in range(3)],
+                    eng.slot_sums(-1)[0], eng.observables(-1)))
+        eng.close()
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    np.testing.assert_array_equal(out[0][2], out[1][2])
