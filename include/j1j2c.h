@@ -71,6 +71,11 @@ extern "C" {
                                     a cycle in one cooperative launch with grid barriers between
                                     the phases (testing; slower than one launch per phase,
                                     never chosen by the tuner)                                   */
+#define J1J2C_FLAG_REPLICA 32768u /* small batches: the lattice replicated in every CTA of a
+                                     thread-block cluster (the largest of 16, 8, 4, 2 CTAs that
+                                     fits), every sweep and the observables of a cycle in one
+                                     launch (testing; slower than one launch per phase, never
+                                     chosen by the tuner)                                        */
 #define J1J2C_FLAG_WOLFF_CS2 128u /* Wolff growth over 2 CTAs per lattice (testing; else tuned)    */
 #define J1J2C_FLAG_WOLFF_CS4 256u /* Wolff growth over 4 CTAs per lattice (testing; else tuned);
                                      both flags: 2 CTAs for the coldest quarter of the slots, one

@@ -649,6 +649,7 @@ cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int n
             return enqueue_split(c, grp, v, a, k, split_cs_of(c, grp), st, bits_of(c, grp));
     }
     if (cycle && c->wolff && (e = enqueue_wolff(c, grp, st)) != cudaSuccess) return e;
+    if (v.rep_cs > 0) return launch_sweep_rep(a, v, nlat, st, false);  // writes the observables
     if (v.cluster > 0) {
         if ((e = cudaMemsetAsync(a.obs + a.lat0, 0, sizeof(LatObs) * nlat, st)) != cudaSuccess)
             return e;
@@ -967,12 +968,42 @@ enum SmallKind {
     kClusterQuad = 2,
     kClusterSite = 3,
     kGlobalSite = 4,
-    kGlobalCoop = 5  // kGlobalSite's phases in one cooperative launch
+    kGlobalCoop = 5,  // kGlobalSite's phases in one cooperative launch
+    kRepCluster = 6   // the lattice replicated in every CTA of a cluster of cs
 };
 struct SmallChoice {
     int kind, cs, nt;
 };
 std::map<std::tuple<int, bool, int, int, int, bool, bool>, SmallChoice> g_small_cache;
+
+// The replicated-lattice cluster form with cs CTAs per lattice: one thread per site of a CTA's
+// share of a colour (up to 1024 threads, which then loop)
+SweepVariant rep_variant(Ctx* c, bool fp64, int cs, int L, int H)
+{
+    SweepVariant v{};
+    v.fp64 = fp64;
+    v.masks = c->masks;
+    v.vac = c->vac;
+    v.mode = kModeSweep;
+    v.rep_cs = cs;
+    const int per = (L / 2) * (L / 2) * (H / 2) / cs;
+    v.threads = std::min(1024, ((per + 31) / 32) * 32);
+    return v;
+}
+
+// Can the replicated-lattice form with cs CTAs per lattice run this group (shape divides, the
+// cluster fits an SM set)?
+bool rep_fits(Ctx* c, const Group& grp, int cs)
+{
+    if (grp.g.Nc % (4 * cs) != 0) return false;
+    const SweepVariant v = rep_variant(c, grp.var.fp64, cs, grp.g.L, grp.g.H);
+    const SweepArgs probe = group_args(c, grp);
+    if (launch_sweep_rep(probe, v, grp.nlat(), nullptr, true) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return true;
+}
 
 // One site per thread in one CTA per lattice (the generic kernel)
 int site_cta_variant(Ctx* c, Group& grp, SweepVariant& v, size_t& smem, int& nt)
@@ -1016,6 +1047,14 @@ int tune_small_batch(Ctx* c, Group& grp)
             return fail(c, J1J2C_EINVAL, "the cooperative form does not fit this batch");
         best = SmallChoice{kGlobalCoop, 0, 64};
         known = true;
+    } else if (c->P.flags & J1J2C_FLAG_REPLICA) {  // pinned: the largest cluster that fits
+        for (const int cs : {16, 8, 4, 2})
+            if (rep_fits(c, grp, cs)) {
+                best = SmallChoice{kRepCluster, cs, 0};
+                known = true;
+                break;
+            }
+        if (!known) return fail(c, J1J2C_EINVAL, "the replicated-lattice form does not fit this batch");
     } else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_small_cache.find(key);
@@ -1066,10 +1105,12 @@ int tune_small_batch(Ctx* c, Group& grp)
                           SmallChoice{kGlobalSite, 0, nt});
             if (rc != J1J2C_OK) return rc;
         }
-        // (the same phases in one cooperative launch per cycle, grid barriers instead of kernel
-        // boundaries, is slower on both the L = 16 single lattice and 16 lattices of 24^3: a
-        // barrier through L2 costs more than a programmatic dependent launch; J1J2C_FLAG_COOP
-        // pins it)
+        // (Two one-launch-per-cycle forms are slower on both the L = 16 single lattice and 16
+        // lattices of 24^3 and are not candidates: the same phases in one cooperative launch, grid
+        // barriers through L2 instead of kernel boundaries (J1J2C_FLAG_COOP pins it); and the
+        // lattice replicated in every CTA of a cluster with cluster barriers (J1J2C_FLAG_REPLICA).
+        // An FP64 colour phase takes ~3 us however many SMs share it, the latency of one site's
+        // dependent FP64 chain, so fewer launch boundaries save little and fewer SMs cost more.)
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_small_cache[key] = best;
     }
@@ -1094,6 +1135,11 @@ int tune_small_batch(Ctx* c, Group& grp)
             if (rc != J1J2C_OK) return rc;
             break;
         }
+        case kRepCluster:
+            grp.var = rep_variant(c, grp.var.fp64, best.cs, grp.g.L, grp.g.H);
+            grp.smem = rep_smem_bytes(grp.g, grp.var.fp64);
+            grp.nthreads = grp.var.threads;
+            break;
         default:
             return J1J2C_OK;
     }

@@ -153,8 +153,10 @@ struct SweepVariant {
     int rpc;       // shape-specialised shared-memory kernel: replicas per CTA (0 or 1: one)
     bool coop;     // global-memory form: every colour phase, sweep and the observables in one
                    // cooperative launch with grid barriers between the phases
-    int threads;   // threads per CTA of the generic global-memory kernels (0: 256) and of the
-                   // cluster kernel (0: 512)
+    int threads;   // threads per CTA of the generic global-memory kernels (0: 256), of the
+                   // cluster kernel (0: 512) and of the replicated-lattice cluster kernel
+    int rep_cs;    // > 0: the lattice replicated in each of this many CTAs of a cluster, one site
+                   // per thread (small batches)
 };
 
 // Global-memory path: one colour phase of sweep t of the cycle, and the observable reduction
@@ -172,6 +174,12 @@ cudaError_t launch_sweep_coop(const SweepArgs& a, const SweepVariant& v, int nla
 // sweeps and the observables, added into a.obs, which the caller zeroes first).
 int cluster_size_for(const Geo& g, bool fp64, bool masks, size_t max_smem);
 int cluster_sizes(const Geo& g, bool fp64, bool masks, size_t max_smem, int* out, int cap);
+// The replicated-lattice cluster form (v.rep_cs > 0): every sweep of the cycle and the
+// observables (written, not added) in one launch; with check, nothing is launched and the result
+// says whether such a cluster can be resident
+cudaError_t launch_sweep_rep(const SweepArgs& a, const SweepVariant& v, int nlat,
+                             cudaStream_t st, bool check);
+size_t rep_smem_bytes(const Geo& g, bool fp64);  // its shared memory per CTA
 cudaError_t launch_sweep_cluster(const SweepArgs& a, const SweepVariant& v, int nlat,
                                  cudaStream_t st);
 

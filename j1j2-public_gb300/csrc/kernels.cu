@@ -1330,6 +1330,175 @@ int cluster_fits_any(const Geo& g, int cs, bool fp64, bool masks)
                 : (masks ? cluster_fits<float, true>(g, cs) : cluster_fits<float, false>(g, cs));
 }
 
+// ------------------------------------------------------------------------------------------------
+// Small batches with the lattice replicated in every CTA of a cluster: each of a lattice's cs CTAs
+// holds the whole lattice (and, where it fits, the whole random field) in its own shared memory
+// and updates a fixed 1/cs of every colour class, one site per thread.  After a colour phase each
+// CTA copies its updated words of that colour into the other CTAs' copies (distributed shared
+// memory stores) and a cluster barrier publishes them, so every neighbour read is a local
+// shared-memory load.  A CTA's copy is written by its peers only in their range of the colour
+// just updated, which no CTA reads during that phase (colour c's update reads colour c only at
+// its own sites).  Per-site arithmetic is site_step's and the Philox words and colour order are
+// those of every other kernel, so the results are theirs bit for bit.  All PTSWAPEVER sweeps and
+// the observables of a cycle run in one launch; rank 0 adds up the CTAs' sums and writes the
+// lattice's observables (no zeroing first).  This is the form for a handful of FP64 lattices,
+// whose colour phase must spread over many SMs (one SM's FP64 rate is ~2 FMA per clock).
+// ------------------------------------------------------------------------------------------------
+constexpr int kRepMaxThreads = 1024;
+constexpr size_t kRepStageLimit = 200 * 1024;  // stage the field while the CTA stays below this
+
+struct RepLayout {
+    size_t field;  // byte offset of the field copy (after the spins)
+    size_t sums;   // byte offset of the CTA's sums
+    size_t total;
+};
+
+inline RepLayout rep_layout(const Geo& g, size_t real_size, bool stage)
+{
+    RepLayout l;
+    l.field = ((size_t)g.N + 15) & ~(size_t)15;
+    l.sums = l.field + (stage ? (((size_t)g.N * real_size + 15) & ~(size_t)15) : 0);
+    l.total = l.sums + ((sizeof(Acc) + 15) & ~(size_t)15);
+    return l;
+}
+
+inline bool rep_stage(const Geo& g, size_t real_size)
+{
+    return rep_layout(g, real_size, true).total <= kRepStageLimit;
+}
+
+// Grid: nlat * cs CTAs in clusters of cs (a lattice's CTAs form one cluster); field_off: byte
+// offset of the field copy in shared memory, 0 when the field is read from global memory
+template <class Real, bool MASKS>
+__global__ void __launch_bounds__(kRepMaxThreads) sweep_rep_kernel(SweepArgs a, int cs,
+                                                                   unsigned field_off,
+                                                                   unsigned sums_off)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    cg::cluster_group cl = cg::this_cluster();
+    const Geo g = a.g;
+    const int rank = (int)cl.block_rank();
+    const int lat = a.lat0 + (int)blockIdx.x / cs;
+    const int conf = lat / a.nrep;
+    const int rep = lat - conf * a.nrep;
+    const int tid = (int)threadIdx.x, NT = (int)blockDim.x;
+    uint8_t* S = smem;
+    uint8_t* Sg = a.spins + (long long)lat * a.lat_stride;
+    const Real* Pg = field_base<Real>(a, conf);
+    block_copy16(S, Sg, g.N);  // N = 8 (L/2)^2 (H/2) is a multiple of 32
+    const Real* P = Pg;
+    if (field_off) {
+        Real* Ps = reinterpret_cast<Real*>(smem + field_off);
+        block_copy16_ldg(Ps, Pg, (int)((size_t)g.N * sizeof(Real)));
+        P = Ps;
+    }
+    const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
+    double beta;
+    uint32_t sweep0;
+    if (a.use_override) {
+        beta = a.beta_override;
+        sweep0 = a.sweep_override;
+    } else {
+        beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+        sweep0 = a.ctl[0] * (uint32_t)a.ptswapever;
+    }
+    const float kb = (float)(-2.0 * beta * 1.4426950408889634);
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    int* fl = flip_row(a, conf, rep);
+    const int per = g.Nc / cs;  // this CTA's sites of one colour (a multiple of 4, host-checked)
+    const int j0 = rank * per, nw = per >> 2;
+    cl.sync();  // every copy is loaded before any peer writes into it
+    Acc acc{0, 0, 0, 0, 0};
+#pragma unroll 1
+    for (int t = 0; t < a.nsweeps; ++t) {
+        const uint32_t sweep = sweep0 + (uint32_t)t;
+#pragma unroll 1
+        for (int c = 0; c < 8; ++c) {
+            for (int k = tid; k < per; k += NT) {
+                const int j = j0 + k, X = j % g.Lh, r = j / g.Lh;
+                site_step<Real, MASKS, kModeSweep, false>(a, g, FlatBytes{S}, P, BM, nullptr, c,
+                                                          X, r % g.Lh, r / g.Lh, sweep,
+                                                          (uint32_t)rep, k0, k1, beta, kb, acc,
+                                                          fl);
+            }
+            __syncthreads();
+            uint32_t* mine = reinterpret_cast<uint32_t*>(S + (size_t)c * g.Nc + j0);
+            for (int k = tid; k < (cs - 1) * nw; k += NT) {
+                const int p = k / nw, w = k - p * nw;
+                cl.map_shared_rank(mine, p < rank ? p : p + 1)[w] = mine[w];
+            }
+            cl.sync();
+        }
+    }
+    // observables of the new configuration: this CTA's sites of every colour
+    acc = Acc{0, 0, 0, 0, 0};
+#pragma unroll 1
+    for (int c = 0; c < 8; ++c)
+        for (int k = tid; k < per; k += NT) {
+            const int j = j0 + k, X = j % g.Lh, r = j / g.Lh;
+            site_step<Real, MASKS, kModeSweep, true>(a, g, FlatBytes{S}, P, BM, nullptr, c, X,
+                                                     r % g.Lh, r / g.Lh, 0u, 0u, 0u, 0u, beta, kb,
+                                                     acc);
+        }
+    const Acc tot = block_reduce(acc);
+    Acc* sums = reinterpret_cast<Acc*>(smem + sums_off);
+    if (tid == 0) *sums = tot;
+    cl.sync();
+    if (rank == 0 && tid == 0) {
+        Acc all{0, 0, 0, 0, 0};
+        for (int p = 0; p < cs; ++p) {  // integer sums: any order gives the same
+            const Acc v = *cl.map_shared_rank(sums, p);
+            all.e += v.e;
+            all.M += v.M;
+            all.SX += v.SX;
+            all.SY += v.SY;
+            all.NB += v.NB;
+        }
+        store_obs(a.obs + lat, all);
+    }
+    // this CTA's range of every colour back to HBM (every copy holds the same configuration)
+    for (int k = tid; k < 8 * nw; k += NT) {
+        const int c = k / nw, w = k - c * nw;
+        reinterpret_cast<uint32_t*>(Sg + (size_t)c * g.Nc + j0)[w] =
+            reinterpret_cast<const uint32_t*>(S + (size_t)c * g.Nc + j0)[w];
+    }
+    cl.sync();  // rank 0 has read every CTA's sums
+}
+
+template <class Real, bool MASKS>
+cudaError_t rep_launch(const SweepArgs& a, int nlat, int cs, int nt, cudaStream_t st, bool check)
+{
+    auto kern = sweep_rep_kernel<Real, MASKS>;
+    const bool stage = rep_stage(a.g, sizeof(Real));
+    const RepLayout lay = rep_layout(a.g, sizeof(Real), stage);
+    if (cs < 2 || cs > 16 || a.g.Nc % (4 * cs) != 0 || nt < 32 || nt > kRepMaxThreads || nt % 32)
+        return cudaErrorInvalidValue;
+    cudaError_t e = raise_smem_limit(kern);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nlat * cs));
+    cfg.blockDim = dim3((unsigned)nt);
+    cfg.dynamicSmemBytes = lay.total;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (check) {
+        int n = 0;
+        e = cudaOccupancyMaxActiveClusters(&n, kern, &cfg);
+        if (e == cudaSuccess && n < 1) e = cudaErrorInvalidConfiguration;
+        return e;
+    }
+    return cudaLaunchKernelEx(&cfg, kern, a, cs, stage ? (unsigned)lay.field : 0u,
+                              (unsigned)lay.sums);
+}
+
 }  // namespace
 
 // CTAs per lattice of the cluster path for a shape (0: none): the smallest of 2, 4, 8 that
@@ -1373,6 +1542,23 @@ cudaError_t launch_sweep_cluster(const SweepArgs& a, const SweepVariant& v, int 
                        : cluster_launch<double, false, false>(a, nlat, cs, nt, st, false);
     return v.masks ? cluster_launch<float, true, false>(a, nlat, cs, nt, st, false)
                    : cluster_launch<float, false, false>(a, nlat, cs, nt, st, false);
+}
+
+size_t rep_smem_bytes(const Geo& g, bool fp64)
+{
+    const size_t rs = fp64 ? sizeof(double) : sizeof(float);
+    return rep_layout(g, rs, rep_stage(g, rs)).total;
+}
+
+cudaError_t launch_sweep_rep(const SweepArgs& a, const SweepVariant& v, int nlat,
+                             cudaStream_t st, bool check)
+{
+    const int cs = v.rep_cs, nt = v.threads;
+    if (v.fp64)
+        return v.masks ? rep_launch<double, true>(a, nlat, cs, nt, st, check)
+                       : rep_launch<double, false>(a, nlat, cs, nt, st, check);
+    return v.masks ? rep_launch<float, true>(a, nlat, cs, nt, st, check)
+                   : rep_launch<float, false>(a, nlat, cs, nt, st, check);
 }
 
 cudaError_t launch_sweep_global(const SweepArgs& a, const SweepVariant& v, int colour, int t,

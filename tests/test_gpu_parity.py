@@ -671,3 +671,54 @@ def test_cooperative_small_batch_fp32_bitwise(engine_mod, oracle):
         np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(out[0][1], out[1][1])
     np.testing.assert_array_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("L,H,nconf,nrep,pp,bonds,ptswapever", [(16, 16, 1, 1, 0.05, 0.0, 1),
+                                                                 (24, 24, 1, 16, 0.0, 0.0, 5),
+                                                                 (8, 4, 2, 2, 0.1, 0.2, 5)])
+def test_replicated_cluster_fp64_bit_identical(engine_mod, oracle, L, H, nconf, nrep, pp, bonds,
+                                               ptswapever):
+    """Small batches with the lattice replicated in every CTA of a thread-block cluster (flag
+    32768; each CTA updates 1/cs of every colour and copies it into its peers' shared memory):
+    FP64 equals the replay bit for bit, the LOCAL shape (one lattice, one sweep per cycle), the PT
+    configuration's shape and diluted bonds included."""
+    jc = engine_mod
+    betas = _betas(nrep) if nrep > 1 else np.array([1.0 / 9.5])
+    eng, models, _ = _setup(jc, oracle, L, H, nconf, nrep, jc.FP64_PLAIN, pp=pp, bonds=bonds,
+                            flags=jc.FLAG_REPLICA, ptswapever=ptswapever, betas=betas)
+    eng.run(3, measure=False)
+    eng.reset_measurements()
+    eng.run(4, measure=True)
+    cfg = eng.config()
+    assert cfg["sites_per_thread"] == 1 and cfg["smem_bytes"] > L * L * H
+    for k in range(nconf):
+        st = oracle.new_pt_state(np.stack([oracle.hot_spins_philox(L, H, SEED, k, q) *
+                                           models[k].occu for q in range(nrep)]))
+        models[k].replay_pt(st, betas, ptswapever, 3, 0, SEED, k, False, 1)
+        obs = models[k].replay_pt(st, betas, ptswapever, 4, 3, SEED, k, True, 1)
+        for r in range(nrep):
+            np.testing.assert_array_equal(eng.spins(k, r), st["spins"][r])
+        np.testing.assert_array_equal(eng.slot_sums(k)[0], st["sums"])
+        np.testing.assert_array_equal(eng.observables(k), obs)
+    eng.close()
+
+
+def test_replicated_cluster_fp32_and_flip_counts_bitwise(engine_mod, oracle):
+    """FP32 with vacancies: the replicated-lattice cluster form equals the generic shared-memory
+    kernels bit for bit, flip counts included."""
+    jc = engine_mod
+    out = []
+    for flags in (jc.FLAG_NO_FIXED, jc.FLAG_REPLICA):
+        eng, _, _ = _setup(jc, oracle, 32, 16, 2, 3, jc.FP32_BATCHED, pp=0.05, flags=flags)
+        eng.set_diagnostics(flip_counts=True)
+        eng.run(4, measure=True)
+        out.append(([eng.spins(k, r) for k in range(2) for r in range(3)],
+                    eng.slot_sums(-1)[0], eng.observables(-1),
+                    [eng.flip_counts(k) for k in range(2)]))
+        eng.close()
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    np.testing.assert_array_equal(out[0][2], out[1][2])
+    for a, b in zip(out[0][3], out[1][3]):
+        np.testing.assert_array_equal(a, b)
