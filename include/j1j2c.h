@@ -76,6 +76,9 @@ extern "C" {
                                      fits), every sweep and the observables of a cycle in one
                                      launch (testing; slower than one launch per phase, never
                                      chosen by the tuner)                                        */
+#define J1J2C_FLAG_WOLFF_ASYNC 65536u /* one-CTA Wolff growths in the level-free form (a work
+                                         queue instead of breadth-first levels; testing: no
+                                         faster, never chosen by the tuner)                     */
 #define J1J2C_FLAG_WOLFF_CS2 128u /* Wolff growth over 2 CTAs per lattice (testing; else tuned)    */
 #define J1J2C_FLAG_WOLFF_CS4 256u /* Wolff growth over 4 CTAs per lattice (testing; else tuned);
                                      both flags: 2 CTAs for the coldest quarter of the slots, one

@@ -191,6 +191,23 @@ cudaError_t dalloc(T** p, size_t n)
     return dev_malloc(reinterpret_cast<void**>(p), n * sizeof(T) + 16);
 }
 
+// The Wolff label scratch and growth list (one int per site of every lattice), filled with
+// empty list entries (all bits set): the growth kernels leave every position they used empty
+// again, and the level-free growth reads an entry as present once it is not empty
+cudaError_t fill_labels(Ctx* c)
+{
+    const cudaError_t e =
+        cudaMemsetAsync(c->d_labels, 0xFF, sizeof(int) * (size_t)c->lab_ints, c->own);
+    return e == cudaSuccess ? cudaStreamSynchronize(c->own) : e;
+}
+
+cudaError_t alloc_labels(Ctx* c)
+{
+    if (c->d_labels) return cudaSuccess;
+    const cudaError_t e = dalloc(&c->d_labels, (size_t)c->lab_ints);
+    return e == cudaSuccess ? fill_labels(c) : e;
+}
+
 void free_graphs(Ctx* c)
 {
     for (int m = 0; m < 2; ++m) {
@@ -486,6 +503,14 @@ int wolff_cs_of(const Ctx* c, const Group& grp)
     return grp.wolff_cs > 0 ? grp.wolff_cs : 1;
 }
 
+// CTAs-per-lattice argument of a growth launch: one-CTA growths in the level-free form (-1)
+// where J1J2C_FLAG_WOLFF_ASYNC pins it
+int grow_cs(const Ctx* c, const Group& grp, int cs)
+{
+    (void)grp;
+    return cs == 1 && (c->P.flags & J1J2C_FLAG_WOLFF_ASYNC) ? -1 : cs;
+}
+
 // Coldest slots that take wolff_cs_of CTAs (0: every slot)
 int wolff_k_of(const Ctx* c, const Group& grp)
 {
@@ -543,8 +568,8 @@ cudaError_t enqueue_wolff_grow(Ctx* c, const Group& grp, const SweepArgs& a, int
                                  grp.lat_stride, cz, st, act, grp.lat_stride);
     }
     if (k <= 0 || k >= grp.nrep || cs == 1)
-        return launch_wolff_grow(a, grp.var.fp64, c->masks, grp.nconf, 0, grp.nrep, cs, lab,
-                                 grp.lat_stride, cz, st);
+        return launch_wolff_grow(a, grp.var.fp64, c->masks, grp.nconf, 0, grp.nrep,
+                                 grow_cs(c, grp, cs), lab, grp.lat_stride, cz, st);
     const size_t gi = (size_t)(&grp - c->G.data());
     cudaError_t e;
     if ((e = cudaEventRecord(c->wfork[gi], st)) != cudaSuccess) return e;
@@ -552,8 +577,9 @@ cudaError_t enqueue_wolff_grow(Ctx* c, const Group& grp, const SweepArgs& a, int
     if ((e = launch_wolff_grow(a, grp.var.fp64, c->masks, grp.nconf, 0, k, cs, lab,
                                grp.lat_stride, cz, st)) != cudaSuccess)
         return e;
-    if ((e = launch_wolff_grow(a, grp.var.fp64, c->masks, grp.nconf, k, grp.nrep - k, 1, lab,
-                               grp.lat_stride, cz, c->wside[gi])) != cudaSuccess)
+    if ((e = launch_wolff_grow(a, grp.var.fp64, c->masks, grp.nconf, k, grp.nrep - k,
+                               grow_cs(c, grp, 1), lab, grp.lat_stride, cz, c->wside[gi])) !=
+        cudaSuccess)
         return e;
     if ((e = cudaEventRecord(c->wjoin[gi], c->wside[gi])) != cudaSuccess) return e;
     return cudaStreamWaitEvent(st, c->wjoin[gi], 0);
@@ -604,8 +630,8 @@ cudaError_t enqueue_split(Ctx* c, const Group& grp, const SweepVariant& v, Sweep
             e = launch_wolff_grow(b, v.fp64, c->masks, grp.nconf, 0, k, 1, lab, grp.lat_stride,
                                   cz, st, act, grp.lat_stride);
         } else {
-            e = launch_wolff_grow(b, v.fp64, c->masks, grp.nconf, s0[h], ns[h], ncs[h], lab,
-                                  grp.lat_stride, cz, ss[h]);
+            e = launch_wolff_grow(b, v.fp64, c->masks, grp.nconf, s0[h], ns[h],
+                                  grow_cs(c, grp, ncs[h]), lab, grp.lat_stride, cz, ss[h]);
         }
         if (e != cudaSuccess) return e;
         b.slot0 = s0[h];
@@ -1153,26 +1179,36 @@ int tune_small_batch(Ctx* c, Group& grp)
 // fastest kept, cached per (device, precision, L, H, lattice count, bond dilution).  The coldest
 // lattices' clusters span a third of the lattice or more and are bound by one SM's issue rate;
 // the hot ones are small, and more CTAs per lattice mean more waves.
-std::map<std::tuple<int, bool, int, int, int, bool>, std::pair<int, int>> g_wolff_cache;
+// J1J2C_TUNE_LOG=1 in the environment: the autotuners print every candidate's time to stderr
+bool tune_log()
+{
+    const char* v = std::getenv("J1J2C_TUNE_LOG");
+    return v && v[0] == '1';
+}
+
+struct WolffChoice {
+    int cs, k;
+};
+std::map<std::tuple<int, bool, int, int, int, bool>, WolffChoice> g_wolff_cache;
 
 int tune_wolff(Ctx* c, Group& grp)
 {
     const uint32_t fl = c->P.flags;
     if (!c->wolff || (fl & (J1J2C_FLAG_GENERIC | J1J2C_FLAG_NO_FIXED | J1J2C_FLAG_WOLFF_CS2 |
-                            J1J2C_FLAG_WOLFF_CS4)))
-        return J1J2C_OK;  // no growth form, or the count is pinned
+                            J1J2C_FLAG_WOLFF_CS4 | J1J2C_FLAG_WOLFF_ASYNC)))
+        return J1J2C_OK;  // no growth form, or the form is pinned
     const auto key =
         std::make_tuple(c->P.device, grp.var.fp64, grp.g.L, grp.g.H, grp.nlat(), c->masks);
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_wolff_cache.find(key);
         if (it != g_wolff_cache.end()) {
-            grp.wolff_cs = it->second.first;
-            grp.wolff_k = it->second.second;
+            grp.wolff_cs = it->second.cs;
+            grp.wolff_k = it->second.k;
             return J1J2C_OK;
         }
     }
-    if (!c->d_labels) CK(c, dalloc(&c->d_labels, (size_t)c->lab_ints));
+    CK(c, alloc_labels(c));
     const int nlat = grp.nlat();
     uint8_t* tmp = nullptr;
     const size_t bytes = (size_t)nlat * grp.lat_stride;
@@ -1185,6 +1221,9 @@ int tune_wolff(Ctx* c, Group& grp)
     struct Cand {
         int cs, k;
     };
+    // (the level-free growth is not a candidate: as fast as the level-synchronous form on
+    // equilibrated L = 96 lattices, whose growth is bound by each cluster site's Philox work,
+    // and ~4x slower on small clusters; J1J2C_FLAG_WOLFF_ASYNC pins it)
     std::vector<Cand> cands{{1, grp.nrep}, {2, grp.nrep}, {4, grp.nrep}};
     if (grp.nrep >= 8)
         for (const int k : {grp.nrep / 8, grp.nrep / 4, grp.nrep / 2}) cands.push_back({2, k});
@@ -1206,6 +1245,8 @@ int tune_wolff(Ctx* c, Group& grp)
             if (e == cudaSuccess) e = cudaEventElapsedTime(&t, c->ev0, c->ev1);
             if (e == cudaSuccess && (k == 0 || t < ms)) ms = t;
         }
+        if (tune_log())
+            std::fprintf(stderr, "[j1j2c tune] wolff cs=%d k=%d: %.4f ms\n", cs, cd.k, ms);
         if (e == cudaSuccess && (cs == 1 || ms < best_ms)) {
             best_ms = ms;
             best = cs;
@@ -1218,15 +1259,8 @@ int tune_wolff(Ctx* c, Group& grp)
     grp.wolff_cs = best;
     grp.wolff_k = best_k;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_wolff_cache[key] = std::make_pair(best, best_k);
+    g_wolff_cache[key] = WolffChoice{best, best_k};
     return J1J2C_OK;
-}
-
-// J1J2C_TUNE_LOG=1 in the environment: the autotuners print every candidate's time to stderr
-bool tune_log()
-{
-    const char* v = std::getenv("J1J2C_TUNE_LOG");
-    return v && v[0] == '1';
 }
 
 // Split Wolff + sweep form (lattices in HBM with Wolff): the whole cycle's Wolff update, sweeps
@@ -1264,7 +1298,7 @@ int tune_split(Ctx* c, Group& grp)
             return J1J2C_OK;
         }
     }
-    if (!c->d_labels) CK(c, dalloc(&c->d_labels, (size_t)c->lab_ints));
+    CK(c, alloc_labels(c));
     {
         const int rc = ensure_act(c);
         if (rc != J1J2C_OK) return rc;
@@ -1440,7 +1474,7 @@ int tune_multi(Ctx* c)
         return J1J2C_OK;
     }
     if (c->P.flags & J1J2C_FLAG_NO_GRAPH) return J1J2C_OK;
-    if (c->wolff && !c->d_labels) CK(c, dalloc(&c->d_labels, (size_t)c->lab_ints));
+    if (c->wolff) CK(c, alloc_labels(c));
     const size_t ne = (size_t)c->nentries;
     uint8_t* keep_s = nullptr;
     LatObs* keep_o = nullptr;
@@ -1747,10 +1781,9 @@ int j1j2c_create_multi(void** out, const j1j2c_params* groups, int32_t ngroups)
     if ((e = cudaMemset(c->d_csize, 0, ne * sizeof(long long))) != cudaSuccess)
         return cfail(e, "memset");
     c->wolff = (p->flags & J1J2C_FLAG_WOLFF) != 0;
-    if (c->wolff && (e = dalloc(&c->d_labels, (size_t)c->lab_ints)) != cudaSuccess)
-        return cfail(e, "Wolff labels");
     if ((e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking)) != cudaSuccess)
         return cfail(e, "stream");
+    if (c->wolff && (e = alloc_labels(c)) != cudaSuccess) return cfail(e, "Wolff labels");
     c->st = c->own;
     if (ngroups > 1) {
         if ((e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming)) != cudaSuccess)
@@ -2213,7 +2246,11 @@ int take_device_error(Ctx* c, int& herr)
 {
     herr = 0;
     CK(c, cudaMemcpy(&herr, c->d_err, sizeof herr, cudaMemcpyDeviceToHost));
-    if (herr) CK(c, cudaMemset(c->d_err, 0, sizeof(int)));
+    if (herr) {
+        CK(c, cudaMemset(c->d_err, 0, sizeof(int)));
+        // a level-free growth that gave up may have left list entries behind
+        if (c->d_labels) CK(c, fill_labels(c));
+    }
     return J1J2C_OK;
 }
 
@@ -2283,9 +2320,9 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
         if (rc != J1J2C_OK) return rc;
         if (herr)
             return fail(c, J1J2C_ETIMEOUT,
-                        "a bounded device wait gave up (Wolff union-find retries, a bulk-copy "
-                        "wait of the streaming sweep kernel or a grid barrier of the cooperative "
-                        "form)");
+                        "a bounded device wait gave up (Wolff union-find retries, a wait of the "
+                        "level-free Wolff growth, a bulk-copy wait of the streaming sweep kernel "
+                        "or a grid barrier of the cooperative form)");
     }
     return J1J2C_OK;
 }
@@ -2297,7 +2334,7 @@ int j1j2c_wolff(void* ctx, int64_t* cluster_sizes)
     for (int k = 0; k < c->nconf; ++k)
         if (!c->have_dis[k] || !c->have_ladder[k] || !c->have_spins[k])
             return fail(c, J1J2C_ESTATE, "every conf needs disorder, ladder and spins");
-    if (!c->d_labels) CK(c, dalloc(&c->d_labels, (size_t)c->lab_ints));
+    CK(c, alloc_labels(c));
     for (auto& grp : c->G)
         if (bits_of(c, grp)) {
             const int rc = ensure_act(c);
@@ -2311,7 +2348,10 @@ int j1j2c_wolff(void* ctx, int64_t* cluster_sizes)
     int herr = 0;
     const int rc = take_device_error(c, herr);
     if (rc != J1J2C_OK) return rc;
-    if (herr) return fail(c, J1J2C_ETIMEOUT, "Wolff union-find exceeded its retry budget");
+    if (herr)
+        return fail(c, J1J2C_ETIMEOUT,
+                    "Wolff union-find exceeded its retry budget, or a wait of the level-free "
+                    "growth gave up");
     return J1J2C_OK;
 }
 

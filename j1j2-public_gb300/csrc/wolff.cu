@@ -573,6 +573,10 @@ __global__ void wolff_flip_kernel(SweepArgs a, int* labels, long long lab_stride
 // bit 2 (or loses the claim), so nothing changes.  The join bits are cleared at the end.
 constexpr int kGrowThreads = 1024;
 constexpr int kGrowRing = 8192;  // queue entries kept in shared memory (32 KiB)
+// An empty list entry: every entry has a Z below 256 (H <= 512), so its bits 28..20 are never all
+// set.  The growth list is all empty entries between updates (allocation fills it, every growth
+// empties what it wrote), which the level-free growth needs to see an entry arrive.
+constexpr int kGrowEmpty = -1;
 
 // CS > 1: a thread-block cluster of CS CTAs grows one lattice's cluster (levels of thousands of
 // sites in the coldest lattices are bound by one SM's issue rate).  The frontier ring and the
@@ -581,6 +585,151 @@ constexpr int kGrowRing = 8192;  // queue entries kept in shared memory (32 KiB)
 // meets the others at a cluster barrier between levels, whose release / acquire ordering makes
 // the level's appends (ring, cluster list) visible to all.
 enum : int { kCtlHead = 0, kCtlEnd = 1, kCtlTail = 2, kCtlRlim = 3, kCtlWlim = 4 };
+
+// One cluster site of the growth: entry e (compact coordinates, original spin byte) tests its ten
+// bonds and claims every neighbour an activated bond reaches; append(entry) queues each new
+// cluster site.  Shared by the level-synchronous and the level-free growth kernels.
+struct GrowLattice {
+    uint8_t* S;        // the lattice's spin bytes
+    uint32_t* S32;     // the same as words (claims and flips are word atomics)
+    const uint8_t* A;  // BITS: the activation bytes of the lattice
+    int rep;
+    uint32_t cycle, k0, k1;
+    double beta;
+    unsigned long long thr2, thr3;  // uniform thresholds of the J2 and J3 bonds
+    int s2, s3;                     // s_i s_j of a satisfied J2 / J3 bond
+};
+
+template <class Real, bool MASKS, bool BITS, class Append>
+__device__ __forceinline__ void grow_entry(const SweepArgs& a, const Geo& g, const Real* P,
+                                           const uint8_t* BM, const GrowLattice& w, uint32_t e,
+                                           Append& append)
+{
+    uint8_t* S = w.S;
+    uint32_t* S32 = w.S32;
+    const int rep = w.rep;
+    const uint32_t cycle = w.cycle, k0 = w.k0, k1 = w.k1;
+    const double beta = w.beta;
+    const unsigned long long thr2 = w.thr2, thr3 = w.thr3;
+    const int s2 = w.s2, s3 = w.s3;
+        const int c = (int)(e >> 29), Z = (int)((e >> 20) & 511), Y = (int)((e >> 11) & 511),
+                  X = (int)((e >> 2) & 511);
+        const int si = (int)(e & 3u) - 1;  // original spin
+        const int i = cidx(g, c, Z, Y, X);
+        const int px = c & 1, py = (c >> 1) & 1, pz = c >> 2;
+        const int Xp = px ? (X + 1 == g.Lh ? 0 : X + 1) : X;   // column of x + 1
+        const int Xm = px ? X : (X == 0 ? g.Lh - 1 : X - 1);   // column of x - 1
+        const int Yp = py ? (Y + 1 == g.Lh ? 0 : Y + 1) : Y;
+        const int Ym = py ? Y : (Y == 0 ? g.Lh - 1 : Y - 1);
+        const int Zp = pz ? (Z + 1 == g.Hh ? 0 : Z + 1) : Z;
+        const int Zm = pz ? Z : (Z == 0 ? g.Hh - 1 : Z - 1);
+        // neighbour d: +x, +y, (+x,+y), (-x,+y), +z own the bond (b = d); -x, -y, (-x,-y),
+        // (+x,-y), -z are the bonds b = d - 5 owned by the neighbour
+        auto cof = [&](int d) {
+            return c ^ (d % 5 == 0 ? 1 : d % 5 == 1 ? 2 : d % 5 == 4 ? 4 : 3);
+        };
+        auto xof = [&](int d) {
+            return (d == 0 || d == 2 || d == 8) ? Xp : (d == 3 || d == 5 || d == 7) ? Xm : X;
+        };
+        auto yof = [&](int d) {
+            return (d == 1 || d == 2 || d == 3) ? Yp : (d == 6 || d == 7 || d == 8) ? Ym : Y;
+        };
+        auto zof = [&](int d) { return d == 4 ? Zp : d == 9 ? Zm : Z; };
+        int jn[10], bn[10];
+#pragma unroll
+        for (int d = 0; d < 10; ++d) jn[d] = cidx(g, cof(d), zof(d), yof(d), xof(d));
+        // every load first (independent, in flight together)
+#pragma unroll
+        for (int d = 0; d < 10; ++d) bn[d] = S[jn[d]];
+        unsigned act_bits = 0;
+        if constexpr (BITS) {
+            // own bonds from the site's byte, the others from their owners' bytes
+            const uint8_t* A = w.A;
+            unsigned ab = A[i] & 31u;
+#pragma unroll
+            for (int d = 5; d < 10; ++d) ab |= (((unsigned)A[jn[d]] >> (d - 5)) & 1u) << d;
+#pragma unroll
+            for (int d = 0; d < 10; ++d) {
+                const int sj = (bn[d] & 3) - 1;
+                if (sj == 0 || (bn[d] & 4)) continue;  // vacancy, or joined already
+                if ((ab >> d) & 1u) act_bits |= 1u << d;
+            }
+        } else {
+            const Real p_i = P[i], p0 = P[jn[0]], p1 = P[jn[1]], p5 = P[jn[5]],
+                       p6 = P[jn[6]];
+            int m_i = 3, m5 = 3, m6 = 3;
+            if (MASKS) {
+                m_i = BM[i];
+                m5 = BM[jn[5]];
+                m6 = BM[jn[6]];
+            }
+            // the bonds' Philox words as independent chains while the loads are in flight:
+            // the site's own in-plane call (bonds 0-3), its +z call, each in-plane
+            // neighbour's own call (the word of the bond it owns) and the -z neighbour's +z
+            // call
+            uint32_t word[10];
+            {
+                const U4 own = philox4x32_10((uint32_t)rep, cycle, (uint32_t)i,
+                                             kTagWolffSite, k0, k1);
+                word[0] = own.x;
+                word[1] = own.y;
+                word[2] = own.z;
+                word[3] = own.w;
+            }
+#pragma unroll
+            for (int d = 4; d < 10; ++d) {
+                const int b = d < 5 ? d : d - 5;
+                if (b < 4) {
+                    word[d] = u4_word(philox4x32_10((uint32_t)rep, cycle, (uint32_t)jn[d],
+                                                    kTagWolffSite, k0, k1),
+                                      b);
+                } else {
+                    const int co = d < 5 ? c : cof(d), Zo = d < 5 ? Z : zof(d);
+                    const int Yo = d < 5 ? Y : yof(d), Xo = d < 5 ? X : xof(d);
+                    const uint32_t grp =
+                        (uint32_t)(((co * g.Hh + Zo) * g.Lh + Yo) * g.Qr + (Xo >> 2));
+                    word[d] = u4_word(
+                        philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffZ, k0, k1), Xo & 3);
+                }
+            }
+#pragma unroll
+            for (int d = 0; d < 10; ++d) {
+                const int sj = (bn[d] & 3) - 1;
+                if (sj == 0 || (bn[d] & 4)) continue;  // vacancy, or joined already
+                const int b = d < 5 ? d : d - 5;
+                bool on;
+                if (b < 2) {
+                    const int mo = d < 5 ? m_i : (d == 5 ? m5 : m6);
+                    const Real po = d < 5 ? p_i : (d == 5 ? p5 : p6);
+                    const Real pt = d == 0 ? p0 : d == 1 ? p1 : p_i;
+                    Real wv;
+                    on = bond_weight<Real>(a, b, si, sj, mo & 1, (mo >> 1) & 1, po, pt,
+                                           wv) &&
+                         bond_trial<Real>(wv, beta, word[d]);
+                } else {
+                    on = si * sj == (b < 4 ? s2 : s3) &&
+                         uniform_trial<Real>(b < 4 ? thr2 : thr3, word[d]);
+                }
+                if (on) act_bits |= 1u << d;
+            }
+        }
+        // claims: every atomic issued before any result is used
+        uint32_t old[10];
+#pragma unroll
+        for (int d = 0; d < 10; ++d)
+            old[d] = ((act_bits >> d) & 1u)
+                         ? atomicOr(&S32[jn[d] >> 2], 4u << (8 * (jn[d] & 3)))
+                         : 4u << (8 * (jn[d] & 3));
+#pragma unroll
+        for (int d = 0; d < 10; ++d) {
+            const int sh = 8 * (jn[d] & 3);
+            if ((old[d] >> sh) & 4u) continue;  // not active, or joined meanwhile
+            atomicXor(&S32[jn[d] >> 2], 2u << sh);
+            append((int)(((uint32_t)cof(d) << 29) | ((uint32_t)zof(d) << 20) |
+                         ((uint32_t)yof(d) << 11) | ((uint32_t)xof(d) << 2) |
+                         ((old[d] >> sh) & 3u)));
+        }
+}
 
 // Grid: the lattices at temperature slots [slot0, slot0 + gridDim.x / (CS nconf)) of the group's
 // nconf configurations, slot-major (coldest slots first: their clusters are the largest, so they
@@ -657,134 +806,33 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
     const unsigned long long thr3 = uniform_threshold<Real>(J3 < Real(0) ? -J3 : J3, beta);
     const int s2 = J2 > Real(0) ? 1 : J2 < Real(0) ? -1 : 0;  // s_i s_j of a satisfied bond
     const int s3 = J3 > Real(0) ? 1 : J3 < Real(0) ? -1 : 0;
+    GrowLattice gl;
+    gl.S = S;
+    gl.S32 = S32;
+    gl.A = BITS ? act + (long long)lat * act_stride : nullptr;
+    gl.rep = rep;
+    gl.cycle = cycle;
+    gl.k0 = k0;
+    gl.k1 = k1;
+    gl.beta = beta;
+    gl.thr2 = thr2;
+    gl.thr3 = thr3;
+    gl.s2 = s2;
+    gl.s3 = s3;
 
     for (int level = 0; level < g.N; ++level) {  // at most N levels: every site joins once
         const int head = ctl[kCtlHead], end = ctl[kCtlEnd], rlim = ctl[kCtlRlim],
                   wlim = ctl[kCtlWlim];
         if (head == end) break;
+        auto append = [&](int entry) {
+            const int pos = atomicAdd(&ctl[kCtlTail], 1);
+            Q[pos] = entry;
+            if (pos < wlim) ring[pos & (kGrowRing - 1)] = entry;
+        };
         for (int idx = head + gt; idx < end; idx += GT) {
             // entry: compact coordinates and original spin byte of a cluster site
             const uint32_t e = (uint32_t)(idx < rlim ? ring[idx & (kGrowRing - 1)] : Q[idx]);
-            const int c = (int)(e >> 29), Z = (int)((e >> 20) & 511), Y = (int)((e >> 11) & 511),
-                      X = (int)((e >> 2) & 511);
-            const int si = (int)(e & 3u) - 1;  // original spin
-            const int i = cidx(g, c, Z, Y, X);
-            const int px = c & 1, py = (c >> 1) & 1, pz = c >> 2;
-            const int Xp = px ? (X + 1 == g.Lh ? 0 : X + 1) : X;   // column of x + 1
-            const int Xm = px ? X : (X == 0 ? g.Lh - 1 : X - 1);   // column of x - 1
-            const int Yp = py ? (Y + 1 == g.Lh ? 0 : Y + 1) : Y;
-            const int Ym = py ? Y : (Y == 0 ? g.Lh - 1 : Y - 1);
-            const int Zp = pz ? (Z + 1 == g.Hh ? 0 : Z + 1) : Z;
-            const int Zm = pz ? Z : (Z == 0 ? g.Hh - 1 : Z - 1);
-            // neighbour d: +x, +y, (+x,+y), (-x,+y), +z own the bond (b = d); -x, -y, (-x,-y),
-            // (+x,-y), -z are the bonds b = d - 5 owned by the neighbour
-            auto cof = [&](int d) {
-                return c ^ (d % 5 == 0 ? 1 : d % 5 == 1 ? 2 : d % 5 == 4 ? 4 : 3);
-            };
-            auto xof = [&](int d) {
-                return (d == 0 || d == 2 || d == 8) ? Xp : (d == 3 || d == 5 || d == 7) ? Xm : X;
-            };
-            auto yof = [&](int d) {
-                return (d == 1 || d == 2 || d == 3) ? Yp : (d == 6 || d == 7 || d == 8) ? Ym : Y;
-            };
-            auto zof = [&](int d) { return d == 4 ? Zp : d == 9 ? Zm : Z; };
-            int jn[10], bn[10];
-#pragma unroll
-            for (int d = 0; d < 10; ++d) jn[d] = cidx(g, cof(d), zof(d), yof(d), xof(d));
-            // every load first (independent, in flight together)
-#pragma unroll
-            for (int d = 0; d < 10; ++d) bn[d] = S[jn[d]];
-            unsigned act_bits = 0;
-            if constexpr (BITS) {
-                // own bonds from the site's byte, the others from their owners' bytes
-                const uint8_t* A = act + (long long)lat * act_stride;
-                unsigned ab = A[i] & 31u;
-#pragma unroll
-                for (int d = 5; d < 10; ++d) ab |= (((unsigned)A[jn[d]] >> (d - 5)) & 1u) << d;
-#pragma unroll
-                for (int d = 0; d < 10; ++d) {
-                    const int sj = (bn[d] & 3) - 1;
-                    if (sj == 0 || (bn[d] & 4)) continue;  // vacancy, or joined already
-                    if ((ab >> d) & 1u) act_bits |= 1u << d;
-                }
-            } else {
-                const Real p_i = P[i], p0 = P[jn[0]], p1 = P[jn[1]], p5 = P[jn[5]],
-                           p6 = P[jn[6]];
-                int m_i = 3, m5 = 3, m6 = 3;
-                if (MASKS) {
-                    m_i = BM[i];
-                    m5 = BM[jn[5]];
-                    m6 = BM[jn[6]];
-                }
-                // the bonds' Philox words as independent chains while the loads are in flight:
-                // the site's own in-plane call (bonds 0-3), its +z call, each in-plane
-                // neighbour's own call (the word of the bond it owns) and the -z neighbour's +z
-                // call
-                uint32_t word[10];
-                {
-                    const U4 own = philox4x32_10((uint32_t)rep, cycle, (uint32_t)i,
-                                                 kTagWolffSite, k0, k1);
-                    word[0] = own.x;
-                    word[1] = own.y;
-                    word[2] = own.z;
-                    word[3] = own.w;
-                }
-#pragma unroll
-                for (int d = 4; d < 10; ++d) {
-                    const int b = d < 5 ? d : d - 5;
-                    if (b < 4) {
-                        word[d] = u4_word(philox4x32_10((uint32_t)rep, cycle, (uint32_t)jn[d],
-                                                        kTagWolffSite, k0, k1),
-                                          b);
-                    } else {
-                        const int co = d < 5 ? c : cof(d), Zo = d < 5 ? Z : zof(d);
-                        const int Yo = d < 5 ? Y : yof(d), Xo = d < 5 ? X : xof(d);
-                        const uint32_t grp =
-                            (uint32_t)(((co * g.Hh + Zo) * g.Lh + Yo) * g.Qr + (Xo >> 2));
-                        word[d] = u4_word(
-                            philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffZ, k0, k1), Xo & 3);
-                    }
-                }
-#pragma unroll
-                for (int d = 0; d < 10; ++d) {
-                    const int sj = (bn[d] & 3) - 1;
-                    if (sj == 0 || (bn[d] & 4)) continue;  // vacancy, or joined already
-                    const int b = d < 5 ? d : d - 5;
-                    bool on;
-                    if (b < 2) {
-                        const int mo = d < 5 ? m_i : (d == 5 ? m5 : m6);
-                        const Real po = d < 5 ? p_i : (d == 5 ? p5 : p6);
-                        const Real pt = d == 0 ? p0 : d == 1 ? p1 : p_i;
-                        Real wv;
-                        on = bond_weight<Real>(a, b, si, sj, mo & 1, (mo >> 1) & 1, po, pt,
-                                               wv) &&
-                             bond_trial<Real>(wv, beta, word[d]);
-                    } else {
-                        on = si * sj == (b < 4 ? s2 : s3) &&
-                             uniform_trial<Real>(b < 4 ? thr2 : thr3, word[d]);
-                    }
-                    if (on) act_bits |= 1u << d;
-                }
-            }
-            // claims: every atomic issued before any result is used
-            uint32_t old[10];
-#pragma unroll
-            for (int d = 0; d < 10; ++d)
-                old[d] = ((act_bits >> d) & 1u)
-                             ? atomicOr(&S32[jn[d] >> 2], 4u << (8 * (jn[d] & 3)))
-                             : 4u << (8 * (jn[d] & 3));
-#pragma unroll
-            for (int d = 0; d < 10; ++d) {
-                const int sh = 8 * (jn[d] & 3);
-                if ((old[d] >> sh) & 4u) continue;  // not active, or joined meanwhile
-                atomicXor(&S32[jn[d] >> 2], 2u << sh);
-                const int pos = atomicAdd(&ctl[kCtlTail], 1);
-                const int entry = (int)(((uint32_t)cof(d) << 29) | ((uint32_t)zof(d) << 20) |
-                                        ((uint32_t)yof(d) << 11) | ((uint32_t)xof(d) << 2) |
-                                        ((old[d] >> sh) & 3u));
-                Q[pos] = entry;
-                if (pos < wlim) ring[pos & (kGrowRing - 1)] = entry;
-            }
+            grow_entry<Real, MASKS, BITS>(a, g, P, BM, gl, e, append);
         }
         sync_all();
         if (rank == 0 && tid == 0) {
@@ -796,13 +844,15 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
         sync_all();
     }
     // clear the join bits of the cluster; atomically, at L2, where the flips were made (a plain
-    // read-modify-write could see a line cached before the flip)
+    // read-modify-write could see a line cached before the flip); the list goes back to empty
+    // entries for the next update
     const int n = ctl[kCtlTail];
     for (int k = gt; k < n; k += GT) {
         const uint32_t e = (uint32_t)Q[k];
         const int i = cidx(g, (int)(e >> 29), (int)((e >> 20) & 511), (int)((e >> 11) & 511),
                            (int)((e >> 2) & 511));
         atomicAnd(&S32[i >> 2], ~(4u << (8 * (i & 3))));
+        Q[k] = kGrowEmpty;
     }
     if (rank == 0 && tid == 0) csize[lat] += n;
     if constexpr (CS > 1) cg::this_cluster().sync();  // the first CTA's counters were read above
@@ -853,6 +903,182 @@ int grow_fits()
     return n;
 }
 
+// ---- level-free seed-cluster growth ------------------------------------------------------------
+// The flipped cluster is the seed's component of the activated-bond graph whatever the order in
+// which its sites are processed: a bond's activation depends only on its owner's Philox word and
+// on the configuration before the update (a site's byte keeps its original spin until the site
+// is claimed, and the claim, an atomic OR, precedes the flip), and every activated bond from a
+// claimed site to an unclaimed one claims the latter.  So this form has no levels: each thread
+// takes the next queued site as soon as one is queued, and no thread waits for a level's slowest
+// site at a barrier (the level-synchronous form's top stall on the coldest lattices).
+//   Queue: a new site's entry goes to the global list at a position from a shared counter and to
+// a shared-memory ring as a (position, entry) pair; the taker of position p reads the ring slot,
+// or the list if a later position has overwritten the slot (the list holds empty entries before
+// the update, and position p is written once, right after it is reserved).
+//   Termination: a thread whose position is beyond every reserved one stops once every reserved
+// site has been processed; a site's reservations precede its completion count (a fence orders
+// them), so no site can still be queued then.
+//   Every wait is bounded: a wait that gives up sets the context's error word and stops the
+// growth (the host reports J1J2C_ETIMEOUT and refills the list with empty entries).
+constexpr int kAsyncRing = 8192;    // ring slots: 64 KiB of dynamic shared memory
+constexpr int kAsyncWait = 1 << 22; // polls of one wait before it gives up
+
+enum : int { kAsyncTail = 0, kAsyncTaken = 1, kAsyncDone = 2, kAsyncFail = 3 };
+
+__device__ __forceinline__ int vload(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
+__device__ __forceinline__ unsigned long long vload64(const unsigned long long* p)
+{
+    return *reinterpret_cast<const volatile unsigned long long*>(p);
+}
+
+// Grid: the lattices at temperature slots [slot0, slot0 + gridDim.x / nconf) of the group's nconf
+// configurations, slot-major (coldest first), one CTA each
+template <class Real, bool MASKS>
+__global__ void __launch_bounds__(kGrowThreads, 1)
+    wolff_grow_async_kernel(SweepArgs a, int* list, long long list_stride, long long* csize,
+                            int slot0, int nconf)
+{
+    extern __shared__ __align__(16) unsigned long long aring[];
+    __shared__ int ctl[4];
+    const Geo g = a.g;
+    const int lb = (int)blockIdx.x;
+    const int slot = slot0 + lb / nconf, conf = lb % nconf;
+    const int rep = a.rep_at_temp[conf * a.nrep + slot];
+    const int lat = conf * a.nrep + rep;
+    const int tid = (int)threadIdx.x, NT = (int)blockDim.x;
+    uint8_t* S = a.spins + (long long)lat * a.lat_stride;
+    uint32_t* S32 = reinterpret_cast<uint32_t*>(S);
+    const Real* P = wfield<Real>(a, conf);
+    const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
+    int* Q = list + (long long)lat * list_stride;
+    for (int k = tid; k < kAsyncRing; k += NT) aring[k] = ~0ull;  // no position
+    const uint32_t cycle = a.ctl[0];
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    __syncthreads();
+    if (tid == 0) {
+        const uint32_t w =
+            philox4x32_10((uint32_t)rep, cycle, 0xFFFFFFFFu, kTagWolffSeed, k0, k1).x;
+        const int seed_site = (int)(((unsigned long long)w * (unsigned long long)g.N) >> 32);
+        const int cs = compact_of_site(g, seed_site);
+        ctl[kAsyncTail] = ctl[kAsyncTaken] = ctl[kAsyncDone] = ctl[kAsyncFail] = 0;
+        const int b = S[cs];
+        if (b != 1) {  // a vacant seed flips nothing
+            S[cs] = (uint8_t)((2 - b) | 4);
+            const int x = seed_site % g.L, y = (seed_site / g.L) % g.L, z = seed_site / (g.L * g.L);
+            const int cc = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+            const int entry = (int)(((uint32_t)cc << 29) | ((uint32_t)(z >> 1) << 20) |
+                                    ((uint32_t)(y >> 1) << 11) | ((uint32_t)(x >> 1) << 2) |
+                                    (uint32_t)b);
+            Q[0] = entry;
+            aring[0] = (unsigned long long)(uint32_t)entry;  // position 0
+            ctl[kAsyncTail] = 1;
+        }
+    }
+    __syncthreads();
+
+    const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+    Real J2, J3;
+    if constexpr (sizeof(Real) == 8) {
+        J2 = a.J2;
+        J3 = a.J3;
+    } else {
+        J2 = a.J2f;
+        J3 = a.J3f;
+    }
+    GrowLattice gl;
+    gl.S = S;
+    gl.S32 = S32;
+    gl.A = nullptr;
+    gl.rep = rep;
+    gl.cycle = cycle;
+    gl.k0 = k0;
+    gl.k1 = k1;
+    gl.beta = beta;
+    gl.thr2 = uniform_threshold<Real>(J2 < Real(0) ? -J2 : J2, beta);
+    gl.thr3 = uniform_threshold<Real>(J3 < Real(0) ? -J3 : J3, beta);
+    gl.s2 = J2 > Real(0) ? 1 : J2 < Real(0) ? -1 : 0;
+    gl.s3 = J3 > Real(0) ? 1 : J3 < Real(0) ? -1 : 0;
+    auto append = [&](int entry) {
+        const int pos = atomicAdd(&ctl[kAsyncTail], 1);
+        Q[pos] = entry;
+        *reinterpret_cast<volatile unsigned long long*>(&aring[pos & (kAsyncRing - 1)]) =
+            ((unsigned long long)(uint32_t)pos << 32) | (uint32_t)entry;
+    };
+    for (;;) {
+        const int idx = atomicAdd(&ctl[kAsyncTaken], 1);
+        // wait until position idx is reserved, or until nothing can be queued any more
+        bool have = false;
+        for (int it = 0;; ++it) {
+            if (idx < vload(&ctl[kAsyncTail])) {
+                have = true;
+                break;
+            }
+            const int done = vload(&ctl[kAsyncDone]);
+            __threadfence_block();
+            if (done == vload(&ctl[kAsyncTail]) || vload(&ctl[kAsyncFail])) break;
+            if (it >= kAsyncWait) {
+                atomicExch(&ctl[kAsyncFail], 1);
+                break;
+            }
+            __nanosleep(64);
+        }
+        if (!have) break;
+        // the entry at position idx: the ring slot, else the list once it is written
+        uint32_t e = 0;
+        bool got = false;
+        for (int it = 0; it < kAsyncWait; ++it) {
+            const unsigned long long v = vload64(&aring[idx & (kAsyncRing - 1)]);
+            if ((uint32_t)(v >> 32) == (uint32_t)idx) {
+                e = (uint32_t)v;
+                got = true;
+                break;
+            }
+            const int q = vload(&Q[idx]);
+            if (q != kGrowEmpty) {
+                e = (uint32_t)q;
+                got = true;
+                break;
+            }
+            __nanosleep(32);
+        }
+        if (got) grow_entry<Real, MASKS, false>(a, g, P, BM, gl, e, append);
+        else atomicExch(&ctl[kAsyncFail], 1);
+        __threadfence_block();  // this site's reservations before its completion
+        atomicAdd(&ctl[kAsyncDone], 1);
+    }
+    __syncthreads();
+    // clear the join bits of the cluster (atomically, at L2, where the flips were made) and
+    // empty the list for the next update; every reserved position was written before its
+    // reserving thread counted its site done
+    const int n = ctl[kAsyncTail];
+    for (int k = tid; k < n; k += NT) {
+        const uint32_t e = (uint32_t)vload(&Q[k]);
+        if (e == (uint32_t)kGrowEmpty) continue;
+        const int i = cidx(g, (int)(e >> 29), (int)((e >> 20) & 511), (int)((e >> 11) & 511),
+                           (int)((e >> 2) & 511));
+        atomicAnd(&S32[i >> 2], ~(4u << (8 * (i & 3))));
+        Q[k] = kGrowEmpty;
+    }
+    if (tid == 0) {
+        csize[lat] += n;
+        if (ctl[kAsyncFail] && a.err) atomicExch(a.err, 1);
+    }
+}
+
+template <class Real, bool MASKS>
+cudaError_t grow_async_launch(const SweepArgs& a, int nconf, int slot0, int nslots, int* list,
+                              long long list_stride, long long* csize, cudaStream_t st)
+{
+    auto kern = wolff_grow_async_kernel<Real, MASKS>;
+    const size_t smem = sizeof(unsigned long long) * kAsyncRing;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<nconf * nslots, kGrowThreads, smem, st>>>(a, list, list_stride, csize, slot0, nconf);
+    return cudaGetLastError();
+}
+
 // act: the activation bits of wolff_bits_kernel (one CTA per lattice), or nullptr
 template <class Real, bool MASKS>
 cudaError_t grow_dispatch(const SweepArgs& a, int nconf, int slot0, int nslots, int cs, int* list,
@@ -862,6 +1088,9 @@ cudaError_t grow_dispatch(const SweepArgs& a, int nconf, int slot0, int nslots, 
     if (act)
         return grow_launch<Real, MASKS, 1, true>(a, nconf, slot0, nslots, list, list_stride,
                                                  csize, act, act_stride, st);
+    if (cs < 0)
+        return grow_async_launch<Real, MASKS>(a, nconf, slot0, nslots, list, list_stride, csize,
+                                              st);
     if (cs == 2)
         return grow_launch<Real, MASKS, 2, false>(a, nconf, slot0, nslots, list, list_stride,
                                                   csize, nullptr, 0, st);

@@ -32,6 +32,7 @@ FLAG_PAIRS = 4096  # two replicas of one configuration per CTA in the shape-spec
 FLAG_MULTI = 8192  # every lattice-shape group in one persistent launch (testing)
 FLAG_COOP = 16384  # small batches: a cycle's colour phases in one cooperative launch (testing)
 FLAG_REPLICA = 32768  # small batches: the lattice replicated in every CTA of a cluster (testing)
+FLAG_WOLFF_ASYNC = 65536  # one-CTA Wolff growths without breadth-first levels (testing)
 
 SUM_FIELDS = ("mag", "absmag", "mag2", "mag4", "en", "en2", "strx_abs", "stry_abs", "strx2",
               "strx4", "stry2", "stry4", "str2", "str4", "absstr", "nem", "nbar", "nbarabs",

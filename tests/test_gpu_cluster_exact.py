@@ -37,7 +37,7 @@ def _engine(jc, L, H, nconf, nrep, precision, flags=0, pp=0.0, bonds=0.0, betas=
 # 4 the per-site global labelling; 128 / 256 the growth over a cluster of 2 / 4 CTAs per lattice,
 # 384 two CTAs for the coldest quarter of the slots and one for the rest (two launches), 2048 the
 # growth from bond activations decided beforehand on every SM (the quad store and, with L/2 odd,
-# the byte stores).  Slab shapes: one slab per lattice (8 x 4), several slabs with
+# the byte stores), 65536 the level-free growth (a work queue instead of breadth-first levels).  Slab shapes: one slab per lattice (8 x 4), several slabs with
 # the +z boundary merge (48^3: 3 slabs of 16 planes; 96 x 8: 2 slabs of 4), one-CTA-per-SM slabs
 # (160 x 4: 2 slabs of 2 planes), no slab fits (200 x 4: the per-site form is used).
 @pytest.mark.parametrize("L,H,pp,bonds,flags", [(8, 4, 0.1, 0.2, 0), (10, 6, 0.0, 0.0, 0),
@@ -52,7 +52,12 @@ def _engine(jc, L, H, nconf, nrep, precision, flags=0, pp=0.0, bonds=0.0, betas=
                                                  (48, 48, 0.05, 0.0, 384),
                                                  (8, 4, 0.1, 0.2, 2048), (10, 6, 0.0, 0.0, 2048),
                                                  (48, 48, 0.05, 0.0, 2048),
-                                                 (96, 8, 0.1, 0.2, 2048), (2, 2, 0.0, 0.0, 2048)])
+                                                 (96, 8, 0.1, 0.2, 2048), (2, 2, 0.0, 0.0, 2048),
+                                                 (8, 4, 0.1, 0.2, 65536),
+                                                 (10, 6, 0.0, 0.0, 65536),
+                                                 (4, 2, 0.0, 0.0, 65536), (2, 2, 0.0, 0.0, 65536),
+                                                 (48, 48, 0.05, 0.0, 65536),
+                                                 (96, 8, 0.1, 0.2, 65536)])
 def test_wolff_step_bit_identical(engine_mod, oracle, L, H, pp, bonds, flags):
     jc = engine_mod
     eng, dis, betas = _engine(jc, L, H, 2, 3, jc.FP64_PLAIN, flags, pp, bonds)
@@ -75,7 +80,7 @@ def test_wolff_step_bit_identical(engine_mod, oracle, L, H, pp, bonds, flags):
 
 
 @pytest.mark.parametrize("nconf,flags", [(40, 0), (80, 0), (40, 128), (40, 256), (80, 384),
-                                         (80, 2048)])
+                                         (80, 2048), (80, 65536)])
 def test_wolff_growth_many_lattices(engine_mod, oracle, nconf, flags):
     """More lattices than SMs (160 and 320 lattices: two and three waves of growth CTAs, coldest
     slots first): the flipped clusters equal the oracle's in the first, middle and last
@@ -111,7 +116,7 @@ def test_wolff_fp32_forms_agree(engine_mod, oracle, L, H, pp, bonds):
     for flags in (jc.FLAG_WOLFF, jc.FLAG_WOLFF | jc.FLAG_NO_FIXED, jc.FLAG_WOLFF | jc.FLAG_GENERIC,
                   jc.FLAG_WOLFF | jc.FLAG_WOLFF_CS2, jc.FLAG_WOLFF | jc.FLAG_WOLFF_CS4,
                   jc.FLAG_WOLFF | jc.FLAG_WOLFF_CS2 | jc.FLAG_WOLFF_CS4,
-                  jc.FLAG_WOLFF | jc.FLAG_WOLFF_BITS):
+                  jc.FLAG_WOLFF | jc.FLAG_WOLFF_BITS, jc.FLAG_WOLFF | jc.FLAG_WOLFF_ASYNC):
         eng, _, _ = _engine(jc, L, H, 2, 3, jc.FP32_BATCHED, flags, pp, bonds)
         sizes = [eng.wolff().copy()]
         eng.run(3, measure=True)
@@ -153,19 +158,21 @@ def test_wolff_inside_pt_cycles(engine_mod, oracle, nrep):
     eng.close()
 
 
-@pytest.mark.parametrize("extra", ["split", "tuned", "split_bits"])
+@pytest.mark.parametrize("extra", ["split", "tuned", "split_bits", "split_async"])
 def test_split_wolff_sweeps_bit_identical(engine_mod, oracle, extra):
     """Lattices in HBM (the one-launch-per-colour kernel; L = 32 is its cross-check shape) with a
     Wolff update per cycle: the Wolff update and sweeps of the coldest slots and of the others
     on two streams, each sweep launch finding its lattices through the temperature map (flag
     1024 pins the split at a quarter of the slots, with flag 2048 the cold slots' bonds decided
-    beforehand; unpinned the tuner times the candidates on equilibrated scratch lattices), equal
+    beforehand, with flag 65536 the one-CTA growths level-free; unpinned the tuner times the candidates on equilibrated scratch lattices), equal
     the replay bit for bit over cycles with replica exchanges."""
     jc = engine_mod
     L, H, nconf, nrep, ncyc = 32, 32, 2, 8, 3
     flags = jc.FLAG_WOLFF | jc.FLAG_GLOBAL | {"split": jc.FLAG_WOLFF_SPLIT, "tuned": 0,
                                               "split_bits": jc.FLAG_WOLFF_SPLIT |
-                                              jc.FLAG_WOLFF_BITS}[extra]
+                                              jc.FLAG_WOLFF_BITS,
+                                              "split_async": jc.FLAG_WOLFF_SPLIT |
+                                              jc.FLAG_WOLFF_ASYNC}[extra]
     eng, dis, betas = _engine(jc, L, H, nconf, nrep, jc.FP64_PLAIN, flags, 0.05)
     states = [oracle.new_pt_state(np.stack([eng.spins(k, r) for r in range(nrep)]))
               for k in range(nconf)]
@@ -192,13 +199,14 @@ def test_split_wolff_sweeps_fp32_equals_unsplit(engine_mod, oracle):
     """FP32, L = 96 with vacancies and 8 replicas: the split cycle (flag 1024), the unsplit one
     (growth pinned to two CTAs per lattice, which also pins the cycle unsplit), the split cycle
     whose cold slots grow from bond activations decided beforehand, and the unsplit cycle that
-    does so for every slot (flag 2048) give bitwise equal spins, running sums, maps and cluster
-    sizes."""
+    does so for every slot (flag 2048), and both cycles with level-free one-CTA growths (flag
+    65536) give bitwise equal spins, running sums, maps and cluster sizes."""
     jc = engine_mod
     out = []
     base = jc.FLAG_WOLFF | jc.FLAG_GLOBAL
     for flags in (base | jc.FLAG_WOLFF_SPLIT, base | jc.FLAG_WOLFF_CS2,
-                  base | jc.FLAG_WOLFF_SPLIT | jc.FLAG_WOLFF_BITS, base | jc.FLAG_WOLFF_BITS):
+                  base | jc.FLAG_WOLFF_SPLIT | jc.FLAG_WOLFF_BITS, base | jc.FLAG_WOLFF_BITS,
+                  base | jc.FLAG_WOLFF_SPLIT | jc.FLAG_WOLFF_ASYNC, base | jc.FLAG_WOLFF_ASYNC):
         eng, _, _ = _engine(jc, 96, 96, 1, 8, jc.FP32_BATCHED, flags, 0.05)
         eng.run(2, measure=True, restart_swap_phase=True)
         out.append(([eng.spins(0, r) for r in range(8)], eng.slot_sums(0)[0], eng.maps(0)[0],
