@@ -1055,6 +1055,8 @@ SweepVariant cluster_variant(const SweepVariant& base, int cs, bool quad, int nt
     return v;
 }
 
+bool tune_log();
+
 int tune_small_batch(Ctx* c, Group& grp)
 {
     int nsm = 0;
@@ -1073,9 +1075,12 @@ int tune_small_batch(Ctx* c, Group& grp)
             return fail(c, J1J2C_EINVAL, "the cooperative form does not fit this batch");
         best = SmallChoice{kGlobalCoop, 0, 64};
         known = true;
-    } else if (c->P.flags & J1J2C_FLAG_REPLICA) {  // pinned: the largest cluster that fits
+    } else if (c->P.flags & J1J2C_FLAG_REPLICA) {
+        // pinned: the largest cluster that fits, or J1J2C_REPLICA_CS from the environment (tests)
+        const char* env = std::getenv("J1J2C_REPLICA_CS");
+        const int want = env ? std::atoi(env) : 0;
         for (const int cs : {16, 8, 4, 2})
-            if (rep_fits(c, grp, cs)) {
+            if ((want == 0 || cs == want) && rep_fits(c, grp, cs)) {
                 best = SmallChoice{kRepCluster, cs, 0};
                 known = true;
                 break;
@@ -1093,9 +1098,15 @@ int tune_small_batch(Ctx* c, Group& grp)
         float best_ms = 0.0f;
         int rc = time_variant(c, grp, grp.var, grp.nthreads, grp.smem, best_ms);
         if (rc != J1J2C_OK) return rc;
+        if (tune_log())
+            std::fprintf(stderr, "[j1j2c tune] small batch default nt=%d: %.4f ms\n",
+                         grp.nthreads, best_ms);
         auto consider = [&](const SweepVariant& v, int nt, size_t smem, SmallChoice ch) {
             float ms = 0.0f;
             const int r = time_variant(c, grp, v, nt, smem, ms);
+            if (tune_log())
+                std::fprintf(stderr, "[j1j2c tune] small batch kind=%d cs=%d nt=%d: %.4f ms\n",
+                             ch.kind, ch.cs, ch.nt, ms);
             if (r == J1J2C_OK && ms < best_ms) {
                 best_ms = ms;
                 best = ch;
@@ -1131,12 +1142,14 @@ int tune_small_batch(Ctx* c, Group& grp)
                           SmallChoice{kGlobalSite, 0, nt});
             if (rc != J1J2C_OK) return rc;
         }
-        // (Two one-launch-per-cycle forms are slower on both the L = 16 single lattice and 16
-        // lattices of 24^3 and are not candidates: the same phases in one cooperative launch, grid
-        // barriers through L2 instead of kernel boundaries (J1J2C_FLAG_COOP pins it); and the
-        // lattice replicated in every CTA of a cluster with cluster barriers (J1J2C_FLAG_REPLICA).
-        // An FP64 colour phase takes ~3 us however many SMs share it, the latency of one site's
-        // dependent FP64 chain, so fewer launch boundaries save little and fewer SMs cost more.)
+        // (Not candidates: two forms with every sweep and the observables of a cycle in one
+        // launch.  The cooperative form, grid barriers through L2 instead of kernel boundaries
+        // (J1J2C_FLAG_COOP pins it), is slower on both the L = 16 single lattice and 16 lattices
+        // of 24^3.  The replicated-lattice cluster form (J1J2C_FLAG_REPLICA; compile-time shape at
+        // L = 16, 24) is at best 8 % faster in isolation on the single lattice, slower at 24^3,
+        // and slower in the whole LOCAL cycle.  A colour phase of an FP64 small batch is bound by
+        // one site's dependent chain (GB300: 64 clocks per dependent FP64 add or FMA), not by
+        // its launch or barrier (a cluster barrier is ~0.2 us).)
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_small_cache[key] = best;
     }

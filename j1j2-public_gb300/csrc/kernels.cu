@@ -1465,6 +1465,243 @@ __global__ void __launch_bounds__(kRepMaxThreads) sweep_rep_kernel(SweepArgs a, 
     cl.sync();  // rank 0 has read every CTA's sums
 }
 
+// Compile-time shape of the replicated-lattice form for the FP64 small batches (L = H = 16, 24;
+// no diluted bond, no audit): a thread's site has the same position in every colour class, so
+// its eleven in-class neighbour offsets (rows Y-1, Y, Y+1 times columns X-1, X, X+1, and planes
+// Z+1, Z-1) and its Philox group are computed once per launch, and each colour phase only adds a
+// class base that is a compile-time constant.  The arithmetic, operation for operation, is
+// site_step's FP64 path (field_fp64, downhill, accept_fp64 on the same Philox word).
+template <int LH, int HH>
+struct RepSite {
+    static constexpr int Nc = LH * LH * HH;
+    static constexpr int Qr = (LH + 3) / 4;
+    int off[3][3];  // [Y-1, Y, Y+1][X-1, X, X+1] within a class
+    int zp, zm;     // (Z+1, Y, X) and (Z-1, Y, X)
+    int g0;         // Philox group within a class
+    int w;          // word of the group
+    __device__ __forceinline__ explicit RepSite(int j)
+    {
+        const int X = j % LH, Y = (j / LH) % LH, Z = j / (LH * LH);
+        const int xs[3] = {X == 0 ? LH - 1 : X - 1, X, X + 1 == LH ? 0 : X + 1};
+        const int ys[3] = {Y == 0 ? LH - 1 : Y - 1, Y, Y + 1 == LH ? 0 : Y + 1};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) off[a][b] = (Z * LH + ys[a]) * LH + xs[b];
+        zp = ((Z + 1 == HH ? 0 : Z + 1) * LH + Y) * LH + X;
+        zm = ((Z == 0 ? HH - 1 : Z - 1) * LH + Y) * LH + X;
+        g0 = (Z * LH + Y) * Qr + (X >> 2);
+        w = X & 3;
+    }
+};
+
+template <int LH, int HH, bool MEASURE>
+__device__ __forceinline__ void rep_site(const SweepArgs& a, uint8_t* S, const double* P,
+                                         const RepSite<LH, HH>& st, int C, uint32_t sweep,
+                                         uint32_t rep, uint32_t k0, uint32_t k1, double beta,
+                                         Acc& acc, int* fl)
+{
+    // one copy of the code for every colour (the fully unrolled form stalled on instruction
+    // fetch with one warp per scheduler): the colour's parities select among the offsets
+    constexpr int Nc = RepSite<LH, HH>::Nc;
+    const bool px = C & 1, py = (C >> 1) & 1, pz = C >> 2;
+    const int B0 = C * Nc, B1 = (C ^ 1) * Nc, B2 = (C ^ 2) * Nc, B3 = (C ^ 3) * Nc,
+              B4 = (C ^ 4) * Nc;
+    const int o = st.off[1][1];
+    const int i = B0 + o;
+    const int b = S[i];
+    if (b == 1) return;  // vacancy: no attempt and no measured term (J:2563, J:2825)
+    // the Philox word first: it does not depend on the field, so its latency overlaps the FP64
+    // chain (the downhill test below decides whether it is used)
+    uint32_t r = 0;
+    if constexpr (!MEASURE) {
+        const uint32_t grp = (uint32_t)(C * HH * LH * RepSite<LH, HH>::Qr + st.g0);
+        r = u4_word(philox4x32_10(rep, sweep, grp, kTagSweep, k0, k1), st.w);
+    }
+    const int i1 = B2 + (py ? st.off[2][1] : o), i2 = B2 + (py ? o : st.off[0][1]);
+    const int i3 = B1 + (px ? st.off[1][2] : o), i4 = B1 + (px ? o : st.off[1][0]);
+    const int dpp = py ? (px ? st.off[2][2] : st.off[2][1]) : (px ? st.off[1][2] : o);
+    const int dpm = py ? (px ? st.off[2][1] : st.off[2][0]) : (px ? o : st.off[1][0]);
+    const int dmp = py ? (px ? st.off[1][2] : o) : (px ? st.off[0][2] : st.off[0][1]);
+    const int dmm = py ? (px ? o : st.off[1][0]) : (px ? st.off[0][1] : st.off[0][0]);
+    const int b1 = S[i1], b2 = S[i2], b3 = S[i3], b4 = S[i4];
+    const int b5 = S[B3 + dpp], b6 = S[B3 + dpm], b7 = S[B3 + dmp], b8 = S[B3 + dmm];
+    const int b9 = S[B4 + (pz ? st.zp : o)];
+    const int b10 = S[B4 + (pz ? o : st.zm)];
+    const int s = b - 1;
+    if constexpr (MEASURE) {
+        acc.M += s;
+        acc.SX += px ? -s : s;
+        acc.SY += py ? -s : s;
+        acc.NB += s * (b3 + b4 - b1 - b2);
+    }
+    Nbr64 n;
+    n.s[0] = b1 - 1;
+    n.s[1] = b2 - 1;
+    n.s[2] = b3 - 1;
+    n.s[3] = b4 - 1;
+    n.s[4] = b5 - 1;
+    n.s[5] = b6 - 1;
+    n.s[6] = b7 - 1;
+    n.s[7] = b8 - 1;
+    n.s[8] = b9 - 1;
+    n.s[9] = b10 - 1;
+    n.p1 = P[i1];
+    n.p2 = P[i2];
+    n.p3 = P[i3];
+    n.p4 = P[i4];
+    n.jv_own = n.jv_m2 = n.jh_own = n.jh_m4 = 1;
+    const double f64 = field_fp64(n, P[i], a.J1h, a.J1v, a.J2, a.J3, nullptr);
+    if constexpr (MEASURE) {
+        acc.e += efix(spin_mul(-s, f64));
+    } else {
+        const bool flip = downhill(f64, s) || accept_fp64(r, metropolis_arg(f64, beta, s));
+        if (flip) {
+            S[i] = (uint8_t)(2 - b);
+            if (fl) fl[i] += 1;
+        }
+    }
+}
+
+// This CTA's words of colour C (sites [j0, j0 + per) of the class) into the other CTAs' copies
+template <int Nc, int CS, int NW>
+__device__ __forceinline__ void rep_push(cg::cluster_group& cl, uint8_t* S, int C, int rank, int j0)
+{
+    uint32_t* mine = reinterpret_cast<uint32_t*>(S + C * Nc + j0);
+    for (int k = (int)threadIdx.x; k < (CS - 1) * NW; k += (int)blockDim.x) {
+        const int p = k / NW, w = k - p * NW;
+        cl.map_shared_rank(mine, p < rank ? p : p + 1)[w] = mine[w];
+    }
+}
+
+// Grid: nlat * CS CTAs of round_up(Nc / CS, 32) threads in clusters of CS; shared memory: the
+// lattice, the FP64 field, the CTA's sums (rep_layout with the field staged)
+template <int LH, int HH, int CS>
+__global__ void __launch_bounds__(((LH * LH * HH / CS) + 31) / 32 * 32)
+    sweep_rep_fixed_kernel(SweepArgs a, unsigned field_off, unsigned sums_off)
+{
+    constexpr int Nc = RepSite<LH, HH>::Nc, N = 8 * Nc, per = Nc / CS, NW = per / 4;
+    static_assert(per % 4 == 0, "a CTA's share of a colour must be whole words");
+    extern __shared__ __align__(16) unsigned char smem[];
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int lat = a.lat0 + (int)blockIdx.x / CS;
+    const int conf = lat / a.nrep;
+    const int rep = lat - conf * a.nrep;
+    const int tid = (int)threadIdx.x;
+    uint8_t* S = smem;
+    uint8_t* Sg = a.spins + (long long)lat * a.lat_stride;
+    double* P = reinterpret_cast<double*>(smem + field_off);
+    block_copy16(S, Sg, N);
+    block_copy16_ldg(P, field_base<double>(a, conf), N * (int)sizeof(double));
+    double beta;
+    uint32_t sweep0;
+    if (a.use_override) {
+        beta = a.beta_override;
+        sweep0 = a.sweep_override;
+    } else {
+        beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+        sweep0 = a.ctl[0] * (uint32_t)a.ptswapever;
+    }
+    const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
+    int* fl = flip_row(a, conf, rep);
+    const int j0 = rank * per;
+    const bool active = tid < per;
+    const RepSite<LH, HH> st(j0 + (active ? tid : 0));
+    cl.sync();  // every copy is loaded before any peer writes into it
+    Acc acc{0, 0, 0, 0, 0};
+#pragma unroll 1
+    for (int t = 0; t < a.nsweeps; ++t) {
+        const uint32_t sweep = sweep0 + (uint32_t)t;
+#pragma unroll 1
+        for (int c = 0; c < 8; ++c) {
+            if (active)
+                rep_site<LH, HH, false>(a, S, P, st, c, sweep, (uint32_t)rep, k0, k1, beta, acc,
+                                        fl);
+            __syncthreads();
+            rep_push<Nc, CS, NW>(cl, S, c, rank, j0);
+            cl.sync();
+        }
+    }
+    // observables of the new configuration: this CTA's site of every colour
+    if (active)
+#pragma unroll 1
+        for (int c = 0; c < 8; ++c)
+            rep_site<LH, HH, true>(a, S, P, st, c, 0u, 0u, 0u, 0u, beta, acc, nullptr);
+    const Acc tot = block_reduce(acc);
+    Acc* sums = reinterpret_cast<Acc*>(smem + sums_off);
+    if (tid == 0) *sums = tot;
+    cl.sync();
+    if (rank == 0 && tid == 0) {
+        Acc all{0, 0, 0, 0, 0};
+        for (int p = 0; p < CS; ++p) {  // integer sums: any order gives the same
+            const Acc v = *cl.map_shared_rank(sums, p);
+            all.e += v.e;
+            all.M += v.M;
+            all.SX += v.SX;
+            all.SY += v.SY;
+            all.NB += v.NB;
+        }
+        store_obs(a.obs + lat, all);
+    }
+    for (int k = tid; k < 8 * NW; k += (int)blockDim.x) {
+        const int c = k / NW, w = k - c * NW;
+        reinterpret_cast<uint32_t*>(Sg + c * Nc + j0)[w] =
+            reinterpret_cast<const uint32_t*>(S + c * Nc + j0)[w];
+    }
+    cl.sync();  // rank 0 has read every CTA's sums
+}
+
+template <int LH, int HH, int CS>
+cudaError_t rep_fixed_launch(const SweepArgs& a, int nlat, cudaStream_t st, bool check)
+{
+    auto kern = sweep_rep_fixed_kernel<LH, HH, CS>;
+    constexpr int NT = ((LH * LH * HH / CS) + 31) / 32 * 32;
+    const RepLayout lay = rep_layout(a.g, sizeof(double), true);
+    cudaError_t e = raise_smem_limit(kern);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nlat * CS));
+    cfg.blockDim = dim3((unsigned)NT);
+    cfg.dynamicSmemBytes = lay.total;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)CS;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (check) {
+        int n = 0;
+        e = cudaOccupancyMaxActiveClusters(&n, kern, &cfg);
+        if (e == cudaSuccess && n < 1) e = cudaErrorInvalidConfiguration;
+        return e;
+    }
+    return cudaLaunchKernelEx(&cfg, kern, a, (unsigned)lay.field, (unsigned)lay.sums);
+}
+
+// The compile-time-shape form where it exists (returns cudaErrorNotSupported otherwise)
+cudaError_t rep_fixed_dispatch(const SweepArgs& a, const SweepVariant& v, int nlat,
+                               cudaStream_t st, bool check)
+{
+    if (!v.fp64 || v.masks || v.mode != kModeSweep || a.g.L != a.g.H)
+        return cudaErrorNotSupported;
+    const int L = a.g.L, cs = v.rep_cs;
+#define J1J2_REP_FIXED(LL, CC)                                                                    \
+    if (L == LL && cs == CC) return rep_fixed_launch<LL / 2, LL / 2, CC>(a, nlat, st, check);
+    J1J2_REP_FIXED(16, 4)
+    J1J2_REP_FIXED(16, 8)
+    J1J2_REP_FIXED(16, 16)
+    J1J2_REP_FIXED(24, 4)
+    J1J2_REP_FIXED(24, 8)
+    J1J2_REP_FIXED(24, 16)
+#undef J1J2_REP_FIXED
+    return cudaErrorNotSupported;
+}
+
 template <class Real, bool MASKS>
 cudaError_t rep_launch(const SweepArgs& a, int nlat, int cs, int nt, cudaStream_t st, bool check)
 {
@@ -1553,6 +1790,8 @@ size_t rep_smem_bytes(const Geo& g, bool fp64)
 cudaError_t launch_sweep_rep(const SweepArgs& a, const SweepVariant& v, int nlat,
                              cudaStream_t st, bool check)
 {
+    const cudaError_t ef = rep_fixed_dispatch(a, v, nlat, st, check);
+    if (ef != cudaErrorNotSupported) return ef;
     const int cs = v.rep_cs, nt = v.threads;
     if (v.fp64)
         return v.masks ? rep_launch<double, true>(a, nlat, cs, nt, st, check)

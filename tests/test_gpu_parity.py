@@ -673,16 +673,21 @@ def test_cooperative_small_batch_fp32_bitwise(engine_mod, oracle):
     np.testing.assert_array_equal(out[0][2], out[1][2])
 
 
-@pytest.mark.parametrize("L,H,nconf,nrep,pp,bonds,ptswapever", [(16, 16, 1, 1, 0.05, 0.0, 1),
-                                                                 (24, 24, 1, 16, 0.0, 0.0, 5),
-                                                                 (8, 4, 2, 2, 0.1, 0.2, 5)])
-def test_replicated_cluster_fp64_bit_identical(engine_mod, oracle, L, H, nconf, nrep, pp, bonds,
-                                               ptswapever):
+@pytest.mark.parametrize("L,H,nconf,nrep,pp,bonds,ptswapever,cs", [
+    (16, 16, 1, 1, 0.05, 0.0, 1, 0), (16, 16, 1, 1, 0.0, 0.0, 1, 4), (16, 16, 1, 2, 0.05, 0.0, 1, 8),
+    (24, 24, 1, 16, 0.0, 0.0, 5, 0), (24, 24, 1, 4, 0.05, 0.0, 5, 8), (24, 24, 2, 2, 0.0, 0.0, 5, 4),
+    (8, 4, 2, 2, 0.1, 0.2, 5, 0)])
+def test_replicated_cluster_fp64_bit_identical(engine_mod, oracle, monkeypatch, L, H, nconf, nrep,
+                                               pp, bonds, ptswapever, cs):
     """Small batches with the lattice replicated in every CTA of a thread-block cluster (flag
     32768; each CTA updates 1/cs of every colour and copies it into its peers' shared memory):
     FP64 equals the replay bit for bit, the LOCAL shape (one lattice, one sweep per cycle), the PT
-    configuration's shape and diluted bonds included."""
+    configuration's shape and diluted bonds included.  L = 16 and 24 run the compile-time-shape
+    kernel with 16 (the pin's default), 8 or 4 CTAs per lattice; 8 x 4 with diluted bonds the
+    runtime-shape one."""
     jc = engine_mod
+    if cs:
+        monkeypatch.setenv("J1J2C_REPLICA_CS", str(cs))
     betas = _betas(nrep) if nrep > 1 else np.array([1.0 / 9.5])
     eng, models, _ = _setup(jc, oracle, L, H, nconf, nrep, jc.FP64_PLAIN, pp=pp, bonds=bonds,
                             flags=jc.FLAG_REPLICA, ptswapever=ptswapever, betas=betas)
