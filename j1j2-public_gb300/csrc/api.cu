@@ -70,6 +70,7 @@ struct Ctx {
     uint8_t* d_bm = nullptr;
     uint8_t* d_occ = nullptr;
     double* d_beta = nullptr;
+    float* d_kb = nullptr;  // by slot: the FP32 acceptance scale of each beta
     int* d_rat = nullptr;
     int* d_tor = nullptr;
     LatObs* d_obs = nullptr;
@@ -223,6 +224,7 @@ void release(Ctx* c)
 {
     free_graphs(c);
     void* ptrs[] = {c->d_spins, c->d_pf,    c->d_pd,   c->d_bm,    c->d_occ,   c->d_beta,
+                    c->d_kb,
                     c->d_rat,   c->d_tor,   c->d_obs,  c->d_sums,  c->d_nmeas, c->d_att,
                     c->d_acc,   c->d_vis,   c->d_last, c->d_ctl,   c->d_nocc,  c->d_rbase,
                     c->d_nreps, c->d_audit, c->d_labels, c->d_act, c->d_csize, c->d_err,
@@ -401,6 +403,7 @@ SweepArgs group_args(Ctx* c, const Group& grp)
     a.bm = c->masks ? c->d_bm + grp.mask_off : nullptr;
     a.p_stride = grp.p_stride;
     a.beta = c->d_beta + grp.rep0;
+    a.kb = c->d_kb + grp.rep0;
     a.temp_of_rep = c->d_tor + grp.rep0;
     a.rep_at_temp = c->d_rat + grp.rep0;
     a.ctl = c->d_ctl;
@@ -1774,6 +1777,7 @@ int j1j2c_create_multi(void** out, const j1j2c_params* groups, int32_t ngroups)
     if ((e = dalloc(&c->d_bm, (size_t)mask_bytes)) != cudaSuccess) return cfail(e, "masks");
     if ((e = dalloc(&c->d_occ, (size_t)mask_bytes)) != cudaSuccess) return cfail(e, "occ");
     if ((e = dalloc(&c->d_beta, ne)) != cudaSuccess) return cfail(e, "beta");
+    if ((e = dalloc(&c->d_kb, ne)) != cudaSuccess) return cfail(e, "beta");
     if ((e = dalloc(&c->d_rat, ne)) != cudaSuccess) return cfail(e, "maps");
     if ((e = dalloc(&c->d_tor, ne)) != cudaSuccess) return cfail(e, "maps");
     if ((e = dalloc(&c->d_obs, ne)) != cudaSuccess) return cfail(e, "obs");
@@ -1956,6 +1960,15 @@ int j1j2c_set_disorder(void* ctx, int32_t conf, const double* p, const int8_t* o
     return J1J2C_OK;
 }
 
+// The FP32 form's acceptance scale of each beta, (float)(-2 beta log2(e)): the same IEEE double
+// operations, in the same order, as the kernels that compute it themselves
+std::vector<float> acceptance_scales(const double* beta, int n)
+{
+    std::vector<float> kb((size_t)n);
+    for (int k = 0; k < n; ++k) kb[(size_t)k] = (float)(-2.0 * beta[k] * 1.4426950408889634);
+    return kb;
+}
+
 int j1j2c_set_ladder(void* ctx, int32_t conf, const double* beta)
 {
     if (!ctx) return J1J2C_EINVAL;
@@ -1968,6 +1981,9 @@ int j1j2c_set_ladder(void* ctx, int32_t conf, const double* beta)
         if (!std::isfinite(beta[k]) || beta[k] < 0.0)
             return fail(c, J1J2C_EINVAL, "beta must be finite and >= 0");
     CK(c, cudaMemcpyAsync(c->d_beta + off, beta, sizeof(double) * n, cudaMemcpyHostToDevice,
+                          c->st));
+    const std::vector<float> kb = acceptance_scales(beta, n);
+    CK(c, cudaMemcpyAsync(c->d_kb + off, kb.data(), sizeof(float) * n, cudaMemcpyHostToDevice,
                           c->st));
     CK(c, cudaStreamSynchronize(c->st));
     if (conf < 0)
@@ -2859,6 +2875,13 @@ int j1j2c_load_state(void* ctx, const void* buf, int64_t size)
     c->host_ctl[1] = h.phase;
     c->host_ctl[2] = 0;
     CK(c, cudaMemcpy(c->d_ctl, c->host_ctl, 4 * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    {  // the acceptance scales follow the restored ladder
+        std::vector<double> beta((size_t)c->nentries);
+        CK(c, cudaMemcpy(beta.data(), c->d_beta, sizeof(double) * beta.size(),
+                         cudaMemcpyDeviceToHost));
+        const std::vector<float> kb = acceptance_scales(beta.data(), c->nentries);
+        CK(c, cudaMemcpy(c->d_kb, kb.data(), sizeof(float) * kb.size(), cudaMemcpyHostToDevice));
+    }
     bool masks = false, vac = false;
     for (int k : c->conf_masks) masks = masks || k;
     for (int k : c->conf_vac) vac = vac || k;

@@ -28,6 +28,8 @@ struct SweepArgs {
     const uint8_t* bm;       // conf c at bm + c*lat_stride: bit0 = jh, bit1 = jv (or nullptr)
     long long p_stride;      // elements, multiple of 4
     const double* beta;      // [nconf*nrep], by slot
+    const float* kb;         // [nconf*nrep], by slot: (float)(-2 beta log2(e)), the FP32 form's
+                             // acceptance scale, rounded once on the host from beta
     const int* temp_of_rep;  // [nconf*nrep]
     const int* rep_at_temp;  // [nconf*nrep]
     const uint32_t* ctl;     // ctl[0] = PT cycle counter

@@ -725,16 +725,23 @@ __global__ void __launch_bounds__(256) sweep_global_kernel(SweepArgs a, int colo
     uint8_t* S = a.spins + (long long)lat * a.lat_stride;
     const Real* P = field_base<Real>(a, conf);
     const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
-    double beta;
+    // FP64 reads the slot's beta, FP32 the slot's acceptance scale (rounded once from beta on
+    // the host: no FP64 operation on a thread that updates one site)
+    double beta = 0.0;
+    float kb = 0.0f;
     uint32_t sweep;
     if (a.use_override) {
         beta = a.beta_override;
+        kb = (float)(-2.0 * beta * 1.4426950408889634);
         sweep = a.sweep_override + (uint32_t)t;
     } else {
-        beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+        const int slot = a.temp_of_rep[conf * a.nrep + rep];
+        if constexpr (sizeof(Real) == 8)
+            beta = a.beta[conf * a.nrep + slot];
+        else
+            kb = a.kb[conf * a.nrep + slot];
         sweep = a.ctl[0] * (uint32_t)a.ptswapever + (uint32_t)t;
     }
-    const float kb = (float)(-2.0 * beta * 1.4426950408889634);
     const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
     const int item = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     Acc acc{0, 0, 0, 0, 0};

@@ -372,9 +372,9 @@ bool usable(const FixedEntry& e, bool fp64, int L, int H, bool vac)
 // Grid: (quads of a colour / NT, lattices).
 // One colour phase of quad o in RPT replicas of one configuration: the field operands are loaded
 // once and shared, the spin operands of every replica are loaded before any is updated.
-template <class Real, int LH, int HH, int C, int RPT, bool VAC>
+template <class Real, int LH, int HH, int C, int RPT, bool VAC, bool SLOTS>
 __device__ __forceinline__ void hbm_phase(const SweepArgs& a, const Real* P, const QuadOff& o,
-                                          int conf, const int* rep, uint32_t sweep)
+                                          int conf, const int* rep, int s0, uint32_t sweep)
 {
     QuadData<Real> d[RPT];
     load_quad_field<Real, LH, HH, C>(P, o, d[0]);
@@ -388,10 +388,17 @@ __device__ __forceinline__ void hbm_phase(const SweepArgs& a, const Real* P, con
     }
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
-        const double beta = a.use_override
-                                ? a.beta_override
-                                : a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep[r]]];
-        const float kb = (float)(-2.0 * beta * 1.4426950408889634);
+        // the replica's slot (s0 + r in the slot-range form), then FP64 its beta, FP32 the slot's
+        // acceptance scale, rounded once from beta on the host (no FP64 operation here)
+        double beta = a.beta_override;
+        float kb = (float)(-2.0 * a.beta_override * 1.4426950408889634);
+        if (!a.use_override) {
+            const int sl = SLOTS ? s0 + r : a.temp_of_rep[conf * a.nrep + rep[r]];
+            if constexpr (sizeof(Real) == 8)
+                beta = a.beta[conf * a.nrep + sl];
+            else
+                kb = a.kb[conf * a.nrep + sl];
+        }
         Acc none{0, 0, 0, 0, 0};
         compute_quad<Real, LH, HH, C, false, VAC, true>(
             a,
@@ -414,11 +421,11 @@ __global__ void __launch_bounds__(NT, sizeof(Real) == 8 ? 1 : RPT == 4 ? 768 / N
     using Sh = Shape<LH, HH>;
     const int q = (int)(blockIdx.x * NT + threadIdx.x);
     if (q >= Sh::CS) return;
-    int conf, rep[RPT];
+    int conf, rep[RPT], s0 = -1;
     if (SLOTS) {
         const int per = a.nslots / RPT;
         conf = a.lat0 / a.nrep + (int)blockIdx.y / per;
-        const int s0 = a.slot0 + ((int)blockIdx.y % per) * RPT;
+        s0 = a.slot0 + ((int)blockIdx.y % per) * RPT;
 #pragma unroll
         for (int r = 0; r < RPT; ++r) rep[r] = a.rep_at_temp[conf * a.nrep + s0 + r];
     } else {
@@ -434,7 +441,7 @@ __global__ void __launch_bounds__(NT, sizeof(Real) == 8 ? 1 : RPT == 4 ? 768 / N
     switch (colour) {
 #define J1J2_HBM_PHASE(C)                                                                     \
     case C:                                                                                   \
-        hbm_phase<Real, LH, HH, C, RPT, VAC>(a, P, o, conf, rep, sweep);                      \
+        hbm_phase<Real, LH, HH, C, RPT, VAC, SLOTS>(a, P, o, conf, rep, s0, sweep);           \
         break;
         J1J2_HBM_PHASE(0)
         J1J2_HBM_PHASE(1)

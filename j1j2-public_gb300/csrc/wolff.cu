@@ -136,16 +136,23 @@ __device__ __forceinline__ bool bond_weight(const SweepArgs& a, int b, int si, i
     return w > Real(0);
 }
 
+// The FP32 trials' scale (float)(-2 beta log2(e)), computed once per lattice: two FP64
+// multiplies and a conversion, which GB300 runs at ~64 clocks each, kept out of the per-bond path
+__device__ __forceinline__ float trial_scale(double beta)
+{
+    return (float)(-2.0 * beta * 1.4426950408889634);
+}
+
 // Activation trial of a bond of weight w > 0 with the uniform of word r: u < 1 - exp(-2 beta w)
+// (FP32: kb = trial_scale(beta))
 template <class Real>
-__device__ __forceinline__ bool bond_trial(Real w, double beta, uint32_t r)
+__device__ __forceinline__ bool bond_trial(Real w, double beta, float kb, uint32_t r)
 {
     if constexpr (sizeof(Real) == 8) {
         const double pa = __dsub_rn(1.0, own_exp(-__dmul_rn(__dmul_rn(2.0, w), beta)));
         return u01_f64(r) < pa;
     } else {
-        const float kb2 = (float)(-2.0 * beta * 1.4426950408889634);
-        const float pa = __fsub_rn(1.0f, ex2_approx(__fmul_rn(kb2, w)));
+        const float pa = __fsub_rn(1.0f, ex2_approx(__fmul_rn(kb, w)));
         return u01_f32(r) < pa;
     }
 }
@@ -174,6 +181,7 @@ __global__ void __launch_bounds__(256) wolff_bond_kernel(SweepArgs a, int* label
     const uint8_t* BM = MASKS ? a.bm + (long long)conf * a.lat_stride : nullptr;
     volatile int* lab = labels + (long long)lat * lab_stride;
     const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+    const float kbw = trial_scale(beta);
     const uint32_t cycle = a.ctl[0];
     const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
     const SiteCoord s = coord_of_compact(g, ci);
@@ -199,7 +207,8 @@ __global__ void __launch_bounds__(256) wolff_bond_kernel(SweepArgs a, int* label
         const uint32_t r =
             b < 4 ? u4_word(inplane, b)
                   : u4_word(philox4x32_10((uint32_t)rep, cycle, grp, kTagWolffZ, k0, k1), X & 3);
-        if (bond_trial<Real>(w, beta, r) && !unite(lab, ci, cj, a.uf_tries)) atomicExch(err, 1);
+        if (bond_trial<Real>(w, beta, kbw, r) && !unite(lab, ci, cj, a.uf_tries))
+            atomicExch(err, 1);
     }
 }
 
@@ -263,8 +272,7 @@ __device__ __forceinline__ unsigned long long uniform_threshold(Real K, double b
         const double pa = __dsub_rn(1.0, own_exp(-__dmul_rn(__dmul_rn(2.0, K), beta)));
         return (unsigned long long)ceil(__dmul_rn(pa, 4294967296.0));
     } else {
-        const float kb2 = (float)(-2.0 * beta * 1.4426950408889634);
-        const float pa = __fsub_rn(1.0f, ex2_approx(__fmul_rn(kb2, K)));
+        const float pa = __fsub_rn(1.0f, ex2_approx(__fmul_rn(trial_scale(beta), K)));
         return (unsigned long long)ceilf(__fmul_rn(pa, 8388608.0f));
     }
 }
@@ -318,6 +326,7 @@ __global__ void __launch_bounds__(512, 2)
 
     // ---- phase A: activated bonds --------------------------------------------------------
     const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+    const float kbw = trial_scale(beta);
     const uint32_t cycle = a.ctl[0];
     const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
     Real J2, J3;
@@ -393,7 +402,7 @@ __global__ void __launch_bounds__(512, 2)
                     have |= 1u << w;
                 }
                 const uint32_t word = b == 4 ? u4_word(rr, w) : u4_word(srr[w], b);
-                const bool on = b < 2 ? bond_trial<Real>(wv[w], beta, word)
+                const bool on = b < 2 ? bond_trial<Real>(wv[w], beta, kbw, word)
                                       : uniform_trial<Real>(b < 4 ? thr2 : thr3, word);
                 if (on) act |= 1u << (5 * w + b);
             }
@@ -514,6 +523,7 @@ __global__ void __launch_bounds__(256) wolff_boundary_kernel(SweepArgs a, int pz
     const uint8_t* S = a.spins + (long long)lat * a.lat_stride;
     volatile int* lab = labels + (long long)lat * lab_stride;
     const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+    const float kbw = trial_scale(beta);
     const uint32_t grp = (uint32_t)(((c * g.Hh + Z) * g.Lh + Y) * g.Qr + Xq);
     const U4 rr = philox4x32_10((uint32_t)rep, a.ctl[0], grp, kTagWolffZ, a.seed,
                                 a.conf_base + (uint32_t)conf);
@@ -526,7 +536,7 @@ __global__ void __launch_bounds__(256) wolff_boundary_kernel(SweepArgs a, int pz
         if (si == 0 || sj == 0) continue;
         Real wv;
         if (!bond_weight<Real>(a, 4, si, sj, 1, 1, Real(0), Real(0), wv)) continue;
-        if (bond_trial<Real>(wv, beta, u4_word(rr, w)) && !unite(lab, ci, cj, a.uf_tries))
+        if (bond_trial<Real>(wv, beta, kbw, u4_word(rr, w)) && !unite(lab, ci, cj, a.uf_tries))
             atomicExch(err, 1);
     }
 }
@@ -596,6 +606,7 @@ struct GrowLattice {
     int rep;
     uint32_t cycle, k0, k1;
     double beta;
+    float kb;                       // trial_scale(beta)
     unsigned long long thr2, thr3;  // uniform thresholds of the J2 and J3 bonds
     int s2, s3;                     // s_i s_j of a satisfied J2 / J3 bond
 };
@@ -610,6 +621,7 @@ __device__ __forceinline__ void grow_entry(const SweepArgs& a, const Geo& g, con
     const int rep = w.rep;
     const uint32_t cycle = w.cycle, k0 = w.k0, k1 = w.k1;
     const double beta = w.beta;
+    const float kbw = w.kb;
     const unsigned long long thr2 = w.thr2, thr3 = w.thr3;
     const int s2 = w.s2, s3 = w.s3;
         const int c = (int)(e >> 29), Z = (int)((e >> 20) & 511), Y = (int)((e >> 11) & 511),
@@ -705,7 +717,7 @@ __device__ __forceinline__ void grow_entry(const SweepArgs& a, const Geo& g, con
                     Real wv;
                     on = bond_weight<Real>(a, b, si, sj, mo & 1, (mo >> 1) & 1, po, pt,
                                            wv) &&
-                         bond_trial<Real>(wv, beta, word[d]);
+                         bond_trial<Real>(wv, beta, kbw, word[d]);
                 } else {
                     on = si * sj == (b < 4 ? s2 : s3) &&
                          uniform_trial<Real>(b < 4 ? thr2 : thr3, word[d]);
@@ -794,6 +806,7 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
     sync_all();
 
     const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+    const float kbw = trial_scale(beta);
     Real J2, J3;
     if constexpr (sizeof(Real) == 8) {
         J2 = a.J2;
@@ -815,6 +828,7 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
     gl.k0 = k0;
     gl.k1 = k1;
     gl.beta = beta;
+    gl.kb = kbw;
     gl.thr2 = thr2;
     gl.thr3 = thr3;
     gl.s2 = s2;
@@ -978,6 +992,7 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
     __syncthreads();
 
     const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+    const float kbw = trial_scale(beta);
     Real J2, J3;
     if constexpr (sizeof(Real) == 8) {
         J2 = a.J2;
@@ -995,6 +1010,7 @@ __global__ void __launch_bounds__(kGrowThreads, 1)
     gl.k0 = k0;
     gl.k1 = k1;
     gl.beta = beta;
+    gl.kb = kbw;
     gl.thr2 = uniform_threshold<Real>(J2 < Real(0) ? -J2 : J2, beta);
     gl.thr3 = uniform_threshold<Real>(J3 < Real(0) ? -J3 : J3, beta);
     gl.s2 = J2 > Real(0) ? 1 : J2 < Real(0) ? -1 : 0;
@@ -1135,6 +1151,7 @@ __global__ void __launch_bounds__(256) wolff_bits_kernel(SweepArgs a, uint8_t* a
     const uint32_t cycle = a.ctl[0];
     const uint32_t k0 = a.seed, k1 = a.conf_base + (uint32_t)conf;
     const double beta = a.beta[conf * a.nrep + a.temp_of_rep[conf * a.nrep + rep]];
+    const float kbw = trial_scale(beta);
     Real J2, J3;
     if constexpr (sizeof(Real) == 8) {
         J2 = a.J2;
@@ -1182,7 +1199,7 @@ __global__ void __launch_bounds__(256) wolff_bits_kernel(SweepArgs a, uint8_t* a
                 Real wv;
                 on = bond_weight<Real>(a, b, si, sj[b], m & 1, (m >> 1) & 1, P[i], P[jn[b]],
                                        wv) &&
-                     bond_trial<Real>(wv, beta, u4_word(own, b));
+                     bond_trial<Real>(wv, beta, kbw, u4_word(own, b));
             } else {
                 on = si * sj[b] == (b < 4 ? s2 : s3) &&
                      uniform_trial<Real>(b < 4 ? thr2 : thr3, b < 4 ? u4_word(own, b)
