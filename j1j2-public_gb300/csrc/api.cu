@@ -1362,8 +1362,19 @@ int tune_split(Ctx* c, Group& grp)
     };
     // (the cold slots' growth from bond activations decided beforehand, bits = true, measured
     // slower on equilibrated L = 96 lattices at every split and is left to its test flag)
+    // split points between 1/4 and 3/4 of the slots: every multiple of 4 there when the ladder
+    // is (the slot-range sweep kernel keeps four replicas per thread only when they divide the
+    // range; L = 96, 48 slots: 8.88 ms at 28 vs 9.03 at 24 and 9.22 at 36), else eighths
     std::vector<SplitChoice> cands{{0, 1, false}};
-    for (const int k : {grp.nrep / 4, grp.nrep / 2, 3 * grp.nrep / 4}) cands.push_back({k, 1, false});
+    auto add = [&](int k) {
+        bool dup = k <= 0 || k >= grp.nrep;
+        for (const SplitChoice& o : cands) dup = dup || o.k == k;
+        if (!dup) cands.push_back({k, 1, false});
+    };
+    if (grp.nrep % 4 == 0 && grp.nrep >= 16)
+        for (int k = grp.nrep / 4; k <= 3 * grp.nrep / 4; k += 4) add(k - k % 4);
+    else
+        for (const int k8 : {2, 3, 4, 5, 6}) add(k8 * grp.nrep / 8);
     // The scratch lattices first run kSplitWarm cycles of the unsplit form at their slots'
     // temperatures (the clusters of a freshly started lattice are far smaller than those of an
     // equilibrated cold one, which decide the choice); each of these cycles reads its own cycle
@@ -1403,7 +1414,7 @@ int tune_split(Ctx* c, Group& grp)
         if (exec) cudaGraphExecDestroy(exec);
         if (e == cudaSuccess && tune_log())
             std::fprintf(stderr,
-                         "j1j2c tune split L=%d H=%d lattices=%d: k=%d cs=%d bits=%d %.3f ms\n",
+                         "[j1j2c tune] split L=%d H=%d lattices=%d: k=%d cs=%d bits=%d %.3f ms\n",
                          grp.g.L, grp.g.H, nlat, cd.k, cd.cs, (int)cd.bits, ms);
         if (e == cudaSuccess && (ci == 0 || ms < best_ms)) {
             best_ms = ms;
