@@ -40,10 +40,13 @@ B_PER_ATTEMPT_FP64 = 21.4
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one sweep-kernel launch (5 sweeps
 # + measure of every lattice), from an ncu capture of the same workload
-TRAFFIC = {"batched_fp32_L32_64x32": 75584000 + 8890368}
+# (the kernel the tuner keeps for the workload: two lattices of one configuration per CTA)
+TRAFFIC = {"batched_fp32_L32_64x32": 75683072 + 8576000}
 # issue-slot utilisation and thread instructions per attempt of the same capture (the kernel is
 # bound by instruction issue inside shared memory, not by DRAM)
-NCU_ISSUE = {"batched_fp32_L32_64x32": {"issue_active": 0.602, "inst_per_attempt": 48.1,
+NCU_ISSUE = {"batched_fp32_L32_64x32": {"issue_active": 0.564, "inst_per_attempt": 44.7,
+                                        "binding_limit": "instruction issue (shared-memory "
+                                                         "resident lattices)",
                                         "source": "profiles/sweep_fixed_fp32_L32_2048lat.md"}}
 
 # name -> lattice-shape groups (L, nconf, nreplica), precision and options
@@ -424,8 +427,7 @@ def run_ours(args):
                      "unit": "GB/s", "frac": round(achieved / hbm, 4),
                      "traffic": None if args.nconf else TRAFFIC.get(wname),
                      "peak_source": peak_src, "bytes_per_attempt": bpa,
-                     "sweep_kernel_ms": round(sweep_ms_avg, 4),
-                     "binding_limit": "instruction issue (shared-memory resident lattices)"},
+                     "sweep_kernel_ms": round(sweep_ms_avg, 4)},
         "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "fp64_plain": dict(fp64, workload="plain_fp64_L24_1x16",
