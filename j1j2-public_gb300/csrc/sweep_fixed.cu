@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_stream_kernel(SweepArgs a, int
     using Sh = Shape<LH, HH>;
     using Lay = StreamLayout<Real, LH, HH>;
     constexpr int QPT = (Sh::CS + NT - 1) / NT;
-    extern __shared__ __align__(128) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char ssmem[];  // 128-aligned bulk-copy buffers
     __shared__ __align__(8) uint64_t bar[3];  // spin buffer 0, spin buffer 1, field
     __shared__ StreamState st;
     const int tid = (int)threadIdx.x;
@@ -247,9 +247,9 @@ __global__ void __launch_bounds__(NT, MINB) sweep_stream_kernel(SweepArgs a, int
         mbar_init(&bar[2], 1);
         mbar_init_fence();
         const int lat = a.lat0 + first;
-        stream_copy_in<Real, LH, HH>(smem + Lay::PB, a.spins + (long long)lat * a.lat_stride,
+        stream_copy_in<Real, LH, HH>(ssmem + Lay::PB, a.spins + (long long)lat * a.lat_stride,
                                      Lay::SB, &bar[0]);
-        stream_copy_in<Real, LH, HH>(smem, field_base<Real>(a, lat / a.nrep), Lay::PB, &bar[2]);
+        stream_copy_in<Real, LH, HH>(ssmem, field_base<Real>(a, lat / a.nrep), Lay::PB, &bar[2]);
         st = StreamState{0u, 1u | 4u, 1, 0};
     }
     OffsetCache<QPT> off;
@@ -257,9 +257,9 @@ __global__ void __launch_bounds__(NT, MINB) sweep_stream_kernel(SweepArgs a, int
     // (the first step's barrier publishes thread 0's initialisation)
 #pragma unroll 1
     for (int l = first; l < last; l += 2) {
-        if (!stream_step<Real, LH, HH, NT, QPT, VAC, 0>(a, smem, bar, &st, off, l, last)) break;
+        if (!stream_step<Real, LH, HH, NT, QPT, VAC, 0>(a, ssmem, bar, &st, off, l, last)) break;
         if (l + 1 < last &&
-            !stream_step<Real, LH, HH, NT, QPT, VAC, 1>(a, smem, bar, &st, off, l + 1, last))
+            !stream_step<Real, LH, HH, NT, QPT, VAC, 1>(a, ssmem, bar, &st, off, l + 1, last))
             break;
     }
     if (tid == 0) {
