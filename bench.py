@@ -207,26 +207,56 @@ def attempts_per_cycle(eng):
     return int((eng.nocc * reps).sum()) * eng.ptswapever
 
 
+class L2Flush:
+    """Empties L2 of a step's data before the next step: a write of a buffer twice the L2's
+    size, then a read of a second one, so that the step starts cold and the lines left in L2
+    are clean (the write alone leaves ~126 MB of dirty lines, whose write-back the step would
+    otherwise pay)."""
+
+    def __init__(self, torch):
+        self.torch = torch
+        self.w = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+        self.r = torch.zeros(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+        self.out = torch.empty((), dtype=torch.float32, device="cuda")
+
+    def __call__(self):
+        self.w.zero_()
+        self.out.copy_(self.r.sum())
+
+
 def time_steps(torch, eng, steps, warmup, flush, cycles=1):
-    """Device time of `steps` steps of `cycles` PT cycles each (CUDA events on the engine's
-    stream), L2 flushed before every step outside the timed interval."""
-    stream = torch.cuda.current_stream()
+    """Device time of `steps` steps of `cycles` PT cycles each: CUDA events on a dedicated
+    stream that also carries the L2 flush before every step (outside the timed interval) and the
+    engine's own launches, so every event, flush and cycle is ordered on one stream."""
+    stream = timing_stream(torch)
     eng.set_stream(stream.cuda_stream)
-    eng.run(warmup, measure=True, restart_swap_phase=True)
-    torch.cuda.synchronize()
-    prof0 = eng.profile()[0]
+    with torch.cuda.stream(stream):
+        eng.run(warmup, measure=True, restart_swap_phase=True)
+        stream.synchronize()
+        prof0 = eng.profile()[0]
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        for k in range(steps):
+            flush()
+            ev[k][0].record(stream)
+            eng.run(cycles, measure=True, restart_swap_phase=False)
+            ev[k][1].record(stream)
+        stream.synchronize()
     total_ms = 0.0
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(steps)]
-    for k in range(steps):
-        flush.zero_()
-        ev[k][0].record(stream)
-        eng.run(cycles, measure=True, restart_swap_phase=False)
-        ev[k][1].record(stream)
-    torch.cuda.synchronize()
     for a, b in ev:
         total_ms += a.elapsed_time(b)
     return total_ms, eng.profile()[0] - prof0
+
+
+_STREAM = []
+
+
+def timing_stream(torch):
+    """One non-default stream for every timed run (a stream handle of 0 would make the engine
+    use its own stream, unordered with the events)."""
+    if not _STREAM:
+        _STREAM.append(torch.cuda.Stream())
+    return _STREAM[0]
 
 
 def time_workload(torch, jc, w, device, flush, steps):
@@ -265,18 +295,19 @@ def wolff_report(torch, jc, w, device, warm=30, n=10):
     stream), flipped-cluster sites per update, sites per ns, and the streaming model of 18 bytes
     per cluster site against the measured copy bandwidth."""
     eng, _ = make_engine(jc, w, device)
-    stream = torch.cuda.current_stream()
+    stream = timing_stream(torch)
     eng.set_stream(stream.cuda_stream)
-    eng.run(warm, measure=False)
-    eng.wolff()
-    torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    sites = 0
-    a.record(stream)
-    for _ in range(n):
-        sites += int(eng.wolff().sum())
-    b.record(stream)
-    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        eng.run(warm, measure=False)
+        eng.wolff()
+        stream.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        sites = 0
+        a.record(stream)
+        for _ in range(n):
+            sites += int(eng.wolff().sum())
+        b.record(stream)
+        stream.synchronize()
     ms = a.elapsed_time(b) / n
     eng.close()
     per = sites / n
@@ -344,7 +375,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    flush = L2Flush(torch)
 
     wname = args.workload
     w = WORKLOADS[wname]
@@ -422,7 +453,7 @@ def run_ours(args):
     clocks = clk.summary()
     config = workload_config(wname, w, ws)
     config["attempts_per_step"] = attempts_per_step * ws
-    config["l2"] = "flushed before each step"
+    config["l2"] = "flushed before each step (256 MB written, then 256 MB read)"
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup,
@@ -527,7 +558,7 @@ def run_reference(args):
     value = attempts * args.steps / total / 1e9
     config = workload_config(args.workload, w, ws)
     config["attempts_per_step"] = attempts
-    config["l2"] = "flushed before each step"
+    config["l2"] = "flushed before each step (256 MB written, then 256 MB read)"
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": UNIT,
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(total * 1e3 / args.steps, 2), "higher_is_better": True,
