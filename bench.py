@@ -236,11 +236,15 @@ def time_steps(torch, eng, steps, warmup, flush, cycles=1):
         prof0 = eng.profile()[0]
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(steps)]
+        # the cycles are enqueued without waiting, so each step's closing event follows its
+        # cycles directly on the stream (j1j2c_run would wait, and the event would also time the
+        # host's return from that wait)
         for k in range(steps):
             flush()
             ev[k][0].record(stream)
-            eng.run(cycles, measure=True, restart_swap_phase=False)
+            eng.enqueue(cycles, measure=True, restart_swap_phase=False)
             ev[k][1].record(stream)
+        eng.sync()
         stream.synchronize()
     total_ms = 0.0
     for a, b in ev:

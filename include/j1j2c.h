@@ -214,6 +214,15 @@ int j1j2c_set_diagnostics(void *ctx, const j1j2c_diagnostics *diag);
  * PTSWAPEVER = 1 it is the LOCAL Equilibration_loop / Measurement_loop (J:2122-2216). */
 int j1j2c_run(void *ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_phase);
 
+/* The same cycles enqueued on the context's stream without waiting for them (j1j2c_run is this
+ * followed by j1j2c_sync): the caller overlaps host work or queues further stream work behind
+ * them.  Until j1j2c_sync returns, no other call may read or change the context's state. */
+int j1j2c_enqueue(void *ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_phase);
+
+/* Waits for every enqueued cycle and reports as j1j2c_run does (J1J2C_ETIMEOUT when a bounded
+ * device wait gave up, the context staying usable). */
+int j1j2c_sync(void *ctx);
+
 /* Drop-in for one call of Metro_sweep (J:2544-2608) on one lattice: nsweeps FP64 sweeps of
  * replica rep of conf at inverse temperature beta, Philox sweep counter starting at sweep_index.
  * On return mag/en/strx/stry (each may be NULL) hold the Measurement values (J:2807-2842) of the

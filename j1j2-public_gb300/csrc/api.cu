@@ -2294,7 +2294,7 @@ int take_device_error(Ctx* c, int& herr)
     return J1J2C_OK;
 }
 
-int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_phase)
+int j1j2c_enqueue(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_phase)
 {
     if (!ctx) return J1J2C_EINVAL;
     Ctx* c = static_cast<Ctx*>(ctx);
@@ -2346,6 +2346,13 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
         }
         CK(c, cudaGraphLaunch(c->graph[m], c->st));
     }
+    return J1J2C_OK;
+}
+
+int j1j2c_sync(void* ctx)
+{
+    if (!ctx) return J1J2C_EINVAL;
+    Ctx* c = static_cast<Ctx*>(ctx);
     CK(c, cudaStreamSynchronize(c->st));
     if (c->profile) {
         const int rc = drain_profile(c);
@@ -2365,6 +2372,12 @@ int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_
                         "or a grid barrier of the cooperative form)");
     }
     return J1J2C_OK;
+}
+
+int j1j2c_run(void* ctx, int32_t ncycles, int32_t measure, int32_t restart_swap_phase)
+{
+    const int rc = j1j2c_enqueue(ctx, ncycles, measure, restart_swap_phase);
+    return rc != J1J2C_OK ? rc : j1j2c_sync(ctx);
 }
 
 int j1j2c_wolff(void* ctx, int64_t* cluster_sizes)

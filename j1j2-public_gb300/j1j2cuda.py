@@ -40,7 +40,8 @@ SUM_FIELDS = ("mag", "absmag", "mag2", "mag4", "en", "en2", "strx_abs", "stry_ab
 
 EXPORTS = ("j1j2c_create", "j1j2c_create_multi", "j1j2c_conf_shape", "j1j2c_destroy", "j1j2c_last_error", "j1j2c_set_stream",
            "j1j2c_set_disorder", "j1j2c_set_ladder", "j1j2c_init_spins",
-           "j1j2c_reset_measurements", "j1j2c_run", "j1j2c_metro_sweep_fp64", "j1j2c_audit_fp32",
+           "j1j2c_reset_measurements", "j1j2c_run", "j1j2c_enqueue", "j1j2c_sync",
+           "j1j2c_metro_sweep_fp64", "j1j2c_audit_fp32",
            "j1j2c_get_slot_sums", "j1j2c_get_pt_stats", "j1j2c_get_maps", "j1j2c_get_spins",
            "j1j2c_get_observables", "j1j2c_get_profile", "j1j2c_get_config",
            "j1j2c_corr_rand_3d", "j1j2c_setup_vacancies", "j1j2c_kiss_spins", "j1j2c_ladder",
@@ -304,6 +305,14 @@ class Engine:
     def run(self, ncycles, measure=True, restart_swap_phase=True):
         self._ck(lib().j1j2c_run(self._ctx, C.c_int32(ncycles), C.c_int32(int(measure)),
                                  C.c_int32(int(restart_swap_phase))))
+
+    def enqueue(self, ncycles, measure=True, restart_swap_phase=True):
+        """run() without waiting: the cycles are queued on the context's stream; sync() waits."""
+        self._ck(lib().j1j2c_enqueue(self._ctx, C.c_int32(ncycles), C.c_int32(int(measure)),
+                                     C.c_int32(int(restart_swap_phase))))
+
+    def sync(self):
+        self._ck(lib().j1j2c_sync(self._ctx))
 
     def metro_sweep_fp64(self, conf, rep, beta, sweep_index, nsweeps=1):
         out = [C.c_double() for _ in range(4)]

@@ -727,3 +727,26 @@ def test_replicated_cluster_fp32_and_flip_counts_bitwise(engine_mod, oracle):
     np.testing.assert_array_equal(out[0][2], out[1][2])
     for a, b in zip(out[0][3], out[1][3]):
         np.testing.assert_array_equal(a, b)
+
+
+def test_enqueue_then_sync_equals_run(engine_mod, oracle):
+    """Cycles queued with j1j2c_enqueue (no wait) and collected with j1j2c_sync give exactly the
+    state j1j2c_run gives (FP64, equal to the replay too)."""
+    jc = engine_mod
+    L, H, nconf, nrep = 16, 8, 2, 4
+    out = []
+    for mode in ("run", "enqueue"):
+        eng, models, betas = _setup(jc, oracle, L, H, nconf, nrep, jc.FP64_PLAIN, pp=0.05)
+        if mode == "run":
+            eng.run(3, measure=True)
+        else:
+            eng.enqueue(1, measure=True, restart_swap_phase=True)
+            eng.enqueue(2, measure=True, restart_swap_phase=False)
+            eng.sync()
+        out.append(([eng.spins(k, r) for k in range(nconf) for r in range(nrep)],
+                    eng.slot_sums(-1)[0], eng.maps(0)[0]))
+        eng.close()
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    np.testing.assert_array_equal(out[0][2], out[1][2])
