@@ -693,16 +693,21 @@ cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int n
         if ((e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st)) != cudaSuccess) return e;
         return launch_sweep_coop(a, v, nlat, bar, st, false);
     }
-    // one launch per colour phase: the observables are zeroed first (no sweep reads them), so
-    // every launch after the first follows a kernel of the same chain and may overlap its tail
-    // (programmatic dependent launch: each kernel waits for its predecessor before any access)
-    if ((e = cudaMemsetAsync(a.obs + a.lat0, 0, sizeof(LatObs) * nlat, st)) != cudaSuccess)
+    // one launch per colour phase, every launch after the first following a kernel of the same
+    // chain and overlapping its tail (programmatic dependent launch: each kernel waits for its
+    // predecessor before any access).  The observables, which no sweep reads, are zeroed by the
+    // first launch of the generic kernel (no graph node of its own) or before the chain.
+    const bool zero_in_kernel = v.fixed_nt <= 0 && a.nsweeps > 0;
+    if (!zero_in_kernel &&
+        (e = cudaMemsetAsync(a.obs + a.lat0, 0, sizeof(LatObs) * nlat, st)) != cudaSuccess)
         return e;
     for (int t = 0; t < a.nsweeps; ++t)
         for (int col = 0; col < 8; ++col) {
             a.pdl = (t > 0 || col > 0) ? 1 : 0;
+            a.zero_obs = zero_in_kernel && t == 0 && col == 0 ? 1 : 0;
             if ((e = launch_sweep_global(a, v, col, t, nlat, st)) != cudaSuccess) return e;
         }
+    a.zero_obs = 0;
     a.pdl = 1;
     (void)grp;
     (void)c;

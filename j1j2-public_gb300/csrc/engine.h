@@ -59,6 +59,8 @@ struct SweepArgs {
     int* err;                // set to 1 when a bounded wait of a kernel gave up (or nullptr)
     int uf_tries;            // union-find attempts per bond before the labelling gives up
     int pdl;                 // host side: the launch may overlap the stream's previous kernel
+    int zero_obs;            // generic global-memory sweep: this launch zeroes its lattices'
+                             // observables (the first colour phase of a cycle)
                              // (programmatic dependent launch; global-memory kernels only)
     int slot0, nslots;       // HBM sweep kernel: temperature slots [slot0, slot0 + nslots) of
                              // every configuration of the launch, each slot's lattice found

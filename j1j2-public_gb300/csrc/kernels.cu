@@ -720,6 +720,8 @@ __global__ void __launch_bounds__(256) sweep_global_kernel(SweepArgs a, int colo
     pdl_release();
     const Geo g = a.g;
     const int lat = a.lat0 + (int)blockIdx.y;
+    if (a.zero_obs && blockIdx.x == 0 && threadIdx.x == 0)  // the measurement launch adds here
+        store_obs(a.obs + lat, Acc{0, 0, 0, 0, 0});
     const int conf = lat / a.nrep;
     const int rep = lat - conf * a.nrep;
     uint8_t* S = a.spins + (long long)lat * a.lat_stride;
