@@ -29,8 +29,8 @@ def _nvcc() -> str:
 
 def _sources():
     cu = [os.path.join(CSRC, f)
-          for f in ("sweep_fixed.cu", "sweep_multi.cu", "kernels.cu", "wolff.cu", "enumerate.cu",
-                    "disorder.cu", "api.cu")]
+          for f in ("sweep_fixed.cu", "sweep_hbm.cu", "sweep_multi.cu", "kernels.cu", "wolff.cu",
+                    "enumerate.cu", "disorder.cu", "api.cu")]
     cpp = [os.path.join(CSRC, f) for f in ("host_model.cpp", "results.cpp")]
     hdr = [os.path.join(CSRC, f) for f in ("device_common.cuh", "engine.h", "sweep_common.cuh",
                                            "quad_sweep.cuh")]
