@@ -1639,6 +1639,12 @@ int autotune(Ctx* c, Group& grp)
             if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
             float ms = 0.0f;
             if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+            if (e == cudaSuccess && tune_log())
+                std::fprintf(stderr,
+                             "[j1j2c tune] sweep L=%d H=%d lattices=%d: nt=%d minb=%d stream=%d "
+                             "rpc=%d %.4f ms\n",
+                             grp.g.L, grp.g.H, nlat, fc[k].nt, fc[k].minb, (int)fc[k].stream,
+                             fc[k].rpc, ms / 3.0f);
             if (e == cudaSuccess && ms < best_ms) {
                 best_ms = ms;
                 best = k;
