@@ -263,14 +263,18 @@ def timing_stream(torch):
     return _STREAM[0]
 
 
-def time_workload(torch, jc, w, device, flush, steps):
+def time_workload(torch, jc, w, device, flush, steps, min_ms=60.0, max_steps=200):
     """Device throughput of one workload (CUDA events per step, L2 flushed between).  The value
     comes from an engine without profiling events (graph event nodes cost microseconds per
     cycle, a sizeable share of a small lattice's cycle); a second engine with them gives its own
-    step time and the sweep launches' share of it, over the same number of steps."""
+    step time and the sweep launches' share of it, over the same number of steps.  A short
+    workload gets more steps (up to max_steps), so that at least min_ms of device time is timed:
+    three steps after three warm-up steps estimate the step time."""
     cycles = w.get("cycles_per_step", 1)
     eng, _ = make_engine(jc, w, device)
-    ms, _ = time_steps(torch, eng, steps, 3, flush, cycles)
+    est, _ = time_steps(torch, eng, 3, 3, flush, cycles)
+    steps = max(steps, min(max_steps, int(np.ceil(min_ms * 3 / max(est, 1e-3)))))
+    ms, _ = time_steps(torch, eng, steps, 1, flush, cycles)
     eng.close()
     eng, _ = make_engine(jc, w, device, flags=jc.FLAG_PROFILE)
     pms, prof_ms = time_steps(torch, eng, steps, 3, flush, cycles)

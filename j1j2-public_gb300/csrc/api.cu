@@ -607,7 +607,7 @@ int split_cs_of(const Ctx* c, const Group& grp)
 // its arguments, whole configurations), split by temperature slot: the k coldest slots of every
 // configuration on stream st, the others on the group's Wolff side stream.  The hot lattices'
 // sweeps run while the cold lattices' clusters still grow; every lattice keeps its own order
-// (its Wolff update, then its sweeps), and the observables follow both halves.
+// (its Wolff update, then its sweeps, then its observables).
 cudaError_t enqueue_split(Ctx* c, const Group& grp, const SweepVariant& v, SweepArgs a, int k,
                           int cs, cudaStream_t st, bool bits)
 {
@@ -644,12 +644,13 @@ cudaError_t enqueue_split(Ctx* c, const Group& grp, const SweepVariant& v, Sweep
                 b.pdl = (t > 0 || col > 0) ? 1 : 0;
                 if ((e = launch_sweep_global(b, v, col, t, nlat, ss[h])) != cudaSuccess) return e;
             }
+        // each half measures its own lattices, so the hot half's measurement overlaps the cold
+        // half's sweeps
+        b.pdl = 1;
+        if ((e = launch_measure_global(b, v, nlat, ss[h])) != cudaSuccess) return e;
     }
     if ((e = cudaEventRecord(c->wjoin[gi], c->wside[gi])) != cudaSuccess) return e;
-    if ((e = cudaStreamWaitEvent(st, c->wjoin[gi], 0)) != cudaSuccess) return e;
-    a.pdl = 0;
-    a.nslots = 0;
-    return launch_measure_global(a, v, nlat, st);
+    return cudaStreamWaitEvent(st, c->wjoin[gi], 0);
 }
 
 // PTSWAPEVER sweeps and the observable reduction of lattices [lat0, lat0 + nlat) of a group

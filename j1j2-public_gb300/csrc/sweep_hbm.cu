@@ -104,15 +104,29 @@ __global__ void __launch_bounds__(NT, sizeof(Real) == 8 ? 1 : RPT == 4 ? 768 / N
 // Observables: one thread per quad in RPT replicas of one configuration (field operands loaded
 // once), grid (quads / NT, lattices / RPT, colour); per-CTA sums are added into the lattices'
 // (zeroed) observables with atomics (integer sums: order-independent).
-template <class Real, int LH, int HH, int NT, int RPT, bool VAC>
+// SLOTS: block row y covers the temperature slots of the sweep kernel's slot-range form, so each
+// half of the split cycle measures its own lattices.
+template <class Real, int LH, int HH, int NT, int RPT, bool VAC, bool SLOTS>
 __global__ void __launch_bounds__(NT) measure_fixed_hbm_kernel(SweepArgs a)
 {
     pdl_wait();
     pdl_release();
     using Sh = Shape<LH, HH>;
     const int q = (int)(blockIdx.x * NT + threadIdx.x);
-    const int lat = a.lat0 + (int)blockIdx.y * RPT;
-    const int conf = lat / a.nrep;
+    int conf, lats[RPT];
+    if (SLOTS) {
+        const int per = a.nslots / RPT;
+        conf = a.lat0 / a.nrep + (int)blockIdx.y / per;
+        const int s0 = a.slot0 + ((int)blockIdx.y % per) * RPT;
+#pragma unroll
+        for (int r = 0; r < RPT; ++r)
+            lats[r] = conf * a.nrep + a.rep_at_temp[conf * a.nrep + s0 + r];
+    } else {
+        const int lat = a.lat0 + (int)blockIdx.y * RPT;
+        conf = lat / a.nrep;
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) lats[r] = lat + r;
+    }
     const Real* P = field_base<Real>(a, conf);
     Acc acc[RPT];
 #pragma unroll
@@ -128,7 +142,7 @@ __global__ void __launch_bounds__(NT) measure_fixed_hbm_kernel(SweepArgs a)
         {                                                                                       \
             if (r > 0) d[r] = d[0];                                                             \
             load_quad_spins<Real, LH, HH, C>(                                                   \
-                reinterpret_cast<const uint32_t*>(a.spins + (long long)(lat + r) * a.lat_stride), \
+                reinterpret_cast<const uint32_t*>(a.spins + (long long)lats[r] * a.lat_stride), \
                 o, d[r]);                                                                       \
         }                                                                                       \
         _Pragma("unroll") for (int r = 0; r < RPT; ++r)                                         \
@@ -153,7 +167,7 @@ __global__ void __launch_bounds__(NT) measure_fixed_hbm_kernel(SweepArgs a)
     for (int r = 0; r < RPT; ++r) {
         const Acc tot = block_reduce(acc[r]);
         if (threadIdx.x == 0) {
-            LatObs* ob = a.obs + lat + r;
+            LatObs* ob = a.obs + lats[r];
             atomicAdd(reinterpret_cast<unsigned long long*>(&ob->eacc), (unsigned long long)tot.e);
             atomicAdd(&ob->M, tot.M);
             atomicAdd(&ob->SX, tot.SX);
@@ -171,15 +185,26 @@ cudaError_t run_hbm(const SweepArgs& a, int colour, int t, int nlat, int rpt, cu
     const unsigned gx = (unsigned)((CS + NT - 1) / NT);
     const bool pdl = a.pdl != 0;
     const dim3 b((unsigned)NT);
+    if (colour < 0 && a.nslots > 0) {  // the slot range of every configuration
+        const unsigned gy = (unsigned)(nlat / a.nrep * (a.nslots / rpt));
+        if (rpt == 4)
+            return launch_k(pdl, dim3(gx, gy, 8u), b, 0, st,
+                            measure_fixed_hbm_kernel<Real, LH, HH, NT, 4, true, true>, a);
+        if (rpt == 2)
+            return launch_k(pdl, dim3(gx, gy, 8u), b, 0, st,
+                            measure_fixed_hbm_kernel<Real, LH, HH, NT, 2, true, true>, a);
+        return launch_k(pdl, dim3(gx, gy, 8u), b, 0, st,
+                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 1, true, true>, a);
+    }
     if (colour < 0 && rpt == 4)
         return launch_k(pdl, dim3(gx, (unsigned)(nlat / 4), 8u), b, 0, st,
-                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 4, true>, a);
+                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 4, true, false>, a);
     if (colour < 0 && rpt == 2)
         return launch_k(pdl, dim3(gx, (unsigned)(nlat / 2), 8u), b, 0, st,
-                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 2, true>, a);
+                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 2, true, false>, a);
     if (colour < 0)
         return launch_k(pdl, dim3(gx, (unsigned)nlat, 8u), b, 0, st,
-                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 1, true>, a);
+                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 1, true, false>, a);
     if (a.nslots > 0) {  // a slot range of every configuration (nlat: whole configurations)
         const unsigned gy = (unsigned)(nlat / a.nrep * (a.nslots / rpt));
         if (rpt == 4)
@@ -238,7 +263,7 @@ cudaError_t launch_fixed_hbm(const SweepArgs& a, bool fp64, int colour, int t, i
     if (rpt > 1 && (a.nrep % rpt != 0 || a.lat0 % a.nrep != 0 || nlat % a.nrep != 0)) rpt = 1;
     if (rpt != 2 && rpt != 4) rpt = 1;
     if (a.nslots > 0) {  // slot ranges: whole configurations, RPT dividing the range
-        if (colour < 0 || a.lat0 % a.nrep != 0 || nlat % a.nrep != 0 || a.slot0 < 0 ||
+        if (a.lat0 % a.nrep != 0 || nlat % a.nrep != 0 || a.slot0 < 0 ||
             a.slot0 + a.nslots > a.nrep)
             return cudaErrorInvalidValue;
         while (rpt > 1 && a.nslots % rpt != 0) rpt /= 2;
