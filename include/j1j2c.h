@@ -55,7 +55,9 @@ extern "C" {
 #define J1J2C_FLAG_WOLFF_SPLIT 1024u /* with J1J2C_FLAG_WOLFF and lattices in HBM (one launch per
                                         colour): the Wolff update and sweeps of the coldest quarter
                                         of the slots on one stream, those of the other slots on a
-                                        second one (testing; else tuned)                          */
+                                        second one; J1J2C_SPLIT="k1,k2,..." in the environment
+                                        splits the slots at k1, k2, ... into up to eight ranges on
+                                        as many streams (testing; else tuned)                     */
 #define J1J2C_FLAG_STREAM 512u   /* the streaming form of the shape-specialised kernels: one CTA
                                     per SM through a range of lattices (testing; else tuned)      */
 #define J1J2C_FLAG_WOLFF_BITS 2048u /* the Wolff growth reads bond activations decided beforehand

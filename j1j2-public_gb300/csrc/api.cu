@@ -34,6 +34,9 @@ void j1j2::set_global_error(const char* msg) { g_create_error = msg; }
 
 namespace {
 
+// Temperature ranges of the split Wolff + sweep cycle at most (one stream each)
+constexpr int kSplitRanges = 8;
+
 struct Group {
     Geo g{};
     int nconf = 0, nrep = 0, conf0 = 0, rep0 = 0, block_threads = 0;
@@ -46,11 +49,13 @@ struct Group {
     bool tuned = false;
     int wolff_cs = 0;  // CTAs per lattice of the Wolff growth kernel (0: not tuned, 1)
     int wolff_k = 0;   // 0 < k < nrep: only the k coldest slots take wolff_cs CTAs, the rest one
-    // HBM sweep form with Wolff: 0 < split_k < nrep runs the Wolff update and sweeps of the
-    // split_k coldest slots of every configuration (split_cs CTAs per growing cluster) on the
-    // main stream and those of the other slots on the Wolff side stream
-    int split_k = 0, split_cs = 1;
-    // the Wolff update of the cold slots (split form: slots [0, split_k); unsplit: every slot)
+    // HBM sweep form with Wolff: 0 < split[0] < nrep runs the Wolff update, sweeps and
+    // observables of every configuration's temperature slots as up to kSplitRanges ranges on as
+    // many streams, the boundaries 0 < split[0] < split[1] < ... < nrep (a 0 ends the list);
+    // the coldest range takes split_cs CTAs per growing cluster
+    int split[kSplitRanges - 1] = {};
+    int split_cs = 1;
+    // the Wolff update of the cold slots (split form: slots [0, split[0]); unsplit: every slot)
     // reads bond activations decided beforehand on every SM (wolff_bits_kernel)
     bool split_bits = false;
     int nlat() const { return nconf * nrep; }
@@ -102,7 +107,8 @@ struct Ctx {
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> join_ev;
     cudaEvent_t fork_ev = nullptr;
-    // per group: the side stream and events of a Wolff update split over two launches
+    // per group: the fork event, and kSplitRanges - 1 side streams with their join events, of
+    // a Wolff update split over two launches or of the split Wolff + sweep cycle
     std::vector<cudaStream_t> wside;
     std::vector<cudaEvent_t> wfork, wjoin;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -522,22 +528,35 @@ int wolff_k_of(const Ctx* c, const Group& grp)
     return f ? 0 : grp.wolff_k;
 }
 
-// The group's Wolff side stream and events (created with the context)
+// The group's Wolff side streams and events (created with the context)
 cudaError_t wolff_side(Ctx* c, const Group& grp)
 {
+    constexpr size_t ns = kSplitRanges - 1;
     const size_t k = (size_t)(&grp - c->G.data());
-    if (c->wside.size() < c->G.size()) {
-        c->wside.resize(c->G.size(), nullptr);
+    if (c->wfork.size() < c->G.size()) {
+        c->wside.resize(c->G.size() * ns, nullptr);
+        c->wjoin.resize(c->G.size() * ns, nullptr);
         c->wfork.resize(c->G.size(), nullptr);
-        c->wjoin.resize(c->G.size(), nullptr);
     }
     cudaError_t e = cudaSuccess;
-    if (!c->wside[k]) e = cudaStreamCreateWithFlags(&c->wside[k], cudaStreamNonBlocking);
+    for (size_t j = k * ns; j < (k + 1) * ns && e == cudaSuccess; ++j) {
+        if (!c->wside[j]) e = cudaStreamCreateWithFlags(&c->wside[j], cudaStreamNonBlocking);
+        if (e == cudaSuccess && !c->wjoin[j])
+            e = cudaEventCreateWithFlags(&c->wjoin[j], cudaEventDisableTiming);
+    }
     if (e == cudaSuccess && !c->wfork[k])
         e = cudaEventCreateWithFlags(&c->wfork[k], cudaEventDisableTiming);
-    if (e == cudaSuccess && !c->wjoin[k])
-        e = cudaEventCreateWithFlags(&c->wjoin[k], cudaEventDisableTiming);
     return e;
+}
+
+// Side stream j (0 .. kSplitRanges - 2) of group gi, and its join event
+cudaStream_t side_of(const Ctx* c, size_t gi, int j)
+{
+    return c->wside[gi * (kSplitRanges - 1) + (size_t)j];
+}
+cudaEvent_t join_of(const Ctx* c, size_t gi, int j)
+{
+    return c->wjoin[gi * (kSplitRanges - 1) + (size_t)j];
 }
 
 // The growth reads bond activations decided beforehand (test flag, or the split tuner's choice)
@@ -575,25 +594,41 @@ cudaError_t enqueue_wolff_grow(Ctx* c, const Group& grp, const SweepArgs& a, int
                                  grow_cs(c, grp, cs), lab, grp.lat_stride, cz, st);
     const size_t gi = (size_t)(&grp - c->G.data());
     cudaError_t e;
+    const cudaStream_t side = side_of(c, gi, 0);
     if ((e = cudaEventRecord(c->wfork[gi], st)) != cudaSuccess) return e;
-    if ((e = cudaStreamWaitEvent(c->wside[gi], c->wfork[gi], 0)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(side, c->wfork[gi], 0)) != cudaSuccess) return e;
     if ((e = launch_wolff_grow(a, grp.var.fp64, c->masks, grp.nconf, 0, k, cs, lab,
                                grp.lat_stride, cz, st)) != cudaSuccess)
         return e;
     if ((e = launch_wolff_grow(a, grp.var.fp64, c->masks, grp.nconf, k, grp.nrep - k,
-                               grow_cs(c, grp, 1), lab, grp.lat_stride, cz, c->wside[gi])) !=
+                               grow_cs(c, grp, 1), lab, grp.lat_stride, cz, side)) !=
         cudaSuccess)
         return e;
-    if ((e = cudaEventRecord(c->wjoin[gi], c->wside[gi])) != cudaSuccess) return e;
-    return cudaStreamWaitEvent(st, c->wjoin[gi], 0);
+    if ((e = cudaEventRecord(join_of(c, gi, 0), side)) != cudaSuccess) return e;
+    return cudaStreamWaitEvent(st, join_of(c, gi, 0), 0);
 }
 
-// Coldest slots of the split Wolff + sweep form (0: not split)
-int split_k_of(const Ctx* c, const Group& grp)
+// The split points of the split Wolff + sweep form into pts (kSplitRanges - 1 entries, a 0
+// ending the list; pts[0] = 0: not split).  J1J2C_FLAG_WOLFF_SPLIT pins them: a quarter of the
+// slots, or J1J2C_SPLIT="k1,k2,..." from the environment (tests); else the tuner's choice.
+void split_of(const Ctx* c, const Group& grp, int* pts)
 {
-    if (!c->wolff || !grp.var.global || grp.var.fixed_nt <= 0) return 0;
-    if (c->P.flags & J1J2C_FLAG_WOLFF_SPLIT) return grp.nrep >= 2 ? (grp.nrep + 3) / 4 : 0;
-    return grp.split_k;
+    for (int j = 0; j < kSplitRanges - 1; ++j) pts[j] = 0;
+    if (!c->wolff || !grp.var.global || grp.var.fixed_nt <= 0) return;
+    if (!(c->P.flags & J1J2C_FLAG_WOLFF_SPLIT)) {
+        for (int j = 0; j < kSplitRanges - 1; ++j) pts[j] = grp.split[j];
+        return;
+    }
+    pts[0] = grp.nrep >= 2 ? (grp.nrep + 3) / 4 : 0;
+    const char* env = std::getenv("J1J2C_SPLIT");
+    // the ascending prefix inside (0, nrep) of the comma-separated list
+    for (int j = 0, prev = 0; env && *env && j < kSplitRanges - 1; ++j) {
+        char* end = nullptr;
+        const long x = std::strtol(env, &end, 10);
+        if (end == env || x <= prev || x >= grp.nrep) break;
+        pts[j] = prev = (int)x;
+        env = *end == ',' ? end + 1 : end;
+    }
 }
 
 // CTAs per growing cluster of the split form's cold slots
@@ -604,12 +639,14 @@ int split_cs_of(const Ctx* c, const Group& grp)
 }
 
 // The Wolff update, PTSWAPEVER sweeps and the observables of a group in the HBM sweep form (a:
-// its arguments, whole configurations), split by temperature slot: the k coldest slots of every
-// configuration on stream st, the others on the group's Wolff side stream.  The hot lattices'
-// sweeps run while the cold lattices' clusters still grow; every lattice keeps its own order
-// (its Wolff update, then its sweeps, then its observables).
-cudaError_t enqueue_split(Ctx* c, const Group& grp, const SweepVariant& v, SweepArgs a, int k,
-                          int cs, cudaStream_t st, bool bits)
+// its arguments, whole configurations), split by temperature slot at the points pts (ascending,
+// a 0 ending the list): the coldest range of every configuration on stream st, each other
+// range on one of the group's side streams.  The hotter lattices' sweeps run while the colder
+// lattices' clusters still grow, and a short coldest range keeps the sweeps that follow the
+// longest growths short; every lattice keeps its own order (its Wolff update, then its sweeps,
+// then its observables).
+cudaError_t enqueue_split(Ctx* c, const Group& grp, const SweepVariant& v, SweepArgs a,
+                          const int* pts, int cs, cudaStream_t st, bool bits)
 {
     const size_t gi = (size_t)(&grp - c->G.data());
     const int nlat = grp.nlat();
@@ -619,11 +656,21 @@ cudaError_t enqueue_split(Ctx* c, const Group& grp, const SweepVariant& v, Sweep
     if ((e = cudaMemsetAsync(cz, 0, sizeof(long long) * nlat, st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(a.obs + a.lat0, 0, sizeof(LatObs) * nlat, st)) != cudaSuccess)
         return e;
+    int s0[kSplitRanges] = {0}, nh = 1;  // range h: slots [s0[h], s0[h + 1])
+    while (nh < kSplitRanges && pts[nh - 1] > s0[nh - 1] && pts[nh - 1] < grp.nrep) {
+        s0[nh] = pts[nh - 1];
+        ++nh;
+    }
+    if (nh < 2) return cudaErrorInvalidValue;
+    const int k = s0[1];
     if ((e = cudaEventRecord(c->wfork[gi], st)) != cudaSuccess) return e;
-    if ((e = cudaStreamWaitEvent(c->wside[gi], c->wfork[gi], 0)) != cudaSuccess) return e;
-    const cudaStream_t ss[2] = {st, c->wside[gi]};
-    const int s0[2] = {0, k}, ns[2] = {k, grp.nrep - k}, ncs[2] = {cs, 1};
-    for (int h = 0; h < 2; ++h) {
+    cudaStream_t ss[kSplitRanges] = {st};
+    for (int h = 1; h < nh; ++h) {
+        ss[h] = side_of(c, gi, h - 1);
+        if ((e = cudaStreamWaitEvent(ss[h], c->wfork[gi], 0)) != cudaSuccess) return e;
+    }
+    for (int h = 0; h < nh; ++h) {
+        const int ns = (h + 1 < nh ? s0[h + 1] : grp.nrep) - s0[h];
         SweepArgs b = a;
         if (h == 0 && bits && c->d_act) {  // the cold slots: activations first, on every SM
             uint8_t* act = c->d_act + grp.spin_off;
@@ -633,24 +680,28 @@ cudaError_t enqueue_split(Ctx* c, const Group& grp, const SweepVariant& v, Sweep
             e = launch_wolff_grow(b, v.fp64, c->masks, grp.nconf, 0, k, 1, lab, grp.lat_stride,
                                   cz, st, act, grp.lat_stride);
         } else {
-            e = launch_wolff_grow(b, v.fp64, c->masks, grp.nconf, s0[h], ns[h],
-                                  grow_cs(c, grp, ncs[h]), lab, grp.lat_stride, cz, ss[h]);
+            e = launch_wolff_grow(b, v.fp64, c->masks, grp.nconf, s0[h], ns,
+                                  grow_cs(c, grp, h == 0 ? cs : 1), lab, grp.lat_stride, cz,
+                                  ss[h]);
         }
         if (e != cudaSuccess) return e;
         b.slot0 = s0[h];
-        b.nslots = ns[h];
+        b.nslots = ns;
         for (int t = 0; t < a.nsweeps; ++t)
             for (int col = 0; col < 8; ++col) {
                 b.pdl = (t > 0 || col > 0) ? 1 : 0;
                 if ((e = launch_sweep_global(b, v, col, t, nlat, ss[h])) != cudaSuccess) return e;
             }
-        // each half measures its own lattices, so the hot half's measurement overlaps the cold
-        // half's sweeps
+        // each range measures its own lattices, so a hotter range's measurement overlaps the
+        // colder ranges' sweeps
         b.pdl = 1;
         if ((e = launch_measure_global(b, v, nlat, ss[h])) != cudaSuccess) return e;
     }
-    if ((e = cudaEventRecord(c->wjoin[gi], c->wside[gi])) != cudaSuccess) return e;
-    return cudaStreamWaitEvent(st, c->wjoin[gi], 0);
+    for (int h = 1; h < nh; ++h) {
+        if ((e = cudaEventRecord(join_of(c, gi, h - 1), ss[h])) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(st, join_of(c, gi, h - 1), 0)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 // PTSWAPEVER sweeps and the observable reduction of lattices [lat0, lat0 + nlat) of a group
@@ -674,9 +725,10 @@ cudaError_t enqueue_group(Ctx* c, const Group& grp, const SweepVariant& v, int n
 {
     cudaError_t e;
     if (cycle && c->wolff && nlat == grp.nlat() && v.global && v.fixed_nt > 0) {
-        const int k = split_k_of(c, grp);
-        if (k > 0)
-            return enqueue_split(c, grp, v, a, k, split_cs_of(c, grp), st, bits_of(c, grp));
+        int pts[kSplitRanges - 1];
+        split_of(c, grp, pts);
+        if (pts[0] > 0)
+            return enqueue_split(c, grp, v, a, pts, split_cs_of(c, grp), st, bits_of(c, grp));
     }
     if (cycle && c->wolff && (e = enqueue_wolff(c, grp, st)) != cudaSuccess) return e;
     if (v.rep_cs > 0) return launch_sweep_rep(a, v, nlat, st, false);  // writes the observables
@@ -1293,8 +1345,18 @@ int tune_wolff(Ctx* c, Group& grp)
 // equilibrated lattices they are the slowest choice (L = 96, 8 x 48: 11.0-12.4 vs 9.6 ms).
 // A split choice: k coldest slots on the main stream (0: unsplit), cs CTAs per cold cluster, the
 // cold slots' (unsplit: every slot's) bond activations decided beforehand
+// "k1,k2,..." of a 0-ended list of split points ("0": unsplit)
+std::string pts_str(const int* pts)
+{
+    std::string out;
+    for (int j = 0; j < kSplitRanges - 1 && (j == 0 || pts[j] > 0); ++j)
+        out += (j ? "," : "") + std::to_string(pts[j]);
+    return out;
+}
+
 struct SplitChoice {
-    int k, cs;
+    int pts[kSplitRanges - 1];  // split points, a 0 ending the list (pts[0] = 0: unsplit)
+    int cs;
     bool bits;
 };
 constexpr int kSplitWarm = 40;  // cycles run on the tuner's scratch lattices before timing
@@ -1314,7 +1376,7 @@ int tune_split(Ctx* c, Group& grp)
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_split_cache.find(key);
         if (it != g_split_cache.end()) {
-            grp.split_k = it->second.k;
+            for (int j = 0; j < kSplitRanges - 1; ++j) grp.split[j] = it->second.pts[j];
             grp.split_cs = it->second.cs;
             grp.split_bits = it->second.bits;
             return J1J2C_OK;
@@ -1344,7 +1406,8 @@ int tune_split(Ctx* c, Group& grp)
     // one cycle of a candidate (the Wolff update, PTSWAPEVER sweeps, the observables) with
     // arguments b, enqueued on the context's stream
     auto enqueue = [&](const SplitChoice& cd, const SweepArgs& b) {
-        if (cd.k > 0) return enqueue_split(c, grp, grp.var, b, cd.k, cd.cs, c->own, cd.bits);
+        if (cd.pts[0] > 0)
+            return enqueue_split(c, grp, grp.var, b, cd.pts, cd.cs, c->own, cd.bits);
         grp.split_bits = cd.bits;  // read by enqueue_wolff_grow
         cudaError_t e1 = enqueue_wolff_grow(c, grp, b, wolff_cs_of(c, grp), wolff_k_of(c, grp),
                                             c->own);
@@ -1371,16 +1434,32 @@ int tune_split(Ctx* c, Group& grp)
     // split points between 1/4 and 3/4 of the slots: every multiple of 4 there when the ladder
     // is (the slot-range sweep kernel keeps four replicas per thread only when they divide the
     // range; L = 96, 48 slots: 8.88 ms at 28 vs 9.03 at 24 and 9.22 at 36), else eighths
-    std::vector<SplitChoice> cands{{0, 1, false}};
-    auto add = [&](int k) {
-        bool dup = k <= 0 || k >= grp.nrep;
-        for (const SplitChoice& o : cands) dup = dup || o.k == k;
-        if (!dup) cands.push_back({k, 1, false});
+    std::vector<SplitChoice> cands{{{}, 1, false}};
+    auto push = [&](const SplitChoice& cd) {  // once each
+        for (const SplitChoice& o : cands)
+            if (std::equal(o.pts, o.pts + kSplitRanges - 1, cd.pts)) return;
+        cands.push_back(cd);
+    };
+    auto two = [&](int k) {  // two ranges, split at k
+        if (k > 0 && k < grp.nrep) push({{k}, 1, false});
     };
     if (grp.nrep % 4 == 0 && grp.nrep >= 16)
-        for (int k = grp.nrep / 4; k <= 3 * grp.nrep / 4; k += 4) add(k - k % 4);
+        for (int k = grp.nrep / 4; k <= 3 * grp.nrep / 4; k += 4) two(k - k % 4);
     else
-        for (const int k8 : {2, 3, 4, 5, 6}) add(k8 * grp.nrep / 8);
+        for (const int k8 : {2, 3, 4, 5, 6}) two(k8 * grp.nrep / 8);
+    // more ranges: the coldest 4 or 8 slots alone, so that their long growths are followed by
+    // the sweeps of few lattices, then ranges 8 slots wide up to a last boundary kl, and the
+    // hottest slots from kl (L = 96, 8 x 48: 7.84 ms at 8,16,24,32,36 and 7.90-7.96 ms for five
+    // other lists of this family, 8.63 ms at 32 alone; ranges 4 slots wide were no faster)
+    if (grp.nrep % 4 == 0 && grp.nrep >= 32)
+        for (int kl = grp.nrep / 2 + 8; kl <= grp.nrep / 2 + 16; kl += 4)
+            for (int c0 = 4; c0 <= 8; c0 += 4)
+                for (int n = 1; c0 + (n - 1) * 8 < kl && n < kSplitRanges - 1; ++n) {
+                    SplitChoice cd{{}, 1, false};
+                    for (int i = 0; i < n; ++i) cd.pts[i] = c0 + i * 8;
+                    cd.pts[n] = kl;
+                    push(cd);
+                }
     // The scratch lattices first run kSplitWarm cycles of the unsplit form at their slots'
     // temperatures (the clusters of a freshly started lattice are far smaller than those of an
     // equilibrated cold one, which decide the choice); each of these cycles reads its own cycle
@@ -1420,8 +1499,10 @@ int tune_split(Ctx* c, Group& grp)
         if (exec) cudaGraphExecDestroy(exec);
         if (e == cudaSuccess && tune_log())
             std::fprintf(stderr,
-                         "[j1j2c tune] split L=%d H=%d lattices=%d: k=%d cs=%d bits=%d %.3f ms\n",
-                         grp.g.L, grp.g.H, nlat, cd.k, cd.cs, (int)cd.bits, ms);
+                         "[j1j2c tune] split L=%d H=%d lattices=%d: at %s cs=%d bits=%d %.3f "
+                         "ms\n",
+                         grp.g.L, grp.g.H, nlat, pts_str(cd.pts).c_str(), cd.cs, (int)cd.bits,
+                         ms);
         if (e == cudaSuccess && (ci == 0 || ms < best_ms)) {
             best_ms = ms;
             best = cd;
@@ -1431,7 +1512,7 @@ int tune_split(Ctx* c, Group& grp)
     cudaFree(tmp);
     cudaFree(tobs);
     if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the split Wolff + sweep form");
-    grp.split_k = best.k;
+    for (int j = 0; j < kSplitRanges - 1; ++j) grp.split[j] = best.pts[j];
     grp.split_cs = best.cs;
     grp.split_bits = best.bits;
     std::lock_guard<std::mutex> lk(g_tune_mu);

@@ -158,21 +158,30 @@ def test_wolff_inside_pt_cycles(engine_mod, oracle, nrep):
     eng.close()
 
 
-@pytest.mark.parametrize("extra", ["split", "tuned", "split_bits", "split_async"])
-def test_split_wolff_sweeps_bit_identical(engine_mod, oracle, extra):
+@pytest.mark.parametrize("extra", ["split", "tuned", "split_bits", "split_async", "split3",
+                                   "split4", "split5"])
+def test_split_wolff_sweeps_bit_identical(engine_mod, oracle, extra, monkeypatch):
     """Lattices in HBM (the one-launch-per-colour kernel; L = 32 is its cross-check shape) with a
     Wolff update per cycle: the Wolff update and sweeps of the coldest slots and of the others
     on two streams, each sweep launch finding its lattices through the temperature map (flag
     1024 pins the split at a quarter of the slots, with flag 2048 the cold slots' bonds decided
-    beforehand, with flag 65536 the one-CTA growths level-free; unpinned the tuner times the candidates on equilibrated scratch lattices), equal
-    the replay bit for bit over cycles with replica exchanges."""
+    beforehand, with flag 65536 the one-CTA growths level-free, with J1J2C_SPLIT=2,5 three
+    ranges on three streams, with 1,3,6 four, with 1,2,4,6 five; unpinned the tuner times the
+    candidates on equilibrated scratch lattices), equal the replay bit for bit over cycles with
+    replica exchanges."""
     jc = engine_mod
+    pins = {"split3": "2,5", "split4": "1,3,6", "split5": "1,2,4,6"}
+    if extra in pins:
+        monkeypatch.setenv("J1J2C_SPLIT", pins[extra])
     L, H, nconf, nrep, ncyc = 32, 32, 2, 8, 3
     flags = jc.FLAG_WOLFF | jc.FLAG_GLOBAL | {"split": jc.FLAG_WOLFF_SPLIT, "tuned": 0,
                                               "split_bits": jc.FLAG_WOLFF_SPLIT |
                                               jc.FLAG_WOLFF_BITS,
                                               "split_async": jc.FLAG_WOLFF_SPLIT |
-                                              jc.FLAG_WOLFF_ASYNC}[extra]
+                                              jc.FLAG_WOLFF_ASYNC,
+                                              "split3": jc.FLAG_WOLFF_SPLIT,
+                                              "split4": jc.FLAG_WOLFF_SPLIT,
+                                              "split5": jc.FLAG_WOLFF_SPLIT}[extra]
     eng, dis, betas = _engine(jc, L, H, nconf, nrep, jc.FP64_PLAIN, flags, 0.05)
     states = [oracle.new_pt_state(np.stack([eng.spins(k, r) for r in range(nrep)]))
               for k in range(nconf)]
@@ -195,18 +204,24 @@ def test_split_wolff_sweeps_bit_identical(engine_mod, oracle, extra):
     eng.close()
 
 
-def test_split_wolff_sweeps_fp32_equals_unsplit(engine_mod, oracle):
+def test_split_wolff_sweeps_fp32_equals_unsplit(engine_mod, oracle, monkeypatch):
     """FP32, L = 96 with vacancies and 8 replicas: the split cycle (flag 1024), the unsplit one
     (growth pinned to two CTAs per lattice, which also pins the cycle unsplit), the split cycle
     whose cold slots grow from bond activations decided beforehand, and the unsplit cycle that
-    does so for every slot (flag 2048), and both cycles with level-free one-CTA growths (flag
-    65536) give bitwise equal spins, running sums, maps and cluster sizes."""
+    does so for every slot (flag 2048), both cycles with level-free one-CTA growths (flag
+    65536), and the split cycle over three, four and five temperature ranges (J1J2C_SPLIT=4,6,
+    2,4,6 and 1,2,4,6) give bitwise equal spins, running sums, maps and cluster sizes."""
     jc = engine_mod
     out = []
     base = jc.FLAG_WOLFF | jc.FLAG_GLOBAL
-    for flags in (base | jc.FLAG_WOLFF_SPLIT, base | jc.FLAG_WOLFF_CS2,
-                  base | jc.FLAG_WOLFF_SPLIT | jc.FLAG_WOLFF_BITS, base | jc.FLAG_WOLFF_BITS,
-                  base | jc.FLAG_WOLFF_SPLIT | jc.FLAG_WOLFF_ASYNC, base | jc.FLAG_WOLFF_ASYNC):
+    for i, flags in enumerate((base | jc.FLAG_WOLFF_SPLIT, base | jc.FLAG_WOLFF_CS2,
+                               base | jc.FLAG_WOLFF_SPLIT | jc.FLAG_WOLFF_BITS,
+                               base | jc.FLAG_WOLFF_BITS,
+                               base | jc.FLAG_WOLFF_SPLIT | jc.FLAG_WOLFF_ASYNC,
+                               base | jc.FLAG_WOLFF_ASYNC, base | jc.FLAG_WOLFF_SPLIT,
+                               base | jc.FLAG_WOLFF_SPLIT, base | jc.FLAG_WOLFF_SPLIT)):
+        if i >= 6:
+            monkeypatch.setenv("J1J2C_SPLIT", ("4,6", "2,4,6", "1,2,4,6")[i - 6])
         eng, _, _ = _engine(jc, 96, 96, 1, 8, jc.FP32_BATCHED, flags, 0.05)
         eng.run(2, measure=True, restart_swap_phase=True)
         out.append(([eng.spins(0, r) for r in range(8)], eng.slot_sums(0)[0], eng.maps(0)[0],
