@@ -1664,7 +1664,7 @@ int autotune(Ctx* c, Group& grp)
         const int rc = tune_cluster(c, grp);
         return rc != J1J2C_OK ? rc : tune_split(c, grp);
     }
-    if (grp.var.global && grp.var.fixed_nt > 0) return J1J2C_OK;
+    if (grp.var.global && grp.var.fixed_nt > 0) return tune_split(c, grp);  // HBM form pinned
     if (grp.block_threads > 0 || (c->P.flags & (J1J2C_FLAG_STREAM | J1J2C_FLAG_PAIRS)))
         return J1J2C_OK;
     if (grp.var.fixed_nt == 0) return small_batch_ok(c, grp) ? tune_small_batch(c, grp) : J1J2C_OK;

@@ -234,6 +234,37 @@ def test_split_wolff_sweeps_fp32_equals_unsplit(engine_mod, oracle, monkeypatch)
             np.testing.assert_array_equal(out[0][i], other[i])
 
 
+def test_split_many_ranges_fp32_equals_unsplit(engine_mod, monkeypatch, capfd):
+    """FP32, L = 32 lattices in HBM with vacancies, 32 replicas (the count from which the tuner
+    also times split lists of three to eight temperature ranges): six ranges pinned by
+    J1J2C_SPLIT (one of them 2 slots wide, so its sweeps take two replicas per thread), the
+    tuner's choice, and the unsplit cycle give bitwise equal spins, running sums, maps and
+    cluster sizes over three cycles; the tuner log shows multi-range candidates timed."""
+    jc = engine_mod
+    nrep = 32
+    base = jc.FLAG_WOLFF | jc.FLAG_GLOBAL
+    out = []
+    for i, flags in enumerate((base | jc.FLAG_WOLFF_CS2, base | jc.FLAG_WOLFF_SPLIT, base)):
+        if i == 1:
+            monkeypatch.setenv("J1J2C_SPLIT", "4,12,20,28,30")
+        if i == 2:
+            monkeypatch.delenv("J1J2C_SPLIT")
+            monkeypatch.setenv("J1J2C_TUNE_LOG", "1")
+        eng, _, _ = _engine(jc, 32, 32, 1, nrep, jc.FP32_BATCHED, flags, 0.05)
+        eng.run(3, measure=True, restart_swap_phase=True)
+        out.append(([eng.spins(0, r) for r in range(nrep)], eng.slot_sums(0)[0], eng.maps(0)[0],
+                    eng.cluster_sizes()))
+        eng.close()
+    log = capfd.readouterr().err
+    multi = [ln for ln in log.splitlines() if "split L=32" in ln and ln.split(" at ")[1].count(",")]
+    assert len(multi) >= 4, log
+    for other in out[1:]:
+        for a, b in zip(out[0][0], other[0]):
+            np.testing.assert_array_equal(a, b)
+        for i in (1, 2, 3):
+            np.testing.assert_array_equal(out[0][i], other[i])
+
+
 def _cpu_exact(oracle, L, H, p, betas):
     M = oracle.Model(L, H, p)
     N = L * L * H
