@@ -1265,6 +1265,8 @@ struct WolffChoice {
 };
 std::map<std::tuple<int, bool, int, int, int, bool>, WolffChoice> g_wolff_cache;
 
+constexpr int kWolffWarm = 40;  // cycles run on the Wolff tuner's scratch lattices before timing
+
 int tune_wolff(Ctx* c, Group& grp)
 {
     const uint32_t fl = c->P.flags;
@@ -1284,13 +1286,49 @@ int tune_wolff(Ctx* c, Group& grp)
     }
     CK(c, alloc_labels(c));
     const int nlat = grp.nlat();
-    uint8_t* tmp = nullptr;
+    uint8_t *tmp = nullptr, *snap = nullptr;
+    LatObs* tobs = nullptr;
+    uint32_t* wctl = nullptr;
     const size_t bytes = (size_t)nlat * grp.lat_stride;
-    CK(c, dev_malloc(&tmp, bytes));
-    cudaError_t e =
-        cudaMemcpyAsync(tmp, c->d_spins + grp.spin_off, bytes, cudaMemcpyDeviceToDevice, c->own);
+    auto release = [&]() {
+        cudaStreamSynchronize(c->own);
+        for (void* p : {(void*)tmp, (void*)snap, (void*)tobs, (void*)wctl})
+            if (p) cudaFree(p);
+    };
+    cudaError_t e = dev_malloc(&tmp, bytes);
+    if (e == cudaSuccess) e = dev_malloc(&snap, bytes);
+    if (e == cudaSuccess) e = dev_malloc(&tobs, sizeof(LatObs) * nlat);
+    if (e == cudaSuccess) e = dev_malloc(&wctl, sizeof(uint32_t) * 4 * kWolffWarm);
+    if (e != cudaSuccess) {
+        release();
+        return fail(c, J1J2C_ENOMEM, "autotuner scratch");
+    }
+    e = cudaMemcpyAsync(tmp, c->d_spins + grp.spin_off, bytes, cudaMemcpyDeviceToDevice, c->own);
     SweepArgs a = group_args(c, grp);
     a.spins = tmp;
+    // The scratch lattices first run kWolffWarm cycles (one-CTA Wolff update, sweeps and
+    // observables) at their slots' temperatures: the clusters of a fresh start are far smaller
+    // than those of an equilibrated cold lattice, which decide the choice.  Each warm-up cycle
+    // reads its own cycle counter, so the random streams move on as in a run.  Every candidate
+    // then starts from this state (restored from a second copy), so all of them are timed on
+    // the same clusters: the forms flip the same clusters, so they also pass through the same
+    // states while timed.
+    if (e == cudaSuccess) {
+        std::vector<uint32_t> h(4 * kWolffWarm, 0u);
+        for (int r = 0; r < kWolffWarm; ++r) h[4 * r] = 0x7B000000u + (uint32_t)r;
+        e = cudaMemcpy(wctl, h.data(), h.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    }
+    for (int r = 0; r < kWolffWarm && e == cudaSuccess; ++r) {
+        SweepArgs b = a;
+        b.ctl = wctl + 4 * r;
+        b.obs = tobs;
+        b.flips = nullptr;
+        e = enqueue_wolff_grow(c, grp, b, 1, 0, c->own);
+        if (e == cudaSuccess)
+            e = enqueue_group(c, grp, grp.var, grp.nthreads, grp.smem, b, nlat, c->own, false);
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(snap, tmp, bytes, cudaMemcpyDeviceToDevice, c->own);
     // candidates (CTAs per lattice, coldest slots that take them; k = nrep: every slot)
     struct Cand {
         int cs, k;
@@ -1308,7 +1346,8 @@ int tune_wolff(Ctx* c, Group& grp)
         if (e != cudaSuccess) break;
         if (cs > 1 && wolff_grow_clusters(grp.var.fp64, c->masks, cs) <= 0) continue;
         auto once = [&]() { return enqueue_wolff_grow(c, grp, a, cs, cd.k, c->own); };
-        e = once();  // warm-up
+        e = cudaMemcpyAsync(tmp, snap, bytes, cudaMemcpyDeviceToDevice, c->own);
+        if (e == cudaSuccess) e = once();  // warm-up
         float ms = 0.0f;
         for (int k = 0; k < 3 && e == cudaSuccess; ++k) {  // the fastest of three
             e = cudaEventRecord(c->ev0, c->own);
@@ -1327,8 +1366,7 @@ int tune_wolff(Ctx* c, Group& grp)
             best_k = cd.k < grp.nrep ? cd.k : 0;
         }
     }
-    cudaStreamSynchronize(c->own);
-    cudaFree(tmp);
+    release();
     if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the Wolff update");
     grp.wolff_cs = best;
     grp.wolff_k = best_k;
