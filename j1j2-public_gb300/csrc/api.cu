@@ -1377,12 +1377,13 @@ int tune_wolff(Ctx* c, Group& grp)
 
 // Split Wolff + sweep form (lattices in HBM with Wolff): the whole cycle's Wolff update, sweeps
 // and observables timed on a scratch copy of the group's lattices (the live state is not
-// touched) unsplit and split at the 1/4, 1/2 and 3/4 coldest slots, one CTA per cluster; the
-// fastest is kept, cached per (device, precision, L, H, lattice count, dilution).  Two CTAs per
-// cold cluster are not candidates: on a fresh HOT start (small clusters) they time fastest, on
-// equilibrated lattices they are the slowest choice (L = 96, 8 x 48: 11.0-12.4 vs 9.6 ms).
-// A split choice: k coldest slots on the main stream (0: unsplit), cs CTAs per cold cluster, the
-// cold slots' (unsplit: every slot's) bond activations decided beforehand
+// touched), equilibrated by kSplitWarm cycles and restored before each candidate: unsplit, and
+// split into two or more temperature ranges (the lists below), one CTA per cluster; the fastest
+// is kept, cached per (device, precision, L, H, lattice count, dilution).  Two CTAs per cold
+// cluster are not candidates: on a fresh HOT start (small clusters) they time fastest, on
+// equilibrated lattices they are slower (L = 96, 8 x 48, two ranges: 11.0-12.4 vs 9.6 ms; the
+// coldest of several ranges: 8.11 vs 7.88 ms).
+
 // "k1,k2,..." of a 0-ended list of split points ("0": unsplit)
 std::string pts_str(const int* pts)
 {
@@ -1392,6 +1393,8 @@ std::string pts_str(const int* pts)
     return out;
 }
 
+// A split choice: the split points, cs CTAs per cluster of the coldest range, the coldest
+// range's (unsplit: every slot's) bond activations decided beforehand
 struct SplitChoice {
     int pts[kSplitRanges - 1];  // split points, a 0 ending the list (pts[0] = 0: unsplit)
     int cs;
@@ -1426,12 +1429,14 @@ int tune_split(Ctx* c, Group& grp)
         if (rc != J1J2C_OK) return rc;
     }
     const int nlat = grp.nlat();
-    uint8_t* tmp = nullptr;
+    uint8_t *tmp = nullptr, *snap = nullptr;
     LatObs* tobs = nullptr;
     const size_t bytes = (size_t)nlat * grp.lat_stride;
     CK(c, dev_malloc(&tmp, bytes));
-    if (dev_malloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess) {
+    if (dev_malloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess ||
+        dev_malloc(&snap, bytes) != cudaSuccess) {
         cudaFree(tmp);
+        if (tobs) cudaFree(tobs);
         return fail(c, J1J2C_ENOMEM, "autotuner scratch");
     }
     cudaError_t e =
@@ -1516,6 +1521,9 @@ int tune_split(Ctx* c, Group& grp)
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->own);
     if (wctl) cudaFree(wctl);
+    // every candidate starts from the warmed state: the forms give the same lattices bit for
+    // bit, so all of them are timed on the same clusters
+    if (e == cudaSuccess) e = cudaMemcpyAsync(snap, tmp, bytes, cudaMemcpyDeviceToDevice, c->own);
     SplitChoice best = cands[0];
     float best_ms = 0.0f;
     for (size_t ci = 0; ci < cands.size(); ++ci) {
@@ -1523,6 +1531,8 @@ int tune_split(Ctx* c, Group& grp)
         if (e != cudaSuccess) break;
         cudaGraphExec_t exec = nullptr;
         e = capture(cd, exec);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(tmp, snap, bytes, cudaMemcpyDeviceToDevice, c->own);
         if (e == cudaSuccess) e = cudaGraphLaunch(exec, c->own);  // warm-up
         float ms = 0.0f;
         for (int r = 0; r < 3 && e == cudaSuccess; ++r) {  // the fastest of three
@@ -1548,6 +1558,7 @@ int tune_split(Ctx* c, Group& grp)
     }
     cudaStreamSynchronize(c->own);
     cudaFree(tmp);
+    cudaFree(snap);
     cudaFree(tobs);
     if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the split Wolff + sweep form");
     for (int j = 0; j < kSplitRanges - 1; ++j) grp.split[j] = best.pts[j];
