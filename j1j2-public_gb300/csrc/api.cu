@@ -970,6 +970,8 @@ int time_variant(Ctx* c, Group& grp, const SweepVariant& v, int nthreads, size_t
 // kernel, r > 0 shape-specialised HBM kernel with r replicas per thread.
 std::map<std::tuple<int, bool, int, int, int, bool, int>, int> g_cluster_cache;
 
+bool tune_log();  // J1J2C_TUNE_LOG=1: the tuners print their candidates' timings
+
 int tune_cluster(Ctx* c, Group& grp)
 {
     const int hbm_nt = hbm_fixed_threads(c, grp, grp.var.fp64);
@@ -995,12 +997,19 @@ int tune_cluster(Ctx* c, Group& grp)
         vg.global = true;
         vg.stage_p = false;
         vg.fixed_nt = hbm_nt;
+        // (eight replicas per thread, 128 registers and two CTAs per SM, measured slower at
+        // L = 96: 5.41 vs 4.90 ms per Metropolis cycle of 8 x 48 lattices)
         for (int r = 1; r <= (hbm_nt > 0 ? 4 : 1); r *= 2) {
             if (grp.nrep % r) continue;
             vg.rpt = r;
             float ms = 0.0f;
             rc = time_variant(c, grp, vg, hbm_nt > 0 ? hbm_nt : 256, 0, ms);
             if (rc != J1J2C_OK) return rc;
+            if (tune_log())
+                std::fprintf(stderr,
+                             "[j1j2c tune] lattices in HBM L=%d H=%d lattices=%d: %d per thread "
+                             "%.3f ms (best before it %.3f ms)\n",
+                             grp.g.L, grp.g.H, grp.nlat(), r, ms, best_ms);
             if (ms < best_ms) {
                 best_ms = ms;
                 choice = hbm_nt > 0 ? r : -1;
@@ -1115,8 +1124,6 @@ SweepVariant cluster_variant(const SweepVariant& base, int cs, bool quad, int nt
     v.stage_p = false;
     return v;
 }
-
-bool tune_log();
 
 int tune_small_batch(Ctx* c, Group& grp)
 {

@@ -178,54 +178,37 @@ __global__ void __launch_bounds__(NT) measure_fixed_hbm_kernel(SweepArgs a)
     }
 }
 
-template <class Real, int LH, int HH, int NT>
-cudaError_t run_hbm(const SweepArgs& a, int colour, int t, int nlat, int rpt, cudaStream_t st)
+// One launch with RPT replicas per thread: the observables (colour < 0) or one colour phase, of
+// whole lattices or (a.nslots > 0) of a slot range of every configuration
+template <class Real, int LH, int HH, int NT, int RPT>
+cudaError_t run_hbm_r(const SweepArgs& a, int colour, int t, int nlat, cudaStream_t st)
 {
     constexpr int CS = Shape<LH, HH>::CS;
     const unsigned gx = (unsigned)((CS + NT - 1) / NT);
     const bool pdl = a.pdl != 0;
     const dim3 b((unsigned)NT);
-    if (colour < 0 && a.nslots > 0) {  // the slot range of every configuration
-        const unsigned gy = (unsigned)(nlat / a.nrep * (a.nslots / rpt));
-        if (rpt == 4)
+    if (a.nslots > 0) {  // nlat: whole configurations
+        const unsigned gy = (unsigned)(nlat / a.nrep * (a.nslots / RPT));
+        if (colour < 0)
             return launch_k(pdl, dim3(gx, gy, 8u), b, 0, st,
-                            measure_fixed_hbm_kernel<Real, LH, HH, NT, 4, true, true>, a);
-        if (rpt == 2)
-            return launch_k(pdl, dim3(gx, gy, 8u), b, 0, st,
-                            measure_fixed_hbm_kernel<Real, LH, HH, NT, 2, true, true>, a);
-        return launch_k(pdl, dim3(gx, gy, 8u), b, 0, st,
-                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 1, true, true>, a);
-    }
-    if (colour < 0 && rpt == 4)
-        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 4), 8u), b, 0, st,
-                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 4, true, false>, a);
-    if (colour < 0 && rpt == 2)
-        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 2), 8u), b, 0, st,
-                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 2, true, false>, a);
-    if (colour < 0)
-        return launch_k(pdl, dim3(gx, (unsigned)nlat, 8u), b, 0, st,
-                        measure_fixed_hbm_kernel<Real, LH, HH, NT, 1, true, false>, a);
-    if (a.nslots > 0) {  // a slot range of every configuration (nlat: whole configurations)
-        const unsigned gy = (unsigned)(nlat / a.nrep * (a.nslots / rpt));
-        if (rpt == 4)
-            return launch_k(pdl, dim3(gx, gy), b, 0, st,
-                            sweep_fixed_hbm_kernel<Real, LH, HH, NT, 4, true, true>, a, colour,
-                            t);
-        if (rpt == 2)
-            return launch_k(pdl, dim3(gx, gy), b, 0, st,
-                            sweep_fixed_hbm_kernel<Real, LH, HH, NT, 2, true, true>, a, colour,
-                            t);
+                            measure_fixed_hbm_kernel<Real, LH, HH, NT, RPT, true, true>, a);
         return launch_k(pdl, dim3(gx, gy), b, 0, st,
-                        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 1, true, true>, a, colour, t);
+                        sweep_fixed_hbm_kernel<Real, LH, HH, NT, RPT, true, true>, a, colour, t);
     }
-    if (rpt == 4)
-        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 4)), b, 0, st,
-                        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 4, true, false>, a, colour, t);
-    if (rpt == 2)
-        return launch_k(pdl, dim3(gx, (unsigned)(nlat / 2)), b, 0, st,
-                        sweep_fixed_hbm_kernel<Real, LH, HH, NT, 2, true, false>, a, colour, t);
-    return launch_k(pdl, dim3(gx, (unsigned)nlat), b, 0, st,
-                    sweep_fixed_hbm_kernel<Real, LH, HH, NT, 1, true, false>, a, colour, t);
+    const unsigned gy = (unsigned)(nlat / RPT);
+    if (colour < 0)
+        return launch_k(pdl, dim3(gx, gy, 8u), b, 0, st,
+                        measure_fixed_hbm_kernel<Real, LH, HH, NT, RPT, true, false>, a);
+    return launch_k(pdl, dim3(gx, gy), b, 0, st,
+                    sweep_fixed_hbm_kernel<Real, LH, HH, NT, RPT, true, false>, a, colour, t);
+}
+
+template <class Real, int LH, int HH, int NT>
+cudaError_t run_hbm(const SweepArgs& a, int colour, int t, int nlat, int rpt, cudaStream_t st)
+{
+    if (rpt == 4) return run_hbm_r<Real, LH, HH, NT, 4>(a, colour, t, nlat, st);
+    if (rpt == 2) return run_hbm_r<Real, LH, HH, NT, 2>(a, colour, t, nlat, st);
+    return run_hbm_r<Real, LH, HH, NT, 1>(a, colour, t, nlat, st);
 }
 
 using HbmFn = cudaError_t (*)(const SweepArgs&, int, int, int, int, cudaStream_t);
