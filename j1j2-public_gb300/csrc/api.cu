@@ -1306,9 +1306,10 @@ int tune_wolff(Ctx* c, Group& grp)
     if (e == cudaSuccess) e = dev_malloc(&snap, bytes);
     if (e == cudaSuccess) e = dev_malloc(&tobs, sizeof(LatObs) * nlat);
     if (e == cudaSuccess) e = dev_malloc(&wctl, sizeof(uint32_t) * 4 * kWolffWarm);
-    if (e != cudaSuccess) {
+    if (e != cudaSuccess) {  // no room for the scratch lattices: one CTA each, nothing cached
         release();
-        return fail(c, J1J2C_ENOMEM, "autotuner scratch");
+        cudaGetLastError();
+        return J1J2C_OK;
     }
     e = cudaMemcpyAsync(tmp, c->d_spins + grp.spin_off, bytes, cudaMemcpyDeviceToDevice, c->own);
     SweepArgs a = group_args(c, grp);
@@ -1431,20 +1432,22 @@ int tune_split(Ctx* c, Group& grp)
         }
     }
     CK(c, alloc_labels(c));
-    {
-        const int rc = ensure_act(c);
-        if (rc != J1J2C_OK) return rc;
-    }
     const int nlat = grp.nlat();
     uint8_t *tmp = nullptr, *snap = nullptr;
     LatObs* tobs = nullptr;
+    uint32_t* wctl = nullptr;
     const size_t bytes = (size_t)nlat * grp.lat_stride;
-    CK(c, dev_malloc(&tmp, bytes));
-    if (dev_malloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess ||
-        dev_malloc(&snap, bytes) != cudaSuccess) {
-        cudaFree(tmp);
-        if (tobs) cudaFree(tobs);
-        return fail(c, J1J2C_ENOMEM, "autotuner scratch");
+    auto release = [&]() {
+        cudaStreamSynchronize(c->own);
+        for (void* p : {(void*)tmp, (void*)snap, (void*)tobs, (void*)wctl})
+            if (p) cudaFree(p);
+    };
+    if (dev_malloc(&tmp, bytes) != cudaSuccess || dev_malloc(&snap, bytes) != cudaSuccess ||
+        dev_malloc(&tobs, sizeof(LatObs) * nlat) != cudaSuccess ||
+        dev_malloc(&wctl, sizeof(uint32_t) * 4 * kSplitWarm) != cudaSuccess) {
+        release();  // no room for the scratch lattices: the cycle stays unsplit, nothing cached
+        cudaGetLastError();
+        return J1J2C_OK;
     }
     cudaError_t e =
         cudaMemcpyAsync(tmp, c->d_spins + grp.spin_off, bytes, cudaMemcpyDeviceToDevice, c->own);
@@ -1514,8 +1517,6 @@ int tune_split(Ctx* c, Group& grp)
     // temperatures (the clusters of a freshly started lattice are far smaller than those of an
     // equilibrated cold one, which decide the choice); each of these cycles reads its own cycle
     // counter, so the random stream moves on as in a run
-    uint32_t* wctl = nullptr;
-    if (e == cudaSuccess) e = dev_malloc(&wctl, sizeof(uint32_t) * 4 * kSplitWarm);
     if (e == cudaSuccess) {
         std::vector<uint32_t> h(4 * kSplitWarm, 0u);
         for (int r = 0; r < kSplitWarm; ++r) h[4 * r] = 0x7A000000u + (uint32_t)r;
@@ -1527,7 +1528,6 @@ int tune_split(Ctx* c, Group& grp)
         e = enqueue(cands[0], b);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->own);
-    if (wctl) cudaFree(wctl);
     // every candidate starts from the warmed state: the forms give the same lattices bit for
     // bit, so all of them are timed on the same clusters
     if (e == cudaSuccess) e = cudaMemcpyAsync(snap, tmp, bytes, cudaMemcpyDeviceToDevice, c->own);
@@ -1564,9 +1564,7 @@ int tune_split(Ctx* c, Group& grp)
         }
     }
     cudaStreamSynchronize(c->own);
-    cudaFree(tmp);
-    cudaFree(snap);
-    cudaFree(tobs);
+    release();
     if (e != cudaSuccess) return cuda_fail(c, e, "autotuning the split Wolff + sweep form");
     for (int j = 0; j < kSplitRanges - 1; ++j) grp.split[j] = best.pts[j];
     grp.split_cs = best.cs;

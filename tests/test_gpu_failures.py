@@ -6,7 +6,8 @@ test here faults, traps or hangs the GPU.
   J1J2C_ETIMEOUT, and the context carries on (the error word is cleared once reported).
 * A one-shot injected failure of a device allocation (J1J2C_ENOMEM) or of a PT-cycle launch
   (J1J2C_ECUDA), reported without calling CUDA: the failed call changes nothing, the next call
-  succeeds, and a failed context creation leaves nothing behind.
+  succeeds, and a failed context creation leaves nothing behind; an autotuner that cannot
+  allocate its scratch lattices keeps the untuned form and the run succeeds.
 
 The reference has no recovery of its own: it stops (MPI_ABORT / stop, sim/J1J2_6tv.f90:443-444,
 :841-925); these are the engine's own error paths behind the C ABI.
@@ -84,6 +85,25 @@ def test_injected_allocation_failure(engine_mod):
     eng.run(2, measure=True)
     eng.close()
     jc.inject_fault(jc.INJECT_NONE)
+
+
+def test_tuner_scratch_allocation_failure_falls_back(engine_mod):
+    """The next device allocation fails at a Wolff context's first run, where the Wolff tuner
+    allocates its scratch lattices: the run goes on with the untuned growth form (one CTA per
+    cluster) and gives the same spins and sums as a context that tuned."""
+    jc = engine_mod
+    out = []
+    for inject in (True, False):
+        eng, _ = _engine(jc, 12, 10, 8, flags=jc.FLAG_WOLFF)
+        if inject:
+            jc.inject_fault(jc.INJECT_ALLOC)
+        eng.run(3, measure=True, restart_swap_phase=True)
+        jc.inject_fault(jc.INJECT_NONE)
+        out.append(([eng.spins(0, r) for r in range(8)], eng.slot_sums(0)[0]))
+        eng.close()
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(out[0][1], out[1][1])
 
 
 def test_injected_launch_failure_changes_nothing(engine_mod, oracle):
