@@ -1503,7 +1503,8 @@ int tune_split(Ctx* c, Group& grp)
     // more ranges: the coldest 4 or 8 slots alone, so that their long growths are followed by
     // the sweeps of few lattices, then ranges 8 slots wide up to a last boundary kl, and the
     // hottest slots from kl (L = 96, 8 x 48: 7.84 ms at 8,16,24,32,36 and 7.90-7.96 ms for five
-    // other lists of this family, 8.63 ms at 32 alone; ranges 4 slots wide were no faster)
+    // other lists of this family, 8.63 ms at 32 alone; ranges 4 or 6 slots wide, and a coldest
+    // range of 2 or 6 slots, were no faster)
     if (grp.nrep % 4 == 0 && grp.nrep >= 32)
         for (int kl = grp.nrep / 2 + 8; kl <= grp.nrep / 2 + 16; kl += 4)
             for (int c0 = 4; c0 <= 8; c0 += 4)
