@@ -382,6 +382,12 @@ int choose_variant(Ctx* c, Group& grp, bool fp64, SweepVariant& v, size_t& smem,
         v.global = true;
         v.stage_p = false;
         v.fixed_nt = hbm_fixed_threads(c, grp, fp64);
+        if (v.fixed_nt > 0 && grp.block_threads > 0) {  // one of the HBM kernel's CTA sizes
+            int sz[4];
+            const int n = fixed_hbm_sizes(fp64, grp.g.L, grp.g.H, sz, 4);
+            for (int k = 0; k < n; ++k)
+                if (sz[k] == grp.block_threads) v.fixed_nt = sz[k];
+        }
         v.rpt = grp.nrep % 4 == 0 ? 4 : grp.nrep % 2 == 0 ? 2 : 1;
         smem = 0;
         nthreads = v.fixed_nt > 0 ? v.fixed_nt : 256;
@@ -996,36 +1002,42 @@ int tune_cluster(Ctx* c, Group& grp)
         vg.cluster = 0;
         vg.global = true;
         vg.stage_p = false;
-        vg.fixed_nt = hbm_nt;
+        // CTA sizes of the shape's HBM kernels (the default first), else the generic kernel
+        int sizes[4] = {0};
+        const int nsz =
+            hbm_nt > 0 ? fixed_hbm_sizes(grp.var.fp64, grp.g.L, grp.g.H, sizes, 4) : 1;
         // (eight replicas per thread, 128 registers and two CTAs per SM, measured slower at
         // L = 96: 5.41 vs 4.90 ms per Metropolis cycle of 8 x 48 lattices)
-        for (int r = 1; r <= (hbm_nt > 0 ? 4 : 1); r *= 2) {
-            if (grp.nrep % r) continue;
-            vg.rpt = r;
-            float ms = 0.0f;
-            rc = time_variant(c, grp, vg, hbm_nt > 0 ? hbm_nt : 256, 0, ms);
-            if (rc != J1J2C_OK) return rc;
-            if (tune_log())
-                std::fprintf(stderr,
-                             "[j1j2c tune] lattices in HBM L=%d H=%d lattices=%d: %d per thread "
-                             "%.3f ms (best before it %.3f ms)\n",
-                             grp.g.L, grp.g.H, grp.nlat(), r, ms, best_ms);
-            if (ms < best_ms) {
-                best_ms = ms;
-                choice = hbm_nt > 0 ? r : -1;
+        for (int si = 0; si < nsz; ++si)
+            for (int r = 1; r <= (sizes[si] > 0 ? 4 : 1); r *= 2) {
+                if (grp.nrep % r) continue;
+                vg.fixed_nt = sizes[si];
+                vg.rpt = r;
+                float ms = 0.0f;
+                rc = time_variant(c, grp, vg, sizes[si] > 0 ? sizes[si] : 256, 0, ms);
+                if (rc != J1J2C_OK) return rc;
+                if (tune_log())
+                    std::fprintf(stderr,
+                                 "[j1j2c tune] lattices in HBM L=%d H=%d lattices=%d: %d threads, "
+                                 "%d per thread %.3f ms (best before it %.3f ms)\n",
+                                 grp.g.L, grp.g.H, grp.nlat(), sizes[si], r, ms, best_ms);
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    choice = sizes[si] > 0 ? (sizes[si] << 4 | r) : -1;  // CTA size and RPT
+                }
             }
-        }
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_cluster_cache[key] = choice;
     }
     if (choice != 0) {
+        const int nt = choice > 0 ? choice >> 4 : 0;
         grp.var.cluster = 0;
         grp.var.global = true;
         grp.var.stage_p = false;
-        grp.var.fixed_nt = choice > 0 ? hbm_nt : 0;
-        grp.var.rpt = choice > 0 ? choice : 1;
+        grp.var.fixed_nt = nt;
+        grp.var.rpt = choice > 0 ? choice & 15 : 1;
         grp.smem = 0;
-        grp.nthreads = choice > 0 ? hbm_nt : 256;
+        grp.nthreads = nt > 0 ? nt : 256;
         free_graphs(c);
     }
     return J1J2C_OK;

@@ -211,8 +211,10 @@ cudaError_t launch_fixed(const SweepArgs& a, bool fp64, bool vac, const FixedCho
 // (sharing the field loads); the launch falls back to 1 when the range is not whole
 // configurations or rpt does not divide the replica count.
 int fixed_hbm_threads(bool fp64, int L, int H, bool masks, bool int_cpl);
-cudaError_t launch_fixed_hbm(const SweepArgs& a, bool fp64, int colour, int t, int nlat, int rpt,
-                             cudaStream_t st);
+// CTA sizes of the shape's HBM kernels (the default first) into out; their number
+int fixed_hbm_sizes(bool fp64, int L, int H, int* out, int cap);
+cudaError_t launch_fixed_hbm(const SweepArgs& a, bool fp64, int nt, int colour, int t, int nlat,
+                             int rpt, cudaStream_t st);
 
 // One persistent launch over several lattice-shape groups (sweep_multi.cu).  A tile is R
 // replicas of one configuration of a group; tile kinds exist for L = H = 16, 24, 32, 48.

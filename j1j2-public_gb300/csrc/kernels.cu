@@ -1812,7 +1812,8 @@ cudaError_t launch_sweep_rep(const SweepArgs& a, const SweepVariant& v, int nlat
 cudaError_t launch_sweep_global(const SweepArgs& a, const SweepVariant& v, int colour, int t,
                                 int nlat, cudaStream_t st)
 {
-    if (v.fixed_nt > 0) return launch_fixed_hbm(a, v.fp64, colour, t, nlat, v.rpt, st);
+    if (v.fixed_nt > 0)
+        return launch_fixed_hbm(a, v.fp64, v.fixed_nt, colour, t, nlat, v.rpt, st);
     return v.fp64 ? global_dispatch<double>(a, v, colour, t, nlat, st, false)
                   : global_dispatch<float>(a, v, colour, t, nlat, st, false);
 }
@@ -1820,7 +1821,7 @@ cudaError_t launch_sweep_global(const SweepArgs& a, const SweepVariant& v, int c
 cudaError_t launch_measure_global(const SweepArgs& a, const SweepVariant& v, int nlat,
                                   cudaStream_t st)
 {
-    if (v.fixed_nt > 0) return launch_fixed_hbm(a, v.fp64, -1, 0, nlat, v.rpt, st);
+    if (v.fixed_nt > 0) return launch_fixed_hbm(a, v.fp64, v.fixed_nt, -1, 0, nlat, v.rpt, st);
     return v.fp64 ? global_dispatch<double>(a, v, 0, 0, nlat, st, true)
                   : global_dispatch<float>(a, v, 0, 0, nlat, st, true);
 }

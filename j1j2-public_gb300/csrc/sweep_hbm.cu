@@ -223,6 +223,8 @@ struct HbmEntry {
 // code against the shared-memory kernels); vacancy handling always on.
 const HbmEntry kHbm[] = {
     {false, 96, 96, 256, run_hbm<float, 48, 48, 256>},
+    {false, 96, 96, 128, run_hbm<float, 48, 48, 128>},
+    {false, 96, 96, 512, run_hbm<float, 48, 48, 512>},
     {true, 96, 96, 256, run_hbm<double, 48, 48, 256>},
     {false, 32, 32, 256, run_hbm<float, 16, 16, 256>},
     {true, 32, 32, 256, run_hbm<double, 16, 16, 256>},
@@ -238,8 +240,16 @@ int fixed_hbm_threads(bool fp64, int L, int H, bool masks, bool int_cpl)
     return 0;
 }
 
-cudaError_t launch_fixed_hbm(const SweepArgs& a, bool fp64, int colour, int t, int nlat, int rpt,
-                             cudaStream_t st)
+int fixed_hbm_sizes(bool fp64, int L, int H, int* out, int cap)
+{
+    int n = 0;
+    for (const auto& e : kHbm)
+        if (e.fp64 == fp64 && e.L == L && e.H == H && n < cap) out[n++] = e.nt;
+    return n;
+}
+
+cudaError_t launch_fixed_hbm(const SweepArgs& a, bool fp64, int nt, int colour, int t, int nlat,
+                             int rpt, cudaStream_t st)
 {
     // replicas per thread only over whole configurations (RPT lattices of one block row share
     // their configuration's field)
@@ -252,7 +262,7 @@ cudaError_t launch_fixed_hbm(const SweepArgs& a, bool fp64, int colour, int t, i
         while (rpt > 1 && a.nslots % rpt != 0) rpt /= 2;
     }
     for (const auto& e : kHbm)
-        if (e.fp64 == fp64 && e.L == a.g.L && e.H == a.g.H)
+        if (e.fp64 == fp64 && e.L == a.g.L && e.H == a.g.H && (nt <= 0 || e.nt == nt))
             return e.fn(a, colour, t, nlat, rpt, st);
     return cudaErrorInvalidValue;
 }

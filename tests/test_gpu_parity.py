@@ -415,14 +415,19 @@ def test_hbm_kernel_L96_fp64_bit_identical_to_replay(engine_mod, oracle):
 
 
 def test_hbm_kernel_L96_fp32_equals_other_paths(engine_mod, oracle):
-    """FP32 96^3 with vacancies: the shape-specialised HBM kernel, the generic global-memory
-    kernel and the default choice (thread-block cluster or HBM kernel, whichever the autotuner
-    keeps) give bitwise equal spins, sums and observables."""
+    """FP32 96^3 with vacancies: the shape-specialised HBM kernel (CTAs of 256, 128 and 512
+    threads), the generic global-memory kernel and the default choice (thread-block cluster or
+    HBM kernel, whichever the autotuner keeps) give bitwise equal spins, sums and
+    observables."""
     jc = engine_mod
     out = []
-    for flags in (jc.FLAG_GLOBAL, jc.FLAG_GLOBAL | jc.FLAG_NO_FIXED, 0):
-        eng, _, _ = _setup(jc, oracle, 96, 96, 1, 3, jc.FP32_BATCHED, pp=0.05, flags=flags)
+    for flags, bt in ((jc.FLAG_GLOBAL, 0), (jc.FLAG_GLOBAL, 128), (jc.FLAG_GLOBAL, 512),
+                      (jc.FLAG_GLOBAL | jc.FLAG_NO_FIXED, 0), (0, 0)):
+        eng, _, _ = _setup(jc, oracle, 96, 96, 1, 3, jc.FP32_BATCHED, pp=0.05, flags=flags,
+                           block_threads=bt)
         eng.run(2, measure=True)
+        if bt:
+            assert eng.config()["block_threads"] == bt
         out.append(([eng.spins(0, r) for r in range(3)], eng.slot_sums(0)[0],
                     eng.observables(-1)))
         eng.close()
