@@ -99,7 +99,9 @@ typedef struct {
     uint32_t conf_base;    /* Philox key word 1 of conf 0 (conf c uses conf_base + c)           */
     int32_t device;        /* CUDA device ordinal                                                */
     uint32_t flags;        /* J1J2C_FLAG_*                                                       */
-    int32_t block_threads; /* 0 = autotuned; otherwise threads per CTA (multiple of 32, <=1024) */
+    int32_t block_threads; /* 0 = autotuned; otherwise threads per CTA (multiple of 32, <=1024;
+                              with lattices in HBM, one of the HBM kernel's sizes 128, 256,
+                              512 where it has that shape)                                   */
 } j1j2c_params;
 
 /* Per (conf, slot) running sums of Pt_measurement_loop (J:1440-1513), in this order. */
